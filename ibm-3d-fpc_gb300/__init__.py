@@ -1,0 +1,225 @@
+"""GB300-native per-timestep solver for the immersed-boundary channel flow.
+
+Python mirror of the reference's driver (main.cu): a :class:`Case` holds the
+CPU setup (geometry, masks, ids, embedded operators, CSR projection
+operators) produced by ``libibmhost.so``; a :class:`Solver` owns one GPU
+context of ``libibmgpu.so`` and advances the state one timestep per
+:meth:`Solver.step`, exactly as the reference's step loop (main.cu:249-376).
+
+Both libraries are C ABIs (include/ibm_host.h, include/ibm_gpu.h); this module
+is a thin ctypes layer. There is no CPU fallback: without the CUDA library
+or a GPU, :class:`Solver` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from typing import Optional
+
+import numpy as np
+
+from . import _native
+from ._native import CaseCounts, CaseParams, GridDesc, SolverParams, SolveStats, StepStats
+
+__all__ = ["CaseParams", "Case", "Solver", "SolverParams", "StepStats", "channel_params", "solver_params",
+           "IBM_OK", "IBM_NOT_CONVERGED", "IBMError", "FIELD_U", "FIELD_V", "FIELD_W", "FIELD_P"]
+
+IBM_OK = 0
+IBM_NOT_CONVERGED = 1
+FIELD_U, FIELD_V, FIELD_W, FIELD_P = 0, 1, 2, 3
+
+
+class IBMError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+def channel_params(nx: int, ny: int, nz: int, *, Lx: float = 2.5, Ly: float = 0.41, Lz: float = 0.41,
+                   rho: float = 1.0, nu: float = 1.0e-3, Um: float = 0.45, dt: float = 1.0e-3,
+                   nsub_beta: int = 10, beta_tol: float = 1.0e-8, alpha_tol: float = 1.0e-10,
+                   xcirc: float = 0.5, ycirc: float = 0.2, Rcirc: float = 0.05) -> CaseParams:
+    """Case parameters; defaults are the benchmark channel (2.5 x 0.41 x 0.41,
+    cylinder of diameter 0.1 at (0.5, 0.2)), which differ from the reference's
+    built-in defaults (common.hpp:49, 64-66)."""
+    return CaseParams(nx, ny, nz, Lx, Ly, Lz, rho, nu, Um, dt, nsub_beta, beta_tol, alpha_tol, xcirc, ycirc, Rcirc)
+
+
+def solver_params(**kw) -> SolverParams:
+    """Solver options starting from the library defaults (the reference's
+    defaults, common.hpp:68-80); keyword arguments override fields."""
+    p = SolverParams()
+    _native.gpu().ibm_solver_params_default(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(f"SolverParams has no field {k!r}")
+        setattr(p, k, v)
+    return p
+
+
+_DTYPES = {1: np.uint8, 4: np.int32, 8: np.float64}
+
+
+class Case:
+    """CPU setup of one channel case (include/ibm_host.h)."""
+
+    def __init__(self, params: CaseParams):
+        self._lib = _native.host()
+        self.params = params
+        self._h = C.c_void_p()
+        rc = self._lib.ibm_case_build(C.byref(params), C.byref(self._h))
+        if rc != 0:
+            raise IBMError(rc, "ibm_case_build failed (bad parameters)")
+        cnt = CaseCounts()
+        self._lib.ibm_case_get_counts(self._h, C.byref(cnt))
+        self.counts = {f: getattr(cnt, f) for f, _ in CaseCounts._fields_}
+        self._cache: dict[str, np.ndarray] = {}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.ibm_case_free(h)
+            self._h = None
+
+    def array(self, name: str) -> np.ndarray:
+        """A named setup array (see include/ibm_host.h), as a numpy view."""
+        if name not in self._cache:
+            es = C.c_int()
+            nb = self._lib.ibm_case_array_bytes(self._h, name.encode(), C.byref(es))
+            if nb < 0:
+                raise KeyError(name)
+            ptr = self._lib.ibm_case_array(self._h, name.encode())
+            buf = (C.c_ubyte * nb).from_address(ptr) if nb else bytearray()
+            self._cache[name] = np.frombuffer(buf, dtype=_DTYPES[es.value]) if nb else np.zeros(0, _DTYPES[es.value])
+        return self._cache[name]
+
+    @property
+    def shape(self):
+        return self.params.nx, self.params.ny, self.params.nz
+
+    def initial_fields(self):
+        """The reference's initial state (main.cu:116-126): zero velocity and
+        pressure, then the BC cleanup with the unramped inlet profile."""
+        nx, ny, nz = self.shape
+        u = np.zeros((nz, ny, nx + 1))
+        v = np.zeros((nz, ny + 1, nx))
+        w = np.zeros((nz + 1, ny, nx))
+        p = np.zeros((nz, ny, nx))
+        u[:, :, 0] = self.array("uin").reshape(nz, ny)
+        return u.ravel(), v.ravel(), w.ravel(), p.ravel()
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class Solver:
+    """One GPU context running the per-timestep hot path (include/ibm_gpu.h)."""
+
+    def __init__(self, case: Case, params: Optional[SolverParams] = None, device: int = 0):
+        self._lib = _native.gpu()
+        self.case = case
+        cp = case.params
+        g = GridDesc(cp.nx, cp.ny, cp.nz, cp.Lx, cp.Ly, cp.Lz, cp.rho, cp.nu, cp.dt, device)
+        self._ctx = C.c_void_p()
+        rc = self._lib.ibm_create(C.byref(g), C.byref(self._ctx))
+        if rc != 0:
+            raise IBMError(rc, self._lib.ibm_last_error(None).decode())
+        nx, ny, nz = case.shape
+        a = case.array
+        self._check(self._lib.ibm_set_operator(self._ctx, FIELD_U, _ptr(a("Au_vals")), nx - 1, ny, nz))
+        self._check(self._lib.ibm_set_operator(self._ctx, FIELD_V, _ptr(a("Av_vals")), nx, ny - 1, nz))
+        self._check(self._lib.ibm_set_operator(self._ctx, FIELD_W, _ptr(a("Aw_vals")), nx, ny, nz - 1))
+        self._check(self._lib.ibm_set_operator(self._ctx, FIELD_P, _ptr(a("Ap_vals")), nx, ny, nz))
+        self._check(self._lib.ibm_set_masks(self._ctx, *[_ptr(a(n)) for n in (
+            "active_u", "active_v", "active_w", "fluid_p", "active_qu", "active_qv", "active_qw",
+            "id_u", "id_v", "id_w", "id_p", "id_qu", "id_qv", "id_qw")]))
+        self._check(self._lib.ibm_set_aux(self._ctx, *[_ptr(a(n)) for n in (
+            "scale_u", "scale_v", "scale_w", "rhs_u_bc", "rhs_v_bc", "rhs_w_bc", "div_bc_unit", "uin")]))
+        cnt = case.counts
+        nq = cnt["nqu"] + cnt["nqv"] + cnt["nqw"]
+        self._check(self._lib.ibm_set_projection_csr(
+            self._ctx, _ptr(a("D_rowptr")), _ptr(a("D_col")), _ptr(a("D_val")), cnt["np"],
+            _ptr(a("G_rowptr")), _ptr(a("G_col")), _ptr(a("G_val")), nq))
+        self.set_params(params if params is not None else solver_params())
+        self.set_fields(*case.initial_fields())
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.ibm_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc: int) -> int:
+        if rc < 0:
+            raise IBMError(rc, self._lib.ibm_last_error(self._ctx).decode())
+        return rc
+
+    def set_params(self, p: SolverParams) -> None:
+        self.params = p
+        self._check(self._lib.ibm_set_solver_params(self._ctx, C.byref(p)))
+
+    def set_fields(self, u=None, v=None, w=None, p=None) -> None:
+        arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (u, v, w, p)]
+        self._check(self._lib.ibm_set_fields(self._ctx, *[None if x is None else _ptr(x) for x in arrs]))
+
+    def fields(self):
+        nx, ny, nz = self.case.shape
+        u = np.empty((nx + 1) * ny * nz)
+        v = np.empty(nx * (ny + 1) * nz)
+        w = np.empty(nx * ny * (nz + 1))
+        p = np.empty(nx * ny * nz)
+        self._check(self._lib.ibm_get_fields(self._ctx, _ptr(u), _ptr(v), _ptr(w), _ptr(p)))
+        return u, v, w, p
+
+    def step(self, ramp: float) -> StepStats:
+        st = StepStats()
+        self._check(self._lib.ibm_step(self._ctx, C.c_double(ramp), C.byref(st)))
+        return st
+
+    def solve(self, field: int, b: np.ndarray, x0: Optional[np.ndarray] = None):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=np.float64)
+        st = SolveStats()
+        self._check(self._lib.ibm_solve(self._ctx, field, _ptr(b), _ptr(x), C.byref(st)))
+        return x, st
+
+    def apply_operator(self, field: int, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty_like(x)
+        self._check(self._lib.ibm_apply_operator(self._ctx, field, _ptr(x), _ptr(y)))
+        return y
+
+    def solver_vector(self, field: int, which: int) -> np.ndarray:
+        nx, ny, nz = self.case.shape
+        n = [(nx - 1) * ny * nz, nx * (ny - 1) * nz, nx * ny * (nz - 1), nx * ny * nz][field]
+        out = np.empty(n)
+        self._check(self._lib.ibm_get_solver_vector(self._ctx, field, which, _ptr(out)))
+        return out
+
+    def launches(self) -> int:
+        return int(self._lib.ibm_kernel_launches(self._ctx))
+
+    def run(self, nsteps: int, ramp_steps: int = 200, start: int = 1, callback=None):
+        """The reference's step loop (main.cu:249-251): ramp = min(1, step/ramp_steps)."""
+        out = []
+        for step in range(start, start + nsteps):
+            ramp = min(1.0, step / float(ramp_steps))
+            st = self.step(ramp)
+            out.append(st)
+            if callback:
+                callback(step, st)
+        return out
+
+
+def stats_dict(st: StepStats) -> dict:
+    d = {"ramp": st.ramp, "div_l2": st.div_l2, "umax": st.umax, "vmax": st.vmax, "wmax": st.wmax,
+         "status": st.status, "t_total_ms": st.t_total_ms, "t_rhs_ms": st.t_rhs_ms, "t_mom_ms": st.t_mom_ms,
+         "t_p_ms": st.t_p_ms, "t_proj_ms": st.t_proj_ms}
+    for f in ("u", "v", "w", "p"):
+        s = getattr(st, f)
+        d[f"its_{f}"] = s.iters
+        d[f"rel_{f}"] = s.rel_res
+    return d

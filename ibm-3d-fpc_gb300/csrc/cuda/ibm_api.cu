@@ -1,0 +1,687 @@
+// The C ABI of include/ibm_gpu.h: context lifecycle, conversion of the
+// reference's inputs (row-major 7-point values, masks and 1-based ids,
+// id-indexed vectors, 1-based CSR) into the device layouts the kernels use,
+// solver wiring and the timestep.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "ibm_ctx.cuh"
+#include "ibm_step.cuh"
+
+namespace ibm {
+
+thread_local long long *g_counter = nullptr;
+void count_launch(long long n) {
+  if (g_counter) *g_counter += n;
+}
+long long launches() { return g_counter ? *g_counter : 0; }
+
+int sm_count() {
+  int dev = 0, n = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  return n > 0 ? n : 1;
+}
+
+int persistent_blocks(int rows, int per_sm) {
+  const long tiles = ((long)rows + kTile - 1) / kTile;
+  const long cap = (long)sm_count() * per_sm;
+  return (int)std::max(1L, std::min(tiles, cap));
+}
+
+namespace {
+
+struct Scope {
+  long long *prev;
+  explicit Scope(ibm_ctx *c) : prev(g_counter) {
+    g_counter = &c->launches;
+    cudaSetDevice(c->device);
+  }
+  ~Scope() { g_counter = prev; }
+};
+
+std::string g_create_error;
+
+template <class F>
+int guarded(ibm_ctx *c, F &&f) {
+  if (!c) return IBM_ERR_ARG;
+  Scope sc(c);
+  try {
+    c->err.clear();
+    return f();
+  } catch (const Error &e) {
+    c->err = e.msg;
+    return e.code;
+  } catch (const std::exception &e) {
+    c->err = e.what();
+    return IBM_ERR_ARG;
+  }
+}
+
+// Copy n elements from a host or device pointer into a host vector.
+template <class T>
+std::vector<T> to_host(const T *src, size_t n) {
+  std::vector<T> h(n);
+  if (n) IBM_CUDA_TRY(cudaMemcpy(h.data(), src, n * sizeof(T), cudaMemcpyDefault));
+  return h;
+}
+
+template <class T>
+void upload(DBuf<T> &dst, const std::vector<T> &h, cudaStream_t st) {
+  dst.alloc(h.size());
+  if (!h.empty()) IBM_CUDA_TRY(cudaMemcpyAsync(dst.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  IBM_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+// Row-major [n][7] -> planes [7][n], inverse diagonal, FP32 copies.
+__global__ void k_op_planes(const double *vals, long n, double *c, double *invd, float *cf, float *invdf) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    for (int s = 0; s < 7; ++s) {
+      const double v = vals[7 * r + s];
+      c[(long)s * n + r] = v;
+      cf[(long)s * n + r] = (float)v;
+    }
+    const double d = vals[7 * r];
+    const double id = d != 0.0 ? 1.0 / d : 0.0;
+    invd[r] = id;
+    invdf[r] = (float)id;
+  }
+}
+
+// Right-Jacobi-scaled operator: cj_s(r) = c_s(r) * invd(neighbour_s(r)).
+__global__ void k_op_jacobi(const double *c, const double *invd, double *cj, Box b) {
+  const long n = b.n, sy = b.nx, sz = (long)b.nx * b.ny;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    row_ijk((int)r, b.nx, b.ny, i, j, k);
+    const long nb[7] = {r, i > 0 ? r - 1 : -1, i < b.nx - 1 ? r + 1 : -1, j > 0 ? r - sy : -1,
+                        j < b.ny - 1 ? r + sy : -1, k > 0 ? r - sz : -1, k < b.nz - 1 ? r + sz : -1};
+    for (int s = 0; s < 7; ++s) cj[(long)s * n + r] = nb[s] >= 0 ? c[(long)s * n + r] * invd[nb[s]] : 0.0;
+  }
+}
+
+__global__ void k_spmv7(const double *c, Box b, const double *x, double *y) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < b.n; r += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    row_ijk((int)r, b.nx, b.ny, i, j, k);
+    y[r] = stencil7_row(c, b.n, x, (int)r, i, j, k, b.nx, b.ny, b.nz);
+  }
+}
+
+int grid1d(long n) {
+  long b = (n + kThreads - 1) / kThreads;
+  return (int)std::max(1L, std::min(b, (long)sm_count() * 8));
+}
+
+const Box &field_box(const ibm_ctx *c, int f) {
+  return f == 0 ? c->g.bu : f == 1 ? c->g.bv : f == 2 ? c->g.bw : c->g.bp;
+}
+
+void mg_apply_cb(void *ctx, cudaStream_t st, int, const VecRef &in, const OutRef &out, const int *gate) {
+  ibm_ctx *c = (ibm_ctx *)ctx;
+  c->mg.apply(st, in, out, gate, out.f != nullptr);
+}
+
+void require_inputs(ibm_ctx *c) {
+  for (int f = 0; f < 4; ++f)
+    if (!c->op[f].set) throw Error(IBM_ERR_STATE, "operator of field " + std::to_string(f) + " not set");
+  if (!c->masks_set) throw Error(IBM_ERR_STATE, "masks not set");
+  if (!c->aux_set) throw Error(IBM_ERR_STATE, "aux vectors not set");
+  if (!c->csr_set) throw Error(IBM_ERR_STATE, "projection operators not set");
+}
+
+void ensure_solvers(ibm_ctx *c) {
+  if (c->solvers_ready && c->solvers_precision == c->prm.precision) return;
+  const ibm_solver_params &p = c->prm;
+  const bool mixed = p.precision == 1;
+  if (!mixed && p.vel_jacobi_iters != 1)
+    throw Error(IBM_ERR_UNSUPPORTED, "FP64 momentum solves support one Jacobi sweep per application");
+  KSysHost hs[3];
+  for (int f = 0; f < 3; ++f) {
+    const Op7 &o = c->op[f];
+    KSysHost &h = hs[f];
+    h.nx = o.b.nx; h.ny = o.b.ny; h.nz = o.b.nz; h.n = o.b.n;
+    h.Ar = o.c.p;
+    h.invd = o.invd.p;
+    h.Af = o.cf.p; h.invdf = o.invdf.p;
+    h.kdim = p.vel_kdim; h.maxit = p.vel_maxit; h.tol = p.vel_tol;
+    if (mixed) { h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps); }
+    else { h.pc = 0; h.A = o.cj.p; }
+  }
+  c->kmom.configure(3, hs);
+  const Op7 &op = c->op[3];
+  KSysHost hp;
+  hp.nx = op.b.nx; hp.ny = op.b.ny; hp.nz = op.b.nz; hp.n = op.b.n;
+  hp.Ar = op.c.p; hp.invd = op.invd.p; hp.Af = op.cf.p; hp.invdf = op.invdf.p;
+  hp.kdim = p.p_kdim; hp.maxit = p.p_maxit; hp.tol = p.p_tol;
+  if (p.p_pc == 1) {
+    MgParams mp;
+    mp.rap = p.p_pc_rap_type == 0 ? 0 : 1;
+    mp.relax = p.p_pc_relax_type == 2 ? 2 : 1;
+    mp.nu1 = p.mg_nu1; mp.nu2 = p.mg_nu2; mp.omega = p.mg_omega;
+    mp.coarse_max = p.mg_coarse_max; mp.max_levels = p.mg_max_levels;
+    mp.cycles = std::max(1, p.p_pc_maxit);
+    const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
+    c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed);
+    if (mixed) { hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; }
+    else { hp.pc = 1; hp.A = op.c.p; }
+  } else {
+    if (mixed) { hp.pc = 2; hp.pc_cb = 0; hp.A = op.c.p; hp.inner_sweeps = 1; }
+    else { hp.pc = 0; hp.A = op.cj.p; }
+  }
+  c->kp.configure(1, &hp);
+  c->solvers_ready = true;
+  c->solvers_precision = p.precision;
+}
+
+int worst(int a, int b) { return std::max(a, b); }
+
+void fill_solve(ibm_solve_stats &o, const KResult &r) {
+  o.iters = r.iters;
+  o.rel_res = r.rel_res;
+  o.status = (r.status == 1) ? IBM_OK : IBM_NOT_CONVERGED;
+}
+
+}  // namespace
+}  // namespace ibm
+
+using namespace ibm;
+
+extern "C" {
+
+void ibm_solver_params_default(ibm_solver_params *p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->vel_tol = 1.0e-6; p->vel_maxit = 250; p->vel_kdim = 50; p->vel_jacobi_iters = 1;
+  p->p_tol = 1.0e-9; p->p_maxit = 250; p->p_kdim = 50;
+  p->p_pc = 1; p->p_pc_maxit = 1; p->p_pc_relax_type = 1; p->p_pc_rap_type = 1;
+  p->mg_nu1 = 1; p->mg_nu2 = 1; p->mg_omega = 2.0 / 3.0; p->mg_coarse_max = 64; p->mg_max_levels = 40;
+  p->use_zero_initial_guess = 1; p->precision = 0; p->use_graph = 0; p->vel_inner_sweeps = 3;
+}
+
+const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int ibm_create(const ibm_grid_desc *grid, ibm_ctx **out) {
+  if (!grid || !out) return IBM_ERR_ARG;
+  *out = nullptr;
+  if (grid->nx < 3 || grid->ny < 3 || grid->nz < 3 || !(grid->dt > 0) || !(grid->rho > 0) || grid->Lx <= 0 ||
+      grid->Ly <= 0 || grid->Lz <= 0) {
+    g_create_error = "ibm_create: bad grid";
+    return IBM_ERR_ARG;
+  }
+  if ((double)(grid->nx + 1) * (grid->ny + 1) * (grid->nz + 1) > 2.0e9) {
+    g_create_error = "ibm_create: grid too large for 32-bit row indices";
+    return IBM_ERR_ARG;
+  }
+  ibm_ctx *c = new ibm_ctx();
+  c->grid = *grid;
+  c->device = grid->device;
+  ibm_solver_params_default(&c->prm);
+  int rc = guarded(c, [&]() {
+    IBM_CUDA_TRY(cudaSetDevice(grid->device));
+    IBM_CUDA_TRY(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    for (auto &e : c->ev) IBM_CUDA_TRY(cudaEventCreate(&e));
+    Geometry &g = c->g;
+    g.nx = grid->nx; g.ny = grid->ny; g.nz = grid->nz;
+    g.NU = (long)(g.nx + 1) * g.ny * g.nz; g.NV = (long)g.nx * (g.ny + 1) * g.nz;
+    g.NW = (long)g.nx * g.ny * (g.nz + 1); g.NP = (long)g.nx * g.ny * g.nz;
+    g.bu = make_box(g.nx - 1, g.ny, g.nz); g.bv = make_box(g.nx, g.ny - 1, g.nz);
+    g.bw = make_box(g.nx, g.ny, g.nz - 1); g.bp = make_box(g.nx, g.ny, g.nz);
+    g.dx = grid->Lx / g.nx; g.dy = grid->Ly / g.ny; g.dz = grid->Lz / g.nz;
+    g.rho = grid->rho; g.nu = grid->nu; g.dt = grid->dt;
+    c->u.alloc(g.NU); c->v.alloc(g.NV); c->w.alloc(g.NW); c->p.alloc(g.NP);
+    c->ut.alloc(g.NU); c->vt.alloc(g.NV); c->wt.alloc(g.NW);
+    for (int f = 0; f < 4; ++f) {
+      c->xb[f].alloc(field_box(c, f).n);
+      c->bb[f].alloc(field_box(c, f).n);
+      c->xb[f].zero(c->st);
+      c->bb[f].zero(c->st);
+    }
+    c->u.zero(c->st); c->v.zero(c->st); c->w.zero(c->st); c->p.zero(c->st);
+    c->diag.alloc(1);
+    c->part.alloc(4 * 1024);
+    IBM_CUDA_TRY(cudaMallocHost((void **)&c->hdiag, sizeof(StepDiag)));
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+  if (rc != IBM_OK) {
+    g_create_error = c->err;
+    ibm_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return IBM_OK;
+}
+
+void ibm_destroy(ibm_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->hdiag) cudaFreeHost(c->hdiag);
+  cudaStream_t st = c->st;
+  delete c;
+  if (st) cudaStreamDestroy(st);
+}
+
+int ibm_set_operator(ibm_ctx *c, int field, const double *vals7, int nbx, int nby, int nbz) {
+  return guarded(c, [&]() {
+    if (field < 0 || field > 3 || !vals7) throw Error(IBM_ERR_ARG, "ibm_set_operator: bad field or pointer");
+    const Box &b = field_box(c, field);
+    if (nbx != b.nx || nby != b.ny || nbz != b.nz)
+      throw Error(IBM_ERR_ARG, "ibm_set_operator: box does not match the field's solve box");
+    Op7 &o = c->op[field];
+    o.b = b;
+    const long n = b.n;
+    DBuf<double> tmp;
+    tmp.alloc((size_t)7 * n);
+    IBM_CUDA_TRY(cudaMemcpyAsync(tmp.p, vals7, sizeof(double) * 7 * n, cudaMemcpyDefault, c->st));
+    o.c.alloc((size_t)7 * n); o.cj.alloc((size_t)7 * n); o.invd.alloc(n);
+    o.cf.alloc((size_t)7 * n); o.invdf.alloc(n);
+    k_op_planes<<<grid1d(n), kThreads, 0, c->st>>>(tmp.p, n, o.c.p, o.invd.p, o.cf.p, o.invdf.p);
+    k_op_jacobi<<<grid1d(n), kThreads, 0, c->st>>>(o.c.p, o.invd.p, o.cj.p, b);
+    count_launch(2);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    IBM_CUDA_TRY(cudaGetLastError());
+    o.set = true;
+    c->solvers_ready = false;
+    return IBM_OK;
+  });
+}
+
+int ibm_set_masks(ibm_ctx *c, const uint8_t *active_u, const uint8_t *active_v, const uint8_t *active_w,
+                  const uint8_t *fluid_p, const uint8_t *active_qu, const uint8_t *active_qv,
+                  const uint8_t *active_qw, const int32_t *id_u, const int32_t *id_v, const int32_t *id_w,
+                  const int32_t *id_p, const int32_t *id_qu, const int32_t *id_qv, const int32_t *id_qw) {
+  return guarded(c, [&]() {
+    if (!active_u || !active_v || !active_w || !fluid_p || !id_u || !id_v || !id_w || !id_p || !id_qu || !id_qv ||
+        !id_qw)
+      throw Error(IBM_ERR_ARG, "ibm_set_masks: null pointer");
+    (void)active_qu; (void)active_qv; (void)active_qw;  // q membership follows the q ids, as the reference packs
+    const Geometry &g = c->g;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    auto au = to_host(active_u, g.NU), av = to_host(active_v, g.NV), aw = to_host(active_w, g.NW),
+         fp = to_host(fluid_p, g.NP);
+    auto iu = to_host(id_u, g.NU), iv = to_host(id_v, g.NV), iw = to_host(id_w, g.NW);
+    c->h_id_p = to_host(id_p, g.NP);
+    c->h_id_qu = to_host(id_qu, g.NU); c->h_id_qv = to_host(id_qv, g.NV); c->h_id_qw = to_host(id_qw, g.NW);
+    std::vector<uint8_t> fu(g.NU), fv(g.NV), fw(g.NW), fc(g.NP);
+    for (long f = 0; f < g.NU; ++f)
+      fu[f] = (au[f] ? kActive : 0) | (c->h_id_qu[f] > 0 ? kQFace : 0) | ((iu[f] > 0 && au[f]) ? kRhsRow : 0);
+    for (long f = 0; f < g.NV; ++f)
+      fv[f] = (av[f] ? kActive : 0) | (c->h_id_qv[f] > 0 ? kQFace : 0) | ((iv[f] > 0 && av[f]) ? kRhsRow : 0);
+    for (long f = 0; f < g.NW; ++f)
+      fw[f] = (aw[f] ? kActive : 0) | (c->h_id_qw[f] > 0 ? kQFace : 0) | ((iw[f] > 0 && aw[f]) ? kRhsRow : 0);
+    int npa = 0;
+    for (long q = 0; q < g.NP; ++q) {
+      fc[q] = (fp[q] && c->h_id_p[q] > 0) ? kFluid : 0;
+      npa = std::max(npa, (int)c->h_id_p[q]);
+    }
+    c->np_active = npa;
+    // inactive interior faces zeroed by the BC cleanup (gpu_dense_ops.hpp:5-10;
+    // w uses the mask one plane below)
+    std::vector<int> zu, zv, zw;
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 1; i < nx; ++i) {
+          const long f = ((long)k * ny + j) * (nx + 1) + i;
+          if (!au[f]) zu.push_back((int)f);
+        }
+    for (int k = 0; k < nz; ++k)
+      for (int j = 1; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const long f = ((long)k * (ny + 1) + j) * nx + i;
+          if (!av[f]) zv.push_back((int)f);
+        }
+    for (int k = 1; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const long f = ((long)k * ny + j) * nx + i;
+          if (!aw[f - (long)nx * ny]) zw.push_back((int)f);
+        }
+    upload(c->fu, fu, c->st); upload(c->fv, fv, c->st); upload(c->fw, fw, c->st); upload(c->fc, fc, c->st);
+    upload(c->zl_u, zu, c->st); upload(c->zl_v, zv, c->st); upload(c->zl_w, zw, c->st);
+    c->masks_set = true;
+    c->aux_set = false;
+    c->csr_set = false;
+    c->solvers_ready = false;
+    // id of each solve-box row, for the conversion of the id-indexed aux vectors
+    c->h_id_u_rows.clear();
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 1; i < nx; ++i) {
+          const long f = ((long)k * ny + j) * (nx + 1) + i;
+          c->h_id_u_rows.push_back((iu[f] > 0 && au[f]) ? iu[f] : 0);
+        }
+    c->h_id_v_rows.clear();
+    for (int k = 0; k < nz; ++k)
+      for (int j = 1; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const long f = ((long)k * (ny + 1) + j) * nx + i;
+          c->h_id_v_rows.push_back((iv[f] > 0 && av[f]) ? iv[f] : 0);
+        }
+    c->h_id_w_rows.clear();
+    for (int k = 1; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          const long f = ((long)k * ny + j) * nx + i;
+          c->h_id_w_rows.push_back((iw[f] > 0 && aw[f]) ? iw[f] : 0);
+        }
+    c->n_id[0] = *std::max_element(iu.begin(), iu.end());
+    c->n_id[1] = *std::max_element(iv.begin(), iv.end());
+    c->n_id[2] = *std::max_element(iw.begin(), iw.end());
+    return IBM_OK;
+  });
+}
+
+int ibm_set_aux(ibm_ctx *c, const double *scale_u, const double *scale_v, const double *scale_w,
+                const double *rhs_u_bc, const double *rhs_v_bc, const double *rhs_w_bc, const double *div_bc_unit,
+                const double *uin) {
+  return guarded(c, [&]() {
+    if (!c->masks_set) throw Error(IBM_ERR_STATE, "ibm_set_aux: call ibm_set_masks first");
+    if (!scale_u || !scale_v || !scale_w || !rhs_u_bc || !rhs_v_bc || !rhs_w_bc || !div_bc_unit || !uin)
+      throw Error(IBM_ERR_ARG, "ibm_set_aux: null pointer");
+    const double *sc[3] = {scale_u, scale_v, scale_w}, *bc[3] = {rhs_u_bc, rhs_v_bc, rhs_w_bc};
+    const std::vector<int32_t> *rows[3] = {&c->h_id_u_rows, &c->h_id_v_rows, &c->h_id_w_rows};
+    for (int f = 0; f < 3; ++f) {
+      const size_t len = (size_t)c->n_id[f] + 1;
+      auto hs = to_host(sc[f], len), hb = to_host(bc[f], len);
+      std::vector<double> s(rows[f]->size()), b(rows[f]->size());
+      for (size_t r = 0; r < rows[f]->size(); ++r) {
+        const int id = (*rows[f])[r];
+        s[r] = id > 0 ? hs[(size_t)id] : 0.0;
+        b[r] = id > 0 ? hb[(size_t)id] : 0.0;
+      }
+      upload(c->scale_box[f], s, c->st);
+      upload(c->bc_box[f], b, c->st);
+    }
+    auto hd = to_host(div_bc_unit, (size_t)c->np_active + 1);
+    std::vector<double> dcell(c->g.NP, 0.0);
+    for (long q = 0; q < c->g.NP; ++q) {
+      const int id = c->h_id_p[q];
+      if (id > 0) dcell[q] = hd[(size_t)id];
+    }
+    upload(c->div_bc_cell, dcell, c->st);
+    upload(c->uin, to_host(uin, (size_t)c->g.ny * c->g.nz), c->st);
+    c->aux_set = true;
+    return IBM_OK;
+  });
+}
+
+int ibm_set_projection_csr(ibm_ctx *c, const int32_t *D_rowptr, const int32_t *D_col, const double *D_val,
+                           int D_nrows, const int32_t *G_rowptr, const int32_t *G_col, const double *G_val,
+                           int G_nrows) {
+  return guarded(c, [&]() {
+    if (!c->masks_set) throw Error(IBM_ERR_STATE, "ibm_set_projection_csr: call ibm_set_masks first");
+    if (!D_rowptr || !D_col || !D_val || !G_rowptr || !G_col || !G_val)
+      throw Error(IBM_ERR_ARG, "ibm_set_projection_csr: null pointer");
+    const Geometry &g = c->g;
+    const int nx = g.nx, ny = g.ny;
+    const int nqu = *std::max_element(c->h_id_qu.begin(), c->h_id_qu.end());
+    const int nqv = *std::max_element(c->h_id_qv.begin(), c->h_id_qv.end());
+    const int nqw = *std::max_element(c->h_id_qw.begin(), c->h_id_qw.end());
+    const int nq = nqu + nqv + nqw, np = c->np_active;
+    if (D_nrows != np || G_nrows != nq) throw Error(IBM_ERR_ARG, "ibm_set_projection_csr: row counts do not match the ids");
+    // inverse id maps
+    std::vector<long> cell_of((size_t)np + 1, -1), face_of((size_t)nq + 1, -1);
+    for (long q = 0; q < g.NP; ++q) if (c->h_id_p[q] > 0) cell_of[(size_t)c->h_id_p[q]] = q;
+    for (long f = 0; f < g.NU; ++f) if (c->h_id_qu[f] > 0) face_of[(size_t)c->h_id_qu[f]] = f;
+    for (long f = 0; f < g.NV; ++f) if (c->h_id_qv[f] > 0) face_of[(size_t)(nqu + c->h_id_qv[f])] = f;
+    for (long f = 0; f < g.NW; ++f) if (c->h_id_qw[f] > 0) face_of[(size_t)(nqu + nqv + c->h_id_qw[f])] = f;
+    auto drp = to_host(D_rowptr, (size_t)np + 1);
+    auto dcol = to_host(D_col, (size_t)drp[(size_t)np]);
+    auto dval = to_host(D_val, (size_t)drp[(size_t)np]);
+    std::vector<double> Dc((size_t)6 * g.NP, 0.0);
+    for (int r = 0; r < np; ++r) {
+      const long cell = cell_of[(size_t)r + 1];
+      if (cell < 0) throw Error(IBM_ERR_ARG, "ibm_set_projection_csr: D row without a cell");
+      const int i = (int)(cell % nx), j = (int)((cell / nx) % ny), k = (int)(cell / ((long)nx * ny));
+      for (int t = drp[(size_t)r]; t < drp[(size_t)r + 1]; ++t) {
+        const int col = dcol[(size_t)t];
+        if (col < 1 || col > nq) throw Error(IBM_ERR_ARG, "ibm_set_projection_csr: D column out of range");
+        const long f = face_of[(size_t)col];
+        int slot = -1;
+        if (col <= nqu) {
+          if (f == ((long)k * ny + j) * (nx + 1) + i) slot = 0;
+          else if (f == ((long)k * ny + j) * (nx + 1) + i + 1) slot = 1;
+        } else if (col <= nqu + nqv) {
+          if (f == ((long)k * (ny + 1) + j) * nx + i) slot = 2;
+          else if (f == ((long)k * (ny + 1) + j + 1) * nx + i) slot = 3;
+        } else {
+          if (f == ((long)k * ny + j) * nx + i) slot = 4;
+          else if (f == ((long)(k + 1) * ny + j) * nx + i) slot = 5;
+        }
+        if (slot < 0) throw Error(IBM_ERR_UNSUPPORTED, "ibm_set_projection_csr: D entry is not a face of its cell");
+        Dc[(size_t)slot * g.NP + cell] = dval[(size_t)t];
+      }
+    }
+    auto grp = to_host(G_rowptr, (size_t)nq + 1);
+    auto gcol = to_host(G_col, (size_t)grp[(size_t)nq]);
+    auto gval = to_host(G_val, (size_t)grp[(size_t)nq]);
+    std::vector<double> Gu((size_t)2 * g.NU, 0.0), Gv((size_t)2 * g.NV, 0.0), Gw((size_t)2 * g.NW, 0.0);
+    for (int r = 0; r < nq; ++r) {
+      const long f = face_of[(size_t)r + 1];
+      const int q = r + 1;
+      for (int t = grp[(size_t)r]; t < grp[(size_t)r + 1]; ++t) {
+        const int col = gcol[(size_t)t];
+        if (col < 1 || col > np) throw Error(IBM_ERR_ARG, "ibm_set_projection_csr: G column out of range");
+        const long cell = cell_of[(size_t)col];
+        int side = -1;
+        if (q <= nqu) {
+          const int i = (int)(f % (nx + 1));
+          const long jk = f / (nx + 1);
+          if (i > 0 && cell == jk * nx + (i - 1)) side = 0;
+          else if (i < nx && cell == jk * nx + i) side = 1;
+          if (side >= 0) Gu[(size_t)side * g.NU + f] = gval[(size_t)t];
+        } else if (q <= nqu + nqv) {
+          const int i = (int)(f % nx);
+          const long jj = f / nx;
+          const int j = (int)(jj % (ny + 1)), k = (int)(jj / (ny + 1));
+          if (j > 0 && cell == ((long)k * ny + (j - 1)) * nx + i) side = 0;
+          else if (j < ny && cell == ((long)k * ny + j) * nx + i) side = 1;
+          if (side >= 0) Gv[(size_t)side * g.NV + f] = gval[(size_t)t];
+        } else {
+          const long plane = (long)nx * ny;
+          const int k = (int)(f / plane);
+          const long rem = f - (long)k * plane;
+          if (k > 0 && cell == (long)(k - 1) * plane + rem) side = 0;
+          else if (k < g.nz && cell == (long)k * plane + rem) side = 1;
+          if (side >= 0) Gw[(size_t)side * g.NW + f] = gval[(size_t)t];
+        }
+        if (side < 0) throw Error(IBM_ERR_UNSUPPORTED, "ibm_set_projection_csr: G entry is not a cell of its face");
+      }
+    }
+    upload(c->Dc, Dc, c->st);
+    upload(c->Gu, Gu, c->st); upload(c->Gv, Gv, c->st); upload(c->Gw, Gw, c->st);
+    c->csr_set = true;
+    return IBM_OK;
+  });
+}
+
+int ibm_set_solver_params(ibm_ctx *c, const ibm_solver_params *p) {
+  return guarded(c, [&]() {
+    if (!p) throw Error(IBM_ERR_ARG, "ibm_set_solver_params: null");
+    if (p->vel_kdim < 1 || p->vel_kdim > kMaxKdim || p->p_kdim < 1 || p->p_kdim > kMaxKdim)
+      throw Error(IBM_ERR_ARG, "kdim must be in [1, 63]");
+    if (p->vel_maxit < 0 || p->p_maxit < 0 || !(p->vel_tol >= 0) || !(p->p_tol >= 0))
+      throw Error(IBM_ERR_ARG, "bad tolerance or iteration limit");
+    if (p->precision != 0 && p->precision != 1) throw Error(IBM_ERR_ARG, "precision must be 0 or 1");
+    if (p->p_pc != 0 && p->p_pc != 1) throw Error(IBM_ERR_ARG, "p_pc must be 0 or 1");
+    if (p->mg_nu1 < 0 || p->mg_nu2 < 0 || p->mg_coarse_max < 1 || p->mg_max_levels < 1)
+      throw Error(IBM_ERR_ARG, "bad multigrid parameters");
+    c->prm = *p;
+    c->solvers_ready = false;
+    return IBM_OK;
+  });
+}
+
+int ibm_get_solver_params(ibm_ctx *c, ibm_solver_params *p) {
+  if (!c || !p) return IBM_ERR_ARG;
+  *p = c->prm;
+  return IBM_OK;
+}
+
+int ibm_set_fields(ibm_ctx *c, const double *u, const double *v, const double *w, const double *p) {
+  return guarded(c, [&]() {
+    if (u) IBM_CUDA_TRY(cudaMemcpyAsync(c->u.p, u, sizeof(double) * c->g.NU, cudaMemcpyDefault, c->st));
+    if (v) IBM_CUDA_TRY(cudaMemcpyAsync(c->v.p, v, sizeof(double) * c->g.NV, cudaMemcpyDefault, c->st));
+    if (w) IBM_CUDA_TRY(cudaMemcpyAsync(c->w.p, w, sizeof(double) * c->g.NW, cudaMemcpyDefault, c->st));
+    if (p) IBM_CUDA_TRY(cudaMemcpyAsync(c->p.p, p, sizeof(double) * c->g.NP, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_get_fields(ibm_ctx *c, double *u, double *v, double *w, double *p) {
+  return guarded(c, [&]() {
+    if (u) IBM_CUDA_TRY(cudaMemcpyAsync(u, c->u.p, sizeof(double) * c->g.NU, cudaMemcpyDefault, c->st));
+    if (v) IBM_CUDA_TRY(cudaMemcpyAsync(v, c->v.p, sizeof(double) * c->g.NV, cudaMemcpyDefault, c->st));
+    if (w) IBM_CUDA_TRY(cudaMemcpyAsync(w, c->w.p, sizeof(double) * c->g.NW, cudaMemcpyDefault, c->st));
+    if (p) IBM_CUDA_TRY(cudaMemcpyAsync(p, c->p.p, sizeof(double) * c->g.NP, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_step(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
+  return guarded(c, [&]() {
+    require_inputs(c);
+    ensure_solvers(c);
+    cudaStream_t st = c->st;
+    IBM_CUDA_TRY(cudaMemsetAsync(c->diag.p, 0, sizeof(StepDiag), st));
+    IBM_CUDA_TRY(cudaEventRecord(c->ev[0], st));
+    launch_bc(c, c->u.p, c->v.p, c->w.p, ramp);
+    launch_momentum_rhs(c);
+    IBM_CUDA_TRY(cudaEventRecord(c->ev[1], st));
+    const double *bm[3] = {c->bb[0].p, c->bb[1].p, c->bb[2].p};
+    double *xm[3] = {c->xb[0].p, c->xb[1].p, c->xb[2].p};
+    KResult rm[3], rp[1];
+    Precond none;
+    c->kmom.solve(st, bm, xm, none, rm);
+    IBM_CUDA_TRY(cudaEventRecord(c->ev[2], st));
+    launch_tilde(c, ramp);
+    launch_pressure_rhs(c, ramp);
+    const double *bp[1] = {c->bb[3].p};
+    double *xp[1] = {c->xb[3].p};
+    Precond mgp;
+    mgp.ctx = c;
+    mgp.apply = mg_apply_cb;
+    c->kp.solve(st, bp, xp, mgp, rp);
+    IBM_CUDA_TRY(cudaEventRecord(c->ev[3], st));
+    launch_projection(c, ramp);
+    IBM_CUDA_TRY(cudaEventRecord(c->ev[4], st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(c->hdiag, c->diag.p, sizeof(StepDiag), cudaMemcpyDeviceToHost, st));
+    IBM_CUDA_TRY(cudaStreamSynchronize(st));
+    IBM_CUDA_TRY(cudaGetLastError());
+    int rc = IBM_OK;
+    const StepDiag &dg = *c->hdiag;
+    if (stats) {
+      memset(stats, 0, sizeof(*stats));
+      stats->ramp = ramp;
+      fill_solve(stats->u, rm[0]); fill_solve(stats->v, rm[1]); fill_solve(stats->w, rm[2]);
+      fill_solve(stats->p, rp[0]);
+      stats->div_l2 = std::sqrt(dg.div2 / std::max(1, c->np_active));
+      stats->umax = dg.umax; stats->vmax = dg.vmax; stats->wmax = dg.wmax;
+      float ms;
+      cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); stats->t_rhs_ms = ms;
+      cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); stats->t_mom_ms = ms;
+      cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); stats->t_p_ms = ms;
+      cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); stats->t_proj_ms = ms;
+      cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); stats->t_total_ms = ms;
+    }
+    for (int f = 0; f < 3; ++f) rc = worst(rc, rm[f].status == 1 ? IBM_OK : IBM_NOT_CONVERGED);
+    rc = worst(rc, rp[0].status == 1 ? IBM_OK : IBM_NOT_CONVERGED);
+    const bool bad_mom = dg.nonfinite_mom || rm[0].nonfinite || rm[1].nonfinite || rm[2].nonfinite;
+    const bool bad_p = dg.nonfinite_p || rp[0].nonfinite;
+    if (bad_mom || bad_p) {
+      rc = IBM_ERR_NONFINITE;
+      c->err = bad_mom ? "non-finite momentum solve (main.cu:302-305)" : "non-finite pressure solve (main.cu:333-336)";
+    }
+    if (stats) stats->status = rc;
+    return rc;
+  });
+}
+
+int ibm_solve(ibm_ctx *c, int field, const double *b, double *x, ibm_solve_stats *stats) {
+  return guarded(c, [&]() {
+    if (field < 0 || field > 3 || !b || !x) throw Error(IBM_ERR_ARG, "ibm_solve: bad arguments");
+    require_inputs(c);
+    ensure_solvers(c);
+    const long n = field_box(c, field).n;
+    IBM_CUDA_TRY(cudaMemcpyAsync(c->bb[field].p, b, sizeof(double) * n, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(c->xb[field].p, x, sizeof(double) * n, cudaMemcpyDefault, c->st));
+    KResult r[3];
+    if (field < 3) {
+      const double *bm[3] = {c->bb[0].p, c->bb[1].p, c->bb[2].p};
+      double *xm[3] = {c->xb[0].p, c->xb[1].p, c->xb[2].p};
+      Precond none;
+      c->kmom.solve(c->st, bm, xm, none, r, 1u << field);
+      r[0] = r[field];
+    } else {
+      const double *bp[1] = {c->bb[3].p};
+      double *xp[1] = {c->xb[3].p};
+      Precond mgp;
+      mgp.ctx = c;
+      mgp.apply = mg_apply_cb;
+      c->kp.solve(c->st, bp, xp, mgp, r);
+    }
+    IBM_CUDA_TRY(cudaMemcpyAsync(x, c->xb[field].p, sizeof(double) * n, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    if (stats) fill_solve(*stats, r[0]);
+    if (r[0].nonfinite) { c->err = "non-finite solve output"; return (int)IBM_ERR_NONFINITE; }
+    return r[0].status == 1 ? (int)IBM_OK : (int)IBM_NOT_CONVERGED;
+  });
+}
+
+int ibm_apply_operator(ibm_ctx *c, int field, const double *x, double *y) {
+  return guarded(c, [&]() {
+    if (field < 0 || field > 3 || !x || !y) throw Error(IBM_ERR_ARG, "ibm_apply_operator: bad arguments");
+    if (!c->op[field].set) throw Error(IBM_ERR_STATE, "operator not set");
+    const Box &b = field_box(c, field);
+    DBuf<double> dx, dy;
+    dx.alloc(b.n); dy.alloc(b.n);
+    IBM_CUDA_TRY(cudaMemcpyAsync(dx.p, x, sizeof(double) * b.n, cudaMemcpyDefault, c->st));
+    k_spmv7<<<grid1d(b.n), kThreads, 0, c->st>>>(c->op[field].c.p, b, dx.p, dy.p);
+    count_launch();
+    IBM_CUDA_TRY(cudaMemcpyAsync(y, dy.p, sizeof(double) * b.n, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_get_solver_vector(ibm_ctx *c, int field, int which, double *out) {
+  return guarded(c, [&]() {
+    if (field < 0 || field > 3 || (which != 0 && which != 1) || !out)
+      throw Error(IBM_ERR_ARG, "ibm_get_solver_vector: bad arguments");
+    const long n = field_box(c, field).n;
+    const double *src = which == 0 ? c->bb[field].p : c->xb[field].p;
+    IBM_CUDA_TRY(cudaMemcpyAsync(out, src, sizeof(double) * n, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_synchronize(ibm_ctx *c) {
+  return guarded(c, [&]() {
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+void *ibm_stream(ibm_ctx *c) { return c ? (void *)c->st : nullptr; }
+
+long long ibm_kernel_launches(ibm_ctx *c) { return c ? c->launches : 0; }
+
+int ibm_device_query(int device, char *buf, int len) {
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return IBM_ERR_CUDA;
+  if (buf && len > 0) snprintf(buf, (size_t)len, "%s sm_%d%d SMs=%d", p.name, p.major, p.minor, p.multiProcessorCount);
+  return IBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,209 @@
+// Internal declarations shared by the CUDA translation units of libibmgpu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "ibm_gpu.h"
+
+namespace ibm {
+
+constexpr int kMaxKdim = 63;          // Krylov basis holds at most 64 vectors
+constexpr int kThreads = 256;         // threads per block of the streaming kernels
+constexpr int kWarps = kThreads / 32;
+constexpr int kRowsPerThread = 4;     // rows per thread per tile in the reduction kernels
+constexpr int kTile = kThreads * kRowsPerThread;
+constexpr int kMaxSys = 4;            // systems solved together (u, v, w momentum batch)
+
+// Error plumbing ------------------------------------------------------------
+struct Status {
+  int code = IBM_OK;
+  std::string msg;
+};
+
+#define IBM_CUDA_TRY(expr)                                                                     \
+  do {                                                                                         \
+    cudaError_t e__ = (expr);                                                                  \
+    if (e__ != cudaSuccess) {                                                                  \
+      char b__[512];                                                                           \
+      snprintf(b__, sizeof(b__), "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e__),      \
+               __FILE__, __LINE__);                                                            \
+      throw ::ibm::Error(IBM_ERR_CUDA, b__);                                                   \
+    }                                                                                          \
+  } while (0)
+
+struct Error {
+  int code;
+  std::string msg;
+  Error(int c, std::string m) : code(c), msg(std::move(m)) {}
+};
+
+// Device buffer -------------------------------------------------------------
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    release();
+    if (count == 0) return;
+    cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      char b[256];
+      snprintf(b, sizeof(b), "cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+      throw Error(IBM_ERR_NOMEM, b);
+    }
+    n = count;
+  }
+  void zero(cudaStream_t s) {
+    if (p) IBM_CUDA_TRY(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+struct Box {
+  int nx = 0, ny = 0, nz = 0, n = 0;
+};
+inline Box make_box(int nx, int ny, int nz) { return Box{nx, ny, nz, nx * ny * nz}; }
+
+// 7-point operator on a solve box: coefficient planes [7][n] (C,-x,+x,-y,+y,-z,+z).
+struct Op7 {
+  Box b;
+  bool set = false;
+  DBuf<double> c;      // as supplied
+  DBuf<double> invd;   // 1 / C
+  DBuf<double> cj;     // C * invd(neighbour): the right-Jacobi-preconditioned operator
+  DBuf<float> cf;      // FP32 coefficients (mixed precision)
+  DBuf<float> invdf;
+};
+
+// Per-system GMRES scalars kept on the device (no host round trip per iteration).
+struct KScal {
+  int kdim, maxit;
+  double tol;
+  int active;         // 1 while an Arnoldi cycle is running
+  int cycle_end;      // 1 when the cycle stopped and the solution update is due
+  int i;              // Arnoldi vectors built in this cycle
+  int iters;
+  int status;         // 0 running, 1 converged, 2 iteration limit, 3 stagnation
+  int claimed;        // the Givens estimate reached the tolerance
+  unsigned ticket;    // last-block-done counter of the reduction kernels
+  int nonfinite;
+  double b_norm, r_norm, eps, real_old;
+  double nu[kMaxKdim + 1];            // norms of the stored (unnormalised) basis vectors
+  double H[(kMaxKdim + 1) * kMaxKdim];  // H(i,j) at [i*kMaxKdim + j]
+  double cs[kMaxKdim], sn[kMaxKdim], g[kMaxKdim + 1], y[kMaxKdim];
+  double coef[kMaxKdim + 1];          // coefficients of the next basis update
+  double h1[kMaxKdim + 1];
+};
+
+// Device view of one linear system for the Krylov kernels.
+struct KSys {
+  int nx, ny, nz, n;
+  const double *A;      // operator applied in the Arnoldi step ([7][n])
+  const double *Ar;     // operator of the true residual ([7][n])
+  const double *invd;   // inverse diagonal (Jacobi solution update)
+  const float *Af;      // FP32 operator (inner FP32 sweeps)
+  const float *invdf;
+  double *V;            // basis, vector k at V + k*ldv
+  long ldv;
+  float *Z;             // flexible basis (FP32), vector k at Z + k*ldv
+  double *w, *x, *r, *z, *z2;
+  const double *b;
+  float *zf, *zf2;      // FP32 work for the inner sweeps
+  double *part;         // block partial sums [nblk][kMaxKdim + 2]
+  int nblk;
+  int pc;               // 0 Jacobi folded into A, 1 explicit z (multigrid), 2 flexible FP32 z
+  int pc_cb;            // pc 2: preconditioner supplied by a callback (else FP32 Jacobi sweeps)
+  KScal *s;
+};
+
+// Host-side mirror of what the loop needs from each system after a step.
+struct KFlags {
+  int active, cycle_end, status, iters, i, nonfinite;
+  double rel;
+};
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Flat row -> (i, j, k) on a box.
+__device__ __forceinline__ void row_ijk(int r, int nx, int ny, int &i, int &j, int &k) {
+  const unsigned plane = (unsigned)nx * (unsigned)ny;
+  k = (int)((unsigned)r / plane);
+  const unsigned rem = (unsigned)r - (unsigned)k * plane;
+  j = (int)(rem / (unsigned)nx);
+  i = (int)(rem - (unsigned)j * (unsigned)nx);
+}
+
+// y_r = sum_s c_s x_{r+off_s}, fused multiply-add chain in slot order
+// C,-x,+x,-y,+y,-z,+z; neighbours outside the box contribute 0.
+template <class T, class X>
+__device__ __forceinline__ double stencil7_row(const T *__restrict__ c, long n, const X *__restrict__ x, int r,
+                                               int i, int j, int k, int nx, int ny, int nz) {
+  const long sy = nx, sz = (long)nx * ny;
+  double acc = 0.0;
+  acc = fma((double)c[r], (double)x[r], acc);
+  acc = fma((double)c[n + r], i > 0 ? (double)x[r - 1] : 0.0, acc);
+  acc = fma((double)c[2 * n + r], i < nx - 1 ? (double)x[r + 1] : 0.0, acc);
+  acc = fma((double)c[3 * n + r], j > 0 ? (double)x[r - sy] : 0.0, acc);
+  acc = fma((double)c[4 * n + r], j < ny - 1 ? (double)x[r + sy] : 0.0, acc);
+  acc = fma((double)c[5 * n + r], k > 0 ? (double)x[r - sz] : 0.0, acc);
+  acc = fma((double)c[6 * n + r], k < nz - 1 ? (double)x[r + sz] : 0.0, acc);
+  return acc;
+}
+
+// FP32 variant.
+__device__ __forceinline__ float stencil7_row_f(const float *__restrict__ c, long n, const float *__restrict__ x,
+                                                int r, int i, int j, int k, int nx, int ny, int nz) {
+  const long sy = nx, sz = (long)nx * ny;
+  float acc = 0.0f;
+  acc = fmaf(c[r], x[r], acc);
+  acc = fmaf(c[n + r], i > 0 ? x[r - 1] : 0.0f, acc);
+  acc = fmaf(c[2 * n + r], i < nx - 1 ? x[r + 1] : 0.0f, acc);
+  acc = fmaf(c[3 * n + r], j > 0 ? x[r - sy] : 0.0f, acc);
+  acc = fmaf(c[4 * n + r], j < ny - 1 ? x[r + sy] : 0.0f, acc);
+  acc = fmaf(c[5 * n + r], k > 0 ? x[r - sz] : 0.0f, acc);
+  acc = fmaf(c[6 * n + r], k < nz - 1 ? x[r + sz] : 0.0f, acc);
+  return acc;
+}
+
+// Grid size for persistent grid-stride kernels: a multiple of the SM count.
+int persistent_blocks(int rows, int blocks_per_sm = 4);
+int sm_count();
+
+// Launch counter (all kernels of the library go through this).
+void count_launch(long long n = 1);
+long long launches();
+
+}  // namespace ibm

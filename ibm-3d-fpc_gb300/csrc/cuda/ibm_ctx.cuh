@@ -1,0 +1,66 @@
+// The solver context behind the C ABI (one GPU, one stream).
+#pragma once
+#include "ibm_common.cuh"
+#include "ibm_krylov.cuh"
+#include "ibm_mg.cuh"
+
+namespace ibm {
+
+// Face flag bits (u, v, w faces; full MAC layouts).
+constexpr uint8_t kActive = 1;   // active_{u,v,w} at the face itself
+constexpr uint8_t kQFace = 2;    // id_q > 0: part of the projection vector q
+constexpr uint8_t kRhsRow = 4;   // id > 0 && active: a solved (non-identity) momentum row
+// Cell flag bit.
+constexpr uint8_t kFluid = 1;    // fluid_p && id_p > 0
+
+struct StepDiag {                // written by the diagnostics kernel
+  double div2, umax, vmax, wmax;
+  int nonfinite_mom, nonfinite_p;
+  unsigned ticket;
+  int pad;
+};
+
+struct Geometry {
+  int nx, ny, nz;
+  long NU, NV, NW, NP;           // full MAC sizes
+  Box bu, bv, bw, bp;            // solve boxes
+  double dx, dy, dz, rho, nu, dt;
+};
+
+}  // namespace ibm
+
+struct ibm_ctx {
+  ibm_grid_desc grid;
+  ibm::Geometry g;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  ibm_solver_params prm;
+  std::string err;
+  long long launches = 0;
+
+  ibm::Op7 op[4];
+  bool masks_set = false, aux_set = false, csr_set = false;
+  int np_active = 0;             // number of fluid cells with an id (the reference's Np)
+  ibm::DBuf<uint8_t> fu, fv, fw, fc;
+  ibm::DBuf<double> scale_box[3], bc_box[3];
+  ibm::DBuf<double> div_bc_cell, uin;
+  ibm::DBuf<double> Dc;          // [6][NP]: u_w, u_e, v_s, v_n, w_b, w_t
+  ibm::DBuf<double> Gu, Gv, Gw;  // [2][faces]: coefficient of the lower / upper cell
+  ibm::DBuf<int> zl_u, zl_v, zl_w;
+  // host copies needed to convert the CSR (kept after ibm_set_masks)
+  std::vector<int32_t> h_id_p, h_id_qu, h_id_qv, h_id_qw;
+  std::vector<int32_t> h_id_u_rows, h_id_v_rows, h_id_w_rows;  // id of each solve-box row (0: identity row)
+  int n_id[3] = {0, 0, 0};       // largest momentum ids
+
+  ibm::DBuf<double> u, v, w, p, ut, vt, wt;
+  ibm::DBuf<double> xb[4], bb[4];
+  ibm::DBuf<double> part;        // diagnostics block partials
+  ibm::DBuf<ibm::StepDiag> diag;
+  ibm::StepDiag *hdiag = nullptr;
+
+  bool solvers_ready = false;
+  int solvers_precision = -1;
+  ibm::Krylov kmom, kp;
+  ibm::Multigrid mg;
+  cudaEvent_t ev[6] = {};
+};

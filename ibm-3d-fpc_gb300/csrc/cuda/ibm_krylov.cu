@@ -1,0 +1,568 @@
+// Restarted, right-preconditioned GMRES for up to kMaxSys independent 7-point
+// systems at once, with every scalar kept on the device.
+//
+// Restates the algorithm of HYPRE_StructGMRESSolve (third-party, called by
+// the reference at main.cu:284-286 and 327): Arnoldi with Givens rotations,
+// stop when the estimated ||r||/||b|| <= tol, confirm with the true residual
+// and restart from it; a cycle whose estimate claimed convergence but whose
+// true residual did not decrease stops (stagnation), as HYPRE does.
+// Orthogonalisation is classical Gram-Schmidt applied twice, so each pass is
+// one sweep over the basis with all dot products batched.
+//
+// Per Arnoldi step, three streaming kernels:
+//   k_arnoldi_spmv : w = A z_j and d1_k = (v_k, w)         (last block: h1, coefficients)
+//   k_arnoldi_orth : w -= V c1, d2_k = (v_k, w), |w|^2       (last block: h2, Givens, stop test)
+//   k_arnoldi_next : v_{j+1} = w - V c2                      (stored unnormalised; norms in nu[])
+// Reductions are deterministic: fixed per-warp order inside a block, block
+// partials summed in block order by the last block to finish.
+#include "ibm_common.cuh"
+#include "ibm_krylov.cuh"
+
+namespace ibm {
+
+namespace {
+
+constexpr int kLd = kMaxKdim + 2;  // stride of block partials
+
+// Sum block partials of `nd` dot products in block order; one warp per dot.
+__device__ void reduce_partials(const double *part, int nblk, int nd, double *out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int k = warp; k < nd; k += kWarps) {
+    double s = 0.0;
+    for (int b = lane; b < nblk; b += 32) s += part[(long)b * kLd + k];
+    s = warp_sum(s);
+    if (lane == 0) out[k] = s;
+  }
+}
+
+// Common tail of the reduction kernels: write this block's sums, and return
+// true in the block that finishes last (after all partials are visible).
+__device__ bool block_partials_and_last(double *sacc, int nd, double *part, unsigned *ticket) {
+  __syncthreads();
+  for (int k = threadIdx.x; k < nd; k += blockDim.x) {
+    double s = 0.0;
+    for (int w = 0; w < kWarps; ++w) s += sacc[k * kWarps + w];
+    part[(long)blockIdx.x * kLd + k] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  __shared__ int last;
+  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (last) __threadfence();
+  return last != 0;
+}
+
+// r = b - Ar x; V_0 = r; |b|^2, |r|^2. Last block: norms, tolerance, state.
+__global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  __shared__ double sacc[2 * kWarps];
+  if (threadIdx.x < 2 * kWarps) sacc[threadIdx.x] = 0.0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+    double pb = 0.0, pr = 0.0;
+#pragma unroll
+    for (int t = 0; t < kRowsPerThread; ++t) {
+      const long r = t0 + t * kThreads + threadIdx.x;
+      if (r < S.n) {
+        int i, j, k;
+        row_ijk((int)r, S.nx, S.ny, i, j, k);
+        const double ax = stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+        const double bv = S.b[r];
+        const double rv = bv - ax;
+        S.r[r] = rv;
+        S.V[r] = rv;
+        pb = fma(bv, bv, pb);
+        pr = fma(rv, rv, pr);
+      }
+    }
+    pb = warp_sum(pb);
+    pr = warp_sum(pr);
+    if (lane == 0) { sacc[warp] += pb; sacc[kWarps + warp] += pr; }
+  }
+  if (!block_partials_and_last(sacc, 2, S.part, &sc->ticket)) return;
+  __shared__ double tot[2];
+  reduce_partials(S.part, gridDim.x, 2, tot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sc->ticket = 0;
+    const double bn = sqrt(tot[0]), rn = sqrt(tot[1]);
+    sc->b_norm = bn;
+    sc->r_norm = rn;
+    sc->eps = sc->tol * (bn > 0.0 ? bn : rn);
+    sc->real_old = bn;
+    sc->iters = 0;
+    sc->i = 0;
+    sc->claimed = 0;
+    sc->cycle_end = 0;
+    sc->nonfinite = !isfinite(rn);
+    if (!isfinite(rn)) { sc->status = 2; sc->active = 0; }
+    else if (rn == 0.0 || rn <= sc->eps) { sc->status = 1; sc->active = 0; }
+    else if (sc->maxit <= 0) { sc->status = 2; sc->active = 0; }
+    else { sc->status = 0; sc->active = 1; }
+    sc->nu[0] = rn;
+    sc->g[0] = rn;
+  }
+}
+
+// w = A z_j (z_j = M v_j by the system's preconditioner mode), d1_k = (V_k, w).
+__global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active) return;
+  const int j = sc->i, nd = j + 1;
+  __shared__ double sacc[(kMaxKdim + 1) * kWarps];
+  for (int t = threadIdx.x; t < nd * kWarps; t += blockDim.x) sacc[t] = 0.0;
+  __shared__ double inv_nu;
+  if (threadIdx.x == 0) inv_nu = 1.0 / sc->nu[j];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double *vj = S.V + (long)j * S.ldv;
+  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+    double wv[kRowsPerThread];
+#pragma unroll
+    for (int t = 0; t < kRowsPerThread; ++t) {
+      const long r = t0 + t * kThreads + threadIdx.x;
+      wv[t] = 0.0;
+      if (r < S.n) {
+        int i, jj, k;
+        row_ijk((int)r, S.nx, S.ny, i, jj, k);
+        double w;
+        if (S.pc == 0) w = stencil7_row(S.A, S.n, vj, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
+        else if (S.pc == 1) w = stencil7_row(S.A, S.n, S.z, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
+        else w = stencil7_row(S.A, S.n, S.Z + (long)j * S.ldv, (int)r, i, jj, k, S.nx, S.ny, S.nz);
+        S.w[r] = w;
+        wv[t] = w;
+      }
+    }
+    for (int kk = 0; kk < nd; ++kk) {
+      const double *vk = S.V + (long)kk * S.ldv;
+      double p = 0.0;
+#pragma unroll
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) p = fma(vk[r], wv[t], p);
+      }
+      p = warp_sum(p);
+      if (lane == 0) sacc[kk * kWarps + warp] += p;
+    }
+  }
+  if (!block_partials_and_last(sacc, nd, S.part, &sc->ticket)) return;
+  __shared__ double tot[kMaxKdim + 1];
+  reduce_partials(S.part, gridDim.x, nd, tot);
+  __syncthreads();
+  for (int kk = threadIdx.x; kk < nd; kk += blockDim.x) {
+    const double h = tot[kk] / sc->nu[kk];
+    sc->h1[kk] = h;
+    sc->coef[kk] = h / sc->nu[kk];
+  }
+  if (threadIdx.x == 0) sc->ticket = 0;
+}
+
+// w -= sum_k coef_k V_k; d2_k = (V_k, w); |w|^2. Last block: second
+// Gram-Schmidt pass coefficients, Hessenberg column, Givens, stop test.
+__global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active) return;
+  const int j = sc->i, nd = j + 1;
+  __shared__ double sacc[(kMaxKdim + 2) * kWarps];
+  __shared__ double cf[kMaxKdim + 1];
+  for (int t = threadIdx.x; t < (nd + 1) * kWarps; t += blockDim.x) sacc[t] = 0.0;
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = sc->coef[t];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+    double wv[kRowsPerThread];
+#pragma unroll
+    for (int t = 0; t < kRowsPerThread; ++t) {
+      const long r = t0 + t * kThreads + threadIdx.x;
+      wv[t] = 0.0;
+      if (r < S.n) {
+        double w = S.w[r];
+        for (int kk = 0; kk < nd; ++kk) w = fma(-cf[kk], S.V[(long)kk * S.ldv + r], w);
+        S.w[r] = w;
+        wv[t] = w;
+      }
+    }
+    for (int kk = 0; kk <= nd; ++kk) {
+      double p = 0.0;
+#pragma unroll
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) p = fma(kk < nd ? S.V[(long)kk * S.ldv + r] : wv[t], wv[t], p);
+      }
+      p = warp_sum(p);
+      if (lane == 0) sacc[kk * kWarps + warp] += p;
+    }
+  }
+  if (!block_partials_and_last(sacc, nd + 1, S.part, &sc->ticket)) return;
+  __shared__ double tot[kMaxKdim + 2];
+  reduce_partials(S.part, gridDim.x, nd + 1, tot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sc->ticket = 0;
+    const int K = kMaxKdim;
+    double h2sq = 0.0;
+    for (int kk = 0; kk < nd; ++kk) {
+      const double h2 = tot[kk] / sc->nu[kk];
+      sc->coef[kk] = h2 / sc->nu[kk];
+      sc->H[kk * K + j] = sc->h1[kk] + h2;
+      h2sq = fma(h2, h2, h2sq);
+    }
+    double nn = tot[nd] - h2sq;
+    const double hn = nn > 0.0 ? sqrt(nn) : 0.0;
+    sc->nu[j + 1] = hn;
+    sc->H[(j + 1) * K + j] = hn;
+    // apply previous rotations to the new column, then a new rotation
+    for (int q = 0; q < j; ++q) {
+      const double t = sc->H[q * K + j];
+      sc->H[q * K + j] = sc->sn[q] * sc->H[(q + 1) * K + j] + sc->cs[q] * t;
+      sc->H[(q + 1) * K + j] = -sc->sn[q] * t + sc->cs[q] * sc->H[(q + 1) * K + j];
+    }
+    const double a = sc->H[j * K + j], b = sc->H[(j + 1) * K + j];
+    double gam = sqrt(b * b + a * a);
+    if (gam == 0.0) gam = 2.220446049250313e-16;
+    sc->cs[j] = a / gam;
+    sc->sn[j] = b / gam;
+    sc->g[j + 1] = -sc->sn[j] * sc->g[j];
+    sc->g[j] = sc->cs[j] * sc->g[j];
+    sc->H[j * K + j] = sc->sn[j] * b + sc->cs[j] * a;
+    sc->i = j + 1;
+    sc->iters += 1;
+    sc->r_norm = fabs(sc->g[j + 1]);
+    const bool claimed = sc->r_norm <= sc->eps || hn == 0.0;
+    if (!isfinite(sc->r_norm)) sc->nonfinite = 1;
+    if (claimed || sc->i >= sc->kdim || sc->iters >= sc->maxit || !isfinite(sc->r_norm)) {
+      sc->claimed = claimed;
+      sc->active = 0;
+      sc->cycle_end = 1;
+      // back substitution H y = g for the i x i upper triangle
+      const int m = sc->i;
+      for (int q = m - 1; q >= 0; --q) {
+        double t = sc->g[q];
+        for (int c = q + 1; c < m; ++c) t -= sc->H[q * K + c] * sc->y[c];
+        sc->y[q] = t / sc->H[q * K + q];
+      }
+      for (int q = 0; q < m; ++q) sc->coef[q] = sc->y[q] / sc->nu[q];
+    }
+  }
+}
+
+// v_{j+1} = w - sum_k coef_k V_k (only while the cycle continues).
+__global__ void __launch_bounds__(kThreads) k_arnoldi_next(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active) return;
+  const int nd = sc->i;  // already advanced: vectors 0..i-1 are used, V_i is written
+  __shared__ double cf[kMaxKdim + 1];
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = sc->coef[t];
+  __syncthreads();
+  double *vn = S.V + (long)nd * S.ldv;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
+    double w = S.w[r];
+    for (int kk = 0; kk < nd; ++kk) w = fma(-cf[kk], S.V[(long)kk * S.ldv + r], w);
+    vn[r] = w;
+  }
+}
+
+// Cycle end, solution update. pc 0: x += invd * (V c); pc 1: z = V c (the
+// caller applies the preconditioner and then k_add_z); pc 2: x += Z y.
+__global__ void __launch_bounds__(kThreads) k_cycle_update(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->cycle_end) return;
+  const int m = sc->i;
+  __shared__ double cf[kMaxKdim + 1];
+  for (int t = threadIdx.x; t < m; t += blockDim.x) cf[t] = S.pc == 2 ? sc->y[t] : sc->coef[t];
+  __syncthreads();
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    if (S.pc == 2) {
+      for (int kk = 0; kk < m; ++kk) acc = fma(cf[kk], (double)S.Z[(long)kk * S.ldv + r], acc);
+      S.x[r] = S.x[r] + acc;
+    } else {
+      for (int kk = 0; kk < m; ++kk) acc = fma(cf[kk], S.V[(long)kk * S.ldv + r], acc);
+      if (S.pc == 0) S.x[r] = fma(S.invd[r], acc, S.x[r]);
+      else S.z[r] = acc;
+    }
+  }
+}
+
+__global__ void k_add_z(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  if (!S.s->cycle_end || S.pc != 1) return;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x)
+    S.x[r] = S.x[r] + S.z2[r];
+}
+
+// True residual after a cycle; decide converged / stop / restart (V_0 = r).
+__global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->cycle_end) return;
+  __shared__ double sacc[kWarps];
+  if (threadIdx.x < kWarps) sacc[threadIdx.x] = 0.0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+    double pr = 0.0;
+#pragma unroll
+    for (int t = 0; t < kRowsPerThread; ++t) {
+      const long r = t0 + t * kThreads + threadIdx.x;
+      if (r < S.n) {
+        int i, j, k;
+        row_ijk((int)r, S.nx, S.ny, i, j, k);
+        const double rv = S.b[r] - stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+        S.r[r] = rv;
+        S.V[r] = rv;
+        pr = fma(rv, rv, pr);
+      }
+    }
+    pr = warp_sum(pr);
+    if (lane == 0) sacc[warp] += pr;
+  }
+  if (!block_partials_and_last(sacc, 1, S.part, &sc->ticket)) return;
+  __shared__ double tot[1];
+  reduce_partials(S.part, gridDim.x, 1, tot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sc->ticket = 0;
+    const double rt = sqrt(tot[0]);
+    sc->cycle_end = 0;
+    sc->r_norm = rt;
+    if (!isfinite(rt)) { sc->nonfinite = 1; sc->status = 2; sc->active = 0; return; }
+    if (rt <= sc->eps) { sc->status = 1; sc->active = 0; return; }
+    if (sc->iters >= sc->maxit) { sc->status = 2; sc->active = 0; return; }
+    if (sc->claimed && rt >= sc->real_old) { sc->status = 3; sc->active = 0; return; }
+    sc->real_old = rt;
+    sc->i = 0;
+    sc->claimed = 0;
+    sc->nu[0] = rt;
+    sc->g[0] = rt;
+    sc->active = 1;
+  }
+}
+
+// FP32 inner preconditioner for the flexible form: zf = D^-1 v (v = V_j / nu_j),
+// then `sweeps-1` Jacobi sweeps zf <- zf + D^-1 (v - A zf); result to Z_j.
+__global__ void __launch_bounds__(kThreads) k_jacobi32_first(KSys *sys, int to_z) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active || S.pc != 2 || S.pc_cb) return;
+  const int j = sc->i;
+  const double inv_nu = 1.0 / sc->nu[j];
+  const double *vj = S.V + (long)j * S.ldv;
+  float *out = to_z ? S.Z + (long)j * S.ldv : S.zf;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x)
+    out[r] = (float)(vj[r] * inv_nu) * S.invdf[r];
+}
+
+__global__ void __launch_bounds__(kThreads) k_jacobi32_sweep(KSys *sys, int src_is_zf, int to_z) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active || S.pc != 2 || S.pc_cb) return;
+  const int j = sc->i;
+  const double inv_nu = 1.0 / sc->nu[j];
+  const double *vj = S.V + (long)j * S.ldv;
+  const float *src = src_is_zf ? S.zf : S.zf2;
+  float *dst = to_z ? S.Z + (long)j * S.ldv : (src_is_zf ? S.zf2 : S.zf);
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
+    int i, jj, k;
+    row_ijk((int)r, S.nx, S.ny, i, jj, k);
+    const float az = stencil7_row_f(S.Af, S.n, src, (int)r, i, jj, k, S.nx, S.ny, S.nz);
+    const float v = (float)(vj[r] * inv_nu);
+    dst[r] = fmaf(S.invdf[r], v - az, src[r]);
+  }
+}
+
+__global__ void k_flags(KSys *sys, int nsys, KFlags *out) {
+  const int t = threadIdx.x;
+  if (t < nsys) {
+    KScal *sc = sys[t].s;
+    out[t].active = sc->active;
+    out[t].cycle_end = sc->cycle_end;
+    out[t].status = sc->status;
+    out[t].iters = sc->iters;
+    out[t].i = sc->i;
+    out[t].nonfinite = sc->nonfinite;
+    out[t].rel = sc->b_norm > 0.0 ? sc->r_norm / sc->b_norm : sc->r_norm;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host driver
+// ---------------------------------------------------------------------------
+void Krylov::configure(int nsys_, const KSysHost *hs) {
+  if (nsys_ < 1 || nsys_ > kMaxSys) throw Error(IBM_ERR_ARG, "Krylov: bad system count");
+  nsys = nsys_;
+  int maxn = 0;
+  for (int s = 0; s < nsys; ++s) {
+    if (hs[s].kdim < 1 || hs[s].kdim > kMaxKdim) throw Error(IBM_ERR_ARG, "GMRES restart length must be in [1, 63]");
+    maxn = std::max(maxn, hs[s].n);
+  }
+  nblk = persistent_blocks(maxn, 4);
+  const size_t need_part = (size_t)nblk * (kMaxKdim + 2);
+  for (int s = 0; s < nsys; ++s) {
+    const KSysHost &h = hs[s];
+    Slot &sl = slot[s];
+    sl.host = h;
+    sl.V.alloc((size_t)(h.kdim + 1) * h.n);
+    sl.w.alloc(h.n);
+    sl.r.alloc(h.n);
+    if (h.pc == 1) { sl.z.alloc(h.n); sl.z2.alloc(h.n); }
+    if (h.pc == 2) {
+      sl.Z.alloc((size_t)h.kdim * h.n);
+      if (!h.pc_cb) { sl.zf.alloc(h.n); sl.zf2.alloc(h.n); }
+    }
+    sl.part.alloc(need_part);
+  }
+  scal.alloc(nsys);
+  dsys.alloc(nsys);
+  dflags.alloc(nsys);
+  if (!hflags) IBM_CUDA_TRY(cudaMallocHost((void **)&hflags, sizeof(KFlags) * kMaxSys));
+}
+
+size_t Krylov::bytes() const {
+  size_t b = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const Slot &sl = slot[s];
+    b += sl.V.bytes() + sl.w.bytes() + sl.r.bytes() + sl.z.bytes() + sl.z2.bytes() + sl.part.bytes() +
+         sl.Z.bytes() + sl.zf.bytes() + sl.zf2.bytes();
+  }
+  return b;
+}
+
+Krylov::~Krylov() {
+  if (hflags) cudaFreeHost(hflags);
+}
+
+void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask) {
+  KSys hsys[kMaxSys];
+  memset(hsys, 0, sizeof(hsys));
+  for (int s = 0; s < nsys; ++s) {
+    const KSysHost &h = slot[s].host;
+    KSys &k = hsys[s];
+    k.nx = h.nx; k.ny = h.ny; k.nz = h.nz; k.n = ((mask >> s) & 1u) ? h.n : 0;
+    k.A = h.A; k.Ar = h.Ar; k.invd = h.invd; k.Af = h.Af; k.invdf = h.invdf;
+    k.V = slot[s].V.p; k.ldv = h.n;
+    k.Z = slot[s].Z.p;
+    k.w = slot[s].w.p; k.r = slot[s].r.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;
+    k.zf = slot[s].zf.p; k.zf2 = slot[s].zf2.p;
+    k.x = x[s]; k.b = b[s];
+    k.part = slot[s].part.p;
+    k.nblk = nblk;
+    k.pc = h.pc;
+    k.pc_cb = h.pc_cb;
+    k.s = scal.p + s;
+  }
+  IBM_CUDA_TRY(cudaMemcpyAsync(dsys.p, hsys, sizeof(KSys) * nsys, cudaMemcpyHostToDevice, st));
+  static KScal init[kMaxSys];
+  memset(init, 0, sizeof(init));
+  for (int s = 0; s < nsys; ++s) {
+    init[s].kdim = slot[s].host.kdim;
+    init[s].maxit = slot[s].host.maxit;
+    init[s].tol = slot[s].host.tol;
+  }
+  IBM_CUDA_TRY(cudaMemcpyAsync(scal.p, init, sizeof(KScal) * nsys, cudaMemcpyHostToDevice, st));
+  // the host copy is staged by the driver before the call returns for pageable memory
+  IBM_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+void Krylov::read_flags(cudaStream_t st) {
+  k_flags<<<1, 32, 0, st>>>(dsys.p, nsys, dflags.p);
+  count_launch();
+  IBM_CUDA_TRY(cudaMemcpyAsync(hflags, dflags.p, sizeof(KFlags) * nsys, cudaMemcpyDeviceToHost, st));
+  IBM_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, const Precond &pc,
+                   KResult *res, unsigned mask) {
+  bind(st, b, x, mask);
+  const dim3 grid(nblk, nsys), gridu(nblk * 2, nsys);
+  k_init<<<grid, kThreads, 0, st>>>(dsys.p, nsys);
+  count_launch();
+  int inner_sweeps = 1;
+  for (int s = 0; s < nsys; ++s)
+    if (slot[s].host.pc == 2 && !slot[s].host.pc_cb) inner_sweeps = std::max(inner_sweeps, slot[s].host.inner_sweeps);
+  KSys *dev = dsys.p;
+  for (long guard = 0;; ++guard) {
+    if (guard > 4L * 1000 * 1000) throw Error(IBM_ERR_CUDA, "GMRES host loop did not terminate");
+    read_flags(st);
+    bool any_active = false, any_end = false;
+    for (int s = 0; s < nsys; ++s) {
+      any_active |= hflags[s].active != 0;
+      any_end |= hflags[s].cycle_end != 0;
+    }
+    if (!any_active && !any_end) break;
+    if (any_end) {
+      // Solution update of the systems whose cycle ended, then the true residual.
+      k_cycle_update<<<gridu, kThreads, 0, st>>>(dev);
+      count_launch();
+      bool cb = false;
+      for (int s = 0; s < nsys; ++s) {
+        if (slot[s].host.pc != 1 || !hflags[s].cycle_end) continue;
+        VecRef in;
+        in.base = slot[s].z.p;
+        OutRef out;
+        out.d = slot[s].z2.p;
+        pc.apply(pc.ctx, st, s, in, out, &scal.p[s].cycle_end);
+        cb = true;
+      }
+      if (cb) { k_add_z<<<gridu, kThreads, 0, st>>>(dev); count_launch(); }
+      k_cycle_residual<<<grid, kThreads, 0, st>>>(dev);
+      count_launch();
+      continue;
+    }
+    // One Arnoldi step for every active system.
+    for (int s = 0; s < nsys; ++s) {
+      if (!hflags[s].active) continue;
+      const KSysHost &h = slot[s].host;
+      if (h.pc == 1) {
+        VecRef in;
+        in.base = slot[s].V.p; in.ld = h.n; in.idx = &scal.p[s].i;
+        OutRef out;
+        out.d = slot[s].z.p;
+        pc.apply(pc.ctx, st, s, in, out, &scal.p[s].active);
+      } else if (h.pc == 2 && h.pc_cb) {
+        VecRef in;
+        in.base = slot[s].V.p; in.ld = h.n; in.idx = &scal.p[s].i; in.nu = scal.p[s].nu;
+        OutRef out;
+        out.f = slot[s].Z.p; out.ld = h.n; out.idx = &scal.p[s].i;
+        pc.apply(pc.ctx, st, s, in, out, &scal.p[s].active);
+      }
+    }
+    bool internal32 = false;
+    for (int s = 0; s < nsys; ++s) internal32 |= (slot[s].host.pc == 2 && !slot[s].host.pc_cb && hflags[s].active);
+    if (internal32) {
+      if (inner_sweeps <= 1) { k_jacobi32_first<<<gridu, kThreads, 0, st>>>(dev, 1); count_launch(); }
+      else {
+        k_jacobi32_first<<<gridu, kThreads, 0, st>>>(dev, 0);
+        count_launch();
+        int src_zf = 1;
+        for (int q = 1; q < inner_sweeps; ++q) {
+          k_jacobi32_sweep<<<gridu, kThreads, 0, st>>>(dev, src_zf, q == inner_sweeps - 1);
+          count_launch();
+          src_zf ^= 1;
+        }
+      }
+    }
+    k_arnoldi_spmv<<<grid, kThreads, 0, st>>>(dev);
+    k_arnoldi_orth<<<grid, kThreads, 0, st>>>(dev);
+    k_arnoldi_next<<<gridu, kThreads, 0, st>>>(dev);
+    count_launch(3);
+  }
+  for (int s = 0; s < nsys; ++s) {
+    res[s].iters = hflags[s].iters;
+    res[s].rel_res = hflags[s].rel;
+    res[s].status = hflags[s].status;
+    res[s].nonfinite = hflags[s].nonfinite;
+  }
+  IBM_CUDA_TRY(cudaGetLastError());
+}
+
+}  // namespace ibm

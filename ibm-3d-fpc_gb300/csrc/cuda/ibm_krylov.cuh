@@ -1,0 +1,74 @@
+// Batched restarted GMRES (see ibm_krylov.cu).
+#pragma once
+#include "ibm_common.cuh"
+
+namespace ibm {
+
+// A vector whose location is resolved on the device: base + (*idx) * ld,
+// optionally scaled by 1 / nu[*idx] (the unnormalised Krylov basis).
+struct VecRef {
+  const double *base = nullptr;
+  long ld = 0;
+  const int *idx = nullptr;
+  const double *nu = nullptr;
+};
+struct OutRef {
+  double *d = nullptr;  // FP64 destination, or
+  float *f = nullptr;   // FP32 destination
+  long ld = 0;
+  const int *idx = nullptr;
+};
+
+// Preconditioner callback: out = M in, every kernel gated on *gate != 0.
+struct Precond {
+  void *ctx = nullptr;
+  void (*apply)(void *ctx, cudaStream_t st, int sys, const VecRef &in, const OutRef &out, const int *gate) = nullptr;
+};
+
+struct KSysHost {
+  int nx = 0, ny = 0, nz = 0, n = 0;
+  const double *A = nullptr;    // Arnoldi operator ([7][n]); A*D^-1 when pc == 0
+  const double *Ar = nullptr;   // operator of the true residual
+  const double *invd = nullptr;
+  const float *Af = nullptr, *invdf = nullptr;
+  int pc = 0;                   // 0 folded Jacobi, 1 explicit FP64 callback, 2 flexible FP32
+  int pc_cb = 0;                // pc 2: 1 = callback, 0 = internal FP32 Jacobi sweeps
+  int inner_sweeps = 1;
+  int kdim = 50, maxit = 250;
+  double tol = 1e-8;
+};
+
+struct KResult {
+  int iters = 0;
+  double rel_res = 0.0;
+  int status = 0;   // 1 converged, 2 iteration limit, 3 stagnation
+  int nonfinite = 0;
+};
+
+class Krylov {
+ public:
+  ~Krylov();
+  void configure(int nsys, const KSysHost *systems);
+  // mask: bit s set = solve system s (the others are skipped).
+  void solve(cudaStream_t st, const double *const *b, double *const *x, const Precond &pc, KResult *res,
+             unsigned mask = ~0u);
+  size_t bytes() const;
+
+ private:
+  struct Slot {
+    KSysHost host;
+    DBuf<double> V, w, r, z, z2, part;
+    DBuf<float> Z, zf, zf2;
+  };
+  void bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask);
+  void read_flags(cudaStream_t st);
+  int nsys = 0;
+  int nblk = 0;
+  Slot slot[kMaxSys];
+  DBuf<KScal> scal;
+  DBuf<KSys> dsys;
+  DBuf<KFlags> dflags;
+  KFlags *hflags = nullptr;
+};
+
+}  // namespace ibm

@@ -1,0 +1,573 @@
+// Semicoarsening multigrid V-cycle used as the pressure preconditioner.
+//
+// Restates the published design of HYPRE's PFMG (third-party; configured by
+// the reference at main.cu:207-221): each level is coarsened by two in one
+// direction (the one with the smallest current spacing), interpolation is
+// operator dependent along that direction (weights -sum(lower plane) /
+// sum(own plane) and -sum(upper plane) / sum(own plane)), restriction is its
+// transpose, coarse operators are Galerkin R A P (27-point), optionally
+// collapsed to 7 points, the smoother is weighted Jacobi or a two-colour
+// relaxation, and the coarsest level is solved with an explicit inverse.
+//
+// The hierarchy is built on the device once per pressure operator; the same
+// kernels run in FP64 (plain form) and FP32 (mixed form, coefficients
+// rounded from the FP64 hierarchy).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "ibm_common.cuh"
+#include "ibm_mg.cuh"
+
+namespace ibm {
+
+namespace {
+
+__constant__ int c_slot7[7] = {13, 12, 14, 10, 16, 4, 22};  // Struct slot -> 27-point slot
+
+__host__ __device__ inline int s27(int ox, int oy, int oz) { return (ox + 1) + 3 * (oy + 1) + 9 * (oz + 1); }
+__host__ __device__ inline int s27_off(int s, int d) { return d == 0 ? s % 3 - 1 : d == 1 ? (s / 3) % 3 - 1 : s / 9 - 1; }
+
+// Position of 27-point slot s among the stored slots (-1 when not stored).
+__device__ inline int stored_slot(int ns, int s) {
+  if (ns == 27) return s;
+  switch (s) {
+    case 13: return 0; case 12: return 1; case 14: return 2; case 10: return 3;
+    case 16: return 4; case 4: return 5; case 22: return 6; default: return -1;
+  }
+}
+
+__device__ inline bool gate_off(const int *gate) { return gate != nullptr && *gate == 0; }
+
+template <class T>
+__device__ inline T fmat(T a, T b, T c);
+template <>
+__device__ inline double fmat<double>(double a, double b, double c) { return fma(a, b, c); }
+template <>
+__device__ inline float fmat<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// (A x)_r for a stored 7- or 27-point level operator.
+template <class T, int NS>
+__device__ inline T apply_row(const T *__restrict__ A, long n, const T *__restrict__ x, int r, int i, int j, int k,
+                              int nx, int ny, int nz) {
+  T acc = T(0);
+  if (NS == 7) {
+    const long sy = nx, sz = (long)nx * ny;
+    acc = fmat<T>(A[r], x[r], acc);
+    acc = fmat<T>(A[n + r], i > 0 ? x[r - 1] : T(0), acc);
+    acc = fmat<T>(A[2 * n + r], i < nx - 1 ? x[r + 1] : T(0), acc);
+    acc = fmat<T>(A[3 * n + r], j > 0 ? x[r - sy] : T(0), acc);
+    acc = fmat<T>(A[4 * n + r], j < ny - 1 ? x[r + sy] : T(0), acc);
+    acc = fmat<T>(A[5 * n + r], k > 0 ? x[r - sz] : T(0), acc);
+    acc = fmat<T>(A[6 * n + r], k < nz - 1 ? x[r + sz] : T(0), acc);
+  } else {
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+      const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+      const bool in = ii >= 0 && ii < nx && jj >= 0 && jj < ny && kk >= 0 && kk < nz;
+      const T xv = in ? x[((long)kk * ny + jj) * nx + ii] : T(0);
+      acc = fmat<T>(A[(long)s * n + r], xv, acc);
+    }
+  }
+  return acc;
+}
+
+// ---------------------------------------------------------------- setup
+__global__ void k_diag(const double *A, long n, double omega, double *invd, double *wd) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    const double d = A[r];  // slot 0 of either layout is... (27-point: centre at plane 13, see caller)
+    const double id = d != 0.0 ? 1.0 / d : 0.0;
+    invd[r] = id;
+    wd[r] = omega * id;
+  }
+}
+
+__global__ void k_interp_weights(const double *A, int ns, long n, int d, double *pm, double *pp) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    double c0 = 0.0, cm = 0.0, cp = 0.0;
+    for (int s = 0; s < 27; ++s) {
+      const int q = stored_slot(ns, s);
+      if (q < 0) continue;
+      const double a = A[(long)q * n + r];
+      const int od = s27_off(s, d);
+      if (od == 0) c0 += a; else if (od < 0) cm += a; else cp += a;
+    }
+    double wm = 0.0, wp = 0.0;
+    if (c0 != 0.0) { wm = -cm / c0; wp = -cp / c0; }
+    pm[r] = wm;
+    pp[r] = wp;
+  }
+}
+
+// Galerkin coarse operator, same summation order as the oracle (for each of
+// the three restricting fine points, each fine stencil entry in slot order,
+// each interpolating coarse point).
+__global__ void k_rap(const double *Af, int ns, Box fb, const double *pm, const double *pp, int d, Box cb,
+                      double *Ac) {
+  for (long I = (long)blockIdx.x * blockDim.x + threadIdx.x; I < cb.n; I += (long)gridDim.x * blockDim.x) {
+    int ci[3];
+    row_ijk((int)I, cb.nx, cb.ny, ci[0], ci[1], ci[2]);
+    double ac[27];
+#pragma unroll
+    for (int s = 0; s < 27; ++s) ac[s] = 0.0;
+    const int fn[3] = {fb.nx, fb.ny, fb.nz};
+    const int cn[3] = {cb.nx, cb.ny, cb.nz};
+    for (int fo = -1; fo <= 1; ++fo) {
+      int f[3] = {ci[0], ci[1], ci[2]};
+      f[d] = 2 * ci[d] + fo;
+      if (f[d] < 0 || f[d] >= fn[d]) continue;
+      const long fr = ((long)f[2] * fb.ny + f[1]) * fb.nx + f[0];
+      const double rw = fo == 0 ? 1.0 : (fo < 0 ? pp[fr] : pm[fr]);
+      if (rw == 0.0) continue;
+      for (int s = 0; s < 27; ++s) {
+        const int q = stored_slot(ns, s);
+        if (q < 0) continue;
+        const double a = Af[(long)q * fb.n + fr];
+        if (a == 0.0) continue;
+        const int o3[3] = {s27_off(s, 0), s27_off(s, 1), s27_off(s, 2)};
+        const int g[3] = {f[0] + o3[0], f[1] + o3[1], f[2] + o3[2]};
+        if (g[0] < 0 || g[0] >= fn[0] || g[1] < 0 || g[1] >= fn[1] || g[2] < 0 || g[2] >= fn[2]) continue;
+        const long gr = ((long)g[2] * fb.ny + g[1]) * fb.nx + g[0];
+        const double ra = rw * a;
+        int jc[2];
+        double pw[2];
+        int nt;
+        if ((g[d] & 1) == 0) { jc[0] = g[d] / 2; pw[0] = 1.0; nt = 1; }
+        else {
+          jc[0] = (g[d] - 1) / 2; pw[0] = pm[gr]; nt = 1;
+          if ((g[d] + 1) / 2 < cn[d]) { jc[1] = (g[d] + 1) / 2; pw[1] = pp[gr]; nt = 2; }
+        }
+        for (int t = 0; t < nt; ++t) {
+          if (pw[t] == 0.0) continue;
+          int oc[3] = {o3[0], o3[1], o3[2]};
+          oc[d] = jc[t] - ci[d];
+          const int sc = s27(oc[0], oc[1], oc[2]);
+#pragma unroll
+          for (int u = 0; u < 27; ++u)
+            if (u == sc) ac[u] = ac[u] + ra * pw[t];
+        }
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < 27; ++s) Ac[(long)s * cb.n + I] = ac[s];
+  }
+}
+
+// 27 -> 7 point collapse preserving constants and linear functions (same order as the oracle).
+__global__ void k_collapse7(const double *A27, long n, double *A7) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    double a[27];
+#pragma unroll
+    for (int s = 0; s < 27; ++s) a[s] = A27[(long)s * n + r];
+    for (int s = 0; s < 27; ++s) {
+      const int o3[3] = {s27_off(s, 0), s27_off(s, 1), s27_off(s, 2)};
+      const int m = (o3[0] != 0) + (o3[1] != 0) + (o3[2] != 0);
+      if (m < 2 || a[s] == 0.0) continue;
+      const double e = a[s];
+      a[s] = 0.0;
+      for (int dd = 0; dd < 3; ++dd) {
+        if (!o3[dd]) continue;
+        int q[3] = {0, 0, 0};
+        q[dd] = o3[dd];
+        const int sq = s27(q[0], q[1], q[2]);
+        a[sq] = a[sq] + e;
+      }
+      a[13] = a[13] - (double)(m - 1) * e;
+    }
+    for (int q = 0; q < 7; ++q) A7[(long)q * n + r] = a[c_slot7[q]];
+  }
+}
+
+template <class T>
+__global__ void k_convert(const double *src, T *dst, long n) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    dst[r] = (T)src[r];
+}
+
+// ---------------------------------------------------------------- V-cycle
+template <class T>
+__global__ void k_load_input(T *bv, long n, VecRef in, const int *gate) {
+  if (gate_off(gate)) return;
+  const long off = in.idx ? (long)(*in.idx) * in.ld : 0;
+  const double sc = in.nu ? 1.0 / in.nu[in.idx ? *in.idx : 0] : 1.0;
+  const double *src = in.base + off;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    bv[r] = (T)(in.nu ? src[r] * sc : src[r]);
+}
+
+template <class T>
+__global__ void k_store_output(const T *x, long n, OutRef out, const int *gate) {
+  if (gate_off(gate)) return;
+  const long off = out.idx ? (long)(*out.idx) * out.ld : 0;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    if (out.d) out.d[off + r] = (double)x[r];
+    else out.f[off + r] = (float)x[r];
+  }
+}
+
+template <class T>
+__global__ void k_relax_zero(const T *wd, const T *b, T *x, long n, const int *gate) {
+  if (gate_off(gate)) return;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    x[r] = wd[r] * b[r];
+}
+
+// Weighted Jacobi: t = x + wd (b - A x).
+template <class T, int NS>
+__global__ void k_relax_jacobi(const T *A, const T *wd, const T *b, const T *x, T *t, Box bx, const int *gate) {
+  if (gate_off(gate)) return;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < bx.n; r += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    row_ijk((int)r, bx.nx, bx.ny, i, j, k);
+    const T ax = apply_row<T, NS>(A, bx.n, x, (int)r, i, j, k, bx.nx, bx.ny, bx.nz);
+    t[r] = fmat<T>(wd[r], b[r] - ax, x[r]);
+  }
+}
+
+// One colour phase of the two-colour relaxation: points of `color` take
+// x + invd (b - A x) from the phase's input; the others are copied.
+// zero_x treats the input as all zeros (first phase of a zero-guess sweep).
+template <class T, int NS>
+__global__ void k_relax_color(const T *A, const T *invd, const T *b, const T *x, T *t, Box bx, int color,
+                              int zero_x, const int *gate) {
+  if (gate_off(gate)) return;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < bx.n; r += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    row_ijk((int)r, bx.nx, bx.ny, i, j, k);
+    if (((i + j + k) & 1) != color) { t[r] = zero_x ? T(0) : x[r]; continue; }
+    if (zero_x) { t[r] = invd[r] * b[r]; continue; }
+    const T ax = apply_row<T, NS>(A, bx.n, x, (int)r, i, j, k, bx.nx, bx.ny, bx.nz);
+    t[r] = fmat<T>(invd[r], b[r] - ax, x[r]);
+  }
+}
+
+template <class T, int NS>
+__global__ void k_residual(const T *A, const T *b, const T *x, T *res, Box bx, const int *gate) {
+  if (gate_off(gate)) return;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < bx.n; r += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    row_ijk((int)r, bx.nx, bx.ny, i, j, k);
+    res[r] = b[r] - apply_row<T, NS>(A, bx.n, x, (int)r, i, j, k, bx.nx, bx.ny, bx.nz);
+  }
+}
+
+template <class T>
+__global__ void k_restrict(const T *res, const T *pm, const T *pp, Box fb, int d, T *bc, Box cb, const int *gate) {
+  if (gate_off(gate)) return;
+  const int fn[3] = {fb.nx, fb.ny, fb.nz};
+  for (long I = (long)blockIdx.x * blockDim.x + threadIdx.x; I < cb.n; I += (long)gridDim.x * blockDim.x) {
+    int ci[3];
+    row_ijk((int)I, cb.nx, cb.ny, ci[0], ci[1], ci[2]);
+    T acc = T(0);
+    for (int fo = -1; fo <= 1; ++fo) {
+      int f[3] = {ci[0], ci[1], ci[2]};
+      f[d] = 2 * ci[d] + fo;
+      if (f[d] < 0 || f[d] >= fn[d]) continue;
+      const long fr = ((long)f[2] * fb.ny + f[1]) * fb.nx + f[0];
+      const T rw = fo == 0 ? T(1) : (fo < 0 ? pp[fr] : pm[fr]);
+      acc = fmat<T>(rw, res[fr], acc);
+    }
+    bc[I] = acc;
+  }
+}
+
+template <class T>
+__global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb, int d, T *x, const int *gate) {
+  if (gate_off(gate)) return;
+  const int cn[3] = {cb.nx, cb.ny, cb.nz};
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < fb.n; r += (long)gridDim.x * blockDim.x) {
+    int f[3];
+    row_ijk((int)r, fb.nx, fb.ny, f[0], f[1], f[2]);
+    T corr;
+    if ((f[d] & 1) == 0) {
+      int c[3] = {f[0], f[1], f[2]};
+      c[d] = f[d] / 2;
+      corr = xc[((long)c[2] * cb.ny + c[1]) * cb.nx + c[0]];
+    } else {
+      int c0[3] = {f[0], f[1], f[2]};
+      c0[d] = (f[d] - 1) / 2;
+      const T x0 = xc[((long)c0[2] * cb.ny + c0[1]) * cb.nx + c0[0]];
+      T x1 = T(0);
+      if ((f[d] + 1) / 2 < cn[d]) {
+        int c1[3] = {f[0], f[1], f[2]};
+        c1[d] = (f[d] + 1) / 2;
+        x1 = xc[((long)c1[2] * cb.ny + c1[1]) * cb.nx + c1[0]];
+      }
+      corr = fmat<T>(pp[r], x1, pm[r] * x0);
+    }
+    x[r] = x[r] + corr;
+  }
+}
+
+// Coarsest level: x = Ainv b (one warp per row).
+template <class T>
+__global__ void k_dense(const T *Ainv, const T *b, T *x, int n, const int *gate) {
+  if (gate_off(gate)) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int r = warp; r < n; r += nw) {
+    double acc = 0.0;
+    for (int c = lane; c < n; c += 32) acc = fma((double)Ainv[(long)r * n + c], (double)b[c], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) x[r] = (T)acc;
+  }
+}
+
+int grid_for(long n) {
+  long b = (n + kThreads - 1) / kThreads;
+  const long cap = (long)sm_count() * 8;
+  if (b > cap) b = cap;
+  return (int)std::max(1L, b);
+}
+
+// Gauss-Jordan inverse with partial pivoting of the assembled coarsest operator.
+void dense_inverse(const std::vector<double> &A, int ns, const Box &b, std::vector<double> &inv) {
+  const long n = b.n;
+  std::vector<double> M((size_t)(n * n), 0.0);
+  for (long r = 0; r < n; ++r) {
+    const int i = (int)(r % b.nx), j = (int)((r / b.nx) % b.ny), k = (int)(r / ((long)b.nx * b.ny));
+    for (int s = 0; s < 27; ++s) {
+      int q = -1;
+      if (ns == 27) q = s;
+      else {
+        static const int map[27] = {-1, -1, -1, -1, 5, -1, -1, -1, -1, -1, 3, -1, 1, 0, 2, -1, 4, -1,
+                                    -1, -1, -1, -1, 6, -1, -1, -1, -1};
+        q = map[s];
+      }
+      if (q < 0) continue;
+      const int ii = i + s27_off(s, 0), jj = j + s27_off(s, 1), kk = k + s27_off(s, 2);
+      if (ii < 0 || ii >= b.nx || jj < 0 || jj >= b.ny || kk < 0 || kk >= b.nz) continue;
+      M[(size_t)(r * n + ((long)kk * b.ny + jj) * b.nx + ii)] += A[(size_t)q * n + r];
+    }
+  }
+  inv.assign((size_t)(n * n), 0.0);
+  for (long r = 0; r < n; ++r) inv[(size_t)(r * n + r)] = 1.0;
+  for (long c = 0; c < n; ++c) {
+    long piv = c;
+    for (long r = c + 1; r < n; ++r)
+      if (std::fabs(M[(size_t)(r * n + c)]) > std::fabs(M[(size_t)(piv * n + c)])) piv = r;
+    if (piv != c)
+      for (long t = 0; t < n; ++t) {
+        std::swap(M[(size_t)(c * n + t)], M[(size_t)(piv * n + t)]);
+        std::swap(inv[(size_t)(c * n + t)], inv[(size_t)(piv * n + t)]);
+      }
+    const double pv = M[(size_t)(c * n + c)];
+    if (pv == 0.0) continue;
+    const double ip = 1.0 / pv;
+    for (long t = 0; t < n; ++t) { M[(size_t)(c * n + t)] *= ip; inv[(size_t)(c * n + t)] *= ip; }
+    for (long r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = M[(size_t)(r * n + c)];
+      if (f == 0.0) continue;
+      for (long t = 0; t < n; ++t) {
+        M[(size_t)(r * n + t)] -= f * M[(size_t)(c * n + t)];
+        inv[(size_t)(r * n + t)] -= f * inv[(size_t)(c * n + t)];
+      }
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+template <>
+void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L, const Box &b0, const double *A7,
+                              const double h0[3]) {
+  L.clear();
+  L.reserve(64);
+  L.emplace_back();
+  L[0].b = b0;
+  L[0].ns = 7;
+  L[0].A = A7;
+  double h[3] = {h0[0], h0[1], h0[2]};
+  for (int l = 0;; ++l) {
+    MgLevelT<double> &F = L[l];
+    const long n = F.b.n;
+    F.wd.alloc(n); F.invd.alloc(n); F.x.alloc(n); F.bv.alloc(n); F.r.alloc(n); F.t.alloc(n);
+    // diagonal: plane 0 of a 7-point level, plane 13 of a 27-point level
+    const double *diag = F.A + (F.ns == 27 ? 13L * n : 0L);
+    k_diag<<<grid_for(n), kThreads, 0, st>>>(diag, n, prm.omega, F.invd.p, F.wd.p);
+    count_launch();
+    int d = -1;
+    const int dims[3] = {F.b.nx, F.b.ny, F.b.nz};
+    for (int dd = 0; dd < 3; ++dd)
+      if (dims[dd] > 1 && (d < 0 || h[dd] < h[d])) d = dd;
+    if (n <= prm.coarse_max || l + 1 >= prm.max_levels || d < 0 || l + 1 >= 60) {
+      F.cdir = -1;
+      if (n > 4096) throw Error(IBM_ERR_ARG, "multigrid coarsest level too large for the dense solve");
+      std::vector<double> hostA((size_t)F.ns * n), inv;
+      IBM_CUDA_TRY(cudaMemcpyAsync(hostA.data(), F.A, sizeof(double) * hostA.size(), cudaMemcpyDeviceToHost, st));
+      IBM_CUDA_TRY(cudaStreamSynchronize(st));
+      dense_inverse(hostA, F.ns, F.b, inv);
+      F.dense.alloc(inv.size());
+      IBM_CUDA_TRY(cudaMemcpyAsync(F.dense.p, inv.data(), sizeof(double) * inv.size(), cudaMemcpyHostToDevice, st));
+      IBM_CUDA_TRY(cudaStreamSynchronize(st));
+      break;
+    }
+    F.cdir = d;
+    h[d] *= 2.0;
+    F.pm.alloc(n); F.pp.alloc(n);
+    k_interp_weights<<<grid_for(n), kThreads, 0, st>>>(F.A, F.ns, n, d, F.pm.p, F.pp.p);
+    count_launch();
+    Box cb = F.b;
+    if (d == 0) cb.nx = (F.b.nx + 1) / 2;
+    if (d == 1) cb.ny = (F.b.ny + 1) / 2;
+    if (d == 2) cb.nz = (F.b.nz + 1) / 2;
+    cb.n = cb.nx * cb.ny * cb.nz;
+    L.emplace_back();
+    MgLevelT<double> &Fr = L[l];  // re-fetch after emplace
+    MgLevelT<double> &C = L[l + 1];
+    C.b = cb;
+    DBuf<double> a27;
+    a27.alloc((size_t)27 * cb.n);
+    k_rap<<<grid_for(cb.n), kThreads, 0, st>>>(Fr.A, Fr.ns, Fr.b, Fr.pm.p, Fr.pp.p, d, cb, a27.p);
+    count_launch();
+    if (prm.rap == 1) {
+      C.Aown.alloc((size_t)7 * cb.n);
+      k_collapse7<<<grid_for(cb.n), kThreads, 0, st>>>(a27.p, cb.n, C.Aown.p);
+      count_launch();
+      IBM_CUDA_TRY(cudaStreamSynchronize(st));
+      C.ns = 7;
+    } else {
+      C.Aown = std::move(a27);
+      C.ns = 27;
+    }
+    C.A = C.Aown.p;
+  }
+  IBM_CUDA_TRY(cudaStreamSynchronize(st));
+  IBM_CUDA_TRY(cudaGetLastError());
+}
+
+void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const float *A7f, const double h[3],
+                      const MgParams &p, bool fp64, bool fp32) {
+  prm = p;
+  (void)fp64;
+  build<double>(st, L64, b, A7, h);
+  L32.clear();
+  if (fp32) {
+    L32.reserve(L64.size());
+    for (size_t l = 0; l < L64.size(); ++l) {
+      const MgLevelT<double> &D = L64[l];
+      L32.emplace_back();
+      MgLevelT<float> &F = L32.back();
+      F.b = D.b; F.cdir = D.cdir; F.ns = D.ns;
+      const long n = D.b.n;
+      if (l == 0) F.A = A7f;
+      else {
+        F.Aown.alloc((size_t)D.ns * n);
+        k_convert<float><<<grid_for((long)D.ns * n), kThreads, 0, st>>>(D.A, F.Aown.p, (long)D.ns * n);
+        count_launch();
+        F.A = F.Aown.p;
+      }
+      auto conv = [&](const DBuf<double> &src, DBuf<float> &dst) {
+        if (!src.p) return;
+        dst.alloc(src.n);
+        k_convert<float><<<grid_for((long)src.n), kThreads, 0, st>>>(src.p, dst.p, (long)src.n);
+        count_launch();
+      };
+      conv(D.wd, F.wd); conv(D.invd, F.invd); conv(D.pm, F.pm); conv(D.pp, F.pp); conv(D.dense, F.dense);
+      F.x.alloc(n); F.bv.alloc(n); F.r.alloc(n); F.t.alloc(n);
+    }
+    IBM_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+}
+
+// Runs the V-cycle from level l with zero initial guess; returns (through the
+// level's x buffer pointer swap-free scheme) the buffer holding the result.
+template <class T>
+static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgParams &p, const int *gate) {
+  MgLevelT<T> &F = L[l];
+  const long n = F.b.n;
+  const int g = grid_for(n);
+  if (F.cdir < 0) {
+    k_dense<T><<<std::max(1, (int)std::min<long>((n + 7) / 8, (long)sm_count() * 4)), kThreads, 0, st>>>(
+        F.dense.p, F.bv.p, F.x.p, (int)n, gate);
+    count_launch();
+    return F.x.p;
+  }
+  T *cur = F.x.p, *oth = F.t.p;
+  auto relax = [&](bool zero) {
+    if (p.relax == 2) {
+      for (int color = 0; color < 2; ++color) {
+        const bool z = zero && color == 0;
+        if (F.ns == 7) k_relax_color<T, 7><<<g, kThreads, 0, st>>>(F.A, F.invd.p, F.bv.p, cur, oth, F.b, color, z, gate);
+        else k_relax_color<T, 27><<<g, kThreads, 0, st>>>(F.A, F.invd.p, F.bv.p, cur, oth, F.b, color, z, gate);
+        count_launch();
+        std::swap(cur, oth);
+      }
+    } else if (zero) {
+      k_relax_zero<T><<<g, kThreads, 0, st>>>(F.wd.p, F.bv.p, cur, n, gate);
+      count_launch();
+    } else {
+      if (F.ns == 7) k_relax_jacobi<T, 7><<<g, kThreads, 0, st>>>(F.A, F.wd.p, F.bv.p, cur, oth, F.b, gate);
+      else k_relax_jacobi<T, 27><<<g, kThreads, 0, st>>>(F.A, F.wd.p, F.bv.p, cur, oth, F.b, gate);
+      count_launch();
+      std::swap(cur, oth);
+    }
+  };
+  if (p.nu1 > 0) {
+    for (int s = 0; s < p.nu1; ++s) relax(s == 0);
+  } else {
+    IBM_CUDA_TRY(cudaMemsetAsync(cur, 0, sizeof(T) * n, st));
+  }
+  if (F.ns == 7) k_residual<T, 7><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
+  else k_residual<T, 27><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
+  count_launch();
+  MgLevelT<T> &C = L[l + 1];
+  k_restrict<T><<<grid_for(C.b.n), kThreads, 0, st>>>(F.r.p, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
+  count_launch();
+  T *xc = vcycle<T>(st, L, l + 1, p, gate);
+  k_prolong<T><<<g, kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, gate);
+  count_launch();
+  for (int s = 0; s < p.nu2; ++s) relax(false);
+  return cur;
+}
+
+void Multigrid::apply(cudaStream_t st, const VecRef &in, const OutRef &out, const int *gate, bool use_fp32) {
+  if (prm.cycles != 1) throw Error(IBM_ERR_UNSUPPORTED, "multigrid: only one V-cycle per application");
+  if (use_fp32) {
+    if (L32.empty()) throw Error(IBM_ERR_STATE, "multigrid: FP32 hierarchy not built");
+    MgLevelT<float> &F = L32[0];
+    k_load_input<float><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, gate);
+    count_launch();
+    float *x = vcycle<float>(st, L32, 0, prm, gate);
+    k_store_output<float><<<grid_for(F.b.n), kThreads, 0, st>>>(x, F.b.n, out, gate);
+    count_launch();
+  } else {
+    MgLevelT<double> &F = L64[0];
+    k_load_input<double><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, gate);
+    count_launch();
+    double *x = vcycle<double>(st, L64, 0, prm, gate);
+    k_store_output<double><<<grid_for(F.b.n), kThreads, 0, st>>>(x, F.b.n, out, gate);
+    count_launch();
+  }
+}
+
+void Multigrid::level_info(int l, int dims[3], int *cdir, int *ns) const {
+  const auto &F = L64.at((size_t)l);
+  dims[0] = F.b.nx; dims[1] = F.b.ny; dims[2] = F.b.nz;
+  *cdir = F.cdir;
+  *ns = F.ns;
+}
+
+void Multigrid::level_coef27(cudaStream_t st, int l, double *host_out) const {
+  const auto &F = L64.at((size_t)l);
+  const long n = F.b.n;
+  std::vector<double> planes((size_t)F.ns * n);
+  IBM_CUDA_TRY(cudaMemcpyAsync(planes.data(), F.A, sizeof(double) * planes.size(), cudaMemcpyDeviceToHost, st));
+  IBM_CUDA_TRY(cudaStreamSynchronize(st));
+  static const int slot7[7] = {13, 12, 14, 10, 16, 4, 22};
+  for (long r = 0; r < n; ++r) {
+    for (int s = 0; s < 27; ++s) host_out[r * 27 + s] = 0.0;
+    for (int q = 0; q < F.ns; ++q) host_out[r * 27 + (F.ns == 27 ? q : slot7[q])] = planes[(size_t)q * n + r];
+  }
+}
+
+size_t Multigrid::bytes() const {
+  size_t b = 0;
+  for (const auto &F : L64) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes();
+  for (const auto &F : L32) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes();
+  return b;
+}
+
+}  // namespace ibm

@@ -1,0 +1,51 @@
+// Semicoarsening multigrid preconditioner for the pressure operator (see ibm_mg.cu).
+#pragma once
+#include "ibm_common.cuh"
+#include "ibm_krylov.cuh"
+
+namespace ibm {
+
+struct MgParams {
+  int rap = 0;          // 0 Galerkin 27-point, 1 collapsed to 7 points
+  int relax = 1;        // 1 weighted Jacobi, 2 two-colour (red-black) relaxation
+  int nu1 = 1, nu2 = 1;
+  double omega = 2.0 / 3.0;
+  int coarse_max = 64;
+  int max_levels = 40;
+  int cycles = 1;       // V-cycles per application
+};
+
+template <class T>
+struct MgLevelT {
+  Box b;
+  int cdir = -1;        // direction coarsened to reach the next level; -1 on the coarsest
+  int ns = 7;           // stencil slots stored: 7 (Struct order) or 27
+  const T *A = nullptr; // [ns][n] planes (level 0 points at the operator itself)
+  DBuf<T> Aown, wd, invd, pm, pp, x, bv, r, t, dense;
+};
+
+class Multigrid {
+ public:
+  // Builds the hierarchy from a 7-point operator (FP64 planes, and FP32 planes
+  // when fp32 is requested). h = grid spacing used to pick coarsening directions.
+  void setup(cudaStream_t st, const Box &b, const double *A7, const float *A7f, const double h[3],
+             const MgParams &p, bool fp64, bool fp32);
+  // out = M in (every kernel gated on *gate when gate != nullptr).
+  void apply(cudaStream_t st, const VecRef &in, const OutRef &out, const int *gate, bool use_fp32);
+  int levels() const { return (int)L64.size() ? (int)L64.size() : (int)L32.size(); }
+  void level_info(int l, int dims[3], int *cdir, int *ns) const;
+  // Copies level l's coefficients as [n][27] (FP64 hierarchy).
+  void level_coef27(cudaStream_t st, int l, double *host_out) const;
+  size_t bytes() const;
+  MgParams prm;
+
+ private:
+  template <class T>
+  void build(cudaStream_t st, std::vector<MgLevelT<T>> &L, const Box &b, const T *A7, const double h[3]);
+  template <class T>
+  void cycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const int *gate);
+  std::vector<MgLevelT<double>> L64;
+  std::vector<MgLevelT<float>> L32;
+};
+
+}  // namespace ibm

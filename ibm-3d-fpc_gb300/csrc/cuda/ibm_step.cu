@@ -1,0 +1,533 @@
+// Dense per-step kernels: boundary conditions, convection + pressure gradient
+// + momentum right-hand side, solution scatter, divergence + pressure
+// right-hand side, projection, and the per-step diagnostics.
+//
+// They restate gpu_dense_ops.hpp with the reference's active-id packing
+// replaced by structured stencils: D and G become per-cell / per-face
+// coefficients (converted from the reference CSR), so q, the packed pressure
+// vector and the unpack kernels disappear. Every floating-point operation is
+// written out (fma() where the reference's device code fuses a CSR
+// accumulation, separately rounded operations elsewhere) so the CPU oracle
+// reproduces the results bit for bit.
+#include "ibm_ctx.cuh"
+#include "ibm_step.cuh"
+
+namespace ibm {
+
+namespace {
+
+struct Dims {
+  int nx, ny, nz;
+};
+
+__device__ __forceinline__ long U3(const Dims &d, int i, int j, int k) { return ((long)k * d.ny + j) * (d.nx + 1) + i; }
+__device__ __forceinline__ long V3(const Dims &d, int i, int j, int k) { return ((long)k * (d.ny + 1) + j) * d.nx + i; }
+__device__ __forceinline__ long W3(const Dims &d, int i, int j, int k) { return ((long)k * d.ny + j) * d.nx + i; }
+__device__ __forceinline__ long P3(const Dims &d, int i, int j, int k) { return ((long)k * d.ny + j) * d.nx + i; }
+
+// Bounds-guarded loads with a fallback outside the arrays (gpu_dense_ops.hpp:1-3).
+__device__ __forceinline__ double ld_u(const double *u, const Dims &d, int i, int j, int k, double fb) {
+  return (i < 0 || i > d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) ? fb : u[U3(d, i, j, k)];
+}
+__device__ __forceinline__ double ld_v(const double *v, const Dims &d, int i, int j, int k, double fb) {
+  return (i < 0 || i >= d.nx || j < 0 || j > d.ny || k < 0 || k >= d.nz) ? fb : v[V3(d, i, j, k)];
+}
+__device__ __forceinline__ double ld_w(const double *w, const Dims &d, int i, int j, int k, double fb) {
+  return (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k > d.nz) ? fb : w[W3(d, i, j, k)];
+}
+
+// Centred advective term, separately rounded operations in the reference's order.
+__device__ __forceinline__ double advect(double c, double dm, double dp, double tdx, double a2, double em, double ep,
+                                         double tdy, double a3, double fm, double fp, double tdz) {
+  const double t1 = __ddiv_rn(__dmul_rn(c, __dsub_rn(dp, dm)), tdx);
+  const double t2 = __ddiv_rn(__dmul_rn(a2, __dsub_rn(ep, em)), tdy);
+  const double t3 = __ddiv_rn(__dmul_rn(a3, __dsub_rn(fp, fm)), tdz);
+  return __dadd_rn(__dadd_rn(t1, t2), t3);
+}
+__device__ __forceinline__ double avg4(double a, double b, double c, double d) {
+  return __dmul_rn(0.25, __dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d));
+}
+// ((rho/dt) u - rho conv - gp + bc) * scale, each operation rounded.
+__device__ __forceinline__ double mom_rhs(double a, double rho, double uc, double conv, double gp, double bc,
+                                          double sc) {
+  double t = __dsub_rn(__dmul_rn(a, uc), __dmul_rn(rho, conv));
+  t = __dsub_rn(t, gp);
+  t = __dadd_rn(t, bc);
+  return __dmul_rn(t, sc);
+}
+// G applied to a cell field at one face: lower cell first (column order).
+__device__ __forceinline__ double grad_face(double gl, double pl, double gr, double pr) {
+  return fma(gr, pr, fma(gl, pl, 0.0));
+}
+
+// ------------------------------------------------------------------ BC
+// Boundary planes (inlet ramp * uin, outlet copy, wall zeros).
+__global__ void k_bc_planes(double *u, double *v, double *w, const double *uin, double ramp, Dims d) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < (long)d.ny * d.nz) {
+    const int j = (int)(t % d.ny), k = (int)(t / d.ny);
+    u[U3(d, 0, j, k)] = __dmul_rn(ramp, uin[t]);
+    u[U3(d, d.nx, j, k)] = u[U3(d, d.nx - 1, j, k)];
+  }
+  if (t < (long)d.nx * d.nz) {
+    const int i = (int)(t % d.nx), k = (int)(t / d.nx);
+    v[V3(d, i, 0, k)] = 0.0;
+    v[V3(d, i, d.ny, k)] = 0.0;
+  }
+  if (t < (long)d.nx * d.ny) {
+    w[t] = 0.0;
+    w[(long)d.nz * d.nx * d.ny + t] = 0.0;
+  }
+}
+
+// Inactive interior faces (precomputed lists) set to zero.
+__global__ void k_bc_zero(double *u, const int *lu, int nu_, double *v, const int *lv, int nv_, double *w,
+                          const int *lw, int nw_) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nu_) u[lu[t]] = 0.0;
+  if (t < nv_) v[lv[t]] = 0.0;
+  if (t < nw_) w[lw[t]] = 0.0;
+}
+
+// ------------------------------------------------------------------ RHS
+struct RhsArgs {
+  Dims d;
+  const double *u, *v, *w, *p;
+  const uint8_t *fu, *fv, *fw, *fc;
+  const double *Gu, *Gv, *Gw;
+  const double *sc[3], *bc[3];
+  double *b[3], *x0[3];
+  long nb[3];
+  double a, rho, tdx, tdy, tdz;
+  int zero_guess;
+};
+
+// One thread per solve-box row of u, v and w (flat index over the three boxes).
+__global__ void __launch_bounds__(kThreads) k_momentum_rhs(RhsArgs A) {
+  const Dims &d = A.d;
+  const long total = A.nb[0] + A.nb[1] + A.nb[2];
+  const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
+             NW = (long)d.nx * d.ny * (d.nz + 1);
+  const long plane_w = (long)d.nx * d.ny;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    if (t < A.nb[0]) {  // u row: face (i+1, j, k) with i in [0, nx-2]
+      const long r = t;
+      const int nxu = d.nx - 1;
+      const int i = (int)(r % nxu) + 1;
+      const long q = r / nxu;
+      const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+      const long f = U3(d, i, j, k);
+      const uint8_t fl = A.fu[f];
+      const double uc = A.u[f];
+      double rhs = 0.0;
+      if (fl & kRhsRow) {
+        double conv = 0.0;
+        if (fl & kActive) {
+          const double va = avg4(ld_v(A.v, d, i - 1, j, k, 0.0), ld_v(A.v, d, i - 1, j + 1, k, 0.0),
+                                 ld_v(A.v, d, i, j, k, 0.0), ld_v(A.v, d, i, j + 1, k, 0.0));
+          const double wa = avg4(ld_w(A.w, d, i - 1, j, k, 0.0), ld_w(A.w, d, i - 1, j, k + 1, 0.0),
+                                 ld_w(A.w, d, i, j, k, 0.0), ld_w(A.w, d, i, j, k + 1, 0.0));
+          conv = advect(uc, ld_u(A.u, d, i - 1, j, k, uc), ld_u(A.u, d, i + 1, j, k, uc), A.tdx, va,
+                        ld_u(A.u, d, i, j - 1, k, uc), ld_u(A.u, d, i, j + 1, k, uc), A.tdy, wa,
+                        ld_u(A.u, d, i, j, k - 1, uc), ld_u(A.u, d, i, j, k + 1, uc), A.tdz);
+        }
+        double gp = 0.0;
+        if (fl & kQFace) {
+          const double pl = (A.fc[P3(d, i - 1, j, k)] & kFluid) ? A.p[P3(d, i - 1, j, k)] : 0.0;
+          const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
+          gp = grad_face(A.Gu[f], pl, A.Gu[NU + f], pr);
+        }
+        rhs = mom_rhs(A.a, A.rho, uc, conv, gp, A.bc[0][r], A.sc[0][r]);
+      }
+      A.b[0][r] = rhs;
+      A.x0[0][r] = A.zero_guess ? 0.0 : uc;
+    } else if (t < A.nb[0] + A.nb[1]) {  // v row: face (i, j+1, k)
+      const long r = t - A.nb[0];
+      const int i = (int)(r % d.nx);
+      const long q = r / d.nx;
+      const int j = (int)(q % (d.ny - 1)) + 1, k = (int)(q / (d.ny - 1));
+      const long f = V3(d, i, j, k);
+      const uint8_t fl = A.fv[f];
+      const double vc = A.v[f];
+      double rhs = 0.0;
+      if (fl & kRhsRow) {
+        double conv = 0.0;
+        if (fl & kActive) {
+          const double ua = avg4(ld_u(A.u, d, i, j - 1, k, 0.0), ld_u(A.u, d, i + 1, j - 1, k, 0.0),
+                                 ld_u(A.u, d, i, j, k, 0.0), ld_u(A.u, d, i + 1, j, k, 0.0));
+          const double wa = avg4(ld_w(A.w, d, i, j - 1, k, 0.0), ld_w(A.w, d, i, j, k, 0.0),
+                                 ld_w(A.w, d, i, j - 1, k + 1, 0.0), ld_w(A.w, d, i, j, k + 1, 0.0));
+          conv = advect(ua, ld_v(A.v, d, i - 1, j, k, vc), ld_v(A.v, d, i + 1, j, k, vc), A.tdx, vc,
+                        ld_v(A.v, d, i, j - 1, k, vc), ld_v(A.v, d, i, j + 1, k, vc), A.tdy, wa,
+                        ld_v(A.v, d, i, j, k - 1, vc), ld_v(A.v, d, i, j, k + 1, vc), A.tdz);
+        }
+        double gp = 0.0;
+        if (fl & kQFace) {
+          const double pl = (A.fc[P3(d, i, j - 1, k)] & kFluid) ? A.p[P3(d, i, j - 1, k)] : 0.0;
+          const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
+          gp = grad_face(A.Gv[f], pl, A.Gv[NV + f], pr);
+        }
+        rhs = mom_rhs(A.a, A.rho, vc, conv, gp, A.bc[1][r], A.sc[1][r]);
+      }
+      A.b[1][r] = rhs;
+      A.x0[1][r] = A.zero_guess ? 0.0 : vc;
+    } else {  // w row: face (i, j, k+1)
+      const long r = t - A.nb[0] - A.nb[1];
+      const int i = (int)(r % d.nx);
+      const long q = r / d.nx;
+      const int j = (int)(q % d.ny), k = (int)(q / d.ny) + 1;
+      const long f = W3(d, i, j, k);
+      const uint8_t fl = A.fw[f];
+      const double wc = A.w[f];
+      double rhs = 0.0;
+      if (fl & kRhsRow) {
+        double conv = 0.0;
+        // the convection of w uses the mask one plane below (gpu_dense_ops.hpp:14)
+        if (A.fw[f - plane_w] & kActive) {
+          const double ua = avg4(ld_u(A.u, d, i, j, k - 1, 0.0), ld_u(A.u, d, i + 1, j, k - 1, 0.0),
+                                 ld_u(A.u, d, i, j, k, 0.0), ld_u(A.u, d, i + 1, j, k, 0.0));
+          const double va = avg4(ld_v(A.v, d, i, j, k - 1, 0.0), ld_v(A.v, d, i, j + 1, k - 1, 0.0),
+                                 ld_v(A.v, d, i, j, k, 0.0), ld_v(A.v, d, i, j + 1, k, 0.0));
+          conv = advect(ua, ld_w(A.w, d, i - 1, j, k, wc), ld_w(A.w, d, i + 1, j, k, wc), A.tdx, va,
+                        ld_w(A.w, d, i, j - 1, k, wc), ld_w(A.w, d, i, j + 1, k, wc), A.tdy, wc,
+                        ld_w(A.w, d, i, j, k - 1, wc), ld_w(A.w, d, i, j, k + 1, wc), A.tdz);
+        }
+        double gp = 0.0;
+        if (fl & kQFace) {
+          const double pl = (A.fc[P3(d, i, j, k - 1)] & kFluid) ? A.p[P3(d, i, j, k - 1)] : 0.0;
+          const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
+          gp = grad_face(A.Gw[f], pl, A.Gw[NW + f], pr);
+        }
+        rhs = mom_rhs(A.a, A.rho, wc, conv, gp, A.bc[2][r], A.sc[2][r]);
+      }
+      A.b[2][r] = rhs;
+      A.x0[2][r] = A.zero_guess ? 0.0 : wc;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ tilde
+// ut = u, interior faces <- solve-box x (gpu_dense_ops.hpp:20-22); flags non-finite x.
+__global__ void k_scatter(const double *u, const double *v, const double *w, const double *xu, const double *xv,
+                          const double *xw, double *ut, double *vt, double *wt, Dims d, StepDiag *dg) {
+  const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
+             NW = (long)d.nx * d.ny * (d.nz + 1);
+  int bad = 0;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < NU + NV + NW; t += (long)gridDim.x * blockDim.x) {
+    if (t < NU) {
+      const long f = t;
+      const int i = (int)(f % (d.nx + 1));
+      const long q = f / (d.nx + 1);
+      double val = u[f];
+      if (i >= 1 && i <= d.nx - 1) { val = xu[q * (d.nx - 1) + (i - 1)]; bad |= !isfinite(val); }
+      ut[f] = val;
+    } else if (t < NU + NV) {
+      const long f = t - NU;
+      const int i = (int)(f % d.nx);
+      const long q = f / d.nx;
+      const int j = (int)(q % (d.ny + 1)), k = (int)(q / (d.ny + 1));
+      double val = v[f];
+      if (j >= 1 && j <= d.ny - 1) { val = xv[((long)k * (d.ny - 1) + (j - 1)) * d.nx + i]; bad |= !isfinite(val); }
+      vt[f] = val;
+    } else {
+      const long f = t - NU - NV;
+      const long plane = (long)d.nx * d.ny;
+      const int k = (int)(f / plane);
+      double val = w[f];
+      if (k >= 1 && k <= d.nz - 1) { val = xw[f - plane]; bad |= !isfinite(val); }
+      wt[f] = val;
+    }
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&dg->nonfinite_mom, 1);
+}
+
+// ------------------------------------------------------------------ pressure RHS
+struct DivArgs {
+  Dims d;
+  const double *ut, *vt, *wt;
+  const uint8_t *fu, *fv, *fw, *fc;
+  const double *Dc;
+  const double *div_bc;
+  double *b, *x0;
+  double neg_a, ramp;
+};
+
+// D applied to the q-faces of a cell, as the reference's CSR row: fused
+// multiply-add chain in column order u_w, u_e, v_s, v_n, w_b, w_t.
+__device__ __forceinline__ double div_cell(const double *Dc, long NPc, long c, double qw, double qe, double qs,
+                                           double qn, double qb, double qt) {
+  double s = 0.0;
+  s = fma(Dc[c], qw, s);
+  s = fma(Dc[NPc + c], qe, s);
+  s = fma(Dc[2 * NPc + c], qs, s);
+  s = fma(Dc[3 * NPc + c], qn, s);
+  s = fma(Dc[4 * NPc + c], qb, s);
+  s = fma(Dc[5 * NPc + c], qt, s);
+  return s;
+}
+
+__global__ void __launch_bounds__(kThreads) k_pressure_rhs(DivArgs A) {
+  const Dims &d = A.d;
+  const long NP = (long)d.nx * d.ny * d.nz;
+  for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < NP; c += (long)gridDim.x * blockDim.x) {
+    double rhs = 0.0;
+    if (A.fc[c] & kFluid) {
+      const int i = (int)(c % d.nx);
+      const long q = c / d.nx;
+      const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+      const long fw_ = U3(d, i, j, k), fe = U3(d, i + 1, j, k);
+      const long fs = V3(d, i, j, k), fn = V3(d, i, j + 1, k);
+      const long fb = W3(d, i, j, k), ft = W3(d, i, j, k + 1);
+      const double s = div_cell(A.Dc, NP, c, (A.fu[fw_] & kQFace) ? A.ut[fw_] : 0.0,
+                                (A.fu[fe] & kQFace) ? A.ut[fe] : 0.0, (A.fv[fs] & kQFace) ? A.vt[fs] : 0.0,
+                                (A.fv[fn] & kQFace) ? A.vt[fn] : 0.0, (A.fw[fb] & kQFace) ? A.wt[fb] : 0.0,
+                                (A.fw[ft] & kQFace) ? A.wt[ft] : 0.0);
+      rhs = __dmul_rn(A.neg_a, fma(A.ramp, A.div_bc[c], s));
+    }
+    A.b[c] = rhs;
+    A.x0[c] = 0.0;
+  }
+}
+
+// ------------------------------------------------------------------ projection
+struct ProjArgs {
+  Dims d;
+  const double *ut, *vt, *wt, *phi;
+  double *u, *v, *w, *p;
+  const uint8_t *fu, *fv, *fw, *fc;
+  const double *Gu, *Gv, *Gw;
+  double factor;
+  StepDiag *dg;
+};
+
+__device__ __forceinline__ double phi_at(const ProjArgs &A, long c) { return (A.fc[c] & kFluid) ? A.phi[c] : 0.0; }
+
+// q = q~ - (dt/rho) G phi on q-faces, other faces keep q~; p += phi on fluid cells.
+__global__ void __launch_bounds__(kThreads) k_project(ProjArgs A) {
+  const Dims &d = A.d;
+  const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
+             NW = (long)d.nx * d.ny * (d.nz + 1), NP = (long)d.nx * d.ny * d.nz;
+  const double nf = -A.factor;
+  int bad = 0;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < NU + NV + NW + NP; t += (long)gridDim.x * blockDim.x) {
+    if (t < NU) {
+      const long f = t;
+      double val = A.ut[f];
+      if (A.fu[f] & kQFace) {
+        const int i = (int)(f % (d.nx + 1));
+        const long q = f / (d.nx + 1);
+        const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+        const double pl = i > 0 ? phi_at(A, P3(d, i - 1, j, k)) : 0.0;
+        const double pr = i < d.nx ? phi_at(A, P3(d, i, j, k)) : 0.0;
+        val = fma(nf, grad_face(A.Gu[f], pl, A.Gu[NU + f], pr), val);
+      }
+      A.u[f] = val;
+    } else if (t < NU + NV) {
+      const long f = t - NU;
+      double val = A.vt[f];
+      if (A.fv[f] & kQFace) {
+        const int i = (int)(f % d.nx);
+        const long q = f / d.nx;
+        const int j = (int)(q % (d.ny + 1)), k = (int)(q / (d.ny + 1));
+        const double pl = j > 0 ? phi_at(A, P3(d, i, j - 1, k)) : 0.0;
+        const double pr = j < d.ny ? phi_at(A, P3(d, i, j, k)) : 0.0;
+        val = fma(nf, grad_face(A.Gv[f], pl, A.Gv[NV + f], pr), val);
+      }
+      A.v[f] = val;
+    } else if (t < NU + NV + NW) {
+      const long f = t - NU - NV;
+      double val = A.wt[f];
+      if (A.fw[f] & kQFace) {
+        const long plane = (long)d.nx * d.ny;
+        const int k = (int)(f / plane);
+        const long c = f - (long)k * plane;
+        const double pl = k > 0 ? phi_at(A, c + (long)(k - 1) * plane) : 0.0;
+        const double pr = k < d.nz ? phi_at(A, c + (long)k * plane) : 0.0;
+        val = fma(nf, grad_face(A.Gw[f], pl, A.Gw[NW + f], pr), val);
+      }
+      A.w[f] = val;
+    } else {
+      const long c = t - NU - NV - NW;
+      bad |= !isfinite(A.phi[c]);
+      if (A.fc[c] & kFluid) A.p[c] = __dadd_rn(A.p[c], A.phi[c]);
+    }
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&A.dg->nonfinite_p, 1);
+}
+
+// ------------------------------------------------------------------ diagnostics
+struct DiagArgs {
+  Dims d;
+  const double *ut, *vt, *wt, *phi;
+  const double *u, *v, *w;
+  const uint8_t *fu, *fv, *fw, *fc;
+  const double *Gu, *Gv, *Gw, *Dc, *div_bc;
+  double factor, ramp;
+  double *part;
+  StepDiag *dg;
+  int np_active;
+};
+
+// Corrected q value of a face (recomputed: the stored field has had the BC applied).
+__device__ __forceinline__ double q_face(const DiagArgs &A, const double *qt, const uint8_t *fl, const double *G,
+                                         long NF, long f, double pl, double pr) {
+  if (!(fl[f] & kQFace)) return 0.0;
+  return fma(-A.factor, grad_face(G[f], pl, G[NF + f], pr), qt[f]);
+}
+
+__global__ void __launch_bounds__(kThreads) k_diagnostics(DiagArgs A) {
+  const Dims &d = A.d;
+  const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
+             NW = (long)d.nx * d.ny * (d.nz + 1), NP = (long)d.nx * d.ny * d.nz;
+  const long plane = (long)d.nx * d.ny;
+  double div2 = 0.0, um = 0.0, vm = 0.0, wm = 0.0;
+  auto ph = [&](long c) { return (A.fc[c] & kFluid) ? A.phi[c] : 0.0; };
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < NP + NU + NV + NW; t += (long)gridDim.x * blockDim.x) {
+    if (t < NP) {
+      const long c = t;
+      if (!(A.fc[c] & kFluid)) continue;
+      const int i = (int)(c % d.nx);
+      const long q = c / d.nx;
+      const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+      const double pc = ph(c);
+      const double pxm = i > 0 ? ph(c - 1) : 0.0, pxp = i < d.nx - 1 ? ph(c + 1) : 0.0;
+      const double pym = j > 0 ? ph(c - d.nx) : 0.0, pyp = j < d.ny - 1 ? ph(c + d.nx) : 0.0;
+      const double pzm = k > 0 ? ph(c - plane) : 0.0, pzp = k < d.nz - 1 ? ph(c + plane) : 0.0;
+      const double s = div_cell(A.Dc, NP, c,
+                                q_face(A, A.ut, A.fu, A.Gu, NU, U3(d, i, j, k), pxm, pc),
+                                q_face(A, A.ut, A.fu, A.Gu, NU, U3(d, i + 1, j, k), pc, pxp),
+                                q_face(A, A.vt, A.fv, A.Gv, NV, V3(d, i, j, k), pym, pc),
+                                q_face(A, A.vt, A.fv, A.Gv, NV, V3(d, i, j + 1, k), pc, pyp),
+                                q_face(A, A.wt, A.fw, A.Gw, NW, W3(d, i, j, k), pzm, pc),
+                                q_face(A, A.wt, A.fw, A.Gw, NW, W3(d, i, j, k + 1), pc, pzp));
+      const double dv = __dadd_rn(s, __dmul_rn(A.ramp, A.div_bc[c]));
+      div2 = __dadd_rn(div2, __dmul_rn(dv, dv));
+    } else if (t < NP + NU) {
+      um = fmax(um, fabs(A.u[t - NP]));
+    } else if (t < NP + NU + NV) {
+      vm = fmax(vm, fabs(A.v[t - NP - NU]));
+    } else {
+      wm = fmax(wm, fabs(A.w[t - NP - NU - NV]));
+    }
+  }
+  __shared__ double s[4][kWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  div2 = warp_sum(div2);
+  um = warp_max(um); vm = warp_max(vm); wm = warp_max(wm);
+  if (lane == 0) { s[0][warp] = div2; s[1][warp] = um; s[2][warp] = vm; s[3][warp] = wm; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0, c = 0.0, e = 0.0;
+    for (int q = 0; q < kWarps; ++q) { a += s[0][q]; b = fmax(b, s[1][q]); c = fmax(c, s[2][q]); e = fmax(e, s[3][q]); }
+    A.part[4 * blockIdx.x + 0] = a; A.part[4 * blockIdx.x + 1] = b;
+    A.part[4 * blockIdx.x + 2] = c; A.part[4 * blockIdx.x + 3] = e;
+  }
+  __threadfence();
+  __syncthreads();
+  __shared__ int last;
+  if (threadIdx.x == 0) last = (atomicAdd(&A.dg->ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0, c = 0.0, e = 0.0;
+    for (int q = 0; q < (int)gridDim.x; ++q) {
+      a += A.part[4 * q]; b = fmax(b, A.part[4 * q + 1]); c = fmax(c, A.part[4 * q + 2]); e = fmax(e, A.part[4 * q + 3]);
+    }
+    A.dg->div2 = a; A.dg->umax = b; A.dg->vmax = c; A.dg->wmax = e;
+    A.dg->ticket = 0;
+  }
+}
+
+Dims dims_of(const ibm_ctx *c) { return Dims{c->g.nx, c->g.ny, c->g.nz}; }
+
+int blocks_for(long n) {
+  long b = (n + kThreads - 1) / kThreads;
+  const long cap = (long)sm_count() * 8;
+  return (int)std::max(1L, std::min(b, cap));
+}
+
+}  // namespace
+
+void launch_bc(ibm_ctx *c, double *u, double *v, double *w, double ramp) {
+  const Dims d = dims_of(c);
+  const long n = std::max((long)d.ny * d.nz, std::max((long)d.nx * d.nz, (long)d.nx * d.ny));
+  k_bc_planes<<<(int)((n + kThreads - 1) / kThreads), kThreads, 0, c->st>>>(u, v, w, c->uin.p, ramp, d);
+  count_launch();
+  const long m = std::max((long)c->zl_u.n, std::max((long)c->zl_v.n, (long)c->zl_w.n));
+  if (m > 0) {
+    k_bc_zero<<<(int)((m + kThreads - 1) / kThreads), kThreads, 0, c->st>>>(u, c->zl_u.p, (int)c->zl_u.n, v, c->zl_v.p,
+                                                                            (int)c->zl_v.n, w, c->zl_w.p, (int)c->zl_w.n);
+    count_launch();
+  }
+}
+
+void launch_momentum_rhs(ibm_ctx *c) {
+  RhsArgs A;
+  A.d = dims_of(c);
+  A.u = c->u.p; A.v = c->v.p; A.w = c->w.p; A.p = c->p.p;
+  A.fu = c->fu.p; A.fv = c->fv.p; A.fw = c->fw.p; A.fc = c->fc.p;
+  A.Gu = c->Gu.p; A.Gv = c->Gv.p; A.Gw = c->Gw.p;
+  for (int f = 0; f < 3; ++f) {
+    A.sc[f] = c->scale_box[f].p; A.bc[f] = c->bc_box[f].p;
+    A.b[f] = c->bb[f].p; A.x0[f] = c->xb[f].p;
+  }
+  A.nb[0] = c->g.bu.n; A.nb[1] = c->g.bv.n; A.nb[2] = c->g.bw.n;
+  A.a = c->g.rho / c->g.dt;
+  A.rho = c->g.rho;
+  A.tdx = 2 * c->g.dx; A.tdy = 2 * c->g.dy; A.tdz = 2 * c->g.dz;
+  A.zero_guess = c->prm.use_zero_initial_guess != 0;
+  k_momentum_rhs<<<blocks_for(A.nb[0] + A.nb[1] + A.nb[2]), kThreads, 0, c->st>>>(A);
+  count_launch();
+}
+
+void launch_tilde(ibm_ctx *c, double ramp) {
+  const Dims d = dims_of(c);
+  k_scatter<<<blocks_for(c->g.NU + c->g.NV + c->g.NW), kThreads, 0, c->st>>>(
+      c->u.p, c->v.p, c->w.p, c->xb[0].p, c->xb[1].p, c->xb[2].p, c->ut.p, c->vt.p, c->wt.p, d, c->diag.p);
+  count_launch();
+  launch_bc(c, c->ut.p, c->vt.p, c->wt.p, ramp);
+}
+
+void launch_pressure_rhs(ibm_ctx *c, double ramp) {
+  DivArgs A;
+  A.d = dims_of(c);
+  A.ut = c->ut.p; A.vt = c->vt.p; A.wt = c->wt.p;
+  A.fu = c->fu.p; A.fv = c->fv.p; A.fw = c->fw.p; A.fc = c->fc.p;
+  A.Dc = c->Dc.p; A.div_bc = c->div_bc_cell.p;
+  A.b = c->bb[3].p; A.x0 = c->xb[3].p;
+  A.neg_a = -(c->g.rho / c->g.dt);
+  A.ramp = ramp;
+  k_pressure_rhs<<<blocks_for(c->g.NP), kThreads, 0, c->st>>>(A);
+  count_launch();
+}
+
+void launch_projection(ibm_ctx *c, double ramp) {
+  ProjArgs A;
+  A.d = dims_of(c);
+  A.ut = c->ut.p; A.vt = c->vt.p; A.wt = c->wt.p; A.phi = c->xb[3].p;
+  A.u = c->u.p; A.v = c->v.p; A.w = c->w.p; A.p = c->p.p;
+  A.fu = c->fu.p; A.fv = c->fv.p; A.fw = c->fw.p; A.fc = c->fc.p;
+  A.Gu = c->Gu.p; A.Gv = c->Gv.p; A.Gw = c->Gw.p;
+  A.factor = c->g.dt / c->g.rho;
+  A.dg = c->diag.p;
+  k_project<<<blocks_for(c->g.NU + c->g.NV + c->g.NW + c->g.NP), kThreads, 0, c->st>>>(A);
+  count_launch();
+  launch_bc(c, c->u.p, c->v.p, c->w.p, ramp);
+  DiagArgs D;
+  D.d = A.d;
+  D.ut = c->ut.p; D.vt = c->vt.p; D.wt = c->wt.p; D.phi = c->xb[3].p;
+  D.u = c->u.p; D.v = c->v.p; D.w = c->w.p;
+  D.fu = c->fu.p; D.fv = c->fv.p; D.fw = c->fw.p; D.fc = c->fc.p;
+  D.Gu = c->Gu.p; D.Gv = c->Gv.p; D.Gw = c->Gw.p; D.Dc = c->Dc.p; D.div_bc = c->div_bc_cell.p;
+  D.factor = A.factor;
+  D.ramp = ramp;
+  const int nb = std::min(blocks_for(c->g.NP + c->g.NU + c->g.NV + c->g.NW), 1024);
+  D.part = c->part.p;
+  D.dg = c->diag.p;
+  D.np_active = c->np_active;
+  k_diagnostics<<<nb, kThreads, 0, c->st>>>(D);
+  count_launch();
+}
+
+}  // namespace ibm

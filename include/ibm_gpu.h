@@ -1,0 +1,168 @@
+/*
+ * ibm_gpu.h — per-timestep solver of the immersed-boundary channel flow on
+ * one GB300 (hand-written sm_103a CUDA kernels behind a plain C ABI).
+ *
+ * This is the drop-in for the reference's hot path (main.cu:249-376): the
+ * convection / momentum right-hand side, the three momentum solves, the
+ * divergence / pressure right-hand side, the pressure Poisson solve, the
+ * projection and the per-step diagnostics. It replaces the reference's HYPRE
+ * Struct interface (hypre_struct_utils.hpp:1-26) and the HYPRE Struct GMRES /
+ * Jacobi / PFMG solvers it configures (main.cu:151-221), plus the dense
+ * kernels of gpu_dense_ops.hpp. Each entry point cites the call it replaces.
+ *
+ * Conventions (all entry points):
+ *  - return IBM_OK (0) on success; IBM_NOT_CONVERGED (1) is a non-fatal
+ *    warning mirroring HYPRE's error 256, which the reference accepts
+ *    (common.hpp:36-43); negative values are errors. Nothing aborts.
+ *  - a context owns every device buffer and one CUDA stream; all work is
+ *    issued on that stream. A context is not thread-safe; distinct contexts
+ *    are independent.
+ *  - array arguments may be host or device pointers (detected per call);
+ *    the context copies what it keeps. Field arrays use the reference's MAC
+ *    layouts, x fastest (common.hpp:230-238): u (nx+1)*ny*nz, v nx*(ny+1)*nz,
+ *    w nx*ny*(nz+1), p nx*ny*nz. Solve-box vectors use the Struct boxes of
+ *    main.cu:151: u (nx-1)*ny*nz, v nx*(ny-1)*nz, w nx*ny*(nz-1), p nx*ny*nz.
+ *  - ids are 1-based with 0 = inactive, as the reference builds them
+ *    (main.cu:73-81); id-indexed vectors have length count+1, index 0 unused.
+ */
+#ifndef IBM_GPU_H
+#define IBM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  IBM_OK = 0,
+  IBM_NOT_CONVERGED = 1,      /* solve stopped above tolerance (HYPRE 256) */
+  IBM_ERR_ARG = -1,
+  IBM_ERR_CUDA = -2,
+  IBM_ERR_NONFINITE = -3,     /* non-finite solve output (main.cu:302-305, 333-336) */
+  IBM_ERR_STATE = -4,         /* a required set_* call is missing */
+  IBM_ERR_NOMEM = -5,
+  IBM_ERR_UNSUPPORTED = -6    /* input not representable (e.g. off-stencil CSR entry) */
+};
+
+enum { IBM_FIELD_U = 0, IBM_FIELD_V = 1, IBM_FIELD_W = 2, IBM_FIELD_P = 3 };
+
+/* Grid and physics, from the reference's Params (common.hpp:45-66). */
+typedef struct ibm_grid_desc {
+  int nx, ny, nz;
+  double Lx, Ly, Lz;
+  double rho, nu, dt;
+  int device;
+} ibm_grid_desc;
+
+/* Solver options (the reference's solver flags, common.hpp:68-80, plus the
+ * choices this implementation adds). */
+typedef struct ibm_solver_params {
+  double vel_tol;        /* -vel-tol: relative residual of the momentum solves */
+  int vel_maxit;         /* -vel-maxit */
+  int vel_kdim;          /* -vel-kdim: GMRES restart length (<= 63) */
+  int vel_jacobi_iters;  /* -vel-jacobi-iters: Jacobi sweeps per preconditioner application */
+  double p_tol;          /* -p-tol */
+  int p_maxit;           /* -p-maxit */
+  int p_kdim;            /* -p-kdim (<= 63) */
+  int p_pc;              /* pressure preconditioner: 0 Jacobi, 1 semicoarsening multigrid */
+  int p_pc_maxit;        /* -p-pc-maxit: V-cycles per preconditioner application */
+  int p_pc_relax_type;   /* -p-pc-relax-type: 1 weighted Jacobi, 2 red-black Gauss-Seidel */
+  int p_pc_rap_type;     /* -p-pc-rap-type: 0 Galerkin (27-point coarse stencils), 1 collapsed 7-point */
+  int mg_nu1, mg_nu2;    /* pre/post relaxation sweeps per level */
+  double mg_omega;       /* weighted-Jacobi weight */
+  int mg_coarse_max;     /* coarsen until a level has at most this many points (dense solve there) */
+  int mg_max_levels;
+  int use_zero_initial_guess; /* -use-zero-initial-guess (momentum) */
+  int precision;         /* 0: FP64 throughout; 1: FP32 preconditioners inside FP64 flexible GMRES */
+  int use_graph;         /* 1: replay the step as a CUDA graph */
+  int vel_inner_sweeps;  /* precision 1: FP32 Jacobi sweeps per momentum preconditioner application */
+} ibm_solver_params;
+
+typedef struct ibm_solve_stats {
+  int iters;       /* HYPRE_StructGMRESGetNumIterations */
+  double rel_res;  /* HYPRE_StructGMRESGetFinalRelativeResidualNorm */
+  int status;      /* IBM_OK or IBM_NOT_CONVERGED */
+} ibm_solve_stats;
+
+/* One row of the reference's per-step table (main.cu:365-368) plus timings. */
+typedef struct ibm_step_stats {
+  double ramp;
+  ibm_solve_stats u, v, w, p;
+  double div_l2, umax, vmax, wmax;
+  double t_rhs_ms, t_mom_ms, t_p_ms, t_proj_ms, t_total_ms;
+  int status;
+} ibm_step_stats;
+
+typedef struct ibm_ctx ibm_ctx;
+
+/* Create a context on grid->device (replaces HYPRE_Initialize + grid/stencil
+ * creation, main.cu:16-18, hypre_struct_utils.hpp:1-11). */
+int ibm_create(const ibm_grid_desc *grid, ibm_ctx **out);
+void ibm_destroy(ibm_ctx *ctx);
+/* Text of the last error on this context (or of the last failed create). */
+const char *ibm_last_error(ibm_ctx *ctx);
+
+/* Operator of one field as the row-major 7-point Struct values the
+ * reference embeds (solver_helpers.hpp:51-84, 227-329): vals[7*row + s],
+ * s = C,-x,+x,-y,+y,-z,+z, on the field's solve box nbx*nby*nbz.
+ * Replaces HYPRE_StructMatrixSetBoxValues (hypre_struct_utils.hpp:12-18). */
+int ibm_set_operator(ibm_ctx *ctx, int field, const double *vals7, int nbx, int nby, int nbz);
+
+/* Masks and 1-based ids (main.cu:128-139 uploads). */
+int ibm_set_masks(ibm_ctx *ctx, const uint8_t *active_u, const uint8_t *active_v, const uint8_t *active_w,
+                  const uint8_t *fluid_p, const uint8_t *active_qu, const uint8_t *active_qv,
+                  const uint8_t *active_qw, const int32_t *id_u, const int32_t *id_v, const int32_t *id_w,
+                  const int32_t *id_p, const int32_t *id_qu, const int32_t *id_qv, const int32_t *id_qw);
+
+/* Row scales, boundary vectors (id-indexed, main.cu:140) and the inlet
+ * profile uin (ny*nz, at Um; main.cu:119). Requires ibm_set_masks first. */
+int ibm_set_aux(ibm_ctx *ctx, const double *scale_u, const double *scale_v, const double *scale_w,
+                const double *rhs_u_bc, const double *rhs_v_bc, const double *rhs_w_bc,
+                const double *div_bc_unit, const double *uin);
+
+/* Projection operators as 1-based CSR (build_managed_csr_1based,
+ * gpu_dense_ops.hpp:32-48): D is np x nq, G is nq x np, columns ascending.
+ * They are converted to structured per-cell / per-face coefficients; an entry
+ * that is not a face-neighbour coupling gives IBM_ERR_UNSUPPORTED. Requires
+ * ibm_set_masks first. */
+int ibm_set_projection_csr(ibm_ctx *ctx, const int32_t *D_rowptr, const int32_t *D_col, const double *D_val,
+                           int D_nrows, const int32_t *G_rowptr, const int32_t *G_col, const double *G_val,
+                           int G_nrows);
+
+/* Solver configuration (main.cu:173-221). */
+void ibm_solver_params_default(ibm_solver_params *p);
+int ibm_set_solver_params(ibm_ctx *ctx, const ibm_solver_params *p);
+int ibm_get_solver_params(ibm_ctx *ctx, ibm_solver_params *p);
+
+/* State fields (full MAC layouts). Either pointer may be NULL to skip it. */
+int ibm_set_fields(ibm_ctx *ctx, const double *u, const double *v, const double *w, const double *p);
+int ibm_get_fields(ibm_ctx *ctx, double *u, double *v, double *w, double *p);
+
+/* One timestep with inlet ramp factor `ramp` (main.cu:249-368). Returns the
+ * worst status of the four solves, or an error. */
+int ibm_step(ibm_ctx *ctx, double ramp, ibm_step_stats *stats);
+
+/* One solve on a field's solve box: x is the initial guess in, the solution
+ * out (HYPRE_StructGMRESSolve, main.cu:284-286, 327). */
+int ibm_solve(ibm_ctx *ctx, int field, const double *b, double *x, ibm_solve_stats *stats);
+
+/* y = A x with the field's operator on its solve box (HYPRE StructMatvec). */
+int ibm_apply_operator(ibm_ctx *ctx, int field, const double *x, double *y);
+
+/* The last right-hand side (which = 0) or solution (which = 1) of a field's
+ * solve box, as HYPRE_StructVectorGetBoxValues returns the reference's
+ * b/x vectors (hypre_struct_utils.hpp:23-24, main.cu:298-300, 332). */
+int ibm_get_solver_vector(ibm_ctx *ctx, int field, int which, double *out);
+
+int ibm_synchronize(ibm_ctx *ctx);
+void *ibm_stream(ibm_ctx *ctx);            /* the context's cudaStream_t */
+long long ibm_kernel_launches(ibm_ctx *ctx); /* kernels this context has launched */
+/* Name and compute capability of a device, for logs. */
+int ibm_device_query(int device, char *buf, int len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IBM_GPU_H */

@@ -1,0 +1,892 @@
+/*
+ * ibm_oracle.c — CPU oracle for the per-timestep hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path (see ibm_oracle.h).
+ * Only tests, the smoke check and the benchmark's CPU-baseline leg load it.
+ *
+ * Floating-point evaluation order is spelled out explicitly (fma() where a
+ * fused multiply-add is meant, separate operations otherwise) and the file is
+ * built with -ffp-contract=off, so the results are the same on every host.
+ * Dot products are summed over fixed 4096-row chunks, then the chunk sums in
+ * order, so results do not depend on the thread count.
+ */
+#include "ibm_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define CHUNK 4096L
+
+typedef struct { int n[3]; long N; } box3;
+
+typedef struct {
+  box3 b;
+  int cdir;                 /* direction coarsened to reach the next level, -1 on the coarsest */
+  double *A;                /* [N][27], slot = (ox+1) + 3(oy+1) + 9(oz+1) */
+  double *wd;               /* omega / diag */
+  double *invd;             /* 1 / diag */
+  double *pm, *pp;          /* interpolation weights at points odd along cdir */
+  double *bv, *xv, *rv;     /* work vectors */
+  double *dense_inv;        /* coarsest: explicit inverse [N][N] */
+} mg_level;
+
+struct oracle {
+  oracle_params prm;
+  oracle_inputs in;
+  int nx, ny, nz;
+  double dx, dy, dz;
+  int nU, nV, nW, nP, nQu, nQv, nQw, nQ;
+  box3 bu, bv, bw, bp;
+  double *u, *v, *w, *p;
+  double *invd[4];          /* Jacobi inverse diagonals of the four operators */
+  int mg_built;
+  int nlev;
+  mg_level lev[40];
+};
+
+/* ------------------------------------------------------------------------ */
+/* small helpers                                                             */
+/* ------------------------------------------------------------------------ */
+static void *xcalloc(size_t n, size_t s) {
+  void *p = calloc(n ? n : 1, s);
+  if (!p) { fprintf(stderr, "oracle: out of memory\n"); abort(); }
+  return p;
+}
+static int max_id(const int32_t *id, long n) {
+  int m = 0;
+  for (long i = 0; i < n; ++i) if (id[i] > m) m = id[i];
+  return m;
+}
+static double dot(const double *a, const double *b, long n) {
+  long nch = (n + CHUNK - 1) / CHUNK;
+  double *part = (double *)xcalloc((size_t)nch, sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < nch; ++c) {
+    long lo = c * CHUNK, hi = lo + CHUNK < n ? lo + CHUNK : n;
+    double s = 0.0;
+    for (long i = lo; i < hi; ++i) s = fma(a[i], b[i], s);
+    part[c] = s;
+  }
+  double s = 0.0;
+  for (long c = 0; c < nch; ++c) s += part[c];
+  free(part);
+  return s;
+}
+static long U3(const oracle *o, int i, int j, int k) { return ((long)k * o->ny + j) * (o->nx + 1) + i; }
+static long V3(const oracle *o, int i, int j, int k) { return ((long)k * (o->ny + 1) + j) * o->nx + i; }
+static long W3(const oracle *o, int i, int j, int k) { return ((long)k * o->ny + j) * o->nx + i; }
+
+static const double *op_vals(const oracle *o, int f) {
+  return f == 0 ? o->in.Au : f == 1 ? o->in.Av : f == 2 ? o->in.Aw : o->in.Ap;
+}
+static const box3 *op_box(const oracle *o, int f) {
+  return f == 0 ? &o->bu : f == 1 ? &o->bv : f == 2 ? &o->bw : &o->bp;
+}
+
+/* y = A x for a 7-point row-major operator; accumulation order C,-x,+x,-y,+y,-z,+z */
+static void spmv7(const box3 *b, const double *A, const double *x, double *y) {
+  const int nx = b->n[0], ny = b->n[1], nz = b->n[2];
+  const long sy = nx, sz = (long)nx * ny;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        long r = k * sz + j * sy + i;
+        const double *a = A + 7 * r;
+        double acc = 0.0;
+        acc = fma(a[0], x[r], acc);
+        acc = fma(a[1], i > 0 ? x[r - 1] : 0.0, acc);
+        acc = fma(a[2], i < nx - 1 ? x[r + 1] : 0.0, acc);
+        acc = fma(a[3], j > 0 ? x[r - sy] : 0.0, acc);
+        acc = fma(a[4], j < ny - 1 ? x[r + sy] : 0.0, acc);
+        acc = fma(a[5], k > 0 ? x[r - sz] : 0.0, acc);
+        acc = fma(a[6], k < nz - 1 ? x[r + sz] : 0.0, acc);
+        y[r] = acc;
+      }
+}
+
+/* y = A x for a 27-point operator stored [N][27]; accumulation in slot order */
+static void spmv27(const box3 *b, const double *A, const double *x, double *y) {
+  const int nx = b->n[0], ny = b->n[1], nz = b->n[2];
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        long r = ((long)k * ny + j) * nx + i;
+        const double *a = A + 27 * r;
+        double acc = 0.0;
+        for (int s = 0; s < 27; ++s) {
+          int ox = s % 3 - 1, oy = (s / 3) % 3 - 1, oz = s / 9 - 1;
+          int ii = i + ox, jj = j + oy, kk = k + oz;
+          double xv = (ii >= 0 && ii < nx && jj >= 0 && jj < ny && kk >= 0 && kk < nz)
+                          ? x[((long)kk * ny + jj) * nx + ii] : 0.0;
+          acc = fma(a[s], xv, acc);
+        }
+        y[r] = acc;
+      }
+}
+
+/* ------------------------------------------------------------------------ */
+/* dense per-step operations (gpu_dense_ops.hpp semantics)                   */
+/* ------------------------------------------------------------------------ */
+
+/* BC cleanup in the order of the CPU twin (immersed_operators.hpp:1036-1053):
+ * boundary planes first (the outlet copies u[nx-1] before any zeroing), then
+ * inactive interior faces. Inactive w faces use the mask one plane below, as
+ * the device kernel does (gpu_dense_ops.hpp:9); the masks are z-invariant. */
+void oracle_bc_cleanup(const oracle *o, double *u, double *v, double *w, const double *uin_step) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j) {
+      u[U3(o, 0, j, k)] = uin_step[j + (long)ny * k];
+      u[U3(o, nx, j, k)] = u[U3(o, nx - 1, j, k)];
+    }
+  for (int k = 0; k < nz; ++k)
+    for (int i = 0; i < nx; ++i) { v[V3(o, i, 0, k)] = 0.0; v[V3(o, i, ny, k)] = 0.0; }
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) { w[W3(o, i, j, 0)] = 0.0; w[W3(o, i, j, nz)] = 0.0; }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 1; i < nx; ++i)
+        if (!o->in.active_u[U3(o, i, j, k)]) u[U3(o, i, j, k)] = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 1; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        if (!o->in.active_v[V3(o, i, j, k)]) v[V3(o, i, j, k)] = 0.0;
+  for (int k = 1; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        if (!o->in.active_w[W3(o, i, j, k - 1)]) w[W3(o, i, j, k)] = 0.0;
+}
+
+static double uval(const oracle *o, const double *u, int i, int j, int k, double fb) {
+  if (i < 0 || i > o->nx || j < 0 || j >= o->ny || k < 0 || k >= o->nz) return fb;
+  return u[U3(o, i, j, k)];
+}
+static double vval(const oracle *o, const double *v, int i, int j, int k, double fb) {
+  if (i < 0 || i >= o->nx || j < 0 || j > o->ny || k < 0 || k >= o->nz) return fb;
+  return v[V3(o, i, j, k)];
+}
+static double wval(const oracle *o, const double *w, int i, int j, int k, double fb) {
+  if (i < 0 || i >= o->nx || j < 0 || j >= o->ny || k < 0 || k > o->nz) return fb;
+  return w[W3(o, i, j, k)];
+}
+
+/* Centred advective form (gpu_dense_ops.hpp:12-14; immersed_operators.hpp:990-1034). */
+void oracle_convection(const oracle *o, const double *u, const double *v, const double *w,
+                       double *cu, double *cv, double *cw) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const double tdx = 2 * o->dx, tdy = 2 * o->dy, tdz = 2 * o->dz;
+  memset(cu, 0, sizeof(double) * (size_t)(nx + 1) * ny * nz);
+  memset(cv, 0, sizeof(double) * (size_t)nx * (ny + 1) * nz);
+  memset(cw, 0, sizeof(double) * (size_t)nx * ny * (nz + 1));
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 1; i < nx; ++i) {
+        if (!o->in.active_u[U3(o, i, j, k)]) continue;
+        double uc = u[U3(o, i, j, k)];
+        double va = 0.25 * (vval(o, v, i - 1, j, k, 0.0) + vval(o, v, i - 1, j + 1, k, 0.0) +
+                            vval(o, v, i, j, k, 0.0) + vval(o, v, i, j + 1, k, 0.0));
+        double wa = 0.25 * (wval(o, w, i - 1, j, k, 0.0) + wval(o, w, i - 1, j, k + 1, 0.0) +
+                            wval(o, w, i, j, k, 0.0) + wval(o, w, i, j, k + 1, 0.0));
+        double ue = uval(o, u, i + 1, j, k, uc), uw = uval(o, u, i - 1, j, k, uc);
+        double un = uval(o, u, i, j + 1, k, uc), us = uval(o, u, i, j - 1, k, uc);
+        double ut = uval(o, u, i, j, k + 1, uc), ub = uval(o, u, i, j, k - 1, uc);
+        cu[U3(o, i, j, k)] = uc * (ue - uw) / tdx + va * (un - us) / tdy + wa * (ut - ub) / tdz;
+      }
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 1; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        if (!o->in.active_v[V3(o, i, j, k)]) continue;
+        double vc = v[V3(o, i, j, k)];
+        double ua = 0.25 * (uval(o, u, i, j - 1, k, 0.0) + uval(o, u, i + 1, j - 1, k, 0.0) +
+                            uval(o, u, i, j, k, 0.0) + uval(o, u, i + 1, j, k, 0.0));
+        double wa = 0.25 * (wval(o, w, i, j - 1, k, 0.0) + wval(o, w, i, j, k, 0.0) +
+                            wval(o, w, i, j - 1, k + 1, 0.0) + wval(o, w, i, j, k + 1, 0.0));
+        double ve = vval(o, v, i + 1, j, k, vc), vw = vval(o, v, i - 1, j, k, vc);
+        double vn = vval(o, v, i, j + 1, k, vc), vs = vval(o, v, i, j - 1, k, vc);
+        double vt = vval(o, v, i, j, k + 1, vc), vb = vval(o, v, i, j, k - 1, vc);
+        cv[V3(o, i, j, k)] = ua * (ve - vw) / tdx + vc * (vn - vs) / tdy + wa * (vt - vb) / tdz;
+      }
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        if (!o->in.active_w[W3(o, i, j, k - 1)]) continue;
+        double wc = w[W3(o, i, j, k)];
+        double ua = 0.25 * (uval(o, u, i, j, k - 1, 0.0) + uval(o, u, i + 1, j, k - 1, 0.0) +
+                            uval(o, u, i, j, k, 0.0) + uval(o, u, i + 1, j, k, 0.0));
+        double va = 0.25 * (vval(o, v, i, j, k - 1, 0.0) + vval(o, v, i, j + 1, k - 1, 0.0) +
+                            vval(o, v, i, j, k, 0.0) + vval(o, v, i, j + 1, k, 0.0));
+        double we = wval(o, w, i + 1, j, k, wc), ww = wval(o, w, i - 1, j, k, wc);
+        double wn = wval(o, w, i, j + 1, k, wc), ws = wval(o, w, i, j - 1, k, wc);
+        double wt = wval(o, w, i, j, k + 1, wc), wb = wval(o, w, i, j, k - 1, wc);
+        cw[W3(o, i, j, k)] = ua * (we - ww) / tdx + va * (wn - ws) / tdy + wc * (wt - wb) / tdz;
+      }
+}
+
+/* y[row] = sum over the sorted CSR row of val * x[col], as a fused multiply-add
+ * chain in column order (gpu_dense_ops.hpp:61-68); x and y are 1-based. */
+static void csr_apply(const int32_t *rp, const int32_t *col, const double *val, long nrows,
+                      const double *x, double *y) {
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < nrows; ++r) {
+    double s = 0.0;
+    for (int t = rp[r]; t < rp[r + 1]; ++t) s = fma(val[t], x[col[t]], s);
+    y[r + 1] = s;
+  }
+}
+
+/* G p unpacked onto the three face arrays (gpu_dense_ops.hpp:70-78). */
+static void gradient_faces(const oracle *o, const double *p, double *gx, double *gy, double *gz) {
+  const long NP = (long)o->nx * o->ny * o->nz;
+  double *pv = (double *)xcalloc((size_t)o->nP + 1, sizeof(double));
+  double *gp = (double *)xcalloc((size_t)o->nQ + 1, sizeof(double));
+  for (long c = 0; c < NP; ++c)
+    if (o->in.fluid_p[c] && o->in.id_p[c] > 0) pv[o->in.id_p[c]] = p[c];
+  csr_apply(o->in.G_rowptr, o->in.G_col, o->in.G_val, o->nQ, pv, gp);
+  const long NU = (long)(o->nx + 1) * o->ny * o->nz, NV = (long)o->nx * (o->ny + 1) * o->nz,
+             NW = (long)o->nx * o->ny * (o->nz + 1);
+  for (long f = 0; f < NU; ++f) { int id = o->in.id_qu[f]; gx[f] = id > 0 ? gp[id] : 0.0; }
+  for (long f = 0; f < NV; ++f) { int id = o->in.id_qv[f]; gy[f] = id > 0 ? gp[o->nQu + id] : 0.0; }
+  for (long f = 0; f < NW; ++f) { int id = o->in.id_qw[f]; gz[f] = id > 0 ? gp[o->nQu + o->nQv + id] : 0.0; }
+  free(pv); free(gp);
+}
+
+/* rhs = ((rho/dt) u - rho conv - gp + rhs_bc[id]) scale[id] on active faces
+ * (gpu_dense_ops.hpp:16-18), each operation rounded separately. */
+static double mom_rhs(double a, double rho, double uc, double conv, double gp, double bc, double sc) {
+  double t = a * uc;
+  double t2 = rho * conv;
+  t = t - t2;
+  t = t - gp;
+  t = t + bc;
+  return t * sc;
+}
+
+void oracle_momentum_rhs(const oracle *o, const double *u, const double *v, const double *w, const double *p,
+                         double *bu, double *bv, double *bw) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const long NU = (long)(nx + 1) * ny * nz, NV = (long)nx * (ny + 1) * nz, NW = (long)nx * ny * (nz + 1);
+  double *cu = (double *)xcalloc((size_t)NU, 8), *cv = (double *)xcalloc((size_t)NV, 8), *cw = (double *)xcalloc((size_t)NW, 8);
+  double *gx = (double *)xcalloc((size_t)NU, 8), *gy = (double *)xcalloc((size_t)NV, 8), *gz = (double *)xcalloc((size_t)NW, 8);
+  oracle_convection(o, u, v, w, cu, cv, cw);
+  gradient_faces(o, p, gx, gy, gz);
+  const double rho = o->prm.rho, a = o->prm.rho / o->prm.dt;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 1; i < nx; ++i) {
+        long f = U3(o, i, j, k), r = ((long)k * ny + j) * (nx - 1) + (i - 1);
+        int id = o->in.id_u[f];
+        bu[r] = (id > 0 && o->in.active_u[f]) ? mom_rhs(a, rho, u[f], cu[f], gx[f], o->in.rhs_u_bc[id], o->in.scale_u[id]) : 0.0;
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 1; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        long f = V3(o, i, j, k), r = ((long)k * (ny - 1) + (j - 1)) * nx + i;
+        int id = o->in.id_v[f];
+        bv[r] = (id > 0 && o->in.active_v[f]) ? mom_rhs(a, rho, v[f], cv[f], gy[f], o->in.rhs_v_bc[id], o->in.scale_v[id]) : 0.0;
+      }
+  for (int k = 1; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        long f = W3(o, i, j, k), r = ((long)(k - 1) * ny + j) * nx + i;
+        int id = o->in.id_w[f];
+        bw[r] = (id > 0 && o->in.active_w[f]) ? mom_rhs(a, rho, w[f], cw[f], gz[f], o->in.rhs_w_bc[id], o->in.scale_w[id]) : 0.0;
+      }
+  free(cu); free(cv); free(cw); free(gx); free(gy); free(gz);
+}
+
+/* Pack the q-active faces (gpu_dense_ops.hpp:80-85) into a 1-based vector. */
+static void pack_q(const oracle *o, const double *u, const double *v, const double *w, double *q) {
+  const long NU = (long)(o->nx + 1) * o->ny * o->nz, NV = (long)o->nx * (o->ny + 1) * o->nz,
+             NW = (long)o->nx * o->ny * (o->nz + 1);
+  memset(q, 0, sizeof(double) * ((size_t)o->nQ + 1));
+  for (long f = 0; f < NU; ++f) { int id = o->in.id_qu[f]; if (id > 0) q[id] = u[f]; }
+  for (long f = 0; f < NV; ++f) { int id = o->in.id_qv[f]; if (id > 0) q[o->nQu + id] = v[f]; }
+  for (long f = 0; f < NW; ++f) { int id = o->in.id_qw[f]; if (id > 0) q[o->nQu + o->nQv + id] = w[f]; }
+}
+
+/* b_p = -(rho/dt) (D q~ + ramp div_bc) on fluid cells (gpu_dense_ops.hpp:87-90). */
+void oracle_pressure_rhs(const oracle *o, const double *ut, const double *vt, const double *wt, double ramp,
+                         double *bp) {
+  const long NP = (long)o->nx * o->ny * o->nz;
+  double *q = (double *)xcalloc((size_t)o->nQ + 1, 8), *dq = (double *)xcalloc((size_t)o->nP + 1, 8);
+  pack_q(o, ut, vt, wt, q);
+  csr_apply(o->in.D_rowptr, o->in.D_col, o->in.D_val, o->nP, q, dq);
+  const double na = -(o->prm.rho / o->prm.dt);
+  for (long c = 0; c < NP; ++c) {
+    int id = o->in.id_p[c];
+    double r = 0.0;
+    if (o->in.fluid_p[c] && id > 0) r = na * fma(ramp, o->in.div_bc_unit[id], dq[id]);
+    bp[c] = r;
+  }
+  free(q); free(dq);
+}
+
+void oracle_apply_operator(const oracle *o, int field, const double *x, double *y) {
+  spmv7(op_box(o, field), op_vals(o, field), x, y);
+}
+
+/* ------------------------------------------------------------------------ */
+/* semicoarsening multigrid (PFMG-style: one direction per level,            */
+/* operator-dependent interpolation, R = P^T, Galerkin coarse operators)     */
+/* ------------------------------------------------------------------------ */
+static const int k7to27[7] = {13, 12, 14, 10, 16, 4, 22};
+static int slot_off(int s, int d) { return d == 0 ? s % 3 - 1 : d == 1 ? (s / 3) % 3 - 1 : s / 9 - 1; }
+
+static void mg_interp_weights(mg_level *L) {
+  const int d = L->cdir;
+  L->pm = (double *)xcalloc((size_t)L->b.N, 8);
+  L->pp = (double *)xcalloc((size_t)L->b.N, 8);
+  for (long r = 0; r < L->b.N; ++r) {
+    const double *a = L->A + 27 * r;
+    double c0 = 0.0, cm = 0.0, cp = 0.0;
+    for (int s = 0; s < 27; ++s) {
+      int od = slot_off(s, d);
+      if (od == 0) c0 += a[s]; else if (od < 0) cm += a[s]; else cp += a[s];
+    }
+    if (c0 != 0.0) { L->pm[r] = -cm / c0; L->pp[r] = -cp / c0; }
+  }
+}
+
+static long lidx(const box3 *b, int i, int j, int k) { return ((long)k * b->n[1] + j) * b->n[0] + i; }
+
+/* Coarse operator R A P for coarsening in direction d: each coarse point sums,
+ * in a fixed order, over the three fine points it restricts from, their
+ * stencil entries, and the coarse points interpolating each neighbour. */
+static void mg_rap(const mg_level *F, mg_level *C) {
+  const int d = F->cdir;
+  const box3 *fb = &F->b, *cb = &C->b;
+  C->A = (double *)xcalloc((size_t)cb->N * 27, 8);
+#pragma omp parallel for schedule(static)
+  for (long I = 0; I < cb->N; ++I) {
+    int ci[3] = {(int)(I % cb->n[0]), (int)((I / cb->n[0]) % cb->n[1]), (int)(I / ((long)cb->n[0] * cb->n[1]))};
+    double *ac = C->A + 27 * I;
+    for (int fo = -1; fo <= 1; ++fo) {
+      int f[3] = {ci[0], ci[1], ci[2]};
+      f[d] = 2 * ci[d] + fo;
+      if (f[d] < 0 || f[d] >= fb->n[d]) continue;
+      long fr = lidx(fb, f[0], f[1], f[2]);
+      double rw = fo == 0 ? 1.0 : (fo < 0 ? F->pp[fr] : F->pm[fr]);
+      if (rw == 0.0) continue;
+      const double *af = F->A + 27 * fr;
+      for (int s = 0; s < 27; ++s) {
+        if (af[s] == 0.0) continue;
+        int g[3] = {f[0] + slot_off(s, 0), f[1] + slot_off(s, 1), f[2] + slot_off(s, 2)};
+        if (g[0] < 0 || g[0] >= fb->n[0] || g[1] < 0 || g[1] >= fb->n[1] || g[2] < 0 || g[2] >= fb->n[2]) continue;
+        long gr = lidx(fb, g[0], g[1], g[2]);
+        double ra = rw * af[s];
+        int jc[2]; double pw[2]; int nt = 0;
+        if ((g[d] & 1) == 0) { jc[0] = g[d] / 2; pw[0] = 1.0; nt = 1; }
+        else {
+          jc[0] = (g[d] - 1) / 2; pw[0] = F->pm[gr]; nt = 1;
+          if ((g[d] + 1) / 2 < cb->n[d]) { jc[1] = (g[d] + 1) / 2; pw[1] = F->pp[gr]; nt = 2; }
+        }
+        for (int t = 0; t < nt; ++t) {
+          if (pw[t] == 0.0) continue;
+          int o3[3] = {slot_off(s, 0), slot_off(s, 1), slot_off(s, 2)};
+          o3[d] = jc[t] - ci[d];
+          int sc = (o3[0] + 1) + 3 * (o3[1] + 1) + 9 * (o3[2] + 1);
+          ac[sc] = ac[sc] + ra * pw[t];
+        }
+      }
+    }
+  }
+}
+
+/* Collapse a 27-point stencil to 7 points keeping the action on constants and
+ * on linear functions: an entry at offset o with m nonzero components moves to
+ * the m axis neighbours along those components and is removed m-1 times from
+ * the centre. */
+static void mg_collapse7(mg_level *L) {
+  for (long r = 0; r < L->b.N; ++r) {
+    double *a = L->A + 27 * r;
+    for (int s = 0; s < 27; ++s) {
+      int o3[3] = {slot_off(s, 0), slot_off(s, 1), slot_off(s, 2)};
+      int m = (o3[0] != 0) + (o3[1] != 0) + (o3[2] != 0);
+      if (m < 2 || a[s] == 0.0) continue;
+      double e = a[s];
+      a[s] = 0.0;
+      for (int dd = 0; dd < 3; ++dd) {
+        if (!o3[dd]) continue;
+        int q[3] = {0, 0, 0};
+        q[dd] = o3[dd];
+        int sq = (q[0] + 1) + 3 * (q[1] + 1) + 9 * (q[2] + 1);
+        a[sq] = a[sq] + e;
+      }
+      a[13] = a[13] - (double)(m - 1) * e;
+    }
+  }
+}
+
+static void mg_finish_level(const oracle *o, mg_level *L) {
+  L->invd = (double *)xcalloc((size_t)L->b.N, 8);
+  L->wd = (double *)xcalloc((size_t)L->b.N, 8);
+  for (long r = 0; r < L->b.N; ++r) {
+    double dgl = L->A[27 * r + 13];
+    L->invd[r] = dgl != 0.0 ? 1.0 / dgl : 0.0;
+    L->wd[r] = o->prm.mg_omega * L->invd[r];
+  }
+  L->bv = (double *)xcalloc((size_t)L->b.N, 8);
+  L->xv = (double *)xcalloc((size_t)L->b.N, 8);
+  L->rv = (double *)xcalloc((size_t)L->b.N, 8);
+}
+
+/* Explicit inverse by Gauss-Jordan elimination with partial pivoting. */
+static void dense_inverse(const double *A27, const box3 *b, double *inv) {
+  const long n = b->N;
+  double *M = (double *)xcalloc((size_t)(n * n), 8);
+  for (long r = 0; r < n; ++r) {
+    int i = (int)(r % b->n[0]), j = (int)((r / b->n[0]) % b->n[1]), k = (int)(r / ((long)b->n[0] * b->n[1]));
+    for (int s = 0; s < 27; ++s) {
+      int ii = i + slot_off(s, 0), jj = j + slot_off(s, 1), kk = k + slot_off(s, 2);
+      if (ii < 0 || ii >= b->n[0] || jj < 0 || jj >= b->n[1] || kk < 0 || kk >= b->n[2]) continue;
+      M[r * n + lidx(b, ii, jj, kk)] += A27[27 * r + s];
+    }
+  }
+  for (long r = 0; r < n; ++r)
+    for (long c = 0; c < n; ++c) inv[r * n + c] = (r == c) ? 1.0 : 0.0;
+  for (long c = 0; c < n; ++c) {
+    long piv = c;
+    for (long r = c + 1; r < n; ++r) if (fabs(M[r * n + c]) > fabs(M[piv * n + c])) piv = r;
+    if (piv != c)
+      for (long t = 0; t < n; ++t) {
+        double x = M[c * n + t]; M[c * n + t] = M[piv * n + t]; M[piv * n + t] = x;
+        x = inv[c * n + t]; inv[c * n + t] = inv[piv * n + t]; inv[piv * n + t] = x;
+      }
+    double pv = M[c * n + c];
+    if (pv == 0.0) continue;
+    double ip = 1.0 / pv;
+    for (long t = 0; t < n; ++t) { M[c * n + t] *= ip; inv[c * n + t] *= ip; }
+    for (long r = 0; r < n; ++r) {
+      if (r == c) continue;
+      double f = M[r * n + c];
+      if (f == 0.0) continue;
+      for (long t = 0; t < n; ++t) { M[r * n + t] -= f * M[c * n + t]; inv[r * n + t] -= f * inv[c * n + t]; }
+    }
+  }
+  free(M);
+}
+
+static void mg_build(oracle *o) {
+  if (o->mg_built) return;
+  mg_level *L0 = &o->lev[0];
+  L0->b = o->bp;
+  L0->A = (double *)xcalloc((size_t)L0->b.N * 27, 8);
+  for (long r = 0; r < L0->b.N; ++r)
+    for (int s = 0; s < 7; ++s) L0->A[27 * r + k7to27[s]] = o->in.Ap[7 * r + s];
+  double h[3] = {o->dx, o->dy, o->dz};
+  int l = 0;
+  for (;;) {
+    mg_level *F = &o->lev[l];
+    mg_finish_level(o, F);
+    int d = -1;
+    for (int dd = 0; dd < 3; ++dd)
+      if (F->b.n[dd] > 1 && (d < 0 || h[dd] < h[d])) d = dd;
+    if (F->b.N <= o->prm.mg_coarse_max || l + 1 >= o->prm.mg_max_levels || d < 0 || l + 1 >= 40) {
+      F->cdir = -1;
+      F->dense_inv = (double *)xcalloc((size_t)(F->b.N * F->b.N), 8);
+      dense_inverse(F->A, &F->b, F->dense_inv);
+      break;
+    }
+    F->cdir = d;
+    h[d] *= 2.0;
+    mg_interp_weights(F);
+    mg_level *C = &o->lev[l + 1];
+    C->b = F->b;
+    C->b.n[d] = (F->b.n[d] + 1) / 2;
+    C->b.N = (long)C->b.n[0] * C->b.n[1] * C->b.n[2];
+    mg_rap(F, C);
+    if (o->prm.mg_rap == 1) mg_collapse7(C);
+    ++l;
+  }
+  o->nlev = l + 1;
+  o->mg_built = 1;
+}
+
+/* One relaxation sweep; zero_guess: x starts from 0. */
+static void mg_relax(const oracle *o, const mg_level *L, const double *b, double *x, int zero_guess) {
+  const long N = L->b.N;
+  if (o->prm.mg_relax == 2) {
+    /* two-colour relaxation: in each colour phase the points of that colour
+     * update from the values at the start of the phase */
+    if (zero_guess) memset(x, 0, sizeof(double) * (size_t)N);
+    double *snap = (double *)xcalloc((size_t)N, 8);
+    for (int color = 0; color < 2; ++color) {
+      memcpy(snap, x, sizeof(double) * (size_t)N);
+      for (long r = 0; r < N; ++r) {
+        int i = (int)(r % L->b.n[0]), j = (int)((r / L->b.n[0]) % L->b.n[1]), k = (int)(r / ((long)L->b.n[0] * L->b.n[1]));
+        if (((i + j + k) & 1) != color) continue;
+        const double *a = L->A + 27 * r;
+        double acc = 0.0;
+        for (int s = 0; s < 27; ++s) {
+          int ii = i + slot_off(s, 0), jj = j + slot_off(s, 1), kk = k + slot_off(s, 2);
+          double xv = (ii >= 0 && ii < L->b.n[0] && jj >= 0 && jj < L->b.n[1] && kk >= 0 && kk < L->b.n[2]) ? snap[lidx(&L->b, ii, jj, kk)] : 0.0;
+          acc = fma(a[s], xv, acc);
+        }
+        x[r] = fma(L->invd[r], b[r] - acc, snap[r]);
+      }
+    }
+    free(snap);
+    return;
+  }
+  if (zero_guess) {
+    for (long r = 0; r < N; ++r) x[r] = L->wd[r] * b[r];
+    return;
+  }
+  double *ax = (double *)xcalloc((size_t)N, 8);
+  spmv27(&L->b, L->A, x, ax);
+  for (long r = 0; r < N; ++r) x[r] = fma(L->wd[r], b[r] - ax[r], x[r]);
+  free(ax);
+}
+
+static void mg_cycle(oracle *o, int l, const double *b, double *x) {
+  mg_level *L = &o->lev[l];
+  const long N = L->b.N;
+  if (L->cdir < 0) {
+    for (long r = 0; r < N; ++r) {
+      double acc = 0.0;
+      for (long c = 0; c < N; ++c) acc = fma(L->dense_inv[r * N + c], b[c], acc);
+      x[r] = acc;
+    }
+    return;
+  }
+  for (int s = 0; s < o->prm.mg_nu1; ++s) mg_relax(o, L, b, x, s == 0);
+  if (o->prm.mg_nu1 == 0) memset(x, 0, sizeof(double) * (size_t)N);
+  double *ax = L->rv;
+  spmv27(&L->b, L->A, x, ax);
+  for (long r = 0; r < N; ++r) ax[r] = b[r] - ax[r];
+  mg_level *C = &o->lev[l + 1];
+  const int d = L->cdir;
+  for (long I = 0; I < C->b.N; ++I) {
+    int ci[3] = {(int)(I % C->b.n[0]), (int)((I / C->b.n[0]) % C->b.n[1]), (int)(I / ((long)C->b.n[0] * C->b.n[1]))};
+    double acc = 0.0;
+    for (int fo = -1; fo <= 1; ++fo) {
+      int f[3] = {ci[0], ci[1], ci[2]};
+      f[d] = 2 * ci[d] + fo;
+      if (f[d] < 0 || f[d] >= L->b.n[d]) continue;
+      long fr = lidx(&L->b, f[0], f[1], f[2]);
+      double rw = fo == 0 ? 1.0 : (fo < 0 ? L->pp[fr] : L->pm[fr]);
+      acc = fma(rw, ax[fr], acc);
+    }
+    C->bv[I] = acc;
+  }
+  mg_cycle(o, l + 1, C->bv, C->xv);
+  for (long r = 0; r < N; ++r) {
+    int f[3] = {(int)(r % L->b.n[0]), (int)((r / L->b.n[0]) % L->b.n[1]), (int)(r / ((long)L->b.n[0] * L->b.n[1]))};
+    double corr;
+    if ((f[d] & 1) == 0) {
+      int c3[3] = {f[0], f[1], f[2]}; c3[d] = f[d] / 2;
+      corr = C->xv[lidx(&C->b, c3[0], c3[1], c3[2])];
+    } else {
+      int c0[3] = {f[0], f[1], f[2]}; c0[d] = (f[d] - 1) / 2;
+      double x0 = C->xv[lidx(&C->b, c0[0], c0[1], c0[2])], x1 = 0.0;
+      if ((f[d] + 1) / 2 < C->b.n[d]) { int c1[3] = {f[0], f[1], f[2]}; c1[d] = (f[d] + 1) / 2; x1 = C->xv[lidx(&C->b, c1[0], c1[1], c1[2])]; }
+      corr = fma(L->pp[r], x1, L->pm[r] * x0);
+    }
+    x[r] = x[r] + corr;
+  }
+  for (int s = 0; s < o->prm.mg_nu2; ++s) mg_relax(o, L, b, x, 0);
+}
+
+void oracle_mg_vcycle(oracle *o, const double *b, double *x) {
+  mg_build(o);
+  mg_cycle(o, 0, b, x);
+}
+int oracle_mg_levels(oracle *o) { mg_build(o); return o->nlev; }
+int oracle_mg_level_info(oracle *o, int l, int *dims, int *cdir, int *nslots) {
+  mg_build(o);
+  if (l < 0 || l >= o->nlev) return -1;
+  dims[0] = o->lev[l].b.n[0]; dims[1] = o->lev[l].b.n[1]; dims[2] = o->lev[l].b.n[2];
+  *cdir = o->lev[l].cdir;
+  *nslots = 27;
+  return 0;
+}
+int oracle_mg_level_coef(oracle *o, int l, double *coef) {
+  mg_build(o);
+  if (l < 0 || l >= o->nlev) return -1;
+  memcpy(coef, o->lev[l].A, sizeof(double) * 27 * (size_t)o->lev[l].b.N);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* restarted, right-preconditioned GMRES with classical Gram-Schmidt applied  */
+/* twice (restating HYPRE_StructGMRESSolve: stop when ||r||/||b|| <= tol,    */
+/* confirm with the true residual, restart from it)                          */
+/* ------------------------------------------------------------------------ */
+static void precond(oracle *o, int field, const double *v, double *z) {
+  const box3 *b = op_box(o, field);
+  const long N = b->N;
+  if (field == 3 && o->prm.p_pc == 1) { oracle_mg_vcycle(o, v, z); return; }
+  const int sweeps = field == 3 ? 1 : (o->prm.vel_jacobi_iters > 0 ? o->prm.vel_jacobi_iters : 1);
+  const double *id = o->invd[field];
+  for (long r = 0; r < N; ++r) z[r] = v[r] * id[r];
+  if (sweeps > 1) {
+    double *az = (double *)xcalloc((size_t)N, 8);
+    for (int s = 1; s < sweeps; ++s) {
+      spmv7(b, op_vals(o, field), z, az);
+      for (long r = 0; r < N; ++r) z[r] = fma(id[r], v[r] - az[r], z[r]);
+    }
+    free(az);
+  }
+}
+
+int oracle_solve(oracle *o, int field, const double *b, double *x, oracle_solve_stats *st) {
+  const box3 *bx = op_box(o, field);
+  const long N = bx->N;
+  const double tol = field == 3 ? o->prm.p_tol : o->prm.vel_tol;
+  const int maxit = field == 3 ? o->prm.p_maxit : o->prm.vel_maxit;
+  const int kdim = field == 3 ? o->prm.p_kdim : o->prm.vel_kdim;
+  const double *A = op_vals(o, field);
+  double *V = (double *)xcalloc((size_t)(kdim + 1) * (size_t)N, 8);
+  double *r = (double *)xcalloc((size_t)N, 8), *z = (double *)xcalloc((size_t)N, 8), *wv = (double *)xcalloc((size_t)N, 8);
+  double *H = (double *)xcalloc((size_t)(kdim + 1) * kdim, 8);
+  double *cs = (double *)xcalloc((size_t)kdim + 1, 8), *sn = (double *)xcalloc((size_t)kdim + 1, 8);
+  double *g = (double *)xcalloc((size_t)kdim + 1, 8), *y = (double *)xcalloc((size_t)kdim + 1, 8);
+  double *hc = (double *)xcalloc((size_t)kdim + 2, 8);
+#define HH(i, j) H[(size_t)(i) * kdim + (j)]
+  const double b_norm = sqrt(dot(b, b, N));
+  spmv7(bx, A, x, r);
+  for (long t = 0; t < N; ++t) r[t] = b[t] - r[t];
+  double r_norm = sqrt(dot(r, r, N));
+  int iters = 0, converged = 0;
+  const double den = b_norm > 0.0 ? b_norm : r_norm;
+  const double eps = tol * den;
+  double real_old = b_norm;
+  if (r_norm == 0.0) converged = 1;
+  while (!converged) {
+    if (r_norm <= eps) { converged = 1; break; }
+    if (iters >= maxit) break;
+    for (long t = 0; t < N; ++t) V[t] = r[t] / r_norm;
+    g[0] = r_norm;
+    int i = 0, claimed = 0;
+    while (i < kdim && iters < maxit) {
+      precond(o, field, V + (size_t)i * N, z);
+      spmv7(bx, A, z, wv);
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int k = 0; k <= i; ++k) hc[k] = dot(V + (size_t)k * N, wv, N);
+        for (long t = 0; t < N; ++t) {
+          double acc = wv[t];
+          for (int k = 0; k <= i; ++k) acc = fma(-hc[k], V[(size_t)k * N + t], acc);
+          wv[t] = acc;
+        }
+        for (int k = 0; k <= i; ++k) HH(k, i) = pass == 0 ? hc[k] : HH(k, i) + hc[k];
+      }
+      double hn = sqrt(dot(wv, wv, N));
+      HH(i + 1, i) = hn;
+      if (hn != 0.0)
+        for (long t = 0; t < N; ++t) V[(size_t)(i + 1) * N + t] = wv[t] / hn;
+      for (int j = 0; j < i; ++j) {
+        double t0 = HH(j, i);
+        HH(j, i) = sn[j] * HH(j + 1, i) + cs[j] * t0;
+        HH(j + 1, i) = -sn[j] * t0 + cs[j] * HH(j + 1, i);
+      }
+      double gam = sqrt(HH(i + 1, i) * HH(i + 1, i) + HH(i, i) * HH(i, i));
+      if (gam == 0.0) gam = 2.220446049250313e-16;
+      cs[i] = HH(i, i) / gam;
+      sn[i] = HH(i + 1, i) / gam;
+      g[i + 1] = -sn[i] * g[i];
+      g[i] = cs[i] * g[i];
+      HH(i, i) = sn[i] * HH(i + 1, i) + cs[i] * HH(i, i);
+      ++i; ++iters;
+      r_norm = fabs(g[i]);
+      if (r_norm <= eps) { claimed = 1; break; }
+    }
+    for (int k = i - 1; k >= 0; --k) {
+      double t0 = g[k];
+      for (int j = k + 1; j < i; ++j) t0 -= HH(k, j) * y[j];
+      y[k] = t0 / HH(k, k);
+    }
+    for (long t = 0; t < N; ++t) {
+      double acc = 0.0;
+      for (int k = 0; k < i; ++k) acc = fma(y[k], V[(size_t)k * N + t], acc);
+      wv[t] = acc;
+    }
+    precond(o, field, wv, z);
+    for (long t = 0; t < N; ++t) x[t] = x[t] + z[t];
+    spmv7(bx, A, x, r);
+    for (long t = 0; t < N; ++t) r[t] = b[t] - r[t];
+    double rt = sqrt(dot(r, r, N));
+    r_norm = rt;
+    if (rt <= eps) { converged = 1; break; }
+    if (claimed && rt >= real_old) break;
+    real_old = rt;
+  }
+#undef HH
+  st->iters = iters;
+  st->rel_res = b_norm > 0.0 ? r_norm / b_norm : r_norm;
+  st->status = converged ? 0 : 1;
+  free(V); free(r); free(z); free(wv); free(H); free(cs); free(sn); free(g); free(y); free(hc);
+  return st->status;
+}
+
+/* ------------------------------------------------------------------------ */
+/* lifecycle and the full step                                               */
+/* ------------------------------------------------------------------------ */
+oracle *oracle_create(const oracle_params *prm, const oracle_inputs *in) {
+  oracle *o = (oracle *)xcalloc(1, sizeof(oracle));
+  o->prm = *prm;
+  o->in = *in;
+  o->nx = prm->nx; o->ny = prm->ny; o->nz = prm->nz;
+  o->dx = prm->Lx / prm->nx; o->dy = prm->Ly / prm->ny; o->dz = prm->Lz / prm->nz;
+  const long NU = (long)(o->nx + 1) * o->ny * o->nz, NV = (long)o->nx * (o->ny + 1) * o->nz,
+             NW = (long)o->nx * o->ny * (o->nz + 1), NP = (long)o->nx * o->ny * o->nz;
+  o->nU = max_id(in->id_u, NU); o->nV = max_id(in->id_v, NV); o->nW = max_id(in->id_w, NW);
+  o->nP = max_id(in->id_p, NP);
+  o->nQu = max_id(in->id_qu, NU); o->nQv = max_id(in->id_qv, NV); o->nQw = max_id(in->id_qw, NW);
+  o->nQ = o->nQu + o->nQv + o->nQw;
+  o->bu = (box3){{o->nx - 1, o->ny, o->nz}, (long)(o->nx - 1) * o->ny * o->nz};
+  o->bv = (box3){{o->nx, o->ny - 1, o->nz}, (long)o->nx * (o->ny - 1) * o->nz};
+  o->bw = (box3){{o->nx, o->ny, o->nz - 1}, (long)o->nx * o->ny * (o->nz - 1)};
+  o->bp = (box3){{o->nx, o->ny, o->nz}, NP};
+  o->u = (double *)xcalloc((size_t)NU, 8); o->v = (double *)xcalloc((size_t)NV, 8);
+  o->w = (double *)xcalloc((size_t)NW, 8); o->p = (double *)xcalloc((size_t)NP, 8);
+  for (int f = 0; f < 4; ++f) {
+    const box3 *b = op_box(o, f);
+    const double *A = op_vals(o, f);
+    o->invd[f] = (double *)xcalloc((size_t)b->N, 8);
+    for (long r = 0; r < b->N; ++r) o->invd[f][r] = A[7 * r] != 0.0 ? 1.0 / A[7 * r] : 0.0;
+  }
+  return o;
+}
+
+void oracle_destroy(oracle *o) {
+  if (!o) return;
+  free(o->u); free(o->v); free(o->w); free(o->p);
+  for (int f = 0; f < 4; ++f) free(o->invd[f]);
+  for (int l = 0; l < o->nlev; ++l) {
+    mg_level *L = &o->lev[l];
+    free(L->A); free(L->wd); free(L->invd); free(L->pm); free(L->pp); free(L->bv); free(L->xv); free(L->rv);
+    free(L->dense_inv);
+  }
+  free(o);
+}
+
+void oracle_set_fields(oracle *o, const double *u, const double *v, const double *w, const double *p) {
+  const long NU = (long)(o->nx + 1) * o->ny * o->nz, NV = (long)o->nx * (o->ny + 1) * o->nz,
+             NW = (long)o->nx * o->ny * (o->nz + 1), NP = (long)o->nx * o->ny * o->nz;
+  if (u) memcpy(o->u, u, 8 * (size_t)NU);
+  if (v) memcpy(o->v, v, 8 * (size_t)NV);
+  if (w) memcpy(o->w, w, 8 * (size_t)NW);
+  if (p) memcpy(o->p, p, 8 * (size_t)NP);
+}
+
+void oracle_get_fields(const oracle *o, double *u, double *v, double *w, double *p) {
+  const long NU = (long)(o->nx + 1) * o->ny * o->nz, NV = (long)o->nx * (o->ny + 1) * o->nz,
+             NW = (long)o->nx * o->ny * (o->nz + 1), NP = (long)o->nx * o->ny * o->nz;
+  if (u) memcpy(u, o->u, 8 * (size_t)NU);
+  if (v) memcpy(v, o->v, 8 * (size_t)NV);
+  if (w) memcpy(w, o->w, 8 * (size_t)NW);
+  if (p) memcpy(p, o->p, 8 * (size_t)NP);
+}
+
+/* u~ = u with the solve-box interior replaced by x, then the BC cleanup
+ * (gpu_dense_ops.hpp:20-22, main.cu:307-312). */
+void oracle_tilde(const oracle *o, const double *xu, const double *xv, const double *xw, double ramp,
+                  double *ut, double *vt, double *wt) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const long NU = (long)(nx + 1) * ny * nz, NV = (long)nx * (ny + 1) * nz, NW = (long)nx * ny * (nz + 1);
+  memcpy(ut, o->u, 8 * (size_t)NU); memcpy(vt, o->v, 8 * (size_t)NV); memcpy(wt, o->w, 8 * (size_t)NW);
+  for (int k = 0; k < nz; ++k) for (int j = 0; j < ny; ++j) for (int i = 1; i < nx; ++i)
+    ut[U3(o, i, j, k)] = xu[((long)k * ny + j) * (nx - 1) + (i - 1)];
+  for (int k = 0; k < nz; ++k) for (int j = 1; j < ny; ++j) for (int i = 0; i < nx; ++i)
+    vt[V3(o, i, j, k)] = xv[((long)k * (ny - 1) + (j - 1)) * nx + i];
+  for (int k = 1; k < nz; ++k) for (int j = 0; j < ny; ++j) for (int i = 0; i < nx; ++i)
+    wt[W3(o, i, j, k)] = xw[((long)(k - 1) * ny + j) * nx + i];
+  double *uin = (double *)xcalloc((size_t)ny * nz, 8);
+  for (long t = 0; t < (long)ny * nz; ++t) uin[t] = ramp * o->in.uin[t];
+  oracle_bc_cleanup(o, ut, vt, wt, uin);
+  free(uin);
+}
+
+/* Projection and diagnostics (main.cu:338-363): q = q~ - (dt/rho) G phi,
+ * u = u~ with q unpacked, BC cleanup, p += phi; writes the oracle's fields. */
+void oracle_projection(oracle *o, const double *ut, const double *vt, const double *wt, const double *xp,
+                       double ramp, oracle_step_stats *st) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const long NU = (long)(nx + 1) * ny * nz, NV = (long)nx * (ny + 1) * nz, NW = (long)nx * ny * (nz + 1),
+             NP = (long)nx * ny * nz;
+  double *uin = (double *)xcalloc((size_t)ny * nz, 8);
+  for (long t = 0; t < (long)ny * nz; ++t) uin[t] = ramp * o->in.uin[t];
+  double *phi = (double *)xcalloc((size_t)o->nP + 1, 8), *gphi = (double *)xcalloc((size_t)o->nQ + 1, 8);
+  double *q = (double *)xcalloc((size_t)o->nQ + 1, 8);
+  for (long c = 0; c < NP; ++c)
+    if (o->in.fluid_p[c] && o->in.id_p[c] > 0) phi[o->in.id_p[c]] = xp[c];
+  pack_q(o, ut, vt, wt, q);
+  csr_apply(o->in.G_rowptr, o->in.G_col, o->in.G_val, o->nQ, phi, gphi);
+  const double factor = o->prm.dt / o->prm.rho;
+  for (long t = 1; t <= o->nQ; ++t) q[t] = fma(-factor, gphi[t], q[t]);
+  memcpy(o->u, ut, 8 * (size_t)NU); memcpy(o->v, vt, 8 * (size_t)NV); memcpy(o->w, wt, 8 * (size_t)NW);
+  for (long f = 0; f < NU; ++f) { int id = o->in.id_qu[f]; if (id > 0) o->u[f] = q[id]; }
+  for (long f = 0; f < NV; ++f) { int id = o->in.id_qv[f]; if (id > 0) o->v[f] = q[o->nQu + id]; }
+  for (long f = 0; f < NW; ++f) { int id = o->in.id_qw[f]; if (id > 0) o->w[f] = q[o->nQu + o->nQv + id]; }
+  oracle_bc_cleanup(o, o->u, o->v, o->w, uin);
+  for (long c = 0; c < NP; ++c)
+    if (o->in.fluid_p[c] && o->in.id_p[c] > 0) o->p[c] = o->p[c] + phi[o->in.id_p[c]];
+  double *dv = (double *)xcalloc((size_t)o->nP + 1, 8);
+  csr_apply(o->in.D_rowptr, o->in.D_col, o->in.D_val, o->nP, q, dv);
+  double div2 = 0.0;
+  for (int i = 1; i <= o->nP; ++i) {
+    double d = dv[i] + ramp * o->in.div_bc_unit[i];
+    div2 += d * d;
+  }
+  st->div_l2 = sqrt(div2 / (o->nP > 1 ? o->nP : 1));
+  double um = 0.0, vm = 0.0, wm = 0.0;
+  for (long f = 0; f < NU; ++f) um = fmax(um, fabs(o->u[f]));
+  for (long f = 0; f < NV; ++f) vm = fmax(vm, fabs(o->v[f]));
+  for (long f = 0; f < NW; ++f) wm = fmax(wm, fabs(o->w[f]));
+  st->umax = um; st->vmax = vm; st->wmax = wm;
+  free(phi); free(gphi); free(q); free(dv); free(uin);
+}
+
+static int all_finite(const double *x, long n) {
+  for (long i = 0; i < n; ++i) if (!isfinite(x[i])) return 0;
+  return 1;
+}
+
+/* One timestep, in the order of main.cu:249-368. */
+int oracle_step(oracle *o, double ramp, oracle_step_stats *st) {
+  memset(st, 0, sizeof(*st));
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const long NU = (long)(nx + 1) * ny * nz, NV = (long)nx * (ny + 1) * nz, NW = (long)nx * ny * (nz + 1),
+             NP = (long)nx * ny * nz;
+  double *uin = (double *)xcalloc((size_t)ny * nz, 8);
+  for (long t = 0; t < (long)ny * nz; ++t) uin[t] = ramp * o->in.uin[t];
+  oracle_bc_cleanup(o, o->u, o->v, o->w, uin);
+  double *bu = (double *)xcalloc((size_t)o->bu.N, 8), *bv = (double *)xcalloc((size_t)o->bv.N, 8),
+         *bw = (double *)xcalloc((size_t)o->bw.N, 8), *bp = (double *)xcalloc((size_t)NP, 8);
+  double *xu = (double *)xcalloc((size_t)o->bu.N, 8), *xv = (double *)xcalloc((size_t)o->bv.N, 8),
+         *xw = (double *)xcalloc((size_t)o->bw.N, 8), *xp = (double *)xcalloc((size_t)NP, 8);
+  oracle_momentum_rhs(o, o->u, o->v, o->w, o->p, bu, bv, bw);
+  if (!o->prm.use_zero_initial_guess) {
+    for (int k = 0; k < nz; ++k) for (int j = 0; j < ny; ++j) for (int i = 1; i < nx; ++i)
+      xu[((long)k * ny + j) * (nx - 1) + (i - 1)] = o->u[U3(o, i, j, k)];
+    for (int k = 0; k < nz; ++k) for (int j = 1; j < ny; ++j) for (int i = 0; i < nx; ++i)
+      xv[((long)k * (ny - 1) + (j - 1)) * nx + i] = o->v[V3(o, i, j, k)];
+    for (int k = 1; k < nz; ++k) for (int j = 0; j < ny; ++j) for (int i = 0; i < nx; ++i)
+      xw[((long)(k - 1) * ny + j) * nx + i] = o->w[W3(o, i, j, k)];
+  }
+  oracle_solve(o, 0, bu, xu, &st->u);
+  oracle_solve(o, 1, bv, xv, &st->v);
+  oracle_solve(o, 2, bw, xw, &st->w);
+  int rc = 0;
+  if (!all_finite(xu, o->bu.N) || !all_finite(xv, o->bv.N) || !all_finite(xw, o->bw.N)) { rc = -3; goto done; }
+  {
+    double *ut = (double *)xcalloc((size_t)NU, 8), *vt = (double *)xcalloc((size_t)NV, 8), *wt = (double *)xcalloc((size_t)NW, 8);
+    oracle_tilde(o, xu, xv, xw, ramp, ut, vt, wt);
+    oracle_pressure_rhs(o, ut, vt, wt, ramp, bp);
+    oracle_solve(o, 3, bp, xp, &st->p);
+    if (!all_finite(xp, NP)) rc = -3;
+    else oracle_projection(o, ut, vt, wt, xp, ramp, st);
+    free(ut); free(vt); free(wt);
+  }
+done:
+  st->status = rc;
+  free(uin); free(bu); free(bv); free(bw); free(bp); free(xu); free(xv); free(xw); free(xp);
+  return rc;
+}

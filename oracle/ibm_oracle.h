@@ -1,0 +1,92 @@
+/*
+ * ibm_oracle.h — CPU oracle for the per-timestep hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is the checker the CUDA path is compared
+ * against; nothing in the product links, loads or calls it. It restates the
+ * reference's timestep (main.cu:249-368) and dense kernels
+ * (gpu_dense_ops.hpp:1-106) in plain C, with the linear solves done by the
+ * oracle's own FP64 restarted GMRES (Jacobi or semicoarsening multigrid
+ * preconditioning), restating the algorithm of HYPRE's Struct GMRES / Jacobi /
+ * PFMG, which the reference calls but does not vendor (version unpinned).
+ *
+ * Pins: the setup arrays it consumes are bit-identical to the reference's
+ * own (checked through the reference compiled from its sources); the BC and
+ * convection restatements are bit-identical to the reference's CPU twins
+ * (immersed_operators.hpp:990-1053); solve outputs are checked by their
+ * residual against the reference-identical operators.
+ */
+#ifndef IBM_ORACLE_H
+#define IBM_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_params {
+  int nx, ny, nz;
+  double Lx, Ly, Lz, rho, nu, dt;
+  int use_zero_initial_guess;
+  double vel_tol; int vel_maxit, vel_kdim, vel_jacobi_iters;
+  double p_tol; int p_maxit, p_kdim;
+  int p_pc;            /* 0: Jacobi, 1: semicoarsening multigrid V-cycle */
+  int mg_rap;          /* 0: Galerkin (27-point coarse stencils), 1: collapsed to 7 points */
+  int mg_relax;        /* 1: weighted Jacobi, 2: red-black Gauss-Seidel */
+  int mg_nu1, mg_nu2;  /* pre/post smoothing sweeps */
+  double mg_omega;     /* weighted-Jacobi weight */
+  int mg_coarse_max;   /* stop coarsening at or below this many points */
+  int mg_max_levels;
+} oracle_params;
+
+typedef struct oracle_inputs {
+  const double *Au, *Av, *Aw, *Ap; /* row-major [box rows][7]: C,-x,+x,-y,+y,-z,+z */
+  const uint8_t *active_u, *active_v, *active_w, *fluid_p, *active_qu, *active_qv, *active_qw;
+  const int32_t *id_u, *id_v, *id_w, *id_p, *id_qu, *id_qv, *id_qw;
+  const double *scale_u, *scale_v, *scale_w, *rhs_u_bc, *rhs_v_bc, *rhs_w_bc, *div_bc_unit;
+  const int32_t *D_rowptr, *D_col; const double *D_val;
+  const int32_t *G_rowptr, *G_col; const double *G_val;
+  const double *uin; /* ny*nz, inlet profile at Um */
+} oracle_inputs;
+
+typedef struct oracle_solve_stats { int iters; double rel_res; int status; } oracle_solve_stats;
+
+typedef struct oracle_step_stats {
+  oracle_solve_stats u, v, w, p;
+  double div_l2, umax, vmax, wmax;
+  int status;
+} oracle_step_stats;
+
+typedef struct oracle oracle;
+
+/* The oracle keeps the input pointers (no copy): they must outlive it. */
+oracle *oracle_create(const oracle_params *prm, const oracle_inputs *in);
+void oracle_destroy(oracle *o);
+void oracle_set_fields(oracle *o, const double *u, const double *v, const double *w, const double *p);
+void oracle_get_fields(const oracle *o, double *u, double *v, double *w, double *p);
+int oracle_step(oracle *o, double ramp, oracle_step_stats *st);
+
+/* Pieces of the step, for kernel-level checks. */
+void oracle_bc_cleanup(const oracle *o, double *u, double *v, double *w, const double *uin_step);
+void oracle_convection(const oracle *o, const double *u, const double *v, const double *w,
+                       double *cu, double *cv, double *cw);
+void oracle_momentum_rhs(const oracle *o, const double *u, const double *v, const double *w, const double *p,
+                         double *bu, double *bv, double *bw);
+void oracle_pressure_rhs(const oracle *o, const double *ut, const double *vt, const double *wt, double ramp,
+                         double *bp);
+void oracle_tilde(const oracle *o, const double *xu, const double *xv, const double *xw, double ramp,
+                  double *ut, double *vt, double *wt);
+void oracle_projection(oracle *o, const double *ut, const double *vt, const double *wt, const double *xp,
+                       double ramp, oracle_step_stats *st);
+/* field: 0 u, 1 v, 2 w, 3 p. y = A x on the field's solve box. */
+void oracle_apply_operator(const oracle *o, int field, const double *x, double *y);
+int oracle_solve(oracle *o, int field, const double *b, double *x, oracle_solve_stats *st);
+/* Multigrid hierarchy of the pressure operator (built on first use). */
+int oracle_mg_levels(oracle *o);
+int oracle_mg_level_info(oracle *o, int l, int *dims /*3*/, int *cdir, int *nslots);
+int oracle_mg_level_coef(oracle *o, int l, double *coef /* [n][27] */);
+void oracle_mg_vcycle(oracle *o, const double *b, double *x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

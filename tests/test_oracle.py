@@ -1,0 +1,216 @@
+"""The CPU oracle, pinned to the reference.
+
+- BC cleanup and convection: bitwise equal to the reference's CPU twins
+  (immersed_operators.hpp:990-1053), live where the reference is compiled
+  here, otherwise against the committed golden fixtures.
+- Solves: the reference's solver (HYPRE) is not vendored; the oracle's
+  solutions are pinned by their residual against the reference-identical
+  operators.
+- Multigrid: the coarse operators equal R A P formed explicitly with sparse
+  matrices.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
+
+
+@pytest.fixture(scope="module")
+def case32(ibm):
+    return ibm.Case(ibm.channel_params(32, 12, 12, Um=0.45, dt=1e-3))
+
+
+def test_bc_and_convection_match_reference_twins_golden(case32, pyoracle):
+    g = np.load(os.path.join(GOLDEN, "twins_channel_32x12x12.npz"))
+    orc = pyoracle.Oracle(case32)
+    ub, vb, wb = orc.bc_cleanup(g["u"], g["v"], g["w"], float(g["ramp"]))
+    assert bits_equal(ub, g["u_bc"]) and bits_equal(vb, g["v_bc"]) and bits_equal(wb, g["w_bc"])
+    cu, cv, cw = orc.convection(ub, vb, wb)
+    assert bits_equal(cu, g["conv_u"]) and bits_equal(cv, g["conv_v"]) and bits_equal(cw, g["conv_w"])
+
+
+@pytest.mark.parametrize("shape", [(48, 16, 16), (40, 24, 8), (160, 32, 32)])
+def test_bc_and_convection_match_reference_twins_live(ibm, pyoracle, shape):
+    if not pyoracle.reference_available():
+        pytest.skip("reference checker not built")
+    prm = ibm.channel_params(*shape, Um=1.3)
+    case = ibm.Case(prm)
+    ref = pyoracle.ReferenceCase(prm)
+    orc = pyoracle.Oracle(case)
+    rng = np.random.default_rng(sum(shape))
+    nx, ny, nz = shape
+    u = rng.standard_normal((nx + 1) * ny * nz)
+    v = rng.standard_normal(nx * (ny + 1) * nz)
+    w = rng.standard_normal(nx * ny * (nz + 1))
+    ramp = 0.37
+    r = ref.enforce_bc(u, v, w, ramp * case.array("uin"))
+    o = orc.bc_cleanup(u, v, w, ramp)
+    for a, b in zip(r, o):
+        assert bits_equal(a, b)
+    rc = ref.convection(*r)
+    oc = orc.convection(*o)
+    for a, b in zip(rc, oc):
+        assert bits_equal(a, b)
+
+
+def test_oracle_steps_match_golden(case32, pyoracle):
+    g = np.load(os.path.join(GOLDEN, "oracle_channel_32x12x12.npz"))
+    orc = pyoracle.Oracle(case32, vel_tol=1e-13, p_tol=1e-13)
+    for step in range(1, int(g["nsteps"]) + 1):
+        orc.step(min(1.0, step / float(g["ramp_steps"])))
+    u, v, w, p = orc.fields()
+    # same machine class: bitwise; other hosts (thread counts do not matter) agree to round-off
+    for a, b in zip((u, v, w, p), (g["u"], g["v"], g["w"], g["p"])):
+        scale = max(np.abs(b).max(), 1e-300)
+        assert np.abs(a - b).max() <= 1e-12 * scale
+
+
+def test_solves_satisfy_reference_equations(case32, pyoracle):
+    """Each oracle solve leaves ||b - A x|| / ||b|| at the requested tolerance,
+    with A the reference-identical embedded operator."""
+    orc = pyoracle.Oracle(case32, vel_tol=1e-12, p_tol=1e-12)
+    rng = np.random.default_rng(3)
+    for field, n in enumerate(orc.box_sizes()):
+        b = rng.standard_normal(n)
+        x, st = orc.solve(field, b)
+        assert st.status == 0
+        r = b - orc.apply_operator(field, x)
+        assert np.linalg.norm(r) / np.linalg.norm(b) <= 1.01e-12
+        assert st.rel_res <= 1e-12
+
+
+def test_operator_apply_matches_dense_matrix(case32, pyoracle):
+    """The 7-point apply equals the explicit matrix assembled from the
+    row-major Struct values (HYPRE Struct stencil semantics)."""
+    orc = pyoracle.Oracle(case32)
+    nx, ny, nz = case32.shape
+    for field, (bx, by, bz), name in ((0, (nx - 1, ny, nz), "Au_vals"), (3, (nx, ny, nz), "Ap_vals")):
+        A = case32.array(name).reshape(-1, 7)
+        n = bx * by * bz
+        x = np.random.default_rng(field).standard_normal(n)
+        X = x.reshape(bz, by, bx)
+        pad = np.zeros((bz + 2, by + 2, bx + 2))
+        pad[1:-1, 1:-1, 1:-1] = X
+        nb = [X, pad[1:-1, 1:-1, :-2], pad[1:-1, 1:-1, 2:], pad[1:-1, :-2, 1:-1], pad[1:-1, 2:, 1:-1],
+              pad[:-2, 1:-1, 1:-1], pad[2:, 1:-1, 1:-1]]
+        y = sum(A[:, s] * nb[s].ravel() for s in range(7))
+        assert np.allclose(orc.apply_operator(field, x), y, rtol=1e-14, atol=1e-12 * np.abs(y).max())
+
+
+def _explicit_A(A27, dims):
+    """Sparse matrix of a 27-point operator stored [n][27]."""
+    import scipy.sparse as sp
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    rows, cols, vals = [], [], []
+    idx = np.arange(n).reshape(nz, ny, nx)
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    for s in range(27):
+        ox, oy, oz = s % 3 - 1, (s // 3) % 3 - 1, s // 9 - 1
+        ii, jj, kk = i + ox, j + oy, k + oz
+        ok = (ii >= 0) & (ii < nx) & (jj >= 0) & (jj < ny) & (kk >= 0) & (kk < nz)
+        r = idx[ok]
+        rows.append(r); cols.append(idx[kk[ok], jj[ok], ii[ok]]); vals.append(A27[r, s])
+    return sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
+
+
+def _explicit_P(dims, d, pm, pp):
+    """Interpolation for semicoarsening along d: even points inject, odd
+    points take pm / pp of their lower / upper coarse neighbours."""
+    import scipy.sparse as sp
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    idx = np.arange(n).reshape(nz, ny, nx)
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    cdims = list(dims)
+    cdims[d] = (dims[d] + 1) // 2
+    cidx = np.arange(cdims[0] * cdims[1] * cdims[2]).reshape(cdims[2], cdims[1], cdims[0])
+    f = [i, j, k][d]
+    pr, pc, pv = [], [], []
+    for sel, cf, wts in ((f % 2 == 0, f // 2, None), (f % 2 == 1, (f - 1) // 2, pm),
+                         ((f % 2 == 1) & ((f + 1) // 2 < cdims[d]), (f + 1) // 2, pp)):
+        c3 = [i, j, k]
+        c3 = [c.copy() for c in c3]
+        c3[d] = cf
+        pr.append(idx[sel]); pc.append(cidx[c3[2][sel], c3[1][sel], c3[0][sel]])
+        pv.append(np.ones(sel.sum()) if wts is None else wts[idx[sel]])
+    return sp.csr_matrix((np.concatenate(pv), (np.concatenate(pr), np.concatenate(pc))),
+                         shape=(n, cdims[0] * cdims[1] * cdims[2]))
+
+
+def _interp_weights(A27, d):
+    od = np.array([(s % 3 - 1, (s // 3) % 3 - 1, s // 9 - 1)[d] for s in range(27)])
+    c0 = A27[:, od == 0].sum(axis=1)
+    cm = A27[:, od < 0].sum(axis=1)
+    cp = A27[:, od > 0].sum(axis=1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(c0 != 0, -cm / c0, 0.0), np.where(c0 != 0, -cp / c0, 0.0)
+
+
+@pytest.mark.parametrize("rap", [0, 1])
+def test_multigrid_coarse_operators_are_rap(case32, pyoracle, rap):
+    orc = pyoracle.Oracle(case32, mg_rap=rap, mg_coarse_max=16)
+    levels = orc.mg_levels()
+    assert len(levels) >= 4
+    dirs = [cd for _, cd in levels[:-1]]
+    assert set(dirs) == {0, 1, 2}  # semicoarsening visits every direction
+    for l in range(min(3, len(levels) - 1)):
+        dims, d = levels[l]
+        Af = orc.mg_level_coef(l)
+        pm, pp = _interp_weights(Af, d)
+        A, P = _explicit_A(Af, dims), _explicit_P(dims, d, pm, pp)
+        Ac = (P.T @ A @ P).toarray()
+        got = _explicit_A(orc.mg_level_coef(l + 1), levels[l + 1][0]).toarray()
+        scale = np.abs(Ac).max()
+        if rap == 0:
+            assert np.abs(got - Ac).max() <= 1e-12 * scale
+        else:
+            # collapsed: same row sums and same action on linear functions
+            assert np.allclose(got.sum(axis=1), Ac.sum(axis=1), atol=1e-9 * scale)
+            nxc, nyc, nzc = levels[l + 1][0]
+            kk, jj, ii = np.meshgrid(np.arange(nzc), np.arange(nyc), np.arange(nxc), indexing="ij")
+            for lin in (ii.ravel(), jj.ravel(), kk.ravel()):
+                inner = np.ones(len(lin), bool)
+                assert np.allclose((got @ lin)[inner], (Ac @ lin)[inner], atol=1e-8 * scale * max(nxc, nyc, nzc))
+
+
+def test_multigrid_vcycle_contracts(case32, pyoracle):
+    """One V-cycle as a stationary iteration reduces the error of the
+    pressure system."""
+    for rap, relax in ((0, 1), (1, 1), (1, 2)):
+        orc = pyoracle.Oracle(case32, mg_rap=rap, mg_relax=relax)
+        n = orc.box_sizes()[3]
+        rng = np.random.default_rng(7)
+        x_true = rng.standard_normal(n)
+        b = orc.apply_operator(3, x_true)
+        x = np.zeros(n)
+        errs = []
+        for _ in range(6):
+            r = b - orc.apply_operator(3, x)
+            x = x + orc.mg_vcycle(r)
+            errs.append(np.linalg.norm(x - x_true) / np.linalg.norm(x_true))
+        assert errs[-1] < 0.2 * errs[0], (rap, relax, errs)
+
+
+def test_step_properties(case32, pyoracle):
+    """After the projection the discrete divergence vanishes to round-off,
+    the outlet u face copies the last interior face, walls are zero."""
+    orc = pyoracle.Oracle(case32, vel_tol=1e-12, p_tol=1e-12)
+    for step in range(1, 4):
+        st = orc.step(min(1.0, step / 2.0))
+        assert st.status == 0 and st.div_l2 < 1e-10
+    u, v, w, p = orc.fields()
+    nx, ny, nz = case32.shape
+    U = u.reshape(nz, ny, nx + 1)
+    assert np.array_equal(U[:, :, nx], U[:, :, nx - 1])
+    assert np.all(v.reshape(nz, ny + 1, nx)[:, [0, ny], :] == 0)
+    assert np.all(w.reshape(nz + 1, ny, nx)[[0, nz], :, :] == 0)
+    assert np.all(p.reshape(-1)[case32.array("fluid_p") == 0] == 0)
