@@ -1,0 +1,414 @@
+#!/usr/bin/env python
+"""Benchmark of the per-timestep hot path on GB300.
+
+Workload (the configuration the headline metric is quoted on): the full
+timestep of the 640x128x128 channel (2.5 x 0.41 x 0.41, cylinder of
+diameter 0.1 at (0.5, 0.2)), Um = 2.25, nu = 1e-3, dt = 2e-4, inlet ramp
+disabled, initial field = the parabolic inflow profile on every active u
+face plus 1e-3 N(0,1) seeded perturbations on active u, v, w faces.
+Synthetic data (no dataset exists for this path).
+
+value      : steps/s of the mixed-precision form (FP32 multigrid / Jacobi
+             preconditioners inside FP64 flexible GMRES, tolerance 1e-8),
+             fields and operators resident in HBM (~25 GB, far above L2).
+fp64_plain : the same steps in FP64 throughout; the velocity error of the
+             mixed form against it is reported (must be <= 1e-6).
+e2e        : steps/s through the C ABI with host buffers: every step copies
+             the state in from pinned host memory, steps, and reads it back.
+roofline   : the kernel class with the largest device time in the timed
+             region, algorithmic bytes per launch over CUDA-event time.
+cpu_baseline: the CPU oracle (the reference's HYPRE path is not available
+             here) on all host cores, on a bounded sample.
+
+--impl reference times the CPU path alone (the oracle port, all cores) on
+bounded samples of the same workload and prints its own line.
+Multi-GPU: the single channel does not shard; N ranks run N replicas
+(weak scaling), timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s @640x128x128: mixed vs FP64 plain (rel err ≤1e-6); solve HBM GB/s"
+CPU_SAMPLE_NZ = 8
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=640)
+    ap.add_argument("--ny", type=int, default=128)
+    ap.add_argument("--nz", type=int, default=128)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def case_params(ibm, nx, ny, nz):
+    return ibm.channel_params(nx, ny, nz, Um=2.25, nu=1e-3, dt=2e-4)
+
+
+def initial_state(case, seed=2026):
+    """Parabolic profile on every active u face + 1e-3 N(0,1) on active faces."""
+    nx, ny, nz = case.shape
+    rng = np.random.default_rng(seed)
+    au = case.array("active_u").reshape(nz, ny, nx + 1).astype(bool)
+    av = case.array("active_v").astype(bool)
+    aw = case.array("active_w").astype(bool)
+    prof = case.array("uin").reshape(nz, ny, 1)
+    u = np.where(au, prof, 0.0)
+    u[:, :, 0] = prof[:, :, 0]
+    u = u.ravel() + 1e-3 * rng.standard_normal(u.size) * au.ravel()
+    v = 1e-3 * rng.standard_normal(av.size) * av
+    w = 1e-3 * rng.standard_normal(aw.size) * aw
+    p = np.zeros(nx * ny * nz)
+    return u, v, w, p
+
+
+def solver_params(ibm, precision):
+    return ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, vel_maxit=250, p_maxit=250, vel_kdim=50, p_kdim=50,
+                             p_pc=1, p_pc_rap_type=1, p_pc_relax_type=2, mg_nu1=1, mg_nu2=1, mg_omega=1.0,
+                             mg_group_ratio=1.5, mg_coarse_max=64, precision=precision, vel_inner_sweeps=3)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def device_timer(ibm_lib, ctx):
+    """CUDA events on the context's own stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(ibm_lib.ibm_stream(ctx))
+    return stream
+
+
+def run_steps(solver, n):
+    worst = 0
+    for _ in range(n):
+        st = solver.step(1.0)
+        worst = max(worst, st.status)
+    return worst
+
+
+def profile_struct(native):
+    import ctypes as C
+
+    class Prof(C.Structure):
+        _fields_ = [("nkernels", C.c_int), ("launches", C.c_longlong * 32), ("bytes", C.c_double * 32),
+                    ("time_ms", C.c_double * 32), ("timed_launches", C.c_longlong * 32),
+                    ("phase_bytes", C.c_double * 5)]
+    lib = native.gpu()
+    lib.ibm_profile_reset.argtypes = [C.c_void_p]
+    lib.ibm_profile_time_kernel.argtypes = [C.c_void_p, C.c_int]
+    lib.ibm_profile_get.argtypes = [C.c_void_p, C.POINTER(Prof)]
+    lib.ibm_kernel_name.restype = C.c_char_p
+    return Prof, lib
+
+
+def read_profile(lib, Prof, ctx):
+    import ctypes as C
+    p = Prof()
+    lib.ibm_profile_get(ctx, C.byref(p))
+    return p
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_for(kernel_name, launch_bytes):
+    """DRAM bytes per launch of the kernel from the committed ncu summary,
+    scaled to this launch's algorithmic bytes (traffic grows with the rows)."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_algorithmic_byte.txt")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        ratio = d["kernels"][kernel_name]["dram_over_algorithmic"]
+        return float(ratio) * launch_bytes
+    except Exception:
+        return None
+
+
+def cpu_baseline(ibm, nx, ny, nz, steps=1):
+    """The CPU oracle on a z-slab of the workload (same x-y plane, nz = 8),
+    all host threads, scaled to the full grid by the cell count."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build(with_reference=False)
+    nzs = min(CPU_SAMPLE_NZ, nz)
+    case = ibm.Case(case_params(ibm, nx, ny, nzs))
+    orc = pyoracle.Oracle(case, vel_tol=1e-8, p_tol=1e-8, mg_rap=1, mg_relax=2, mg_omega=1.0, mg_group_ratio=1.5)
+    orc.set_fields(*initial_state(case))
+    orc.step(1.0)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        orc.step(1.0)
+    dt = (time.perf_counter() - t0) / steps
+    scale = nz / float(nzs)
+    return {"value": 1.0 / (dt * scale), "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{steps} timestep(s) of a {nx}x{ny}x{nzs} z-slab of the same channel, "
+                      f"{dt:.2f} s each, scaled by the cell count ({scale:g}x)"}
+
+
+def reference_arm(args):
+    ws, rank, _ = dist()
+    if rank != 0:
+        return
+    ibm = importlib.import_module("ibm-3d-fpc_gb300")
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build(with_reference=False)
+    nzs = min(CPU_SAMPLE_NZ, args.nz)
+    case = ibm.Case(case_params(ibm, args.nx, args.ny, nzs))
+    orc = pyoracle.Oracle(case, vel_tol=1e-8, p_tol=1e-8, mg_rap=1, mg_relax=2, mg_omega=1.0, mg_group_ratio=1.5)
+    orc.set_fields(*initial_state(case))
+    for _ in range(args.warmup):
+        orc.step(1.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.step(1.0)
+    dt = (time.perf_counter() - t0) / max(1, args.steps)
+    scale = args.nz / float(nzs)
+    value = 1.0 / (dt * scale)
+    sample = (f"each step: one timestep of a {args.nx}x{args.ny}x{nzs} z-slab of the channel on the CPU "
+              f"oracle (FP64 GMRES + semicoarsening multigrid), scaled by the cell count ({scale:g}x)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * scale * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"full timestep {args.nx}x{args.ny}x{args.nz} channel, Um=2.25, dt=2e-4",
+                       "grid": [args.nx, args.ny, args.nz]},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    ws, rank, local = dist()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist_
+        dist_.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ibm = importlib.import_module("ibm-3d-fpc_gb300")
+    native = importlib.import_module("ibm-3d-fpc_gb300._native")
+    Prof, plib = profile_struct(native)
+    nx, ny, nz = args.nx, args.ny, args.nz
+    t_setup = time.perf_counter()
+    case = ibm.Case(case_params(ibm, nx, ny, nz))
+    state = initial_state(case)
+    mixed = ibm.Solver(case, solver_params(ibm, 1), device=local)
+    mixed.set_fields(*state)
+    setup_s = time.perf_counter() - t_setup
+
+    # warm-up (also builds the multigrid hierarchy)
+    run_steps(mixed, args.warmup)
+    # pick the dominant kernel class: one step per candidate with its launches timed
+    candidates = [k for k in range(22)]
+    per_class = {}
+    for k in candidates:
+        plib.ibm_profile_reset(mixed._ctx)
+        plib.ibm_profile_time_kernel(mixed._ctx, k)
+        run_steps(mixed, 1)
+        p = read_profile(plib, Prof, mixed._ctx)
+        per_class[k] = p.time_ms[k]
+    n_cal = len(candidates)
+    dom = max(per_class, key=lambda k: per_class[k])
+    plib.ibm_profile_reset(mixed._ctx)
+    plib.ibm_profile_time_kernel(mixed._ctx, dom)
+
+    stream = device_timer(plib, mixed._ctx)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = mixed.launches()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_stats = []
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step_stats.append(mixed.step(1.0))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = mixed.launches() - l0
+    prof = read_profile(plib, Prof, mixed._ctx)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = ws * args.steps / (ms / 1e3)
+
+    t_p = sum(s.t_p_ms for s in step_stats)
+    t_mom = sum(s.t_mom_ms for s in step_stats)
+    solve_gbs = {"pressure": prof.phase_bytes[2] / (t_p * 1e-3) / 1e9 if t_p > 0 else None,
+                 "momentum": prof.phase_bytes[1] / (t_mom * 1e-3) / 1e9 if t_mom > 0 else None,
+                 "step": sum(prof.phase_bytes) / (ms * 1e-3) / 1e9}
+    its = {f: float(np.mean([getattr(s, f).iters for s in step_stats])) for f in ("u", "v", "w", "p")}
+    peak, peak_kind = measured_peaks()
+    kname = plib.ibm_kernel_name(dom).decode()
+    n_l = max(1, prof.timed_launches[dom])
+    bytes_per_launch = prof.bytes[dom] / max(1, prof.launches[dom])
+    achieved = bytes_per_launch / (prof.time_ms[dom] / n_l * 1e-3) / 1e9 if prof.time_ms[dom] > 0 else 0.0
+    roofline = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": traffic_for(kname, bytes_per_launch),
+                "algorithmic_bytes_per_launch": bytes_per_launch,
+                "share_of_step_device_time": prof.time_ms[dom] / ms}
+    mixed_fields = mixed.fields()
+
+    out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+           "config": {"workload": f"full timestep {nx}x{ny}x{nz} channel (cylinder D=0.1 at (0.5,0.2)), Um=2.25, "
+                                  f"nu=1e-3, dt=2e-4, mixed FP32-preconditioned FP64 FGMRES tol 1e-8",
+                      "grid": [nx, ny, nz], "parallelism": f"replicas x{ws}",
+                      "l2": "inputs larger than L2 (operators + fields ~25 GB resident)",
+                      "pressure_pc": "semicoarsening MG, grouped, 7-point coarse, two-colour relaxation, FP32",
+                      "momentum_pc": "3 FP32 Jacobi sweeps"},
+           "solve_gbs": solve_gbs, "iterations_mean": its, "gpu_launches": int(launches),
+           "setup_s": setup_s, "calibration_steps": n_cal}
+
+    if not args.no_fp64:
+        fp64 = ibm.Solver(case, solver_params(ibm, 0), device=local)
+        fp64.set_fields(*state)
+        run_steps(fp64, args.warmup + n_cal)
+        torch.cuda.synchronize()
+        s64 = device_timer(plib, fp64._ctx)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s64)
+        st64 = [fp64.step(1.0) for _ in range(args.steps)]
+        e1.record(s64)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        f64 = fp64.fields()
+        vel_err = max(float(np.abs(a - b).max()) for a, b in zip(mixed_fields[:3], f64[:3])) / float(np.abs(f64[0]).max())
+        p_err = float(np.abs(mixed_fields[3] - f64[3]).max() / max(np.abs(f64[3]).max(), 1e-300))
+        out["fp64_plain"] = {"value": ws * args.steps / (ms64 / 1e3), "ms_per_step": ms64 / args.steps,
+                             "iterations_mean": {f: float(np.mean([getattr(s, f).iters for s in st64]))
+                                                 for f in ("u", "v", "w", "p")}}
+        out["speedup_vs_fp64"] = out["fp64_plain"]["ms_per_step"] / ms_per_step
+        out["velocity_rel_err_vs_fp64"] = vel_err
+        out["pressure_rel_err_vs_fp64"] = p_err
+        fp64.close()
+
+    if not args.no_e2e:
+        pinned = [torch.from_numpy(np.array(x)).pin_memory() for x in mixed_fields]
+        outs = [torch.empty_like(x).pin_memory() for x in pinned]
+        import ctypes as C
+        lib = native.gpu()
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            mixed._check(lib.ibm_set_fields(mixed._ctx, *[ptr(t) for t in pinned]))
+            mixed.step(1.0)
+            mixed._check(lib.ibm_get_fields(mixed._ctx, *[ptr(t) for t in outs]))
+        dt = time.perf_counter() - t0
+        nbytes = sum(t.numel() * 8 for t in pinned)
+        out["e2e"] = {"value": ws * args.steps / dt, "unit": "steps/s", "h2d_bytes_per_step": nbytes + 8,
+                      "d2h_bytes_per_step": nbytes + 4 * 8}
+    out["roofline"] = roofline
+    out["clocks"] = clk.summary()
+    if rank == 0 and not args.no_cpu:
+        try:
+            out["cpu_baseline"] = cpu_baseline(ibm, nx, ny, nz)
+        except Exception as e:  # the line must still print
+            out["cpu_baseline"] = {"value": None, "error": str(e)}
+    mixed.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -37,11 +37,16 @@ namespace {
 
 struct Scope {
   long long *prev;
-  explicit Scope(ibm_ctx *c) : prev(g_counter) {
+  Prof *prev_prof;
+  explicit Scope(ibm_ctx *c) : prev(g_counter), prev_prof(current_prof()) {
     g_counter = &c->launches;
+    current_prof() = &c->prof;
     cudaSetDevice(c->device);
   }
-  ~Scope() { g_counter = prev; }
+  ~Scope() {
+    g_counter = prev;
+    current_prof() = prev_prof;
+  }
 };
 
 std::string g_create_error;
@@ -165,6 +170,7 @@ void ensure_solvers(ibm_ctx *c) {
     mp.nu1 = p.mg_nu1; mp.nu2 = p.mg_nu2; mp.omega = p.mg_omega;
     mp.coarse_max = p.mg_coarse_max; mp.max_levels = p.mg_max_levels;
     mp.cycles = std::max(1, p.p_pc_maxit);
+    mp.group_ratio = p.mg_group_ratio;
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed);
     if (mixed) { hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; }
@@ -176,14 +182,84 @@ void ensure_solvers(ibm_ctx *c) {
   c->kp.configure(1, &hp);
   c->solvers_ready = true;
   c->solvers_precision = p.precision;
+  c->graph_ready = false;
+  c->graph_bound = false;
 }
 
 int worst(int a, int b) { return std::max(a, b); }
 
+// HYPRE's GMRES returns success when it stops because the true residual no
+// longer decreases (it only flags reaching max_iter above tolerance); the
+// true relative residual is reported either way.
+int solve_status(const KResult &r) {
+  return (r.status == 1 || r.status == 3) ? IBM_OK : IBM_NOT_CONVERGED;
+}
+
+void invalidate_graph(ibm_ctx *c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  c->gexec = nullptr;
+  c->graph_ready = false;
+}
+
+// Captures one timestep into c->gexec. Launch accounting during the capture
+// goes to a scratch counter; per step it is the fixed launches plus the loop
+// bodies the device ran (counted on the device).
+void build_step_graph(ibm_ctx *c, const Precond &none, const Precond &mgp) {
+  invalidate_graph(c);
+  cudaStream_t st = c->st;
+  Prof *saved_prof = current_prof();
+  long long *saved_counter = g_counter;
+  long long cap_count = 0;
+  current_prof() = nullptr;
+  g_counter = &cap_count;
+  cudaGraph_t graph = nullptr;
+  Krylov::GraphCounts gm, gp;
+  try {
+    IBM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    IBM_CUDA_TRY(cudaMemcpyAsync(c->dramp.p, c->hramp, sizeof(double), cudaMemcpyHostToDevice, st));
+    IBM_CUDA_TRY(cudaMemsetAsync(c->diag.p, 0, sizeof(StepDiag), st));
+    IBM_CUDA_TRY(cudaMemsetAsync(c->dloops.p, 0, sizeof(unsigned long long) * 4, st));
+    IBM_CUDA_TRY(cudaEventRecordWithFlags(c->ev[0], st, cudaEventRecordExternal));
+    launch_bc(c, c->u.p, c->v.p, c->w.p);
+    launch_momentum_rhs(c);
+    IBM_CUDA_TRY(cudaEventRecordWithFlags(c->ev[1], st, cudaEventRecordExternal));
+    gm = c->kmom.enqueue_graph(st, c->cap, none, c->hflags_graph, c->dloops.p);
+    IBM_CUDA_TRY(cudaEventRecordWithFlags(c->ev[2], st, cudaEventRecordExternal));
+    launch_tilde(c);
+    launch_pressure_rhs(c);
+    IBM_CUDA_TRY(cudaEventRecordWithFlags(c->ev[5], st, cudaEventRecordExternal));
+    gp = c->kp.enqueue_graph(st, c->cap, mgp, c->hflags_graph + 3, c->dloops.p + 2);
+    IBM_CUDA_TRY(cudaEventRecordWithFlags(c->ev[3], st, cudaEventRecordExternal));
+    launch_projection(c);
+    IBM_CUDA_TRY(cudaEventRecordWithFlags(c->ev[4], st, cudaEventRecordExternal));
+    IBM_CUDA_TRY(cudaMemcpyAsync(c->hdiag, c->diag.p, sizeof(StepDiag), cudaMemcpyDeviceToHost, st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(c->hloops, c->dloops.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
+    IBM_CUDA_TRY(cudaStreamEndCapture(st, &graph));
+  } catch (...) {
+    cudaGraph_t junk = nullptr;
+    cudaStreamEndCapture(st, &junk);
+    if (junk) cudaGraphDestroy(junk);
+    current_prof() = saved_prof;
+    g_counter = saved_counter;
+    throw;
+  }
+  current_prof() = saved_prof;
+  g_counter = saved_counter;
+  const cudaError_t e = cudaGraphInstantiate(&c->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  IBM_CUDA_TRY(e);
+  c->graph_fixed_launches = cap_count - gm.loop - gp.loop;
+  c->graph_body_launches[0] = gm.end_body;
+  c->graph_body_launches[1] = gm.arnoldi_body;
+  c->graph_body_launches[2] = gp.end_body;
+  c->graph_body_launches[3] = gp.arnoldi_body;
+  c->graph_ready = true;
+}
+
 void fill_solve(ibm_solve_stats &o, const KResult &r) {
   o.iters = r.iters;
   o.rel_res = r.rel_res;
-  o.status = (r.status == 1) ? IBM_OK : IBM_NOT_CONVERGED;
+  o.status = solve_status(r);
 }
 
 }  // namespace
@@ -201,6 +277,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->p_pc = 1; p->p_pc_maxit = 1; p->p_pc_relax_type = 1; p->p_pc_rap_type = 1;
   p->mg_nu1 = 1; p->mg_nu2 = 1; p->mg_omega = 2.0 / 3.0; p->mg_coarse_max = 64; p->mg_max_levels = 40;
   p->use_zero_initial_guess = 1; p->precision = 0; p->use_graph = 0; p->vel_inner_sweeps = 3;
+  p->mg_group_ratio = 0.0;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -243,6 +320,13 @@ int ibm_create(const ibm_grid_desc *grid, ibm_ctx **out) {
     }
     c->u.zero(c->st); c->v.zero(c->st); c->w.zero(c->st); c->p.zero(c->st);
     c->diag.alloc(1);
+    c->dramp.alloc(1);
+    c->dloops.alloc(4);
+    IBM_CUDA_TRY(cudaMallocHost((void **)&c->hramp, sizeof(double)));
+    *c->hramp = 1.0;
+    IBM_CUDA_TRY(cudaMallocHost((void **)&c->hflags_graph, sizeof(KFlags) * 4));
+    IBM_CUDA_TRY(cudaMallocHost((void **)&c->hloops, sizeof(unsigned long long) * 4));
+    for (auto &s : c->cap) IBM_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     c->part.alloc(4 * 1024);
     IBM_CUDA_TRY(cudaMallocHost((void **)&c->hdiag, sizeof(StepDiag)));
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
@@ -264,6 +348,12 @@ void ibm_destroy(ibm_ctx *c) {
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->hdiag) cudaFreeHost(c->hdiag);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->hramp) cudaFreeHost(c->hramp);
+  if (c->hflags_graph) cudaFreeHost(c->hflags_graph);
+  if (c->hloops) cudaFreeHost(c->hloops);
+  for (auto s : c->cap)
+    if (s) cudaStreamDestroy(s);
   cudaStream_t st = c->st;
   delete c;
   if (st) cudaStreamDestroy(st);
@@ -283,13 +373,16 @@ int ibm_set_operator(ibm_ctx *c, int field, const double *vals7, int nbx, int nb
     IBM_CUDA_TRY(cudaMemcpyAsync(tmp.p, vals7, sizeof(double) * 7 * n, cudaMemcpyDefault, c->st));
     o.c.alloc((size_t)7 * n); o.cj.alloc((size_t)7 * n); o.invd.alloc(n);
     o.cf.alloc((size_t)7 * n); o.invdf.alloc(n);
-    k_op_planes<<<grid1d(n), kThreads, 0, c->st>>>(tmp.p, n, o.c.p, o.invd.p, o.cf.p, o.invdf.p);
-    k_op_jacobi<<<grid1d(n), kThreads, 0, c->st>>>(o.c.p, o.invd.p, o.cj.p, b);
-    count_launch(2);
+    {
+      LaunchScope ls(K_SETUP, c->st, 0.0, 2);
+      k_op_planes<<<grid1d(n), kThreads, 0, c->st>>>(tmp.p, n, o.c.p, o.invd.p, o.cf.p, o.invdf.p);
+      k_op_jacobi<<<grid1d(n), kThreads, 0, c->st>>>(o.c.p, o.invd.p, o.cj.p, b);
+    }
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
     IBM_CUDA_TRY(cudaGetLastError());
     o.set = true;
     c->solvers_ready = false;
+    invalidate_graph(c);
     return IBM_OK;
   });
 }
@@ -350,6 +443,7 @@ int ibm_set_masks(ibm_ctx *c, const uint8_t *active_u, const uint8_t *active_v, 
     c->aux_set = false;
     c->csr_set = false;
     c->solvers_ready = false;
+    invalidate_graph(c);
     // id of each solve-box row, for the conversion of the id-indexed aux vectors
     c->h_id_u_rows.clear();
     for (int k = 0; k < nz; ++k)
@@ -409,6 +503,7 @@ int ibm_set_aux(ibm_ctx *c, const double *scale_u, const double *scale_v, const 
     upload(c->div_bc_cell, dcell, c->st);
     upload(c->uin, to_host(uin, (size_t)c->g.ny * c->g.nz), c->st);
     c->aux_set = true;
+    invalidate_graph(c);
     return IBM_OK;
   });
 }
@@ -499,6 +594,7 @@ int ibm_set_projection_csr(ibm_ctx *c, const int32_t *D_rowptr, const int32_t *D
     upload(c->Dc, Dc, c->st);
     upload(c->Gu, Gu, c->st); upload(c->Gv, Gv, c->st); upload(c->Gw, Gw, c->st);
     c->csr_set = true;
+    invalidate_graph(c);
     return IBM_OK;
   });
 }
@@ -516,6 +612,7 @@ int ibm_set_solver_params(ibm_ctx *c, const ibm_solver_params *p) {
       throw Error(IBM_ERR_ARG, "bad multigrid parameters");
     c->prm = *p;
     c->solvers_ready = false;
+    invalidate_graph(c);
     return IBM_OK;
   });
 }
@@ -553,31 +650,71 @@ int ibm_step(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
     require_inputs(c);
     ensure_solvers(c);
     cudaStream_t st = c->st;
-    IBM_CUDA_TRY(cudaMemsetAsync(c->diag.p, 0, sizeof(StepDiag), st));
-    IBM_CUDA_TRY(cudaEventRecord(c->ev[0], st));
-    launch_bc(c, c->u.p, c->v.p, c->w.p, ramp);
-    launch_momentum_rhs(c);
-    IBM_CUDA_TRY(cudaEventRecord(c->ev[1], st));
+    *c->hramp = ramp;
+    KResult rm[3], rp[1];
     const double *bm[3] = {c->bb[0].p, c->bb[1].p, c->bb[2].p};
     double *xm[3] = {c->xb[0].p, c->xb[1].p, c->xb[2].p};
-    KResult rm[3], rp[1];
-    Precond none;
-    c->kmom.solve(st, bm, xm, none, rm);
-    IBM_CUDA_TRY(cudaEventRecord(c->ev[2], st));
-    launch_tilde(c, ramp);
-    launch_pressure_rhs(c, ramp);
     const double *bp[1] = {c->bb[3].p};
     double *xp[1] = {c->xb[3].p};
-    Precond mgp;
+    Precond none, mgp;
     mgp.ctx = c;
     mgp.apply = mg_apply_cb;
-    c->kp.solve(st, bp, xp, mgp, rp);
-    IBM_CUDA_TRY(cudaEventRecord(c->ev[3], st));
-    launch_projection(c, ramp);
-    IBM_CUDA_TRY(cudaEventRecord(c->ev[4], st));
-    IBM_CUDA_TRY(cudaMemcpyAsync(c->hdiag, c->diag.p, sizeof(StepDiag), cudaMemcpyDeviceToHost, st));
-    IBM_CUDA_TRY(cudaStreamSynchronize(st));
-    IBM_CUDA_TRY(cudaGetLastError());
+    if (c->prm.use_graph) {
+      // The whole step as one graph launch; the GMRES loops run on the device.
+      if (!c->graph_ready || !c->graph_bound) {
+        c->kmom.bind(st, bm, xm, ~0u);
+        c->kp.bind(st, bp, xp, ~0u);
+        c->graph_bound = true;
+      }
+      if (!c->graph_ready) build_step_graph(c, none, mgp);
+      IBM_CUDA_TRY(cudaGraphLaunch(c->gexec, st));
+      IBM_CUDA_TRY(cudaStreamSynchronize(st));
+      IBM_CUDA_TRY(cudaGetLastError());
+      for (int s = 0; s < 4; ++s) {
+        const KFlags &f = c->hflags_graph[s];
+        KResult &r = s < 3 ? rm[s] : rp[0];
+        r.iters = f.iters; r.rel_res = f.rel; r.status = f.status; r.nonfinite = f.nonfinite;
+      }
+      const unsigned long long *lp = c->hloops;
+      c->launches += c->graph_fixed_launches + (long long)lp[0] * c->graph_body_launches[0] +
+                     (long long)lp[1] * c->graph_body_launches[1] + (long long)lp[2] * c->graph_body_launches[2] +
+                     (long long)lp[3] * c->graph_body_launches[3];
+    } else {
+      IBM_CUDA_TRY(cudaMemcpyAsync(c->dramp.p, c->hramp, sizeof(double), cudaMemcpyHostToDevice, st));
+      IBM_CUDA_TRY(cudaMemsetAsync(c->diag.p, 0, sizeof(StepDiag), st));
+      IBM_CUDA_TRY(cudaEventRecord(c->ev[0], st));
+      {
+        PhaseScope ph(PH_RHS);
+        launch_bc(c, c->u.p, c->v.p, c->w.p);
+        launch_momentum_rhs(c);
+      }
+      IBM_CUDA_TRY(cudaEventRecord(c->ev[1], st));
+      {
+        PhaseScope ph(PH_MOM);
+        c->kmom.solve(st, bm, xm, none, rm);
+      }
+      IBM_CUDA_TRY(cudaEventRecord(c->ev[2], st));
+      {
+        PhaseScope ph(PH_RHS);
+        launch_tilde(c);
+        launch_pressure_rhs(c);
+      }
+      IBM_CUDA_TRY(cudaEventRecord(c->ev[5], st));
+      {
+        PhaseScope ph(PH_P);
+        c->kp.solve(st, bp, xp, mgp, rp);
+      }
+      IBM_CUDA_TRY(cudaEventRecord(c->ev[3], st));
+      {
+        PhaseScope ph(PH_PROJ);
+        launch_projection(c);
+      }
+      IBM_CUDA_TRY(cudaEventRecord(c->ev[4], st));
+      IBM_CUDA_TRY(cudaMemcpyAsync(c->hdiag, c->diag.p, sizeof(StepDiag), cudaMemcpyDeviceToHost, st));
+      IBM_CUDA_TRY(cudaStreamSynchronize(st));
+      IBM_CUDA_TRY(cudaGetLastError());
+      c->prof.drain();
+    }
     int rc = IBM_OK;
     const StepDiag &dg = *c->hdiag;
     if (stats) {
@@ -589,13 +726,14 @@ int ibm_step(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
       stats->umax = dg.umax; stats->vmax = dg.vmax; stats->wmax = dg.wmax;
       float ms;
       cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); stats->t_rhs_ms = ms;
+      cudaEventElapsedTime(&ms, c->ev[2], c->ev[5]); stats->t_rhs_ms += ms;
       cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); stats->t_mom_ms = ms;
-      cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); stats->t_p_ms = ms;
+      cudaEventElapsedTime(&ms, c->ev[5], c->ev[3]); stats->t_p_ms = ms;
       cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); stats->t_proj_ms = ms;
       cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); stats->t_total_ms = ms;
     }
-    for (int f = 0; f < 3; ++f) rc = worst(rc, rm[f].status == 1 ? IBM_OK : IBM_NOT_CONVERGED);
-    rc = worst(rc, rp[0].status == 1 ? IBM_OK : IBM_NOT_CONVERGED);
+    for (int f = 0; f < 3; ++f) rc = worst(rc, solve_status(rm[f]));
+    rc = worst(rc, solve_status(rp[0]));
     const bool bad_mom = dg.nonfinite_mom || rm[0].nonfinite || rm[1].nonfinite || rm[2].nonfinite;
     const bool bad_p = dg.nonfinite_p || rp[0].nonfinite;
     if (bad_mom || bad_p) {
@@ -621,6 +759,7 @@ int ibm_solve(ibm_ctx *c, int field, const double *b, double *x, ibm_solve_stats
       double *xm[3] = {c->xb[0].p, c->xb[1].p, c->xb[2].p};
       Precond none;
       c->kmom.solve(c->st, bm, xm, none, r, 1u << field);
+      c->graph_bound = false;
       r[0] = r[field];
     } else {
       const double *bp[1] = {c->bb[3].p};
@@ -634,7 +773,7 @@ int ibm_solve(ibm_ctx *c, int field, const double *b, double *x, ibm_solve_stats
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
     if (stats) fill_solve(*stats, r[0]);
     if (r[0].nonfinite) { c->err = "non-finite solve output"; return (int)IBM_ERR_NONFINITE; }
-    return r[0].status == 1 ? (int)IBM_OK : (int)IBM_NOT_CONVERGED;
+    return solve_status(r[0]);
   });
 }
 
@@ -646,8 +785,10 @@ int ibm_apply_operator(ibm_ctx *c, int field, const double *x, double *y) {
     DBuf<double> dx, dy;
     dx.alloc(b.n); dy.alloc(b.n);
     IBM_CUDA_TRY(cudaMemcpyAsync(dx.p, x, sizeof(double) * b.n, cudaMemcpyDefault, c->st));
-    k_spmv7<<<grid1d(b.n), kThreads, 0, c->st>>>(c->op[field].c.p, b, dx.p, dy.p);
-    count_launch();
+    {
+      LaunchScope ls(K_SETUP, c->st, 72.0 * b.n);
+      k_spmv7<<<grid1d(b.n), kThreads, 0, c->st>>>(c->op[field].c.p, b, dx.p, dy.p);
+    }
     IBM_CUDA_TRY(cudaMemcpyAsync(y, dy.p, sizeof(double) * b.n, cudaMemcpyDefault, c->st));
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
     return IBM_OK;
@@ -674,6 +815,34 @@ int ibm_synchronize(ibm_ctx *c) {
 }
 
 void *ibm_stream(ibm_ctx *c) { return c ? (void *)c->st : nullptr; }
+
+int ibm_profile_reset(ibm_ctx *c) {
+  if (!c) return IBM_ERR_ARG;
+  c->prof.reset();
+  return IBM_OK;
+}
+
+int ibm_profile_time_kernel(ibm_ctx *c, int kernel) {
+  if (!c || kernel < -1 || kernel >= K_COUNT) return IBM_ERR_ARG;
+  c->prof.timed_kernel = kernel;
+  return IBM_OK;
+}
+
+int ibm_profile_get(ibm_ctx *c, ibm_profile *out) {
+  if (!c || !out) return IBM_ERR_ARG;
+  memset(out, 0, sizeof(*out));
+  out->nkernels = K_COUNT;
+  for (int k = 0; k < K_COUNT && k < IBM_PROFILE_MAX_KERNELS; ++k) {
+    out->launches[k] = c->prof.launches[k];
+    out->bytes[k] = c->prof.bytes[k];
+    out->time_ms[k] = c->prof.ms[k];
+    out->timed_launches[k] = c->prof.timed[k];
+  }
+  for (int q = 0; q < PH_COUNT && q < 5; ++q) out->phase_bytes[q] = c->prof.phase_bytes[q];
+  return IBM_OK;
+}
+
+const char *ibm_kernel_name(int kernel) { return kernel_name(kernel); }
 
 long long ibm_kernel_launches(ibm_ctx *c) { return c ? c->launches : 0; }
 

@@ -206,4 +206,54 @@ int sm_count();
 void count_launch(long long n = 1);
 long long launches();
 
+// Kernel classes for accounting (ibm_profile in include/ibm_gpu.h).
+enum KernelId {
+  K_BC = 0, K_RHS, K_SCATTER, K_PRHS, K_PROJECT, K_DIAG,
+  K_GM_INIT, K_GM_SPMV, K_GM_ORTH, K_GM_NEXT, K_GM_UPDATE, K_GM_RESID, K_GM_ADDZ, K_GM_JAC32,
+  K_MG_LOAD, K_MG_RELAX, K_MG_RESID, K_MG_RESTRICT, K_MG_PROLONG, K_MG_DENSE, K_MG_STORE,
+  K_SETUP, K_COUNT
+};
+const char *kernel_name(int k);
+
+// Records one launch of kernel class k moving `bytes` algorithmic bytes; when
+// k is the context's timed class, the launch is bracketed by CUDA events on
+// stream st. Construct immediately before the launch, destroy after it.
+struct LaunchScope {
+  LaunchScope(KernelId k, cudaStream_t st, double bytes, long long n = 1);
+  ~LaunchScope();
+  KernelId k;
+  cudaStream_t st;
+  int slot = -1;
+};
+
+// Per-context accounting state (one per ibm_ctx; current one is thread-local).
+enum Phase { PH_RHS = 0, PH_MOM, PH_P, PH_PROJ, PH_OTHER, PH_COUNT };
+struct Prof {
+  long long launches[K_COUNT] = {};
+  double bytes[K_COUNT] = {};
+  double ms[K_COUNT] = {};
+  long long timed[K_COUNT] = {};
+  double phase_bytes[PH_COUNT] = {};
+  int phase = PH_OTHER;
+  int timed_kernel = -1;
+  std::vector<cudaEvent_t> pool;
+  struct Pending { int k; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  void reset();
+  void drain();  // call after the stream is synchronised
+  ~Prof();
+};
+Prof *&current_prof();
+struct PhaseScope {
+  int prev;
+  explicit PhaseScope(int ph) {
+    Prof *p = current_prof();
+    prev = p ? p->phase : PH_OTHER;
+    if (p) p->phase = ph;
+  }
+  ~PhaseScope() {
+    if (Prof *p = current_prof()) p->phase = prev;
+  }
+};
+
 }  // namespace ibm

@@ -63,4 +63,19 @@ struct ibm_ctx {
   ibm::Krylov kmom, kp;
   ibm::Multigrid mg;
   cudaEvent_t ev[6] = {};
+  ibm::Prof prof;
+
+  // Inlet ramp of the current step, read by the kernels on the device.
+  ibm::DBuf<double> dramp;
+  double *hramp = nullptr;            // pinned staging copy
+  // Captured step (use_graph): one launch runs the whole step, GMRES loops included.
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_ready = false;
+  bool graph_bound = false;           // the Krylov system tables hold the step's full masks
+  cudaStream_t cap[2] = {};           // streams that capture conditional-node bodies
+  ibm::KFlags *hflags_graph = nullptr;  // pinned: u, v, w, p solve flags after a graph step
+  ibm::DBuf<unsigned long long> dloops;  // loop-body counters (momentum x2, pressure x2)
+  unsigned long long *hloops = nullptr;  // pinned copy
+  long long graph_fixed_launches = 0;
+  long long graph_body_launches[4] = {0, 0, 0, 0};
 };

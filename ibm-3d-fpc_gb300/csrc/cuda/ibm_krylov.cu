@@ -11,8 +11,9 @@
 //
 // Per Arnoldi step, three streaming kernels:
 //   k_arnoldi_spmv : w = A z_j and d1_k = (v_k, w)         (last block: h1, coefficients)
-//   k_arnoldi_orth : w -= V c1, d2_k = (v_k, w), |w|^2       (last block: h2, Givens, stop test)
-//   k_arnoldi_next : v_{j+1} = w - V c2                      (stored unnormalised; norms in nu[])
+//   k_arnoldi_orth : w -= V c1, d2_k = (v_k, w)              (last block: h2, Hessenberg column)
+//   k_arnoldi_next : v_{j+1} = w - V c2, |v_{j+1}|^2          (last block: Givens, stop test)
+// Basis vectors are stored unnormalised with their exact norms in nu[].
 // Reductions are deterministic: fixed per-warp order inside a block, block
 // partials summed in block order by the last block to finish.
 #include "ibm_common.cuh"
@@ -161,16 +162,16 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
   if (threadIdx.x == 0) sc->ticket = 0;
 }
 
-// w -= sum_k coef_k V_k; d2_k = (V_k, w); |w|^2. Last block: second
-// Gram-Schmidt pass coefficients, Hessenberg column, Givens, stop test.
+// w -= sum_k coef_k V_k (first pass), d2_k = (V_k, w). Last block: the
+// second-pass coefficients and the Hessenberg column above the diagonal.
 __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
   KSys &S = sys[blockIdx.y];
   KScal *sc = S.s;
   if (!sc->active) return;
   const int j = sc->i, nd = j + 1;
-  __shared__ double sacc[(kMaxKdim + 2) * kWarps];
+  __shared__ double sacc[(kMaxKdim + 1) * kWarps];
   __shared__ double cf[kMaxKdim + 1];
-  for (int t = threadIdx.x; t < (nd + 1) * kWarps; t += blockDim.x) sacc[t] = 0.0;
+  for (int t = threadIdx.x; t < nd * kWarps; t += blockDim.x) sacc[t] = 0.0;
   for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = sc->coef[t];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -187,33 +188,68 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
         wv[t] = w;
       }
     }
-    for (int kk = 0; kk <= nd; ++kk) {
+    for (int kk = 0; kk < nd; ++kk) {
       double p = 0.0;
 #pragma unroll
       for (int t = 0; t < kRowsPerThread; ++t) {
         const long r = t0 + t * kThreads + threadIdx.x;
-        if (r < S.n) p = fma(kk < nd ? S.V[(long)kk * S.ldv + r] : wv[t], wv[t], p);
+        if (r < S.n) p = fma(S.V[(long)kk * S.ldv + r], wv[t], p);
       }
       p = warp_sum(p);
       if (lane == 0) sacc[kk * kWarps + warp] += p;
     }
   }
-  if (!block_partials_and_last(sacc, nd + 1, S.part, &sc->ticket)) return;
-  __shared__ double tot[kMaxKdim + 2];
-  reduce_partials(S.part, gridDim.x, nd + 1, tot);
+  if (!block_partials_and_last(sacc, nd, S.part, &sc->ticket)) return;
+  __shared__ double tot[kMaxKdim + 1];
+  reduce_partials(S.part, gridDim.x, nd, tot);
+  __syncthreads();
+  for (int kk = threadIdx.x; kk < nd; kk += blockDim.x) {
+    const double h2 = tot[kk] / sc->nu[kk];
+    sc->coef[kk] = h2 / sc->nu[kk];
+    sc->H[kk * kMaxKdim + j] = sc->h1[kk] + h2;
+  }
+  if (threadIdx.x == 0) sc->ticket = 0;
+}
+
+// v_{j+1} = w - sum_k coef_k V_k, stored unnormalised, with its exact norm.
+// Last block: Hessenberg column, Givens rotation, stop test, and at the end
+// of a cycle the back substitution.
+__global__ void __launch_bounds__(kThreads) k_arnoldi_next(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active) return;
+  const int j = sc->i, nd = j + 1;
+  __shared__ double cf[kMaxKdim + 1];
+  __shared__ double sacc[kWarps];
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = sc->coef[t];
+  if (threadIdx.x < kWarps) sacc[threadIdx.x] = 0.0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *vn = S.V + (long)nd * S.ldv;
+  const bool store = nd < sc->kdim;  // the last vector of a full cycle is never used
+  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+    double p = 0.0;
+#pragma unroll
+    for (int t = 0; t < kRowsPerThread; ++t) {
+      const long r = t0 + t * kThreads + threadIdx.x;
+      if (r < S.n) {
+        double w = S.w[r];
+        for (int kk = 0; kk < nd; ++kk) w = fma(-cf[kk], S.V[(long)kk * S.ldv + r], w);
+        if (store) vn[r] = w;
+        p = fma(w, w, p);
+      }
+    }
+    p = warp_sum(p);
+    if (lane == 0) sacc[warp] += p;
+  }
+  if (!block_partials_and_last(sacc, 1, S.part, &sc->ticket)) return;
+  __shared__ double tot[1];
+  reduce_partials(S.part, gridDim.x, 1, tot);
   __syncthreads();
   if (threadIdx.x == 0) {
     sc->ticket = 0;
     const int K = kMaxKdim;
-    double h2sq = 0.0;
-    for (int kk = 0; kk < nd; ++kk) {
-      const double h2 = tot[kk] / sc->nu[kk];
-      sc->coef[kk] = h2 / sc->nu[kk];
-      sc->H[kk * K + j] = sc->h1[kk] + h2;
-      h2sq = fma(h2, h2, h2sq);
-    }
-    double nn = tot[nd] - h2sq;
-    const double hn = nn > 0.0 ? sqrt(nn) : 0.0;
+    const double hn = sqrt(tot[0]);
     sc->nu[j + 1] = hn;
     sc->H[(j + 1) * K + j] = hn;
     // apply previous rotations to the new column, then a new rotation
@@ -248,23 +284,6 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
       }
       for (int q = 0; q < m; ++q) sc->coef[q] = sc->y[q] / sc->nu[q];
     }
-  }
-}
-
-// v_{j+1} = w - sum_k coef_k V_k (only while the cycle continues).
-__global__ void __launch_bounds__(kThreads) k_arnoldi_next(KSys *sys) {
-  KSys &S = sys[blockIdx.y];
-  KScal *sc = S.s;
-  if (!sc->active) return;
-  const int nd = sc->i;  // already advanced: vectors 0..i-1 are used, V_i is written
-  __shared__ double cf[kMaxKdim + 1];
-  for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = sc->coef[t];
-  __syncthreads();
-  double *vn = S.V + (long)nd * S.ldv;
-  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
-    double w = S.w[r];
-    for (int kk = 0; kk < nd; ++kk) w = fma(-cf[kk], S.V[(long)kk * S.ldv + r], w);
-    vn[r] = w;
   }
 }
 
@@ -392,6 +411,24 @@ __global__ void k_flags(KSys *sys, int nsys, KFlags *out) {
   }
 }
 
+// Loop control of the graph form: WHILE runs while any system is active or
+// has a finished cycle to close; the SWITCH picks the cycle-end body (0) when
+// any system closed a cycle, else the Arnoldi body (1).
+__global__ void k_set_while(KSys *sys, int nsys, cudaGraphConditionalHandle hw) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned run = 0;
+  for (int s = 0; s < nsys; ++s) run |= (sys[s].s->active | sys[s].s->cycle_end) ? 1u : 0u;
+  cudaGraphSetConditional(hw, run);
+}
+
+__global__ void k_set_switch(KSys *sys, int nsys, cudaGraphConditionalHandle hs, unsigned long long *loops) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int end = 0;
+  for (int s = 0; s < nsys; ++s) end |= sys[s].s->cycle_end;
+  cudaGraphSetConditional(hs, end ? 0u : 1u);
+  loops[end ? 0 : 1] += 1;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -442,6 +479,7 @@ Krylov::~Krylov() {
 }
 
 void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask) {
+  bound_mask = mask;
   KSys hsys[kMaxSys];
   memset(hsys, 0, sizeof(hsys));
   for (int s = 0; s < nsys; ++s) {
@@ -469,27 +507,130 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     init[s].tol = slot[s].host.tol;
   }
   IBM_CUDA_TRY(cudaMemcpyAsync(scal.p, init, sizeof(KScal) * nsys, cudaMemcpyHostToDevice, st));
-  // the host copy is staged by the driver before the call returns for pageable memory
   IBM_CUDA_TRY(cudaStreamSynchronize(st));
 }
 
 void Krylov::read_flags(cudaStream_t st) {
-  k_flags<<<1, 32, 0, st>>>(dsys.p, nsys, dflags.p);
-  count_launch();
+  {
+    LaunchScope ls(K_GM_UPDATE, st, 0.0);
+    k_flags<<<1, 32, 0, st>>>(dsys.p, nsys, dflags.p);
+  }
   IBM_CUDA_TRY(cudaMemcpyAsync(hflags, dflags.p, sizeof(KFlags) * nsys, cudaMemcpyDeviceToHost, st));
   IBM_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
+// Algorithmic bytes per row (FP64 = 8): the operator's 7 coefficients, the
+// vectors each kernel must read or write once, and the basis vectors it
+// sweeps. In the graph form the flags are not known on the host and no
+// bytes are attributed.
+void Krylov::launch_cycle_end(cudaStream_t st, const Precond &pc, const KFlags *fl, unsigned mask) {
+  const dim3 grid(nblk, nsys), gridu(nblk * 2, nsys);
+  KSys *dev = dsys.p;
+  auto rows = [&](int s) { return ((mask >> s) & 1u) ? (double)slot[s].host.n : 0.0; };
+  double bu = 0.0, br = 0.0, ba = 0.0;
+  if (fl) {
+    for (int s = 0; s < nsys; ++s) {
+      if (!fl[s].cycle_end) continue;
+      const int m = fl[s].i, pcm = slot[s].host.pc;
+      bu += rows(s) * (pcm == 2 ? 4.0 * m + 16.0 : pcm == 1 ? 8.0 * m + 8.0 : 8.0 * m + 24.0);
+      br += 88.0 * rows(s);
+      if (pcm == 1) ba += 24.0 * rows(s);
+    }
+  }
+  {
+    LaunchScope ls(K_GM_UPDATE, st, bu);
+    k_cycle_update<<<gridu, kThreads, 0, st>>>(dev);
+  }
+  bool cb = false;
+  for (int s = 0; s < nsys; ++s) {
+    if (slot[s].host.pc != 1 || !((mask >> s) & 1u) || (fl && !fl[s].cycle_end)) continue;
+    VecRef in;
+    in.base = slot[s].z.p;
+    OutRef out;
+    out.d = slot[s].z2.p;
+    pc.apply(pc.ctx, st, s, in, out, &scal.p[s].cycle_end);
+    cb = true;
+  }
+  if (cb) {
+    LaunchScope ls(K_GM_ADDZ, st, ba);
+    k_add_z<<<gridu, kThreads, 0, st>>>(dev);
+  }
+  LaunchScope ls(K_GM_RESID, st, br);
+  k_cycle_residual<<<grid, kThreads, 0, st>>>(dev);
+}
+
+void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl, unsigned mask) {
+  const dim3 grid(nblk, nsys), gridu(nblk * 2, nsys);
+  KSys *dev = dsys.p;
+  auto rows = [&](int s) { return ((mask >> s) & 1u) ? (double)slot[s].host.n : 0.0; };
+  for (int s = 0; s < nsys; ++s) {
+    if (!((mask >> s) & 1u) || (fl && !fl[s].active)) continue;
+    const KSysHost &h = slot[s].host;
+    if (h.pc == 1) {
+      VecRef in;
+      in.base = slot[s].V.p; in.ld = h.n; in.idx = &scal.p[s].i;
+      OutRef out;
+      out.d = slot[s].z.p;
+      pc.apply(pc.ctx, st, s, in, out, &scal.p[s].active);
+    } else if (h.pc == 2 && h.pc_cb) {
+      VecRef in;
+      in.base = slot[s].V.p; in.ld = h.n; in.idx = &scal.p[s].i; in.nu = scal.p[s].nu;
+      OutRef out;
+      out.f = slot[s].Z.p; out.ld = h.n; out.idx = &scal.p[s].i;
+      pc.apply(pc.ctx, st, s, in, out, &scal.p[s].active);
+    }
+  }
+  int inner_sweeps = 0;
+  double r32 = 0.0, bsp = 0.0, bor = 0.0;
+  for (int s = 0; s < nsys; ++s) {
+    if (!((mask >> s) & 1u)) continue;
+    if (slot[s].host.pc == 2 && !slot[s].host.pc_cb && (!fl || fl[s].active))
+      inner_sweeps = std::max(inner_sweeps, std::max(1, slot[s].host.inner_sweeps));
+    if (!fl || !fl[s].active) continue;
+    const double j1 = fl[s].i + 1.0;
+    if (slot[s].host.pc == 2 && !slot[s].host.pc_cb) r32 += rows(s);
+    bsp += rows(s) * ((slot[s].host.pc == 2 ? 68.0 : 72.0) + 8.0 * j1);
+    bor += rows(s) * (16.0 + 8.0 * j1);
+  }
+  if (inner_sweeps > 0) {
+    if (inner_sweeps == 1) {
+      LaunchScope ls(K_GM_JAC32, st, 16.0 * r32);
+      k_jacobi32_first<<<gridu, kThreads, 0, st>>>(dev, 1);
+    } else {
+      {
+        LaunchScope ls(K_GM_JAC32, st, 16.0 * r32);
+        k_jacobi32_first<<<gridu, kThreads, 0, st>>>(dev, 0);
+      }
+      int src_zf = 1;
+      for (int q = 1; q < inner_sweeps; ++q) {
+        LaunchScope ls(K_GM_JAC32, st, 48.0 * r32);
+        k_jacobi32_sweep<<<gridu, kThreads, 0, st>>>(dev, src_zf, q == inner_sweeps - 1);
+        src_zf ^= 1;
+      }
+    }
+  }
+  {
+    LaunchScope ls(K_GM_SPMV, st, bsp);
+    k_arnoldi_spmv<<<grid, kThreads, 0, st>>>(dev);
+  }
+  {
+    LaunchScope ls(K_GM_ORTH, st, bor);
+    k_arnoldi_orth<<<grid, kThreads, 0, st>>>(dev);
+  }
+  LaunchScope ls(K_GM_NEXT, st, bor);
+  k_arnoldi_next<<<grid, kThreads, 0, st>>>(dev);
 }
 
 void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, const Precond &pc,
                    KResult *res, unsigned mask) {
   bind(st, b, x, mask);
-  const dim3 grid(nblk, nsys), gridu(nblk * 2, nsys);
-  k_init<<<grid, kThreads, 0, st>>>(dsys.p, nsys);
-  count_launch();
-  int inner_sweeps = 1;
-  for (int s = 0; s < nsys; ++s)
-    if (slot[s].host.pc == 2 && !slot[s].host.pc_cb) inner_sweeps = std::max(inner_sweeps, slot[s].host.inner_sweeps);
-  KSys *dev = dsys.p;
+  const dim3 grid(nblk, nsys);
+  double all_rows = 0.0;
+  for (int s = 0; s < nsys; ++s) all_rows += ((mask >> s) & 1u) ? (double)slot[s].host.n : 0.0;
+  {
+    LaunchScope ls(K_GM_INIT, st, 88.0 * all_rows);
+    k_init<<<grid, kThreads, 0, st>>>(dsys.p, nsys);
+  }
   for (long guard = 0;; ++guard) {
     if (guard > 4L * 1000 * 1000) throw Error(IBM_ERR_CUDA, "GMRES host loop did not terminate");
     read_flags(st);
@@ -499,62 +640,8 @@ void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, co
       any_end |= hflags[s].cycle_end != 0;
     }
     if (!any_active && !any_end) break;
-    if (any_end) {
-      // Solution update of the systems whose cycle ended, then the true residual.
-      k_cycle_update<<<gridu, kThreads, 0, st>>>(dev);
-      count_launch();
-      bool cb = false;
-      for (int s = 0; s < nsys; ++s) {
-        if (slot[s].host.pc != 1 || !hflags[s].cycle_end) continue;
-        VecRef in;
-        in.base = slot[s].z.p;
-        OutRef out;
-        out.d = slot[s].z2.p;
-        pc.apply(pc.ctx, st, s, in, out, &scal.p[s].cycle_end);
-        cb = true;
-      }
-      if (cb) { k_add_z<<<gridu, kThreads, 0, st>>>(dev); count_launch(); }
-      k_cycle_residual<<<grid, kThreads, 0, st>>>(dev);
-      count_launch();
-      continue;
-    }
-    // One Arnoldi step for every active system.
-    for (int s = 0; s < nsys; ++s) {
-      if (!hflags[s].active) continue;
-      const KSysHost &h = slot[s].host;
-      if (h.pc == 1) {
-        VecRef in;
-        in.base = slot[s].V.p; in.ld = h.n; in.idx = &scal.p[s].i;
-        OutRef out;
-        out.d = slot[s].z.p;
-        pc.apply(pc.ctx, st, s, in, out, &scal.p[s].active);
-      } else if (h.pc == 2 && h.pc_cb) {
-        VecRef in;
-        in.base = slot[s].V.p; in.ld = h.n; in.idx = &scal.p[s].i; in.nu = scal.p[s].nu;
-        OutRef out;
-        out.f = slot[s].Z.p; out.ld = h.n; out.idx = &scal.p[s].i;
-        pc.apply(pc.ctx, st, s, in, out, &scal.p[s].active);
-      }
-    }
-    bool internal32 = false;
-    for (int s = 0; s < nsys; ++s) internal32 |= (slot[s].host.pc == 2 && !slot[s].host.pc_cb && hflags[s].active);
-    if (internal32) {
-      if (inner_sweeps <= 1) { k_jacobi32_first<<<gridu, kThreads, 0, st>>>(dev, 1); count_launch(); }
-      else {
-        k_jacobi32_first<<<gridu, kThreads, 0, st>>>(dev, 0);
-        count_launch();
-        int src_zf = 1;
-        for (int q = 1; q < inner_sweeps; ++q) {
-          k_jacobi32_sweep<<<gridu, kThreads, 0, st>>>(dev, src_zf, q == inner_sweeps - 1);
-          count_launch();
-          src_zf ^= 1;
-        }
-      }
-    }
-    k_arnoldi_spmv<<<grid, kThreads, 0, st>>>(dev);
-    k_arnoldi_orth<<<grid, kThreads, 0, st>>>(dev);
-    k_arnoldi_next<<<gridu, kThreads, 0, st>>>(dev);
-    count_launch(3);
+    if (any_end) launch_cycle_end(st, pc, hflags, mask);
+    else launch_arnoldi(st, pc, hflags, mask);
   }
   for (int s = 0; s < nsys; ++s) {
     res[s].iters = hflags[s].iters;
@@ -563,6 +650,96 @@ void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, co
     res[s].nonfinite = hflags[s].nonfinite;
   }
   IBM_CUDA_TRY(cudaGetLastError());
+}
+
+namespace {
+
+// Adds a conditional node after the current dependencies of the capture on
+// `st` and makes it the new dependency; returns its body graphs.
+void add_conditional(cudaStream_t st, cudaGraphConditionalHandle *h, cudaGraphConditionalNodeType type,
+                     unsigned size, cudaGraph_t *bodies) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *ed = nullptr;
+  size_t nd = 0;
+  IBM_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &ed, &nd));
+  if (cs != cudaStreamCaptureStatusActive) throw Error(IBM_ERR_STATE, "graph capture not active");
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = *h;
+  p.conditional.type = type;
+  p.conditional.size = size;
+  cudaGraphNode_t node;
+  IBM_CUDA_TRY(cudaGraphAddNode(&node, g, deps, ed, nd, &p));
+  for (unsigned i = 0; i < size; ++i) bodies[i] = p.conditional.phGraph_out[i];
+  IBM_CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+}
+
+cudaGraph_t capture_graph_of(cudaStream_t st) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  IBM_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  return g;
+}
+
+template <class F>
+long long capture_body(cudaGraph_t body, cudaStream_t bs, F &&fn) {
+  const long long before = launches();
+  IBM_CUDA_TRY(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  fn(bs);
+  cudaGraph_t out = nullptr;
+  IBM_CUDA_TRY(cudaStreamEndCapture(bs, &out));
+  return launches() - before;
+}
+
+}  // namespace
+
+Krylov::GraphCounts Krylov::enqueue_graph(cudaStream_t st, const cudaStream_t body_st[2], const Precond &pc,
+                                          KFlags *host_flags, unsigned long long *loops) {
+  GraphCounts gc;
+  const long long t0 = launches();
+  const dim3 grid(nblk, nsys);
+  KSys *dev = dsys.p;
+  const unsigned mask = bound_mask;
+  {
+    LaunchScope ls(K_GM_INIT, st, 0.0);
+    k_init<<<grid, kThreads, 0, st>>>(dev, nsys);
+  }
+  cudaGraphConditionalHandle hw;
+  IBM_CUDA_TRY(cudaGraphConditionalHandleCreate(&hw, capture_graph_of(st), 0, 0));
+  {
+    LaunchScope ls(K_GM_UPDATE, st, 0.0);
+    k_set_while<<<1, 32, 0, st>>>(dev, nsys, hw);
+  }
+  cudaGraph_t wbody;
+  add_conditional(st, &hw, cudaGraphCondTypeWhile, 1, &wbody);
+  long long end_l = 0, arn_l = 0;
+  const long long loop_l = capture_body(wbody, body_st[0], [&](cudaStream_t b0) {
+    cudaGraphConditionalHandle hs;
+    IBM_CUDA_TRY(cudaGraphConditionalHandleCreate(&hs, wbody, 0, 0));
+    {
+      LaunchScope ls(K_GM_UPDATE, b0, 0.0);
+      k_set_switch<<<1, 32, 0, b0>>>(dev, nsys, hs, loops);
+    }
+    cudaGraph_t cases[2];
+    add_conditional(b0, &hs, cudaGraphCondTypeSwitch, 2, cases);
+    end_l = capture_body(cases[0], body_st[1], [&](cudaStream_t b1) { launch_cycle_end(b1, pc, nullptr, mask); });
+    arn_l = capture_body(cases[1], body_st[1], [&](cudaStream_t b1) { launch_arnoldi(b1, pc, nullptr, mask); });
+    LaunchScope ls(K_GM_UPDATE, b0, 0.0);
+    k_set_while<<<1, 32, 0, b0>>>(dev, nsys, hw);
+  });
+  {
+    LaunchScope ls(K_GM_UPDATE, st, 0.0);
+    k_flags<<<1, 32, 0, st>>>(dev, nsys, dflags.p);
+  }
+  IBM_CUDA_TRY(cudaMemcpyAsync(host_flags, dflags.p, sizeof(KFlags) * nsys, cudaMemcpyDeviceToHost, st));
+  const long long per_iter = loop_l - end_l - arn_l;  // the two control kernels
+  gc.end_body = end_l + per_iter;
+  gc.arnoldi_body = arn_l + per_iter;
+  gc.fixed = (launches() - t0) - loop_l;
+  gc.loop = loop_l;
+  return gc;
 }
 
 }  // namespace ibm

@@ -54,14 +54,31 @@ class Krylov {
              unsigned mask = ~0u);
   size_t bytes() const;
 
+  // Graph form. bind() fixes the vectors (outside any capture); enqueue_graph()
+  // records the whole solve into the capture running on `st`: the restart /
+  // Arnoldi loop is a WHILE node whose body SWITCHes between the cycle-end
+  // and the Arnoldi-step bodies, captured on body_st[0] / body_st[1].
+  // After the solve the per-system flags land in host_flags (pinned) and the
+  // numbers of cycle-end / Arnoldi bodies run in loops[0] / loops[1].
+  // Returns the launches recorded outside the loop and per body kind.
+  struct GraphCounts { long long fixed = 0, end_body = 0, arnoldi_body = 0, loop = 0; };
+  void bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask);
+  GraphCounts enqueue_graph(cudaStream_t st, const cudaStream_t body_st[2], const Precond &pc, KFlags *host_flags,
+                            unsigned long long *loops);
+
  private:
   struct Slot {
     KSysHost host;
     DBuf<double> V, w, r, z, z2, part;
     DBuf<float> Z, zf, zf2;
   };
-  void bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask);
   void read_flags(cudaStream_t st);
+  // Launch sequences shared by the host-driven and the graph form. With
+  // flags == nullptr every launch is recorded (each kernel is gated on the
+  // device flags of its system); otherwise only what the flags require.
+  void launch_cycle_end(cudaStream_t st, const Precond &pc, const KFlags *flags, unsigned mask);
+  void launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *flags, unsigned mask);
+  unsigned bound_mask = ~0u;
   int nsys = 0;
   int nblk = 0;
   Slot slot[kMaxSys];

@@ -272,7 +272,8 @@ __global__ void k_restrict(const T *res, const T *pm, const T *pp, Box fb, int d
 }
 
 template <class T>
-__global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb, int d, T *x, const int *gate) {
+__global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb, int d, T *x, int accumulate,
+                          const int *gate) {
   if (gate_off(gate)) return;
   const int cn[3] = {cb.nx, cb.ny, cb.nz};
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < fb.n; r += (long)gridDim.x * blockDim.x) {
@@ -295,7 +296,7 @@ __global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb,
       }
       corr = fmat<T>(pp[r], x1, pm[r] * x0);
     }
-    x[r] = x[r] + corr;
+    x[r] = accumulate ? x[r] + corr : corr;
   }
 }
 
@@ -380,20 +381,46 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
   L[0].ns = 7;
   L[0].A = A7;
   double h[3] = {h0[0], h0[1], h0[2]};
+  int queue[3], nq = 0;  // directions still to coarsen in the current group
   for (int l = 0;; ++l) {
     MgLevelT<double> &F = L[l];
     const long n = F.b.n;
     F.wd.alloc(n); F.invd.alloc(n); F.x.alloc(n); F.bv.alloc(n); F.r.alloc(n); F.t.alloc(n);
     // diagonal: plane 0 of a 7-point level, plane 13 of a 27-point level
     const double *diag = F.A + (F.ns == 27 ? 13L * n : 0L);
-    k_diag<<<grid_for(n), kThreads, 0, st>>>(diag, n, prm.omega, F.invd.p, F.wd.p);
-    count_launch();
-    int d = -1;
+    {
+      LaunchScope ls(K_SETUP, st, 0.0);
+      k_diag<<<grid_for(n), kThreads, 0, st>>>(diag, n, prm.omega, F.invd.p, F.wd.p);
+    }
     const int dims[3] = {F.b.nx, F.b.ny, F.b.nz};
-    for (int dd = 0; dd < 3; ++dd)
-      if (dims[dd] > 1 && (d < 0 || h[dd] < h[d])) d = dd;
+    // A group starts at a relaxed level: every direction whose spacing is
+    // within group_ratio of the smallest is coarsened once (smallest spacing
+    // first); levels inside the group are not relaxed.
+    F.relax = (nq == 0);
+    if (nq == 0) {
+      double hmin = 0.0;
+      bool any = false;
+      for (int dd = 0; dd < 3; ++dd)
+        if (dims[dd] > 1 && (!any || h[dd] < hmin)) { hmin = h[dd]; any = true; }
+      int cand[3], nc = 0;
+      for (int dd = 0; dd < 3; ++dd)
+        if (dims[dd] > 1 && (h[dd] == hmin || (prm.group_ratio > 0.0 && h[dd] <= prm.group_ratio * hmin)))
+          cand[nc++] = dd;
+      for (int a = 0; a < nc; ++a)
+        for (int b2 = a + 1; b2 < nc; ++b2)
+          if (h[cand[b2]] < h[cand[a]]) std::swap(cand[a], cand[b2]);
+      if (prm.group_ratio <= 0.0 && nc > 1) nc = 1;
+      for (int a = 0; a < nc; ++a) queue[a] = cand[nc - 1 - a];
+      nq = nc;
+    }
+    int d = -1;
+    while (nq > 0 && d < 0) {
+      const int q = queue[--nq];
+      if (dims[q] > 1) d = q;
+    }
     if (n <= prm.coarse_max || l + 1 >= prm.max_levels || d < 0 || l + 1 >= 60) {
       F.cdir = -1;
+      F.relax = 1;
       if (n > 4096) throw Error(IBM_ERR_ARG, "multigrid coarsest level too large for the dense solve");
       std::vector<double> hostA((size_t)F.ns * n), inv;
       IBM_CUDA_TRY(cudaMemcpyAsync(hostA.data(), F.A, sizeof(double) * hostA.size(), cudaMemcpyDeviceToHost, st));
@@ -407,8 +434,10 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
     F.cdir = d;
     h[d] *= 2.0;
     F.pm.alloc(n); F.pp.alloc(n);
-    k_interp_weights<<<grid_for(n), kThreads, 0, st>>>(F.A, F.ns, n, d, F.pm.p, F.pp.p);
-    count_launch();
+    {
+      LaunchScope ls(K_SETUP, st, 0.0);
+      k_interp_weights<<<grid_for(n), kThreads, 0, st>>>(F.A, F.ns, n, d, F.pm.p, F.pp.p);
+    }
     Box cb = F.b;
     if (d == 0) cb.nx = (F.b.nx + 1) / 2;
     if (d == 1) cb.ny = (F.b.ny + 1) / 2;
@@ -420,12 +449,16 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
     C.b = cb;
     DBuf<double> a27;
     a27.alloc((size_t)27 * cb.n);
-    k_rap<<<grid_for(cb.n), kThreads, 0, st>>>(Fr.A, Fr.ns, Fr.b, Fr.pm.p, Fr.pp.p, d, cb, a27.p);
-    count_launch();
+    {
+      LaunchScope ls(K_SETUP, st, 0.0);
+      k_rap<<<grid_for(cb.n), kThreads, 0, st>>>(Fr.A, Fr.ns, Fr.b, Fr.pm.p, Fr.pp.p, d, cb, a27.p);
+    }
     if (prm.rap == 1) {
       C.Aown.alloc((size_t)7 * cb.n);
-      k_collapse7<<<grid_for(cb.n), kThreads, 0, st>>>(a27.p, cb.n, C.Aown.p);
-      count_launch();
+      {
+        LaunchScope ls(K_SETUP, st, 0.0);
+        k_collapse7<<<grid_for(cb.n), kThreads, 0, st>>>(a27.p, cb.n, C.Aown.p);
+      }
       IBM_CUDA_TRY(cudaStreamSynchronize(st));
       C.ns = 7;
     } else {
@@ -455,15 +488,19 @@ void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const flo
       if (l == 0) F.A = A7f;
       else {
         F.Aown.alloc((size_t)D.ns * n);
-        k_convert<float><<<grid_for((long)D.ns * n), kThreads, 0, st>>>(D.A, F.Aown.p, (long)D.ns * n);
-        count_launch();
+        {
+          LaunchScope ls(K_SETUP, st, 0.0);
+          k_convert<float><<<grid_for((long)D.ns * n), kThreads, 0, st>>>(D.A, F.Aown.p, (long)D.ns * n);
+        }
         F.A = F.Aown.p;
       }
       auto conv = [&](const DBuf<double> &src, DBuf<float> &dst) {
         if (!src.p) return;
         dst.alloc(src.n);
-        k_convert<float><<<grid_for((long)src.n), kThreads, 0, st>>>(src.p, dst.p, (long)src.n);
-        count_launch();
+        {
+          LaunchScope ls(K_SETUP, st, 0.0);
+          k_convert<float><<<grid_for((long)src.n), kThreads, 0, st>>>(src.p, dst.p, (long)src.n);
+        }
       };
       conv(D.wd, F.wd); conv(D.invd, F.invd); conv(D.pm, F.pm); conv(D.pp, F.pp); conv(D.dense, F.dense);
       F.x.alloc(n); F.bv.alloc(n); F.r.alloc(n); F.t.alloc(n);
@@ -478,68 +515,82 @@ template <class T>
 static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgParams &p, const int *gate) {
   MgLevelT<T> &F = L[l];
   const long n = F.b.n;
+  const double T_ = sizeof(T);
   const int g = grid_for(n);
   if (F.cdir < 0) {
+    LaunchScope ls(K_MG_DENSE, st, T_ * ((double)n * n + 2.0 * n));
     k_dense<T><<<std::max(1, (int)std::min<long>((n + 7) / 8, (long)sm_count() * 4)), kThreads, 0, st>>>(
         F.dense.p, F.bv.p, F.x.p, (int)n, gate);
-    count_launch();
     return F.x.p;
   }
   T *cur = F.x.p, *oth = F.t.p;
+  const double sweep_bytes = T_ * n * (F.ns + 4.0);
   auto relax = [&](bool zero) {
     if (p.relax == 2) {
       for (int color = 0; color < 2; ++color) {
         const bool z = zero && color == 0;
+        LaunchScope ls(K_MG_RELAX, st, z ? 3.0 * T_ * n : sweep_bytes);
         if (F.ns == 7) k_relax_color<T, 7><<<g, kThreads, 0, st>>>(F.A, F.invd.p, F.bv.p, cur, oth, F.b, color, z, gate);
         else k_relax_color<T, 27><<<g, kThreads, 0, st>>>(F.A, F.invd.p, F.bv.p, cur, oth, F.b, color, z, gate);
-        count_launch();
         std::swap(cur, oth);
       }
     } else if (zero) {
+      LaunchScope ls(K_MG_RELAX, st, 3.0 * T_ * n);
       k_relax_zero<T><<<g, kThreads, 0, st>>>(F.wd.p, F.bv.p, cur, n, gate);
-      count_launch();
     } else {
+      LaunchScope ls(K_MG_RELAX, st, sweep_bytes);
       if (F.ns == 7) k_relax_jacobi<T, 7><<<g, kThreads, 0, st>>>(F.A, F.wd.p, F.bv.p, cur, oth, F.b, gate);
       else k_relax_jacobi<T, 27><<<g, kThreads, 0, st>>>(F.A, F.wd.p, F.bv.p, cur, oth, F.b, gate);
-      count_launch();
       std::swap(cur, oth);
     }
   };
-  if (p.nu1 > 0) {
-    for (int s = 0; s < p.nu1; ++s) relax(s == 0);
-  } else {
-    IBM_CUDA_TRY(cudaMemsetAsync(cur, 0, sizeof(T) * n, st));
+  // Inside a coarsening group (F.relax == 0) the level only passes the
+  // right-hand side down and the correction up.
+  const int nu1 = F.relax ? p.nu1 : 0, nu2 = F.relax ? p.nu2 : 0;
+  for (int s = 0; s < nu1; ++s) relax(s == 0);
+  const T *res = F.bv.p;  // residual of a zero initial guess is b
+  if (nu1 > 0) {
+    LaunchScope ls(K_MG_RESID, st, T_ * n * (F.ns + 3.0));
+    if (F.ns == 7) k_residual<T, 7><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
+    else k_residual<T, 27><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
+    res = F.r.p;
   }
-  if (F.ns == 7) k_residual<T, 7><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
-  else k_residual<T, 27><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
-  count_launch();
   MgLevelT<T> &C = L[l + 1];
-  k_restrict<T><<<grid_for(C.b.n), kThreads, 0, st>>>(F.r.p, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
-  count_launch();
+  {
+    LaunchScope ls(K_MG_RESTRICT, st, T_ * (3.0 * n + C.b.n));
+    k_restrict<T><<<grid_for(C.b.n), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
+  }
   T *xc = vcycle<T>(st, L, l + 1, p, gate);
-  k_prolong<T><<<g, kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, gate);
-  count_launch();
-  for (int s = 0; s < p.nu2; ++s) relax(false);
+  {
+    LaunchScope ls(K_MG_PROLONG, st, T_ * ((nu1 > 0 ? 4.0 : 3.0) * n + C.b.n));
+    k_prolong<T><<<g, kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, nu1 > 0, gate);
+  }
+  for (int s = 0; s < nu2; ++s) relax(false);
   return cur;
 }
 
 void Multigrid::apply(cudaStream_t st, const VecRef &in, const OutRef &out, const int *gate, bool use_fp32) {
   if (prm.cycles != 1) throw Error(IBM_ERR_UNSUPPORTED, "multigrid: only one V-cycle per application");
+  const double ob = out.d ? 8.0 : 4.0;
   if (use_fp32) {
     if (L32.empty()) throw Error(IBM_ERR_STATE, "multigrid: FP32 hierarchy not built");
     MgLevelT<float> &F = L32[0];
-    k_load_input<float><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, gate);
-    count_launch();
+    {
+      LaunchScope ls(K_MG_LOAD, st, 12.0 * F.b.n);
+      k_load_input<float><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, gate);
+    }
     float *x = vcycle<float>(st, L32, 0, prm, gate);
+    LaunchScope ls(K_MG_STORE, st, (4.0 + ob) * F.b.n);
     k_store_output<float><<<grid_for(F.b.n), kThreads, 0, st>>>(x, F.b.n, out, gate);
-    count_launch();
   } else {
     MgLevelT<double> &F = L64[0];
-    k_load_input<double><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, gate);
-    count_launch();
+    {
+      LaunchScope ls(K_MG_LOAD, st, 16.0 * F.b.n);
+      k_load_input<double><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, gate);
+    }
     double *x = vcycle<double>(st, L64, 0, prm, gate);
+    LaunchScope ls(K_MG_STORE, st, (8.0 + ob) * F.b.n);
     k_store_output<double><<<grid_for(F.b.n), kThreads, 0, st>>>(x, F.b.n, out, gate);
-    count_launch();
   }
 }
 

@@ -13,12 +13,14 @@ struct MgParams {
   int coarse_max = 64;
   int max_levels = 40;
   int cycles = 1;       // V-cycles per application
+  double group_ratio = 0.0;  // see ibm_solver_params.mg_group_ratio
 };
 
 template <class T>
 struct MgLevelT {
   Box b;
   int cdir = -1;        // direction coarsened to reach the next level; -1 on the coarsest
+  int relax = 1;        // 0 inside a coarsening group: restrict and interpolate only
   int ns = 7;           // stencil slots stored: 7 (Struct order) or 27
   const T *A = nullptr; // [ns][n] planes (level 0 points at the operator itself)
   DBuf<T> Aown, wd, invd, pm, pp, x, bv, r, t, dense;

@@ -62,11 +62,11 @@ __device__ __forceinline__ double grad_face(double gl, double pl, double gr, dou
 
 // ------------------------------------------------------------------ BC
 // Boundary planes (inlet ramp * uin, outlet copy, wall zeros).
-__global__ void k_bc_planes(double *u, double *v, double *w, const double *uin, double ramp, Dims d) {
+__global__ void k_bc_planes(double *u, double *v, double *w, const double *uin, const double *ramp, Dims d) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long)d.ny * d.nz) {
     const int j = (int)(t % d.ny), k = (int)(t / d.ny);
-    u[U3(d, 0, j, k)] = __dmul_rn(ramp, uin[t]);
+    u[U3(d, 0, j, k)] = __dmul_rn(*ramp, uin[t]);
     u[U3(d, d.nx, j, k)] = u[U3(d, d.nx - 1, j, k)];
   }
   if (t < (long)d.nx * d.nz) {
@@ -249,7 +249,8 @@ struct DivArgs {
   const double *Dc;
   const double *div_bc;
   double *b, *x0;
-  double neg_a, ramp;
+  double neg_a;
+  const double *ramp;
 };
 
 // D applied to the q-faces of a cell, as the reference's CSR row: fused
@@ -282,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) k_pressure_rhs(DivArgs A) {
                                 (A.fu[fe] & kQFace) ? A.ut[fe] : 0.0, (A.fv[fs] & kQFace) ? A.vt[fs] : 0.0,
                                 (A.fv[fn] & kQFace) ? A.vt[fn] : 0.0, (A.fw[fb] & kQFace) ? A.wt[fb] : 0.0,
                                 (A.fw[ft] & kQFace) ? A.wt[ft] : 0.0);
-      rhs = __dmul_rn(A.neg_a, fma(A.ramp, A.div_bc[c], s));
+      rhs = __dmul_rn(A.neg_a, fma(*A.ramp, A.div_bc[c], s));
     }
     A.b[c] = rhs;
     A.x0[c] = 0.0;
@@ -362,7 +363,8 @@ struct DiagArgs {
   const double *u, *v, *w;
   const uint8_t *fu, *fv, *fw, *fc;
   const double *Gu, *Gv, *Gw, *Dc, *div_bc;
-  double factor, ramp;
+  double factor;
+  const double *ramp;
   double *part;
   StepDiag *dg;
   int np_active;
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(kThreads) k_diagnostics(DiagArgs A) {
                                 q_face(A, A.vt, A.fv, A.Gv, NV, V3(d, i, j + 1, k), pc, pyp),
                                 q_face(A, A.wt, A.fw, A.Gw, NW, W3(d, i, j, k), pzm, pc),
                                 q_face(A, A.wt, A.fw, A.Gw, NW, W3(d, i, j, k + 1), pc, pzp));
-      const double dv = __dadd_rn(s, __dmul_rn(A.ramp, A.div_bc[c]));
+      const double dv = __dadd_rn(s, __dmul_rn(*A.ramp, A.div_bc[c]));
       div2 = __dadd_rn(div2, __dmul_rn(dv, dv));
     } else if (t < NP + NU) {
       um = fmax(um, fabs(A.u[t - NP]));
@@ -449,16 +451,20 @@ int blocks_for(long n) {
 
 }  // namespace
 
-void launch_bc(ibm_ctx *c, double *u, double *v, double *w, double ramp) {
+// Algorithmic bytes of each launch count every array element the kernel must
+// touch once (stencil neighbours are reuse, not extra traffic).
+void launch_bc(ibm_ctx *c, double *u, double *v, double *w) {
   const Dims d = dims_of(c);
   const long n = std::max((long)d.ny * d.nz, std::max((long)d.nx * d.nz, (long)d.nx * d.ny));
-  k_bc_planes<<<(int)((n + kThreads - 1) / kThreads), kThreads, 0, c->st>>>(u, v, w, c->uin.p, ramp, d);
-  count_launch();
+  {
+    LaunchScope ls(K_BC, c->st, 32.0 * d.ny * d.nz + 16.0 * d.nx * d.nz + 16.0 * d.nx * d.ny);
+    k_bc_planes<<<(int)((n + kThreads - 1) / kThreads), kThreads, 0, c->st>>>(u, v, w, c->uin.p, c->dramp.p, d);
+  }
   const long m = std::max((long)c->zl_u.n, std::max((long)c->zl_v.n, (long)c->zl_w.n));
   if (m > 0) {
+    LaunchScope ls(K_BC, c->st, 12.0 * (double)(c->zl_u.n + c->zl_v.n + c->zl_w.n));
     k_bc_zero<<<(int)((m + kThreads - 1) / kThreads), kThreads, 0, c->st>>>(u, c->zl_u.p, (int)c->zl_u.n, v, c->zl_v.p,
                                                                             (int)c->zl_v.n, w, c->zl_w.p, (int)c->zl_w.n);
-    count_launch();
   }
 }
 
@@ -477,19 +483,23 @@ void launch_momentum_rhs(ibm_ctx *c) {
   A.rho = c->g.rho;
   A.tdx = 2 * c->g.dx; A.tdy = 2 * c->g.dy; A.tdz = 2 * c->g.dz;
   A.zero_guess = c->prm.use_zero_initial_guess != 0;
+  const double faces = (double)(c->g.NU + c->g.NV + c->g.NW), nbox = (double)(A.nb[0] + A.nb[1] + A.nb[2]);
+  LaunchScope ls(K_RHS, c->st, 8.0 * faces + 9.0 * c->g.NP + nbox * (1 + 16 + 32));
   k_momentum_rhs<<<blocks_for(A.nb[0] + A.nb[1] + A.nb[2]), kThreads, 0, c->st>>>(A);
-  count_launch();
 }
 
-void launch_tilde(ibm_ctx *c, double ramp) {
+void launch_tilde(ibm_ctx *c) {
   const Dims d = dims_of(c);
-  k_scatter<<<blocks_for(c->g.NU + c->g.NV + c->g.NW), kThreads, 0, c->st>>>(
-      c->u.p, c->v.p, c->w.p, c->xb[0].p, c->xb[1].p, c->xb[2].p, c->ut.p, c->vt.p, c->wt.p, d, c->diag.p);
-  count_launch();
-  launch_bc(c, c->ut.p, c->vt.p, c->wt.p, ramp);
+  {
+    const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
+    LaunchScope ls(K_SCATTER, c->st, 16.0 * faces + 8.0 * (c->g.bu.n + c->g.bv.n + c->g.bw.n));
+    k_scatter<<<blocks_for(c->g.NU + c->g.NV + c->g.NW), kThreads, 0, c->st>>>(
+        c->u.p, c->v.p, c->w.p, c->xb[0].p, c->xb[1].p, c->xb[2].p, c->ut.p, c->vt.p, c->wt.p, d, c->diag.p);
+  }
+  launch_bc(c, c->ut.p, c->vt.p, c->wt.p);
 }
 
-void launch_pressure_rhs(ibm_ctx *c, double ramp) {
+void launch_pressure_rhs(ibm_ctx *c) {
   DivArgs A;
   A.d = dims_of(c);
   A.ut = c->ut.p; A.vt = c->vt.p; A.wt = c->wt.p;
@@ -497,12 +507,13 @@ void launch_pressure_rhs(ibm_ctx *c, double ramp) {
   A.Dc = c->Dc.p; A.div_bc = c->div_bc_cell.p;
   A.b = c->bb[3].p; A.x0 = c->xb[3].p;
   A.neg_a = -(c->g.rho / c->g.dt);
-  A.ramp = ramp;
+  A.ramp = c->dramp.p;
+  const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
+  LaunchScope ls(K_PRHS, c->st, 9.0 * faces + 73.0 * c->g.NP);
   k_pressure_rhs<<<blocks_for(c->g.NP), kThreads, 0, c->st>>>(A);
-  count_launch();
 }
 
-void launch_projection(ibm_ctx *c, double ramp) {
+void launch_projection(ibm_ctx *c) {
   ProjArgs A;
   A.d = dims_of(c);
   A.ut = c->ut.p; A.vt = c->vt.p; A.wt = c->wt.p; A.phi = c->xb[3].p;
@@ -511,9 +522,12 @@ void launch_projection(ibm_ctx *c, double ramp) {
   A.Gu = c->Gu.p; A.Gv = c->Gv.p; A.Gw = c->Gw.p;
   A.factor = c->g.dt / c->g.rho;
   A.dg = c->diag.p;
-  k_project<<<blocks_for(c->g.NU + c->g.NV + c->g.NW + c->g.NP), kThreads, 0, c->st>>>(A);
-  count_launch();
-  launch_bc(c, c->u.p, c->v.p, c->w.p, ramp);
+  const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
+  {
+    LaunchScope ls(K_PROJECT, c->st, 33.0 * faces + 25.0 * c->g.NP);
+    k_project<<<blocks_for(c->g.NU + c->g.NV + c->g.NW + c->g.NP), kThreads, 0, c->st>>>(A);
+  }
+  launch_bc(c, c->u.p, c->v.p, c->w.p);
   DiagArgs D;
   D.d = A.d;
   D.ut = c->ut.p; D.vt = c->vt.p; D.wt = c->wt.p; D.phi = c->xb[3].p;
@@ -521,13 +535,13 @@ void launch_projection(ibm_ctx *c, double ramp) {
   D.fu = c->fu.p; D.fv = c->fv.p; D.fw = c->fw.p; D.fc = c->fc.p;
   D.Gu = c->Gu.p; D.Gv = c->Gv.p; D.Gw = c->Gw.p; D.Dc = c->Dc.p; D.div_bc = c->div_bc_cell.p;
   D.factor = A.factor;
-  D.ramp = ramp;
+  D.ramp = c->dramp.p;
   const int nb = std::min(blocks_for(c->g.NP + c->g.NU + c->g.NV + c->g.NW), 1024);
   D.part = c->part.p;
   D.dg = c->diag.p;
   D.np_active = c->np_active;
+  LaunchScope ls(K_DIAG, c->st, 33.0 * faces + 65.0 * c->g.NP);
   k_diagnostics<<<nb, kThreads, 0, c->st>>>(D);
-  count_launch();
 }
 
 }  // namespace ibm

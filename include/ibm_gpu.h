@@ -78,6 +78,8 @@ typedef struct ibm_solver_params {
   int precision;         /* 0: FP64 throughout; 1: FP32 preconditioners inside FP64 flexible GMRES */
   int use_graph;         /* 1: replay the step as a CUDA graph */
   int vel_inner_sweeps;  /* precision 1: FP32 Jacobi sweeps per momentum preconditioner application */
+  double mg_group_ratio; /* between relaxed levels, coarsen every direction whose spacing is within
+                            this factor of the smallest (0: one direction per relaxed level) */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {
@@ -155,6 +157,27 @@ int ibm_apply_operator(ibm_ctx *ctx, int field, const double *x, double *y);
  * solve box, as HYPRE_StructVectorGetBoxValues returns the reference's
  * b/x vectors (hypre_struct_utils.hpp:23-24, main.cu:298-300, 332). */
 int ibm_get_solver_vector(ibm_ctx *ctx, int field, int which, double *out);
+
+/* Launch accounting (replaces the reference's MPI_Wtime buckets,
+ * main.cu:247-389, with per-kernel-class counts, algorithmic bytes — every
+ * element a kernel must read or write once — and CUDA-event time of one
+ * selected class). Phases: right-hand sides, momentum solves, pressure
+ * solve, projection, other. */
+#define IBM_PROFILE_MAX_KERNELS 32
+typedef struct ibm_profile {
+  int nkernels;
+  long long launches[IBM_PROFILE_MAX_KERNELS];
+  double bytes[IBM_PROFILE_MAX_KERNELS];
+  double time_ms[IBM_PROFILE_MAX_KERNELS];
+  long long timed_launches[IBM_PROFILE_MAX_KERNELS];
+  double phase_bytes[5];
+} ibm_profile;
+int ibm_profile_reset(ibm_ctx *ctx);
+/* Bracket every launch of kernel class `kernel` with CUDA events on the
+ * context stream (-1: none). */
+int ibm_profile_time_kernel(ibm_ctx *ctx, int kernel);
+int ibm_profile_get(ibm_ctx *ctx, ibm_profile *out);
+const char *ibm_kernel_name(int kernel);
 
 int ibm_synchronize(ibm_ctx *ctx);
 void *ibm_stream(ibm_ctx *ctx);            /* the context's cudaStream_t */

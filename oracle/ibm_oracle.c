@@ -24,6 +24,7 @@ typedef struct { int n[3]; long N; } box3;
 typedef struct {
   box3 b;
   int cdir;                 /* direction coarsened to reach the next level, -1 on the coarsest */
+  int relax;                /* 0 inside a coarsening group: restrict / interpolate only */
   double *A;                /* [N][27], slot = (ox+1) + 3(oy+1) + 9(oz+1) */
   double *wd;               /* omega / diag */
   double *invd;             /* 1 / diag */
@@ -479,17 +480,46 @@ static void mg_build(oracle *o) {
   L0->b = o->bp;
   L0->A = (double *)xcalloc((size_t)L0->b.N * 27, 8);
   for (long r = 0; r < L0->b.N; ++r)
-    for (int s = 0; s < 7; ++s) L0->A[27 * r + k7to27[s]] = o->in.Ap[7 * r + s];
+    for (int s = 0; s < 7; ++s) {
+      const double a = o->in.Ap[7 * r + s];
+      /* symmetric form: fluid rows scaled by their open fraction */
+      L0->A[27 * r + k7to27[s]] = (o->prm.mg_sym && o->in.fluid_p[r]) ? o->in.beta_p[r] * a : a;
+    }
   double h[3] = {o->dx, o->dy, o->dz};
+  int queue[3], nq = 0;  /* directions still to coarsen in the current group */
   int l = 0;
   for (;;) {
     mg_level *F = &o->lev[l];
     mg_finish_level(o, F);
+    /* A group starts at a relaxed level: every direction whose spacing is
+     * within mg_group_ratio of the smallest is coarsened once, smallest
+     * spacing first; the levels inside the group are not relaxed. A ratio of
+     * 0 gives one direction per relaxed level. */
+    F->relax = (nq == 0);
+    if (nq == 0) {
+      double hmin = 0.0;
+      int any = 0;
+      for (int dd = 0; dd < 3; ++dd)
+        if (F->b.n[dd] > 1 && (!any || h[dd] < hmin)) { hmin = h[dd]; any = 1; }
+      int cand[3], nc = 0;
+      for (int dd = 0; dd < 3; ++dd)
+        if (F->b.n[dd] > 1 && (h[dd] == hmin || (o->prm.mg_group_ratio > 0.0 && h[dd] <= o->prm.mg_group_ratio * hmin)))
+          cand[nc++] = dd;
+      for (int a = 0; a < nc; ++a)
+        for (int b2 = a + 1; b2 < nc; ++b2)
+          if (h[cand[b2]] < h[cand[a]]) { int t = cand[a]; cand[a] = cand[b2]; cand[b2] = t; }
+      if (o->prm.mg_group_ratio <= 0.0 && nc > 1) nc = 1;
+      for (int a = 0; a < nc; ++a) queue[a] = cand[nc - 1 - a];
+      nq = nc;
+    }
     int d = -1;
-    for (int dd = 0; dd < 3; ++dd)
-      if (F->b.n[dd] > 1 && (d < 0 || h[dd] < h[d])) d = dd;
+    while (nq > 0 && d < 0) {
+      int q = queue[--nq];
+      if (F->b.n[q] > 1) d = q;
+    }
     if (F->b.N <= o->prm.mg_coarse_max || l + 1 >= o->prm.mg_max_levels || d < 0 || l + 1 >= 40) {
       F->cdir = -1;
+      F->relax = 1;
       F->dense_inv = (double *)xcalloc((size_t)(F->b.N * F->b.N), 8);
       dense_inverse(F->A, &F->b, F->dense_inv);
       break;
@@ -556,11 +586,15 @@ static void mg_cycle(oracle *o, int l, const double *b, double *x) {
     }
     return;
   }
-  for (int s = 0; s < o->prm.mg_nu1; ++s) mg_relax(o, L, b, x, s == 0);
-  if (o->prm.mg_nu1 == 0) memset(x, 0, sizeof(double) * (size_t)N);
+  const int nu1 = L->relax ? o->prm.mg_nu1 : 0, nu2 = L->relax ? o->prm.mg_nu2 : 0;
+  for (int s = 0; s < nu1; ++s) mg_relax(o, L, b, x, s == 0);
+  if (nu1 == 0) memset(x, 0, sizeof(double) * (size_t)N);
   double *ax = L->rv;
-  spmv27(&L->b, L->A, x, ax);
-  for (long r = 0; r < N; ++r) ax[r] = b[r] - ax[r];
+  if (nu1 == 0) memcpy(ax, b, sizeof(double) * (size_t)N);
+  else {
+    spmv27(&L->b, L->A, x, ax);
+    for (long r = 0; r < N; ++r) ax[r] = b[r] - ax[r];
+  }
   mg_level *C = &o->lev[l + 1];
   const int d = L->cdir;
   for (long I = 0; I < C->b.N; ++I) {
@@ -591,12 +625,17 @@ static void mg_cycle(oracle *o, int l, const double *b, double *x) {
     }
     x[r] = x[r] + corr;
   }
-  for (int s = 0; s < o->prm.mg_nu2; ++s) mg_relax(o, L, b, x, 0);
+  for (int s = 0; s < nu2; ++s) mg_relax(o, L, b, x, 0);
 }
 
 void oracle_mg_vcycle(oracle *o, const double *b, double *x) {
   mg_build(o);
-  mg_cycle(o, 0, b, x);
+  if (!o->prm.mg_sym) { mg_cycle(o, 0, b, x); return; }
+  const long N = o->lev[0].b.N;
+  double *bs = (double *)xcalloc((size_t)N, 8);
+  for (long r = 0; r < N; ++r) bs[r] = o->in.fluid_p[r] ? o->in.beta_p[r] * b[r] : b[r];
+  mg_cycle(o, 0, bs, x);
+  free(bs);
 }
 int oracle_mg_levels(oracle *o) { mg_build(o); return o->nlev; }
 int oracle_mg_level_info(oracle *o, int l, int *dims, int *cdir, int *nslots) {
@@ -714,7 +753,8 @@ int oracle_solve(oracle *o, int field, const double *b, double *x, oracle_solve_
     double rt = sqrt(dot(r, r, N));
     r_norm = rt;
     if (rt <= eps) { converged = 1; break; }
-    if (claimed && rt >= real_old) break;
+    /* stagnation: HYPRE stops and reports success (no error below max_iter) */
+    if (claimed && rt >= real_old) { converged = 1; break; }
     real_old = rt;
   }
 #undef HH

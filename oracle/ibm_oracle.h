@@ -36,6 +36,9 @@ typedef struct oracle_params {
   double mg_omega;     /* weighted-Jacobi weight */
   int mg_coarse_max;   /* stop coarsening at or below this many points */
   int mg_max_levels;
+  double mg_group_ratio; /* coarsen every direction with spacing <= ratio * smallest between
+                            relaxations (0: one direction per relaxed level) */
+  int mg_sym;          /* 1: hierarchy of L = B Ap (B = diag(beta)), applied to B r */
 } oracle_params;
 
 typedef struct oracle_inputs {
@@ -46,6 +49,7 @@ typedef struct oracle_inputs {
   const int32_t *D_rowptr, *D_col; const double *D_val;
   const int32_t *G_rowptr, *G_col; const double *G_val;
   const double *uin; /* ny*nz, inlet profile at Um */
+  const double *beta_p; /* cell open fractions (multigrid on the symmetric form B Ap) */
 } oracle_inputs;
 
 typedef struct oracle_solve_stats { int iters; double rel_res; int status; } oracle_solve_stats;

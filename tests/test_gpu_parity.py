@@ -118,6 +118,26 @@ def test_multistep_parity(ibm, pyoracle, case48, rap, relax):
         assert rel_err(a, b) <= REL_TOL, name
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_step_matches_stream_step(ibm, case48, precision):
+    """The captured step (one graph launch, GMRES loops on the device) gives
+    the same fields and iteration counts as the host-driven step."""
+    kw = dict(vel_tol=1e-10, p_tol=1e-10, precision=precision, p_pc_relax_type=2, mg_omega=1.0,
+              mg_group_ratio=1.5)
+    a = ibm.Solver(case48, ibm.solver_params(use_graph=0, **kw))
+    b = ibm.Solver(case48, ibm.solver_params(use_graph=1, **kw))
+    for step in range(1, 6):
+        sa = a.step(min(1.0, step / 3.0))
+        l0 = b.launches()
+        sb = b.step(min(1.0, step / 3.0))
+        assert b.launches() > l0
+        assert sb.status == sa.status == ibm.IBM_OK
+        for f in "uvwp":
+            assert getattr(sa, f).iters == getattr(sb, f).iters, f
+    for x, y, name in zip(a.fields(), b.fields(), "uvwp"):
+        assert bits_equal(x, y), name
+
+
 def test_golden_oracle_steps(ibm, case32):
     g = np.load(os.path.join(GOLDEN, "oracle_channel_32x12x12.npz"))
     s = ibm.Solver(case32, tight(ibm))
