@@ -70,11 +70,24 @@ def build_gpu(jobs: int = 8) -> str:
     return out
 
 
+def build_driver() -> str:
+    """ibm_run: the reference's application (main.cu) on the two C ABIs."""
+    src = os.path.join(HERE, "csrc", "driver", "ibm_run.cpp")
+    out = os.path.join(BUILD, "ibm_run")
+    deps = [src, os.path.join(INCLUDE, "ibm_gpu.h"), os.path.join(INCLUDE, "ibm_host.h"),
+            os.path.join(BUILD, "libibmgpu.so"), os.path.join(BUILD, "libibmhost.so")]
+    if _newer(out, deps):
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + INCLUDE, src, "-o", out, "-L" + BUILD, "-libmgpu",
+              "-libmhost", "-Wl,-rpath,$ORIGIN"])
+    return out
+
+
 def build_all() -> None:
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
         fs = [ex.submit(build_host), ex.submit(build_gpu)]
         for f in fs:
             f.result()
+    build_driver()
 
 
 if __name__ == "__main__":

@@ -18,6 +18,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <memory>
 #include <random>
 #include <string>
 #include <unordered_map>
@@ -647,6 +648,81 @@ const void *ibm_case_array(const ibm_case *c, const char *name) {
   auto it = c->arrays.find(name);
   if (it == c->arrays.end()) return nullptr;
   return it->second.bytes.data();
+}
+
+// File layout: magic "IBMCASE\0", u32 version, the ibm_case_params bytes,
+// the counts, u32 array count, then per array: u32 name length, name,
+// i32 element size, u64 byte count, bytes. Little-endian host order.
+static const char kMagic[8] = {'I', 'B', 'M', 'C', 'A', 'S', 'E', 0};
+static const uint32_t kVersion = 1;
+
+int ibm_case_save(const ibm_case *c, const char *path) {
+  if (!c || !path) return -1;
+  const std::string tmp = std::string(path) + ".tmp";
+  std::FILE *f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return -2;
+  bool ok = std::fwrite(kMagic, 1, 8, f) == 8;
+  ok = ok && std::fwrite(&kVersion, sizeof(kVersion), 1, f) == 1;
+  ok = ok && std::fwrite(&c->par, sizeof(c->par), 1, f) == 1;
+  ok = ok && std::fwrite(&c->counts, sizeof(c->counts), 1, f) == 1;
+  const uint32_t na = (uint32_t)c->arrays.size();
+  ok = ok && std::fwrite(&na, sizeof(na), 1, f) == 1;
+  for (const auto &kv : c->arrays) {
+    const uint32_t ln = (uint32_t)kv.first.size();
+    const int32_t es = kv.second.elem;
+    const uint64_t nb = kv.second.bytes.size();
+    ok = ok && std::fwrite(&ln, sizeof(ln), 1, f) == 1 && std::fwrite(kv.first.data(), 1, ln, f) == ln;
+    ok = ok && std::fwrite(&es, sizeof(es), 1, f) == 1 && std::fwrite(&nb, sizeof(nb), 1, f) == 1;
+    ok = ok && (nb == 0 || std::fwrite(kv.second.bytes.data(), 1, nb, f) == nb);
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) { std::remove(tmp.c_str()); return -2; }
+  return std::rename(tmp.c_str(), path) == 0 ? 0 : -2;
+}
+
+int ibm_case_load(const ibm_case_params *p, const char *path, ibm_case **out) {
+  if (!p || !path || !out) return -1;
+  *out = nullptr;
+  std::FILE *f = std::fopen(path, "rb");
+  if (!f) return 1;
+  char magic[8];
+  uint32_t ver = 0;
+  ibm_case_params fp;
+  std::unique_ptr<ibm_case> c(new ibm_case());
+  bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kMagic, 8) == 0;
+  ok = ok && std::fread(&ver, sizeof(ver), 1, f) == 1 && ver == kVersion;
+  ok = ok && std::fread(&fp, sizeof(fp), 1, f) == 1 && std::memcmp(&fp, p, sizeof(fp)) == 0;
+  if (!ok) { std::fclose(f); return 1; }
+  c->par = fp;
+  uint32_t na = 0;
+  ok = std::fread(&c->counts, sizeof(c->counts), 1, f) == 1 && std::fread(&na, sizeof(na), 1, f) == 1;
+  for (uint32_t a = 0; ok && a < na; ++a) {
+    uint32_t ln = 0;
+    int32_t es = 0;
+    uint64_t nb = 0;
+    ok = std::fread(&ln, sizeof(ln), 1, f) == 1 && ln < 256;
+    std::string name(ok ? ln : 0, '\0');
+    ok = ok && std::fread(&name[0], 1, ln, f) == ln;
+    ok = ok && std::fread(&es, sizeof(es), 1, f) == 1 && std::fread(&nb, sizeof(nb), 1, f) == 1;
+    if (!ok) break;
+    Array &arr = c->arrays[name];
+    arr.elem = es;
+    arr.bytes.resize((size_t)nb);
+    ok = nb == 0 || std::fread(arr.bytes.data(), 1, (size_t)nb, f) == nb;
+  }
+  std::fclose(f);
+  if (!ok) return -2;
+  *out = c.release();
+  return 0;
+}
+
+int ibm_case_build_cached(const ibm_case_params *p, const char *path, ibm_case **out) {
+  const int rc = ibm_case_load(p, path, out);
+  if (rc == 0) return 0;
+  const int b = ibm_case_build(p, out);
+  if (b != 0) return b;
+  ibm_case_save(*out, path);  // a cache that cannot be written is not an error
+  return 0;
 }
 
 int ibm_host_check_sum_order(int ntrials, unsigned seed) {

@@ -71,6 +71,17 @@ long ibm_case_array_bytes(const ibm_case *c, const char *name, int *elem_size);
 const void *ibm_case_array(const ibm_case *c, const char *name);
 
 /*
+ * Case cache on disk: a versioned binary of every named array, keyed by the
+ * full parameter struct. ibm_case_load returns 0 when the file holds a case
+ * built with exactly *p, 1 when the file is absent or for other parameters
+ * or another format version (nothing is loaded), negative on I/O errors.
+ * ibm_case_build_cached loads when it can, else builds and saves.
+ */
+int ibm_case_save(const ibm_case *c, const char *path);
+int ibm_case_load(const ibm_case_params *p, const char *path, ibm_case **out);
+int ibm_case_build_cached(const ibm_case_params *p, const char *path, ibm_case **out);
+
+/*
  * Self-check of the hash-iteration-order model used to reproduce the
  * reference's summation order: inserts ntrials random key sets into the real
  * standard-library hash map this library was compiled with and compares the
