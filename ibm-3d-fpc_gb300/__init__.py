@@ -192,6 +192,12 @@ class Solver:
         self._check(self._lib.ibm_apply_operator(self._ctx, field, _ptr(x), _ptr(y)))
         return y
 
+    def apply_preconditioner(self, field: int, r: np.ndarray) -> np.ndarray:
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.empty_like(r)
+        self._check(self._lib.ibm_apply_preconditioner(self._ctx, field, _ptr(r), _ptr(z)))
+        return z
+
     def solver_vector(self, field: int, which: int) -> np.ndarray:
         nx, ny, nz = self.case.shape
         n = [(nx - 1) * ny * nz, nx * (ny - 1) * nz, nx * ny * (nz - 1), nx * ny * nz][field]

@@ -120,6 +120,11 @@ def gpu() -> C.CDLL:
         lib.ibm_solve.argtypes = [vp, i, vp, vp, P(SolveStats)]
         lib.ibm_apply_operator.argtypes = [vp, i, vp, vp]
         lib.ibm_get_solver_vector.argtypes = [vp, i, i, vp]
+        lib.ibm_apply_preconditioner.argtypes = [vp, i, vp, vp]
+        lib.ibm_profile_reset.argtypes = [vp]
+        lib.ibm_profile_time_kernel.argtypes = [vp, i]
+        lib.ibm_kernel_name.argtypes = [i]
+        lib.ibm_kernel_name.restype = C.c_char_p
         lib.ibm_synchronize.argtypes = [vp]
         lib.ibm_stream.argtypes = [vp]
         lib.ibm_stream.restype = vp

@@ -610,8 +610,11 @@ int ibm_set_solver_params(ibm_ctx *c, const ibm_solver_params *p) {
     if (p->p_pc != 0 && p->p_pc != 1) throw Error(IBM_ERR_ARG, "p_pc must be 0 or 1");
     if (p->mg_nu1 < 0 || p->mg_nu2 < 0 || p->mg_coarse_max < 1 || p->mg_max_levels < 1)
       throw Error(IBM_ERR_ARG, "bad multigrid parameters");
+    // switching between the graph and the host-driven step keeps the solvers
+    ibm_solver_params a = c->prm, b = *p;
+    a.use_graph = b.use_graph = 0;
+    if (std::memcmp(&a, &b, sizeof(a)) != 0) c->solvers_ready = false;
     c->prm = *p;
-    c->solvers_ready = false;
     invalidate_graph(c);
     return IBM_OK;
   });
@@ -790,6 +793,46 @@ int ibm_apply_operator(ibm_ctx *c, int field, const double *x, double *y) {
       k_spmv7<<<grid1d(b.n), kThreads, 0, c->st>>>(c->op[field].c.p, b, dx.p, dy.p);
     }
     IBM_CUDA_TRY(cudaMemcpyAsync(y, dy.p, sizeof(double) * b.n, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_apply_preconditioner(ibm_ctx *c, int field, const double *r, double *z) {
+  return guarded(c, [&]() {
+    if (field < 0 || field > 3 || !r || !z) throw Error(IBM_ERR_ARG, "ibm_apply_preconditioner: bad arguments");
+    require_inputs(c);
+    ensure_solvers(c);
+    const Box &b = field_box(c, field);
+    DBuf<double> dr, dz;
+    dr.alloc(b.n); dz.alloc(b.n);
+    IBM_CUDA_TRY(cudaMemcpyAsync(dr.p, r, sizeof(double) * b.n, cudaMemcpyDefault, c->st));
+    if (field == 3 && c->prm.p_pc == 1) {
+      VecRef in;
+      in.base = dr.p;
+      if (c->prm.precision == 1) {
+        DBuf<float> zf;
+        zf.alloc(b.n);
+        OutRef out;
+        out.f = zf.p;
+        c->mg.apply(c->st, in, out, nullptr, true);
+        std::vector<float> hz(b.n);
+        IBM_CUDA_TRY(cudaMemcpyAsync(hz.data(), zf.p, sizeof(float) * b.n, cudaMemcpyDeviceToHost, c->st));
+        IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+        std::vector<double> zd(hz.begin(), hz.end());
+        IBM_CUDA_TRY(cudaMemcpy(z, zd.data(), sizeof(double) * b.n, cudaMemcpyDefault));
+        return IBM_OK;
+      }
+      OutRef out;
+      out.d = dz.p;
+      c->mg.apply(c->st, in, out, nullptr, false);
+    } else {
+      // one Jacobi sweep from a zero guess: z = r / diag
+      std::vector<double> hr = to_host(r, (size_t)b.n), hd = to_host(c->op[field].invd.p, (size_t)b.n);
+      for (long i = 0; i < b.n; ++i) hr[(size_t)i] *= hd[(size_t)i];
+      IBM_CUDA_TRY(cudaMemcpy(dz.p, hr.data(), sizeof(double) * b.n, cudaMemcpyHostToDevice));
+    }
+    IBM_CUDA_TRY(cudaMemcpyAsync(z, dz.p, sizeof(double) * b.n, cudaMemcpyDefault, c->st));
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
     return IBM_OK;
   });

@@ -153,6 +153,11 @@ int ibm_solve(ibm_ctx *ctx, int field, const double *b, double *x, ibm_solve_sta
 /* y = A x with the field's operator on its solve box (HYPRE StructMatvec). */
 int ibm_apply_operator(ibm_ctx *ctx, int field, const double *x, double *y);
 
+/* z = M r: one application of the field's preconditioner from a zero guess,
+ * as the solver applies it (HYPRE_StructPFMGSolve / HYPRE_StructJacobiSolve
+ * with maxit 1, main.cu:182, 212-218). precision 1 applies the FP32 form. */
+int ibm_apply_preconditioner(ibm_ctx *ctx, int field, const double *r, double *z);
+
 /* The last right-hand side (which = 0) or solution (which = 1) of a field's
  * solve box, as HYPRE_StructVectorGetBoxValues returns the reference's
  * b/x vectors (hypre_struct_utils.hpp:23-24, main.cu:298-300, 332). */
