@@ -43,7 +43,8 @@ enum {
   IBM_ERR_NONFINITE = -3,     /* non-finite solve output (main.cu:302-305, 333-336) */
   IBM_ERR_STATE = -4,         /* a required set_* call is missing */
   IBM_ERR_NOMEM = -5,
-  IBM_ERR_UNSUPPORTED = -6    /* input not representable (e.g. off-stencil CSR entry) */
+  IBM_ERR_UNSUPPORTED = -6,   /* input not representable (e.g. off-stencil CSR entry) */
+  IBM_ERR_TOO_LARGE = -7      /* problem larger than a fixed-size buffer allows */
 };
 
 enum { IBM_FIELD_U = 0, IBM_FIELD_V = 1, IBM_FIELD_W = 2, IBM_FIELD_P = 3 };
@@ -189,6 +190,31 @@ void *ibm_stream(ibm_ctx *ctx);            /* the context's cudaStream_t */
 long long ibm_kernel_launches(ibm_ctx *ctx); /* kernels this context has launched */
 /* Name and compute capability of a device, for logs. */
 int ibm_device_query(int device, char *buf, int len);
+
+/* r = b - A x and norms[0] = ||r||_2, norms[1] = ||b||_2 for one 7-point
+ * operator, allocating nothing. No counterpart in the reference: it serves
+ * callers that cannot call cudaMalloc (those that give all device memory to
+ * their own pool allocator, run under a fixed memory budget, or cannot take
+ * the device-wide synchronisation of cudaFree), for whom creating a context
+ * is not an option.
+ *  - vals (7 values per row, the reference's row-major Struct layout, as
+ *    ibm_set_operator takes), x, b, r (nx*ny*nz doubles each) and norms (2
+ *    doubles) are caller-owned device (or managed) memory on the current
+ *    device; host pointers are rejected with IBM_ERR_ARG.
+ *  - nx*ny*nz above IBM_NOALLOC_MAX_ROWS returns IBM_ERR_TOO_LARGE.
+ *  - scratch is one fixed array inside the library (512 KiB per device,
+ *    held until the process exits). The first call on a device, made with
+ *    that device current, looks up the array's address there
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - work is queued on `stream` (a cudaStream_t; NULL = default stream) and
+ *    the call returns without waiting: r and norms are valid once the stream
+ *    has reached this point. Every call shares the array, which keeps the
+ *    last call's contents; the counter that must start at zero is cleared on
+ *    the stream before each launch. Calls whose work overlaps on the GPU
+ *    (other streams, other host threads) race on the array: order them. */
+#define IBM_NOALLOC_MAX_ROWS 33554432L /* 2^25 rows */
+int ibm_residual_noalloc(const double *vals, int nx, int ny, int nz, const double *x, const double *b,
+                         double *r, double *norms, void *stream);
 
 #ifdef __cplusplus
 }
