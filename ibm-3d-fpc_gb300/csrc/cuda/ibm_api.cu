@@ -122,6 +122,61 @@ int grid1d(long n) {
   return (int)std::max(1L, std::min(b, (long)sm_count() * 8));
 }
 
+// Diagonal symmetrizer of a 7-point operator (row-major values): W with
+// A = W S, S symmetric. The cut-cell divergence of the pressure operator
+// divides each cell's row by its open fraction, so the pressure operator has
+// this form. Each connected set of coupled rows is walked breadth first from
+// its lowest row (w = 1), neighbours in slot order, w_c = w_r A[c][r] / A[r][c];
+// then every coupling is checked. Returns false (winv all ones) when A is not
+// of that form. winv = 1 / w.
+bool diagonal_symmetrizer(const std::vector<double> &A7, const Box &b, std::vector<double> &winv) {
+  const long N = b.n;
+  std::vector<double> w((size_t)N, 0.0);
+  std::vector<long> queue((size_t)N);
+  std::vector<unsigned char> seen((size_t)N, 0);
+  const long sy = b.nx, sz = (long)b.nx * b.ny;
+  const long off[7] = {0, -1, 1, -sy, sy, -sz, sz};
+  static const int opp[7] = {0, 2, 1, 4, 3, 6, 5};
+  auto inside = [&](long r, int s) {
+    const int i = (int)(r % b.nx), j = (int)((r / b.nx) % b.ny), k = (int)(r / sz);
+    switch (s) {
+      case 1: return i > 0; case 2: return i < b.nx - 1; case 3: return j > 0; case 4: return j < b.ny - 1;
+      case 5: return k > 0; case 6: return k < b.nz - 1; default: return true;
+    }
+  };
+  bool ok = true;
+  for (long root = 0; root < N && ok; ++root) {
+    if (seen[root]) continue;
+    seen[root] = 1;
+    w[root] = 1.0;
+    long head = 0, tail = 0;
+    queue[tail++] = root;
+    while (head < tail && ok) {
+      const long r = queue[head++];
+      for (int s = 1; s < 7; ++s) {
+        if (!inside(r, s) || A7[7 * r + s] == 0.0) continue;
+        const long c2 = r + off[s];
+        const double back = A7[7 * c2 + opp[s]];
+        if (back == 0.0) { ok = false; break; }
+        if (seen[c2]) continue;
+        seen[c2] = 1;
+        w[c2] = w[r] * back / A7[7 * r + s];
+        queue[tail++] = c2;
+      }
+    }
+  }
+  for (long r = 0; r < N && ok; ++r)
+    for (int s = 1; s < 7; ++s) {
+      if (!inside(r, s)) continue;
+      const double x = A7[7 * r + s] / w[r], y = A7[7 * (r + off[s]) + opp[s]] / w[r + off[s]];
+      if (std::fabs(x - y) > 1e-10 * std::max(std::fabs(x), std::fabs(y))) { ok = false; break; }
+    }
+  winv.assign((size_t)N, 1.0);
+  if (ok)
+    for (long r = 0; r < N; ++r) winv[r] = 1.0 / w[r];
+  return ok;
+}
+
 const Box &field_box(const ibm_ctx *c, int f) {
   return f == 0 ? c->g.bu : f == 1 ? c->g.bv : f == 2 ? c->g.bw : c->g.bp;
 }
@@ -171,8 +226,10 @@ void ensure_solvers(ibm_ctx *c) {
     mp.coarse_max = p.mg_coarse_max; mp.max_levels = p.mg_max_levels;
     mp.cycles = std::max(1, p.p_pc_maxit);
     mp.group_ratio = p.mg_group_ratio;
+    mp.options = p.mg_options;
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
-    c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed);
+    const double *winv = ((p.mg_options & 2) && c->p_sym) ? c->p_winv.p : nullptr;
+    c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
     if (mixed) { hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; }
     else { hp.pc = 1; hp.A = op.c.p; }
   } else {
@@ -278,6 +335,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->mg_nu1 = 1; p->mg_nu2 = 1; p->mg_omega = 2.0 / 3.0; p->mg_coarse_max = 64; p->mg_max_levels = 40;
   p->use_zero_initial_guess = 1; p->precision = 0; p->use_graph = 0; p->vel_inner_sweeps = 3;
   p->mg_group_ratio = 0.0;
+  p->mg_options = 3;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -380,6 +438,13 @@ int ibm_set_operator(ibm_ctx *c, int field, const double *vals7, int nbx, int nb
     }
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
     IBM_CUDA_TRY(cudaGetLastError());
+    if (field == 3) {
+      const std::vector<double> hv = to_host(vals7, (size_t)7 * n);
+      std::vector<double> winv;
+      c->p_sym = diagonal_symmetrizer(hv, b, winv);
+      upload(c->p_winv, winv, c->st);
+      IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    }
     o.set = true;
     c->solvers_ready = false;
     invalidate_graph(c);

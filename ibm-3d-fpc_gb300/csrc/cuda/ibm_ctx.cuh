@@ -39,6 +39,8 @@ struct ibm_ctx {
   long long launches = 0;
 
   ibm::Op7 op[4];
+  bool p_sym = false;            // the pressure operator is W S (W diagonal, S symmetric)
+  ibm::DBuf<double> p_winv;      // 1 / W
   bool masks_set = false, aux_set = false, csr_set = false;
   int np_active = 0;             // number of fluid cells with an id (the reference's Np)
   ibm::DBuf<uint8_t> fu, fv, fw, fc;

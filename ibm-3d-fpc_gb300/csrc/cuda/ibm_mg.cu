@@ -82,7 +82,25 @@ __global__ void k_diag(const double *A, long n, double omega, double *invd, doub
   }
 }
 
-__global__ void k_interp_weights(const double *A, int ns, long n, int d, double *pm, double *pp) {
+// 1 where a row has any off-diagonal coupling (0: an uncoupled point, e.g. a
+// solid cell kept as an identity row).
+__global__ void k_coupled(const double *A, int ns, long n, unsigned char *coupled) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    unsigned char c = 0;
+    for (int q = 0; q < ns; ++q)
+      if (q != (ns == 27 ? 13 : 0) && A[(long)q * n + r] != 0.0) c = 1;
+    coupled[r] = c;
+  }
+}
+
+// PFMG's operator-dependent weights. With `aware`, a coupled point that has no
+// coupling along d (0/0 otherwise, e.g. a cut cell between the cylinder and a
+// closed face) takes the constant from those of its two coarse neighbours that
+// are coupled, so interpolation keeps reproducing constants there.
+__global__ void k_interp_weights(const double *A, int ns, Box b, int d, const unsigned char *coupled, int aware,
+                                 double *pm, double *pp) {
+  const long n = b.n;
+  const long stride = d == 0 ? 1 : d == 1 ? (long)b.nx : (long)b.nx * b.ny;
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
     double c0 = 0.0, cm = 0.0, cp = 0.0;
     for (int s = 0; s < 27; ++s) {
@@ -93,10 +111,29 @@ __global__ void k_interp_weights(const double *A, int ns, long n, int d, double 
       if (od == 0) c0 += a; else if (od < 0) cm += a; else cp += a;
     }
     double wm = 0.0, wp = 0.0;
-    if (c0 != 0.0) { wm = -cm / c0; wp = -cp / c0; }
+    if (aware && coupled[r] && cm == 0.0 && cp == 0.0) {
+      int idx[3];
+      row_ijk((int)r, b.nx, b.ny, idx[0], idx[1], idx[2]);
+      const int nd = d == 0 ? b.nx : d == 1 ? b.ny : b.nz;
+      const int lo = idx[d] > 0 && coupled[r - stride];
+      const int hi = idx[d] < nd - 1 && coupled[r + stride];
+      if (lo + hi > 0) {
+        wm = lo ? 1.0 / (lo + hi) : 0.0;
+        wp = hi ? 1.0 / (lo + hi) : 0.0;
+      }
+    } else if (c0 != 0.0) {
+      wm = -cm / c0;
+      wp = -cp / c0;
+    }
     pm[r] = wm;
     pp[r] = wp;
   }
+}
+
+// Level-0 operator of the symmetrized hierarchy: row r scaled by winv[r].
+__global__ void k_scale_rows(const double *A7, const double *winv, long n, double *S7) {
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < 7 * n; t += (long)gridDim.x * blockDim.x)
+    S7[t] = A7[t] * winv[t % n];
 }
 
 // Galerkin coarse operator, same summation order as the oracle (for each of
@@ -154,7 +191,14 @@ __global__ void k_rap(const double *Af, int ns, Box fb, const double *pm, const 
 }
 
 // 27 -> 7 point collapse preserving constants and linear functions (same order as the oracle).
-__global__ void k_collapse7(const double *A27, long n, double *A7) {
+// 27 -> 7 points: each off-axis entry moves to the axis neighbours it spans,
+// the centre keeping the row sum. With `aware`, only coupled axis neighbours
+// receive it (a coupling moved onto an uncoupled point, such as a solid cell,
+// would make a Neumann wall act as a Dirichlet one on the coarse grid); with
+// none the entry is lumped into the centre.
+__global__ void k_collapse7(const double *A27, Box b, const unsigned char *coupled, int aware, double *A7) {
+  const long n = b.n;
+  const long st[3] = {1, (long)b.nx, (long)b.nx * b.ny};
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
     double a[27];
 #pragma unroll
@@ -165,14 +209,17 @@ __global__ void k_collapse7(const double *A27, long n, double *A7) {
       if (m < 2 || a[s] == 0.0) continue;
       const double e = a[s];
       a[s] = 0.0;
+      int t = 0;
       for (int dd = 0; dd < 3; ++dd) {
         if (!o3[dd]) continue;
+        if (aware && !coupled[r + o3[dd] * st[dd]]) continue;
         int q[3] = {0, 0, 0};
         q[dd] = o3[dd];
         const int sq = s27(q[0], q[1], q[2]);
         a[sq] = a[sq] + e;
+        ++t;
       }
-      a[13] = a[13] - (double)(m - 1) * e;
+      a[13] = a[13] - (double)(t - 1) * e;
     }
     for (int q = 0; q < 7; ++q) A7[(long)q * n + r] = a[c_slot7[q]];
   }
@@ -186,13 +233,16 @@ __global__ void k_convert(const double *src, T *dst, long n) {
 
 // ---------------------------------------------------------------- V-cycle
 template <class T>
-__global__ void k_load_input(T *bv, long n, VecRef in, const int *gate) {
+__global__ void k_load_input(T *bv, long n, VecRef in, const double *winv, const int *gate) {
   if (gate_off(gate)) return;
   const long off = in.idx ? (long)(*in.idx) * in.ld : 0;
   const double sc = in.nu ? 1.0 / in.nu[in.idx ? *in.idx : 0] : 1.0;
   const double *src = in.base + off;
-  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
-    bv[r] = (T)(in.nu ? src[r] * sc : src[r]);
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    double v = in.nu ? src[r] * sc : src[r];
+    if (winv) v = v * winv[r];
+    bv[r] = (T)v;
+  }
 }
 
 template <class T>
@@ -380,6 +430,16 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
   L[0].b = b0;
   L[0].ns = 7;
   L[0].A = A7;
+  if (winv_) {
+    L[0].Aown.alloc((size_t)7 * b0.n);
+    {
+      LaunchScope ls(K_SETUP, st, 0.0);
+      k_scale_rows<<<grid_for(7 * b0.n), kThreads, 0, st>>>(A7, winv_, b0.n, L[0].Aown.p);
+    }
+    L[0].A = L[0].Aown.p;
+  }
+  const int aware = prm.options & 1;
+  DBuf<unsigned char> coupled;
   double h[3] = {h0[0], h0[1], h0[2]};
   int queue[3], nq = 0;  // directions still to coarsen in the current group
   for (int l = 0;; ++l) {
@@ -434,9 +494,11 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
     F.cdir = d;
     h[d] *= 2.0;
     F.pm.alloc(n); F.pp.alloc(n);
+    coupled.alloc(n);
     {
       LaunchScope ls(K_SETUP, st, 0.0);
-      k_interp_weights<<<grid_for(n), kThreads, 0, st>>>(F.A, F.ns, n, d, F.pm.p, F.pp.p);
+      k_coupled<<<grid_for(n), kThreads, 0, st>>>(F.A, F.ns, n, coupled.p);
+      k_interp_weights<<<grid_for(n), kThreads, 0, st>>>(F.A, F.ns, F.b, d, coupled.p, aware, F.pm.p, F.pp.p);
     }
     Box cb = F.b;
     if (d == 0) cb.nx = (F.b.nx + 1) / 2;
@@ -455,9 +517,12 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
     }
     if (prm.rap == 1) {
       C.Aown.alloc((size_t)7 * cb.n);
+      DBuf<unsigned char> ccoupled;
+      ccoupled.alloc(cb.n);
       {
         LaunchScope ls(K_SETUP, st, 0.0);
-        k_collapse7<<<grid_for(cb.n), kThreads, 0, st>>>(a27.p, cb.n, C.Aown.p);
+        k_coupled<<<grid_for(cb.n), kThreads, 0, st>>>(a27.p, 27, cb.n, ccoupled.p);
+        k_collapse7<<<grid_for(cb.n), kThreads, 0, st>>>(a27.p, cb, ccoupled.p, aware, C.Aown.p);
       }
       IBM_CUDA_TRY(cudaStreamSynchronize(st));
       C.ns = 7;
@@ -472,8 +537,9 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
 }
 
 void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const float *A7f, const double h[3],
-                      const MgParams &p, bool fp64, bool fp32) {
+                      const MgParams &p, bool fp64, bool fp32, const double *winv) {
   prm = p;
+  winv_ = winv;
   (void)fp64;
   build<double>(st, L64, b, A7, h);
   L32.clear();
@@ -483,9 +549,9 @@ void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const flo
       const MgLevelT<double> &D = L64[l];
       L32.emplace_back();
       MgLevelT<float> &F = L32.back();
-      F.b = D.b; F.cdir = D.cdir; F.ns = D.ns;
+      F.b = D.b; F.cdir = D.cdir; F.ns = D.ns; F.relax = D.relax;
       const long n = D.b.n;
-      if (l == 0) F.A = A7f;
+      if (l == 0 && !winv_) F.A = A7f;
       else {
         F.Aown.alloc((size_t)D.ns * n);
         {
@@ -576,8 +642,8 @@ void Multigrid::apply(cudaStream_t st, const VecRef &in, const OutRef &out, cons
     if (L32.empty()) throw Error(IBM_ERR_STATE, "multigrid: FP32 hierarchy not built");
     MgLevelT<float> &F = L32[0];
     {
-      LaunchScope ls(K_MG_LOAD, st, 12.0 * F.b.n);
-      k_load_input<float><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, gate);
+      LaunchScope ls(K_MG_LOAD, st, (winv_ ? 20.0 : 12.0) * F.b.n);
+      k_load_input<float><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, winv_, gate);
     }
     float *x = vcycle<float>(st, L32, 0, prm, gate);
     LaunchScope ls(K_MG_STORE, st, (4.0 + ob) * F.b.n);
@@ -585,8 +651,8 @@ void Multigrid::apply(cudaStream_t st, const VecRef &in, const OutRef &out, cons
   } else {
     MgLevelT<double> &F = L64[0];
     {
-      LaunchScope ls(K_MG_LOAD, st, 16.0 * F.b.n);
-      k_load_input<double><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, gate);
+      LaunchScope ls(K_MG_LOAD, st, (winv_ ? 24.0 : 16.0) * F.b.n);
+      k_load_input<double><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, winv_, gate);
     }
     double *x = vcycle<double>(st, L64, 0, prm, gate);
     LaunchScope ls(K_MG_STORE, st, (8.0 + ob) * F.b.n);

@@ -14,6 +14,7 @@ struct MgParams {
   int max_levels = 40;
   int cycles = 1;       // V-cycles per application
   double group_ratio = 0.0;  // see ibm_solver_params.mg_group_ratio
+  int options = 3;      // see ibm_solver_params.mg_options
 };
 
 template <class T>
@@ -30,8 +31,10 @@ class Multigrid {
  public:
   // Builds the hierarchy from a 7-point operator (FP64 planes, and FP32 planes
   // when fp32 is requested). h = grid spacing used to pick coarsening directions.
+  // winv (device, may be null): the hierarchy is built on diag(winv) A and
+  // every application scales its input by winv.
   void setup(cudaStream_t st, const Box &b, const double *A7, const float *A7f, const double h[3],
-             const MgParams &p, bool fp64, bool fp32);
+             const MgParams &p, bool fp64, bool fp32, const double *winv);
   // out = M in (every kernel gated on *gate when gate != nullptr).
   void apply(cudaStream_t st, const VecRef &in, const OutRef &out, const int *gate, bool use_fp32);
   int levels() const { return (int)L64.size() ? (int)L64.size() : (int)L32.size(); }
@@ -48,6 +51,7 @@ class Multigrid {
   void cycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const int *gate);
   std::vector<MgLevelT<double>> L64;
   std::vector<MgLevelT<float>> L32;
+  const double *winv_ = nullptr;
 };
 
 }  // namespace ibm

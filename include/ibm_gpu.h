@@ -81,6 +81,12 @@ typedef struct ibm_solver_params {
   int vel_inner_sweeps;  /* precision 1: FP32 Jacobi sweeps per momentum preconditioner application */
   double mg_group_ratio; /* between relaxed levels, coarsen every direction whose spacing is within
                             this factor of the smallest (0: one direction per relaxed level) */
+  int mg_options;        /* bit 0: points with no coupling along the coarsening direction
+                            interpolate constants from their coupled coarse neighbours, and the
+                            7-point collapse moves no coupling onto an uncoupled (solid) point;
+                            bit 1: when Ap = W S with W diagonal and S symmetric (the cut-cell
+                            divergence scales rows by 1 / open fraction), build the hierarchy on
+                            S and apply it to W^-1 r. 0 = PFMG's plain rules. Default 3. */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {

@@ -43,6 +43,8 @@ struct oracle {
   double *u, *v, *w, *p;
   double *invd[4];          /* Jacobi inverse diagonals of the four operators */
   int mg_built;
+  int mg_sym;               /* the hierarchy is built on W^-1 Ap */
+  double *mg_winv;          /* 1 / W (ones when not symmetrized) */
   int nlev;
   mg_level lev[40];
 };
@@ -340,19 +342,94 @@ void oracle_apply_operator(const oracle *o, int field, const double *x, double *
 static const int k7to27[7] = {13, 12, 14, 10, 16, 4, 22};
 static int slot_off(int s, int d) { return d == 0 ? s % 3 - 1 : d == 1 ? (s / 3) % 3 - 1 : s / 9 - 1; }
 
-static void mg_interp_weights(mg_level *L) {
+
+/* Operator-dependent interpolation weights (PFMG's: minus the couplings to the
+ * lower / upper neighbour along cdir over the sum of the in-plane entries).
+ * With mg_options bit 0, a coupled point that has no coupling along cdir
+ * (0/0 above, e.g. a cut cell between the cylinder and a closed face) takes
+ * the constant from those of its two coarse neighbours that are coupled
+ * points, so that interpolation keeps reproducing constants there. */
+static void mg_interp_weights(const oracle *o, mg_level *L) {
   const int d = L->cdir;
-  L->pm = (double *)xcalloc((size_t)L->b.N, 8);
-  L->pp = (double *)xcalloc((size_t)L->b.N, 8);
-  for (long r = 0; r < L->b.N; ++r) {
+  const long N = L->b.N;
+  L->pm = (double *)xcalloc((size_t)N, 8);
+  L->pp = (double *)xcalloc((size_t)N, 8);
+  uint8_t *coupled = (uint8_t *)xcalloc((size_t)N, 1);
+  for (long r = 0; r < N; ++r)
+    for (int s = 0; s < 27; ++s)
+      if (s != 13 && L->A[27 * r + s] != 0.0) { coupled[r] = 1; break; }
+  const long stride = d == 0 ? 1 : d == 1 ? L->b.n[0] : (long)L->b.n[0] * L->b.n[1];
+  for (long r = 0; r < N; ++r) {
     const double *a = L->A + 27 * r;
     double c0 = 0.0, cm = 0.0, cp = 0.0;
     for (int s = 0; s < 27; ++s) {
       int od = slot_off(s, d);
       if (od == 0) c0 += a[s]; else if (od < 0) cm += a[s]; else cp += a[s];
     }
+    if ((o->prm.mg_options & 1) && coupled[r] && cm == 0.0 && cp == 0.0) {
+      const int idx[3] = {(int)(r % L->b.n[0]), (int)((r / L->b.n[0]) % L->b.n[1]),
+                          (int)(r / ((long)L->b.n[0] * L->b.n[1]))};
+      const int lo = idx[d] > 0 && coupled[r - stride];
+      const int hi = idx[d] < L->b.n[d] - 1 && coupled[r + stride];
+      if (lo + hi > 0) {
+        L->pm[r] = lo ? 1.0 / (lo + hi) : 0.0;
+        L->pp[r] = hi ? 1.0 / (lo + hi) : 0.0;
+      }
+      continue;
+    }
     if (c0 != 0.0) { L->pm[r] = -cm / c0; L->pp[r] = -cp / c0; }
   }
+  free(coupled);
+}
+
+/* Diagonal symmetrizer of a 7-point operator: W with A = W S, S symmetric.
+ * Each connected set of coupled rows is walked breadth first from its lowest
+ * row (w = 1), neighbours in slot order, w_c = w_r A[c][r] / A[r][c]; then
+ * every coupling is checked. Returns 0 (and leaves winv at 1) when A is not
+ * of that form. winv = 1 / w. */
+static int mg_symmetrizer(const double *A7, const box3 *b, double *winv) {
+  const long N = b->N;
+  double *w = (double *)xcalloc((size_t)N, 8);
+  long *queue = (long *)xcalloc((size_t)N, sizeof(long));
+  uint8_t *seen = (uint8_t *)xcalloc((size_t)N, 1);
+  const long sy = b->n[0], sz = (long)b->n[0] * b->n[1];
+  const long off[7] = {0, -1, 1, -sy, sy, -sz, sz};
+  static const int opp[7] = {0, 2, 1, 4, 3, 6, 5};
+  int ok = 1;
+  for (long root = 0; root < N && ok; ++root) {
+    if (seen[root]) continue;
+    seen[root] = 1;
+    w[root] = 1.0;
+    long head = 0, tail = 0;
+    queue[tail++] = root;
+    while (head < tail && ok) {
+      const long r = queue[head++];
+      const int i = (int)(r % b->n[0]), j = (int)((r / b->n[0]) % b->n[1]), k = (int)(r / sz);
+      const int in[7] = {1, i > 0, i < b->n[0] - 1, j > 0, j < b->n[1] - 1, k > 0, k < b->n[2] - 1};
+      for (int s = 1; s < 7; ++s) {
+        if (!in[s] || A7[7 * r + s] == 0.0) continue;
+        const long c = r + off[s];
+        const double back = A7[7 * c + opp[s]];
+        if (back == 0.0) { ok = 0; break; }
+        if (seen[c]) continue;
+        seen[c] = 1;
+        w[c] = w[r] * back / A7[7 * r + s];
+        queue[tail++] = c;
+      }
+    }
+  }
+  for (long r = 0; r < N && ok; ++r) {
+    const int i = (int)(r % b->n[0]), j = (int)((r / b->n[0]) % b->n[1]), k = (int)(r / sz);
+    const int in[7] = {1, i > 0, i < b->n[0] - 1, j > 0, j < b->n[1] - 1, k > 0, k < b->n[2] - 1};
+    for (int s = 1; s < 7; ++s) {
+      if (!in[s]) continue;
+      const double x = A7[7 * r + s] / w[r], y = A7[7 * (r + off[s]) + opp[s]] / w[r + off[s]];
+      if (fabs(x - y) > 1e-10 * fmax(fabs(x), fabs(y))) { ok = 0; break; }
+    }
+  }
+  for (long r = 0; r < N; ++r) winv[r] = ok ? 1.0 / w[r] : 1.0;
+  free(w); free(queue); free(seen);
+  return ok;
 }
 
 static long lidx(const box3 *b, int i, int j, int k) { return ((long)k * b->n[1] + j) * b->n[0] + i; }
@@ -404,8 +481,21 @@ static void mg_rap(const mg_level *F, mg_level *C) {
  * on linear functions: an entry at offset o with m nonzero components moves to
  * the m axis neighbours along those components and is removed m-1 times from
  * the centre. */
-static void mg_collapse7(mg_level *L) {
-  for (long r = 0; r < L->b.N; ++r) {
+/* Collapse a 27-point coarse stencil to 7 points: each off-axis entry moves
+ * to the axis neighbours it spans, the centre keeping the row sum. With
+ * mg_options bit 0, only coupled axis neighbours receive it (moving a
+ * coupling onto an uncoupled point, such as a solid cell of the cylinder,
+ * would turn a Neumann wall into a Dirichlet one on the coarse grid); with
+ * none the entry is lumped into the centre. */
+static void mg_collapse7(const oracle *o, mg_level *L) {
+  const long N = L->b.N;
+  const int aware = o->prm.mg_options & 1;
+  uint8_t *coupled = (uint8_t *)xcalloc((size_t)N, 1);
+  for (long r = 0; r < N; ++r)
+    for (int s = 0; s < 27; ++s)
+      if (s != 13 && L->A[27 * r + s] != 0.0) { coupled[r] = 1; break; }
+  const long st[3] = {1, L->b.n[0], (long)L->b.n[0] * L->b.n[1]};
+  for (long r = 0; r < N; ++r) {
     double *a = L->A + 27 * r;
     for (int s = 0; s < 27; ++s) {
       int o3[3] = {slot_off(s, 0), slot_off(s, 1), slot_off(s, 2)};
@@ -413,16 +503,20 @@ static void mg_collapse7(mg_level *L) {
       if (m < 2 || a[s] == 0.0) continue;
       double e = a[s];
       a[s] = 0.0;
+      int t = 0;
       for (int dd = 0; dd < 3; ++dd) {
         if (!o3[dd]) continue;
+        if (aware && !coupled[r + o3[dd] * st[dd]]) continue;
         int q[3] = {0, 0, 0};
         q[dd] = o3[dd];
         int sq = (q[0] + 1) + 3 * (q[1] + 1) + 9 * (q[2] + 1);
         a[sq] = a[sq] + e;
+        ++t;
       }
-      a[13] = a[13] - (double)(m - 1) * e;
+      a[13] = a[13] - (double)(t - 1) * e;
     }
   }
+  free(coupled);
 }
 
 static void mg_finish_level(const oracle *o, mg_level *L) {
@@ -479,11 +573,15 @@ static void mg_build(oracle *o) {
   mg_level *L0 = &o->lev[0];
   L0->b = o->bp;
   L0->A = (double *)xcalloc((size_t)L0->b.N * 27, 8);
+  o->mg_winv = (double *)xcalloc((size_t)L0->b.N, 8);
+  const int sym = (o->prm.mg_options & 2) ? mg_symmetrizer(o->in.Ap, &L0->b, o->mg_winv) : 0;
+  if (!sym)
+    for (long r = 0; r < L0->b.N; ++r) o->mg_winv[r] = 1.0;
+  o->mg_sym = sym;
   for (long r = 0; r < L0->b.N; ++r)
     for (int s = 0; s < 7; ++s) {
       const double a = o->in.Ap[7 * r + s];
-      /* symmetric form: fluid rows scaled by their open fraction */
-      L0->A[27 * r + k7to27[s]] = (o->prm.mg_sym && o->in.fluid_p[r]) ? o->in.beta_p[r] * a : a;
+      L0->A[27 * r + k7to27[s]] = sym ? a * o->mg_winv[r] : a;
     }
   double h[3] = {o->dx, o->dy, o->dz};
   int queue[3], nq = 0;  /* directions still to coarsen in the current group */
@@ -526,13 +624,13 @@ static void mg_build(oracle *o) {
     }
     F->cdir = d;
     h[d] *= 2.0;
-    mg_interp_weights(F);
+    mg_interp_weights(o, F);
     mg_level *C = &o->lev[l + 1];
     C->b = F->b;
     C->b.n[d] = (F->b.n[d] + 1) / 2;
     C->b.N = (long)C->b.n[0] * C->b.n[1] * C->b.n[2];
     mg_rap(F, C);
-    if (o->prm.mg_rap == 1) mg_collapse7(C);
+    if (o->prm.mg_rap == 1) mg_collapse7(o, C);
     ++l;
   }
   o->nlev = l + 1;
@@ -630,10 +728,10 @@ static void mg_cycle(oracle *o, int l, const double *b, double *x) {
 
 void oracle_mg_vcycle(oracle *o, const double *b, double *x) {
   mg_build(o);
-  if (!o->prm.mg_sym) { mg_cycle(o, 0, b, x); return; }
+  if (!o->mg_sym) { mg_cycle(o, 0, b, x); return; }
   const long N = o->lev[0].b.N;
   double *bs = (double *)xcalloc((size_t)N, 8);
-  for (long r = 0; r < N; ++r) bs[r] = o->in.fluid_p[r] ? o->in.beta_p[r] * b[r] : b[r];
+  for (long r = 0; r < N; ++r) bs[r] = b[r] * o->mg_winv[r];
   mg_cycle(o, 0, bs, x);
   free(bs);
 }
@@ -799,6 +897,7 @@ void oracle_destroy(oracle *o) {
   if (!o) return;
   free(o->u); free(o->v); free(o->w); free(o->p);
   for (int f = 0; f < 4; ++f) free(o->invd[f]);
+  free(o->mg_winv);
   for (int l = 0; l < o->nlev; ++l) {
     mg_level *L = &o->lev[l];
     free(L->A); free(L->wd); free(L->invd); free(L->pm); free(L->pp); free(L->bv); free(L->xv); free(L->rv);

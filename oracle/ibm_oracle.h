@@ -38,7 +38,11 @@ typedef struct oracle_params {
   int mg_max_levels;
   double mg_group_ratio; /* coarsen every direction with spacing <= ratio * smallest between
                             relaxations (0: one direction per relaxed level) */
-  int mg_sym;          /* 1: hierarchy of L = B Ap (B = diag(beta)), applied to B r */
+  int mg_options;      /* bit 0: points with no coupling along the coarsening direction
+                          interpolate the constant from their coupled coarse neighbours
+                          (plain operator-dependent weights give them 0);
+                          bit 1: hierarchy of S = W^-1 Ap, where Ap = W S with W diagonal
+                          and S symmetric (found from the couplings), applied to W^-1 r */
 } oracle_params;
 
 typedef struct oracle_inputs {
@@ -49,7 +53,6 @@ typedef struct oracle_inputs {
   const int32_t *D_rowptr, *D_col; const double *D_val;
   const int32_t *G_rowptr, *G_col; const double *G_val;
   const double *uin; /* ny*nz, inlet profile at Um */
-  const double *beta_p; /* cell open fractions (multigrid on the symmetric form B Ap) */
 } oracle_inputs;
 
 typedef struct oracle_solve_stats { int iters; double rel_res; int status; } oracle_solve_stats;

@@ -61,16 +61,20 @@ def test_bc_and_convection_match_reference_twins_live(ibm, pyoracle, shape):
         assert bits_equal(a, b)
 
 
-def test_oracle_steps_match_golden(case32, pyoracle):
+@pytest.mark.parametrize("mg_options,tol", [(0, 1e-12), (3, 1e-10)])
+def test_oracle_steps_match_golden(case32, pyoracle, mg_options, tol):
+    """The fixture was made with PFMG's plain multigrid rules (mg_options 0):
+    with those the oracle reproduces it to round-off; with the cut-cell-aware
+    hierarchy (the default) the solves stop at other iterates of the same
+    tight tolerance, which moves the fields by at most 1e-10 relative."""
     g = np.load(os.path.join(GOLDEN, "oracle_channel_32x12x12.npz"))
-    orc = pyoracle.Oracle(case32, vel_tol=1e-13, p_tol=1e-13)
+    orc = pyoracle.Oracle(case32, vel_tol=1e-13, p_tol=1e-13, mg_options=mg_options)
     for step in range(1, int(g["nsteps"]) + 1):
         orc.step(min(1.0, step / float(g["ramp_steps"])))
     u, v, w, p = orc.fields()
-    # same machine class: bitwise; other hosts (thread counts do not matter) agree to round-off
     for a, b in zip((u, v, w, p), (g["u"], g["v"], g["w"], g["p"])):
         scale = max(np.abs(b).max(), 1e-300)
-        assert np.abs(a - b).max() <= 1e-12 * scale
+        assert np.abs(a - b).max() <= tol * scale
 
 
 def test_solves_satisfy_reference_equations(case32, pyoracle):
@@ -146,18 +150,41 @@ def _explicit_P(dims, d, pm, pp):
                          shape=(n, cdims[0] * cdims[1] * cdims[2]))
 
 
-def _interp_weights(A27, d):
+def _coupled(A27):
+    off = A27.copy()
+    off[:, 13] = 0.0
+    return np.any(off != 0.0, axis=1)
+
+
+def _interp_weights(A27, d, dims=None, aware=False):
+    """PFMG's weights; with `aware`, coupled points without coupling along d
+    take the constant from their coupled coarse neighbours."""
     od = np.array([(s % 3 - 1, (s // 3) % 3 - 1, s // 9 - 1)[d] for s in range(27)])
     c0 = A27[:, od == 0].sum(axis=1)
     cm = A27[:, od < 0].sum(axis=1)
     cp = A27[:, od > 0].sum(axis=1)
     with np.errstate(divide="ignore", invalid="ignore"):
-        return np.where(c0 != 0, -cm / c0, 0.0), np.where(c0 != 0, -cp / c0, 0.0)
+        pm, pp = np.where(c0 != 0, -cm / c0, 0.0), np.where(c0 != 0, -cp / c0, 0.0)
+    if aware:
+        cpl = _coupled(A27)
+        n = len(pm)
+        stride = [1, dims[0], dims[0] * dims[1]][d]
+        idx = np.arange(n)
+        coord = [idx % dims[0], (idx // dims[0]) % dims[1], idx // (dims[0] * dims[1])][d]
+        lo = np.zeros(n, bool)
+        hi = np.zeros(n, bool)
+        lo[coord > 0] = cpl[idx[coord > 0] - stride]
+        hi[coord < dims[d] - 1] = cpl[idx[coord < dims[d] - 1] + stride]
+        dec = cpl & (cm == 0) & (cp == 0)
+        nf = lo.astype(float) + hi.astype(float)
+        pm = np.where(dec, np.where(nf > 0, lo / np.maximum(nf, 1), 0.0), pm)
+        pp = np.where(dec, np.where(nf > 0, hi / np.maximum(nf, 1), 0.0), pp)
+    return pm, pp
 
 
-@pytest.mark.parametrize("rap", [0, 1])
-def test_multigrid_coarse_operators_are_rap(case32, pyoracle, rap):
-    orc = pyoracle.Oracle(case32, mg_rap=rap, mg_coarse_max=16)
+@pytest.mark.parametrize("rap,options", [(0, 0), (1, 0), (0, 3), (1, 3)])
+def test_multigrid_coarse_operators_are_rap(case32, pyoracle, rap, options):
+    orc = pyoracle.Oracle(case32, mg_rap=rap, mg_coarse_max=16, mg_options=options)
     levels = orc.mg_levels()
     assert len(levels) >= 4
     dirs = [cd for _, cd in levels[:-1]]
@@ -165,21 +192,58 @@ def test_multigrid_coarse_operators_are_rap(case32, pyoracle, rap):
     for l in range(min(3, len(levels) - 1)):
         dims, d = levels[l]
         Af = orc.mg_level_coef(l)
-        pm, pp = _interp_weights(Af, d)
+        pm, pp = _interp_weights(Af, d, dims, aware=bool(options & 1))
         A, P = _explicit_A(Af, dims), _explicit_P(dims, d, pm, pp)
         Ac = (P.T @ A @ P).toarray()
-        got = _explicit_A(orc.mg_level_coef(l + 1), levels[l + 1][0]).toarray()
+        Cc = orc.mg_level_coef(l + 1)
+        got = _explicit_A(Cc, levels[l + 1][0]).toarray()
         scale = np.abs(Ac).max()
         if rap == 0:
             assert np.abs(got - Ac).max() <= 1e-12 * scale
+            continue
+        # collapsed: same row sums
+        assert np.allclose(got.sum(axis=1), Ac.sum(axis=1), atol=1e-9 * scale)
+        nxc, nyc, nzc = levels[l + 1][0]
+        if options & 1:
+            # no collapsed coupling lands on an uncoupled point
+            cpl = _coupled(_to27_from_dense(Ac, levels[l + 1][0]))
+            assert not np.any((got != 0) & ~np.eye(len(got), dtype=bool) & ~cpl[None, :])
         else:
-            # collapsed: same row sums and same action on linear functions
-            assert np.allclose(got.sum(axis=1), Ac.sum(axis=1), atol=1e-9 * scale)
-            nxc, nyc, nzc = levels[l + 1][0]
+            # plain collapse: same action on linear functions
             kk, jj, ii = np.meshgrid(np.arange(nzc), np.arange(nyc), np.arange(nxc), indexing="ij")
             for lin in (ii.ravel(), jj.ravel(), kk.ravel()):
-                inner = np.ones(len(lin), bool)
-                assert np.allclose((got @ lin)[inner], (Ac @ lin)[inner], atol=1e-8 * scale * max(nxc, nyc, nzc))
+                assert np.allclose(got @ lin, Ac @ lin, atol=1e-8 * scale * max(nxc, nyc, nzc))
+
+
+def _to27_from_dense(M, dims):
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    out = np.zeros((n, 27))
+    r, c = np.nonzero(M)
+    ri, rj, rk = r % nx, (r // nx) % ny, r // (nx * ny)
+    ci, cj, ck = c % nx, (c // nx) % ny, c // (nx * ny)
+    out[r, (ci - ri + 1) + 3 * (cj - rj + 1) + 9 * (ck - rk + 1)] = M[r, c]
+    return out
+
+
+def test_pressure_operator_is_diagonally_symmetrizable(case32):
+    """The cut-cell pressure operator is W S with S symmetric and W the
+    inverse open fraction of cut cells: the form the symmetrized hierarchy
+    (mg_options bit 1) relies on."""
+    nx, ny, nz = case32.shape
+    ap = case32.array("Ap_vals").reshape(-1, 7)
+    beta = case32.array("beta_p")
+    fl = case32.array("fluid_p").astype(bool)
+    S = ap * np.where(fl, beta, 1.0)[:, None]
+    sy, sz = nx, nx * ny
+    idx = np.arange(nx * ny * nz)
+    i, j, k = idx % nx, (idx // nx) % ny, idx // (nx * ny)
+    for s, (off, opp, ok) in enumerate([(1, 1, i < nx - 1), (sy, 3, j < ny - 1), (sz, 5, k < nz - 1)]):
+        up = 2 * s + 2  # +x, +y, +z slots
+        r = idx[ok]
+        assert np.allclose(S[r, up], S[r + off, opp], rtol=1e-12, atol=0)
+    r = idx[j < ny - 1]
+    assert np.abs(ap[r, 4] - ap[r + sy, 3]).max() > 0  # the operator itself is not symmetric
 
 
 def test_multigrid_vcycle_contracts(case32, pyoracle):
