@@ -90,9 +90,9 @@ def initial_state(case, seed=2026):
 
 def solver_params(ibm, precision, graph=0):
     return ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, vel_maxit=250, p_maxit=250, vel_kdim=50, p_kdim=50,
-                             p_pc=1, p_pc_rap_type=1, p_pc_relax_type=2, mg_nu1=1, mg_nu2=1, mg_omega=1.0,
-                             mg_group_ratio=1.5, mg_coarse_max=64, precision=precision, vel_inner_sweeps=3,
-                             use_graph=graph)
+                             p_pc=1, p_pc_rap_type=0, p_pc_relax_type=2, mg_nu1=2, mg_nu2=2, mg_omega=1.0,
+                             mg_group_ratio=1.5, mg_coarse_max=64, mg_options=3, precision=precision,
+                             vel_inner_sweeps=3, use_graph=graph)
 
 
 class ClockSampler:
@@ -301,7 +301,10 @@ def profile_pass(solver, plib, Prof, ibm):
     plib.ibm_profile_time_kernel(solver._ctx, -1)
     names = {k: plib.ibm_kernel_name(k).decode() for k in per_class}
     kernel_ms = {names[k]: round(per_class[k], 4) for k in per_class if per_launch[k] > 0}
-    return dom, names[dom], pr, st, kernel_ms, 21 + 2
+    # algorithmic bytes of the class / its CUDA-event time
+    kernel_gbs = {names[k]: round(per_bytes[k] / (per_class[k] * 1e-3) / 1e9, 1)
+                  for k in per_class if per_launch[k] > 0 and per_class[k] > 0}
+    return dom, names[dom], pr, st, kernel_ms, kernel_gbs, 21 + 2
 
 
 def main():
@@ -353,7 +356,7 @@ def main():
     value = ws * args.steps / (ms / 1e3)
 
     # roofline and solve bandwidth from the host-driven pass
-    dom, kname, prof, pst, kernel_ms, n_prof = profile_pass(mixed, plib, Prof, ibm)
+    dom, kname, prof, pst, kernel_ms, kernel_gbs, n_prof = profile_pass(mixed, plib, Prof, ibm)
     ph = phase_means(pst)
     solve_gbs = {"pressure": prof.phase_bytes[2] / 2 / (ph["pressure"] * 1e-3) / 1e9,
                  "momentum": prof.phase_bytes[1] / 2 / (ph["momentum"] * 1e-3) / 1e9,
@@ -380,10 +383,12 @@ def main():
                                   f"graph-captured step",
                       "grid": [nx, ny, nz], "parallelism": f"replicas x{ws}",
                       "l2": "inputs larger than L2 (operators + fields + Krylov bases, tens of GB resident)",
-                      "pressure_pc": "semicoarsening MG (grouped), 7-point coarse, two-colour relaxation, FP32",
+                      "pressure_pc": "semicoarsening MG (grouped, symmetrized, cut-cell-aware interpolation), "
+                                     "Galerkin 27-point coarse levels, 2+2 two-colour sweeps, FP32",
                       "momentum_pc": "FP32 Jacobi sweeps"},
            "phase_ms": phase_means(step_stats), "iterations_mean": iters_mean(step_stats),
-           "solve_gbs": solve_gbs, "kernel_ms_per_step": kernel_ms, "gpu_launches": int(launches),
+           "solve_gbs": solve_gbs, "kernel_ms_per_step": kernel_ms, "kernel_gbs": kernel_gbs,
+           "gpu_launches": int(launches),
            "setup_s": setup_s}
 
     if not args.no_fp64:

@@ -291,6 +291,79 @@ __global__ void k_relax_color(const T *A, const T *invd, const T *b, const T *x,
   }
 }
 
+// Colour-split coefficients of a 7-point level with an even nx. Rows 2m and
+// 2m+1 lie on one x line and have opposite colours (parity of i+j+k), so the
+// pair index m numbers the points of either colour; planes [c][q][m] hold, for
+// the colour-c point of pair m, q = 0 the inverse diagonal and q = 1..6 the
+// couplings -x,+x,-y,+y,-z,+z. A colour phase streams only its own half.
+__device__ __forceinline__ long rb_row(long m, int color, int nx, int ny, int &i, int &j, int &k) {
+  const long q = 2 * m;
+  const long line = q / nx;
+  j = (int)(line % ny);
+  k = (int)(line / ny);
+  const long r = q + ((j + k + color) & 1);
+  i = (int)(r - line * nx);
+  return r;
+}
+
+template <class T>
+__global__ void k_split_colors(const T *A, const T *invd, Box bx, T *R) {
+  const long h = bx.n / 2;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < 2 * h; t += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(t / h);
+    const long m = t - c * h;
+    int i, j, k;
+    const long r = rb_row(m, c, bx.nx, bx.ny, i, j, k);
+    T *o = R + (long)c * 7 * h + m;
+    o[0] = invd[r];
+    for (int s = 1; s < 7; ++s) o[(long)s * h] = A[(long)s * bx.n + r];
+  }
+}
+
+// One colour phase in place: x_r = invd_r (b_r - sum of the couplings to the
+// other colour's points). Points of one colour are not coupled to each other
+// in a 7-point stencil, so the phase reads only values it does not write.
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_relax_rb(const T *__restrict__ R, const T *__restrict__ b, T *x,
+                                                       Box bx, int color, const int *gate) {
+  if (gate_off(gate)) return;
+  const long h = bx.n / 2;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const long sy = nx, sz = (long)nx * ny;
+  const T *__restrict__ P = R + (long)color * 7 * h;
+  for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const long r = rb_row(m, color, nx, ny, i, j, k);
+    const T xw = i > 0 ? x[r - 1] : T(0);
+    const T xe = i < nx - 1 ? x[r + 1] : T(0);
+    const T xs = j > 0 ? x[r - sy] : T(0);
+    const T xn = j < ny - 1 ? x[r + sy] : T(0);
+    const T xb = k > 0 ? x[r - sz] : T(0);
+    const T xt = k < nz - 1 ? x[r + sz] : T(0);
+    T acc = T(0);
+    acc = fmat<T>(P[h + m], xw, acc);
+    acc = fmat<T>(P[2 * h + m], xe, acc);
+    acc = fmat<T>(P[3 * h + m], xs, acc);
+    acc = fmat<T>(P[4 * h + m], xn, acc);
+    acc = fmat<T>(P[5 * h + m], xb, acc);
+    acc = fmat<T>(P[6 * h + m], xt, acc);
+    x[r] = P[m] * (b[r] - acc);
+  }
+}
+
+// First phase from a zero guess: colour-0 points take invd b, colour-1 points 0.
+template <class T>
+__global__ void k_relax_rb_zero(const T *__restrict__ R, const T *__restrict__ b, T *x, Box bx, const int *gate) {
+  if (gate_off(gate)) return;
+  const long h = bx.n / 2;
+  for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const long r = rb_row(m, 0, bx.nx, bx.ny, i, j, k);
+    x[r] = R[m] * b[r];
+    x[r ^ 1] = T(0);
+  }
+}
+
 template <class T, int NS>
 __global__ void k_residual(const T *A, const T *b, const T *x, T *res, Box bx, const int *gate) {
   if (gate_off(gate)) return;
@@ -421,6 +494,16 @@ void dense_inverse(const std::vector<double> &A, int ns, const Box &b, std::vect
 }  // namespace
 
 // ---------------------------------------------------------------- host side
+// Colour-split copy of a relaxed 7-point level with an even nx (the fine
+// level), used by the in-place two-colour relaxation.
+template <class T>
+static void split_colors(cudaStream_t st, MgLevelT<T> &F, const MgParams &prm) {
+  if (prm.relax != 2 || F.ns != 7 || (F.b.nx & 1) || F.b.n < 2) return;
+  F.rb.alloc((size_t)7 * F.b.n);
+  LaunchScope ls(K_SETUP, st, 0.0);
+  k_split_colors<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, F.rb.p);
+}
+
 template <>
 void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L, const Box &b0, const double *A7,
                               const double h0[3]) {
@@ -452,6 +535,7 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
       LaunchScope ls(K_SETUP, st, 0.0);
       k_diag<<<grid_for(n), kThreads, 0, st>>>(diag, n, prm.omega, F.invd.p, F.wd.p);
     }
+    split_colors(st, F, prm);
     const int dims[3] = {F.b.nx, F.b.ny, F.b.nz};
     // A group starts at a relaxed level: every direction whose spacing is
     // within group_ratio of the smallest is coarsened once (smallest spacing
@@ -569,6 +653,7 @@ void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const flo
         }
       };
       conv(D.wd, F.wd); conv(D.invd, F.invd); conv(D.pm, F.pm); conv(D.pp, F.pp); conv(D.dense, F.dense);
+      split_colors(st, F, prm);
       F.x.alloc(n); F.bv.alloc(n); F.r.alloc(n); F.t.alloc(n);
     }
     IBM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -591,8 +676,17 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   }
   T *cur = F.x.p, *oth = F.t.p;
   const double sweep_bytes = T_ * n * (F.ns + 4.0);
+  const long h = n / 2;
   auto relax = [&](bool zero) {
-    if (p.relax == 2) {
+    if (p.relax == 2 && F.rb.p) {
+      {
+        LaunchScope ls(K_MG_RELAX, st, zero ? 2.5 * T_ * n : 5.0 * T_ * n);
+        if (zero) k_relax_rb_zero<T><<<grid_for(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, gate);
+        else k_relax_rb<T><<<grid_for(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 0, gate);
+      }
+      LaunchScope ls(K_MG_RELAX, st, 5.0 * T_ * n);
+      k_relax_rb<T><<<grid_for(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 1, gate);
+    } else if (p.relax == 2) {
       for (int color = 0; color < 2; ++color) {
         const bool z = zero && color == 0;
         LaunchScope ls(K_MG_RELAX, st, z ? 3.0 * T_ * n : sweep_bytes);
@@ -682,8 +776,8 @@ void Multigrid::level_coef27(cudaStream_t st, int l, double *host_out) const {
 
 size_t Multigrid::bytes() const {
   size_t b = 0;
-  for (const auto &F : L64) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes();
-  for (const auto &F : L32) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes();
+  for (const auto &F : L64) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes();
+  for (const auto &F : L32) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes();
   return b;
 }
 

@@ -25,6 +25,7 @@ struct MgLevelT {
   int ns = 7;           // stencil slots stored: 7 (Struct order) or 27
   const T *A = nullptr; // [ns][n] planes (level 0 points at the operator itself)
   DBuf<T> Aown, wd, invd, pm, pp, x, bv, r, t, dense;
+  DBuf<T> rb;           // colour-split coefficients for the in-place two-colour relaxation (7-point, even nx)
 };
 
 class Multigrid {
