@@ -351,6 +351,54 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb(const T *__restrict__ R, 
   }
 }
 
+// 27-point levels (even nx): planes [c][q][m] hold the 27 coefficients of the
+// colour-c point of pair m (q = 27-point slot) and, at q = 27, its inverse
+// diagonal. Diagonal neighbours share a colour, so a phase cannot update in
+// place: it writes every point of the pair to the other buffer (the own-colour
+// point relaxed, the other copied), with the same arithmetic as k_relax_color.
+template <class T>
+__global__ void k_split_colors27(const T *A, const T *invd, Box bx, T *R) {
+  const long h = bx.n / 2;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < 2 * h; t += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(t / h);
+    const long m = t - c * h;
+    int i, j, k;
+    const long r = rb_row(m, c, bx.nx, bx.ny, i, j, k);
+    T *o = R + (long)c * 28 * h + m;
+    for (int s = 0; s < 27; ++s) o[(long)s * h] = A[(long)s * bx.n + r];
+    o[27L * h] = invd[r];
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_relax_rb27(const T *__restrict__ R, const T *__restrict__ b,
+                                                         const T *__restrict__ x, T *__restrict__ t, Box bx,
+                                                         int color, int zero_x, const int *gate) {
+  if (gate_off(gate)) return;
+  const long h = bx.n / 2;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const T *__restrict__ P = R + (long)color * 28 * h;
+  for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const long r = rb_row(m, color, nx, ny, i, j, k);
+    if (zero_x) {
+      t[r] = P[27 * h + m] * b[r];
+      t[r ^ 1] = T(0);
+      continue;
+    }
+    T acc = T(0);
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+      const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+      const bool in = ii >= 0 && ii < nx && jj >= 0 && jj < ny && kk >= 0 && kk < nz;
+      const T xv = in ? x[((long)kk * ny + jj) * nx + ii] : T(0);
+      acc = fmat<T>(P[(long)s * h + m], xv, acc);
+    }
+    t[r] = fmat<T>(P[27 * h + m], b[r] - acc, x[r]);
+    t[r ^ 1] = x[r ^ 1];
+  }
+}
+
 // First phase from a zero guess: colour-0 points take invd b, colour-1 points 0.
 template <class T>
 __global__ void k_relax_rb_zero(const T *__restrict__ R, const T *__restrict__ b, T *x, Box bx, const int *gate) {
@@ -498,10 +546,15 @@ void dense_inverse(const std::vector<double> &A, int ns, const Box &b, std::vect
 // level), used by the in-place two-colour relaxation.
 template <class T>
 static void split_colors(cudaStream_t st, MgLevelT<T> &F, const MgParams &prm) {
-  if (prm.relax != 2 || F.ns != 7 || (F.b.nx & 1) || F.b.n < 2) return;
-  F.rb.alloc((size_t)7 * F.b.n);
+  if (prm.relax != 2 || (F.b.nx & 1) || F.b.n < 2) return;
   LaunchScope ls(K_SETUP, st, 0.0);
-  k_split_colors<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, F.rb.p);
+  if (F.ns == 7) {
+    F.rb.alloc((size_t)7 * F.b.n);
+    k_split_colors<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, F.rb.p);
+  } else {
+    F.rb27.alloc((size_t)28 * F.b.n);
+    k_split_colors27<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, F.rb27.p);
+  }
 }
 
 template <>
@@ -686,6 +739,13 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
       }
       LaunchScope ls(K_MG_RELAX, st, 5.0 * T_ * n);
       k_relax_rb<T><<<grid_for(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 1, gate);
+    } else if (p.relax == 2 && F.rb27.p) {
+      for (int color = 0; color < 2; ++color) {
+        const bool z = zero && color == 0;
+        LaunchScope ls(K_MG_RELAX, st, z ? 2.5 * T_ * n : T_ * n * (14.0 + 3.0));
+        k_relax_rb27<T><<<grid_for(h), kThreads, 0, st>>>(F.rb27.p, F.bv.p, cur, oth, F.b, color, z, gate);
+        std::swap(cur, oth);
+      }
     } else if (p.relax == 2) {
       for (int color = 0; color < 2; ++color) {
         const bool z = zero && color == 0;
@@ -776,8 +836,8 @@ void Multigrid::level_coef27(cudaStream_t st, int l, double *host_out) const {
 
 size_t Multigrid::bytes() const {
   size_t b = 0;
-  for (const auto &F : L64) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes();
-  for (const auto &F : L32) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes();
+  for (const auto &F : L64) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes() + F.rb27.bytes();
+  for (const auto &F : L32) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes() + F.rb27.bytes();
   return b;
 }
 

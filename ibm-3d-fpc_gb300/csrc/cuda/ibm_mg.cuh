@@ -26,6 +26,7 @@ struct MgLevelT {
   const T *A = nullptr; // [ns][n] planes (level 0 points at the operator itself)
   DBuf<T> Aown, wd, invd, pm, pp, x, bv, r, t, dense;
   DBuf<T> rb;           // colour-split coefficients for the in-place two-colour relaxation (7-point, even nx)
+  DBuf<T> rb27;         // colour-split 27-point coefficients + inverse diagonal (two-colour relaxation)
 };
 
 class Multigrid {
