@@ -194,10 +194,16 @@ void require_inputs(ibm_ctx *c) {
   if (!c->csr_set) throw Error(IBM_ERR_STATE, "projection operators not set");
 }
 
+// precision 2: each FP32 Arnoldi cycle stops once its residual estimate fell
+// by this factor (about what an FP32 basis resolves); the FP64 restart then
+// measures the true residual.
+constexpr double kCycleRtol32 = 1e-5;
+
 void ensure_solvers(ibm_ctx *c) {
   if (c->solvers_ready && c->solvers_precision == c->prm.precision) return;
   const ibm_solver_params &p = c->prm;
-  const bool mixed = p.precision == 1;
+  const bool mixed = p.precision >= 1;
+  const int a32 = p.precision == 2;
   if (!mixed && p.vel_jacobi_iters != 1)
     throw Error(IBM_ERR_UNSUPPORTED, "FP64 momentum solves support one Jacobi sweep per application");
   KSysHost hs[3];
@@ -209,7 +215,10 @@ void ensure_solvers(ibm_ctx *c) {
     h.invd = o.invd.p;
     h.Af = o.cf.p; h.invdf = o.invdf.p;
     h.kdim = p.vel_kdim; h.maxit = p.vel_maxit; h.tol = p.vel_tol;
-    if (mixed) { h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps); }
+    if (mixed) {
+      h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps);
+      h.a32 = a32; h.cycle_rtol = kCycleRtol32;
+    }
     else { h.pc = 0; h.A = o.cj.p; }
   }
   c->kmom.configure(3, hs);
@@ -230,10 +239,13 @@ void ensure_solvers(ibm_ctx *c) {
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
     const double *winv = ((p.mg_options & 2) && c->p_sym) ? c->p_winv.p : nullptr;
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
-    if (mixed) { hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; }
+    if (mixed) { hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; hp.a32 = a32; hp.cycle_rtol = kCycleRtol32; }
     else { hp.pc = 1; hp.A = op.c.p; }
   } else {
-    if (mixed) { hp.pc = 2; hp.pc_cb = 0; hp.A = op.c.p; hp.inner_sweeps = 1; }
+    if (mixed) {
+      hp.pc = 2; hp.pc_cb = 0; hp.A = op.c.p; hp.inner_sweeps = 1;
+      hp.a32 = a32; hp.cycle_rtol = kCycleRtol32;
+    }
     else { hp.pc = 0; hp.A = op.cj.p; }
   }
   c->kp.configure(1, &hp);
@@ -671,7 +683,7 @@ int ibm_set_solver_params(ibm_ctx *c, const ibm_solver_params *p) {
       throw Error(IBM_ERR_ARG, "kdim must be in [1, 63]");
     if (p->vel_maxit < 0 || p->p_maxit < 0 || !(p->vel_tol >= 0) || !(p->p_tol >= 0))
       throw Error(IBM_ERR_ARG, "bad tolerance or iteration limit");
-    if (p->precision != 0 && p->precision != 1) throw Error(IBM_ERR_ARG, "precision must be 0 or 1");
+    if (p->precision < 0 || p->precision > 2) throw Error(IBM_ERR_ARG, "precision must be 0, 1 or 2");
     if (p->p_pc != 0 && p->p_pc != 1) throw Error(IBM_ERR_ARG, "p_pc must be 0 or 1");
     if (p->mg_nu1 < 0 || p->mg_nu2 < 0 || p->mg_coarse_max < 1 || p->mg_max_levels < 1)
       throw Error(IBM_ERR_ARG, "bad multigrid parameters");
@@ -875,7 +887,7 @@ int ibm_apply_preconditioner(ibm_ctx *c, int field, const double *r, double *z) 
     if (field == 3 && c->prm.p_pc == 1) {
       VecRef in;
       in.base = dr.p;
-      if (c->prm.precision == 1) {
+      if (c->prm.precision >= 1) {
         DBuf<float> zf;
         zf.alloc(b.n);
         OutRef out;

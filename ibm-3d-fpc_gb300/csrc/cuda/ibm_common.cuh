@@ -109,6 +109,8 @@ struct KScal {
   unsigned ticket;    // last-block-done counter of the reduction kernels
   int nonfinite;
   double b_norm, r_norm, eps, real_old;
+  double cyc_eps;     // the current cycle also ends when the estimate reaches this
+  double cyc_rtol;    // cyc_eps = max(eps, cyc_rtol * true residual at the cycle start)
   double nu[kMaxKdim + 1];            // norms of the stored (unnormalised) basis vectors
   double H[(kMaxKdim + 1) * kMaxKdim];  // H(i,j) at [i*kMaxKdim + j]
   double cs[kMaxKdim], sn[kMaxKdim], g[kMaxKdim + 1], y[kMaxKdim];
@@ -131,6 +133,8 @@ struct KSys {
   const double *b;
   float *zf, *zf2;      // FP32 work for the inner sweeps
   double *part;         // block partial sums [nblk][kMaxKdim + 2]
+  float *Vf, *wf;       // FP32 basis and work vector of the FP32 Arnoldi cycles (a32)
+  int a32;              // Arnoldi cycles in FP32 (basis, operator, dots per thread), restarts in FP64
   int nblk;
   int pc;               // 0 Jacobi folded into A, 1 explicit z (multigrid), 2 flexible FP32 z
   int pc_cb;            // pc 2: preconditioner supplied by a callback (else FP32 Jacobi sweeps)

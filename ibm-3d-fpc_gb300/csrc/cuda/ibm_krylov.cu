@@ -74,7 +74,8 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
         const double bv = S.b[r];
         const double rv = bv - ax;
         S.r[r] = rv;
-        S.V[r] = rv;
+        if (S.a32) S.Vf[r] = (float)rv;
+        else S.V[r] = rv;
         pb = fma(bv, bv, pb);
         pr = fma(rv, rv, pr);
       }
@@ -93,6 +94,7 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
     sc->b_norm = bn;
     sc->r_norm = rn;
     sc->eps = sc->tol * (bn > 0.0 ? bn : rn);
+    sc->cyc_eps = fmax(sc->eps, sc->cyc_rtol * rn);
     sc->real_old = bn;
     sc->iters = 0;
     sc->i = 0;
@@ -109,10 +111,53 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
 }
 
 // w = A z_j (z_j = M v_j by the system's preconditioner mode), d1_k = (V_k, w).
+// Closes Arnoldi step j (one thread): h(j+1,j) = |v_{j+1}| = hn, the previous
+// rotations applied to the new Hessenberg column, a new Givens rotation, the
+// residual estimate and the stop tests; at the end of a cycle the
+// back-substitution H y = g and the update coefficients y / nu.
+__device__ void arnoldi_finalize(KScal *sc, int j, double hn) {
+  const int K = kMaxKdim;
+  sc->nu[j + 1] = hn;
+  sc->H[(j + 1) * K + j] = hn;
+  // apply previous rotations to the new column, then a new rotation
+  for (int q = 0; q < j; ++q) {
+    const double t = sc->H[q * K + j];
+    sc->H[q * K + j] = sc->sn[q] * sc->H[(q + 1) * K + j] + sc->cs[q] * t;
+    sc->H[(q + 1) * K + j] = -sc->sn[q] * t + sc->cs[q] * sc->H[(q + 1) * K + j];
+  }
+  const double a = sc->H[j * K + j], b = sc->H[(j + 1) * K + j];
+  double gam = sqrt(b * b + a * a);
+  if (gam == 0.0) gam = 2.220446049250313e-16;
+  sc->cs[j] = a / gam;
+  sc->sn[j] = b / gam;
+  sc->g[j + 1] = -sc->sn[j] * sc->g[j];
+  sc->g[j] = sc->cs[j] * sc->g[j];
+  sc->H[j * K + j] = sc->sn[j] * b + sc->cs[j] * a;
+  sc->i = j + 1;
+  sc->iters += 1;
+  sc->r_norm = fabs(sc->g[j + 1]);
+  const bool claimed = sc->r_norm <= sc->eps || hn == 0.0;
+  const bool cycle_done = sc->r_norm <= sc->cyc_eps;
+  if (!isfinite(sc->r_norm)) sc->nonfinite = 1;
+  if (claimed || cycle_done || sc->i >= sc->kdim || sc->iters >= sc->maxit || !isfinite(sc->r_norm)) {
+    sc->claimed = claimed;
+    sc->active = 0;
+    sc->cycle_end = 1;
+    // back substitution H y = g for the i x i upper triangle
+    const int m = sc->i;
+    for (int q = m - 1; q >= 0; --q) {
+      double t = sc->g[q];
+      for (int c = q + 1; c < m; ++c) t -= sc->H[q * K + c] * sc->y[c];
+      sc->y[q] = t / sc->H[q * K + q];
+    }
+    for (int q = 0; q < m; ++q) sc->coef[q] = sc->y[q] / sc->nu[q];
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
   KSys &S = sys[blockIdx.y];
   KScal *sc = S.s;
-  if (!sc->active) return;
+  if (!sc->active || S.a32) return;
   const int j = sc->i, nd = j + 1;
   __shared__ double sacc[(kMaxKdim + 1) * kWarps];
   for (int t = threadIdx.x; t < nd * kWarps; t += blockDim.x) sacc[t] = 0.0;
@@ -167,7 +212,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
 __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
   KSys &S = sys[blockIdx.y];
   KScal *sc = S.s;
-  if (!sc->active) return;
+  if (!sc->active || S.a32) return;
   const int j = sc->i, nd = j + 1;
   __shared__ double sacc[(kMaxKdim + 1) * kWarps];
   __shared__ double cf[kMaxKdim + 1];
@@ -217,7 +262,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
 __global__ void __launch_bounds__(kThreads) k_arnoldi_next(KSys *sys) {
   KSys &S = sys[blockIdx.y];
   KScal *sc = S.s;
-  if (!sc->active) return;
+  if (!sc->active || S.a32) return;
   const int j = sc->i, nd = j + 1;
   __shared__ double cf[kMaxKdim + 1];
   __shared__ double sacc[kWarps];
@@ -248,42 +293,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next(KSys *sys) {
   __syncthreads();
   if (threadIdx.x == 0) {
     sc->ticket = 0;
-    const int K = kMaxKdim;
-    const double hn = sqrt(tot[0]);
-    sc->nu[j + 1] = hn;
-    sc->H[(j + 1) * K + j] = hn;
-    // apply previous rotations to the new column, then a new rotation
-    for (int q = 0; q < j; ++q) {
-      const double t = sc->H[q * K + j];
-      sc->H[q * K + j] = sc->sn[q] * sc->H[(q + 1) * K + j] + sc->cs[q] * t;
-      sc->H[(q + 1) * K + j] = -sc->sn[q] * t + sc->cs[q] * sc->H[(q + 1) * K + j];
-    }
-    const double a = sc->H[j * K + j], b = sc->H[(j + 1) * K + j];
-    double gam = sqrt(b * b + a * a);
-    if (gam == 0.0) gam = 2.220446049250313e-16;
-    sc->cs[j] = a / gam;
-    sc->sn[j] = b / gam;
-    sc->g[j + 1] = -sc->sn[j] * sc->g[j];
-    sc->g[j] = sc->cs[j] * sc->g[j];
-    sc->H[j * K + j] = sc->sn[j] * b + sc->cs[j] * a;
-    sc->i = j + 1;
-    sc->iters += 1;
-    sc->r_norm = fabs(sc->g[j + 1]);
-    const bool claimed = sc->r_norm <= sc->eps || hn == 0.0;
-    if (!isfinite(sc->r_norm)) sc->nonfinite = 1;
-    if (claimed || sc->i >= sc->kdim || sc->iters >= sc->maxit || !isfinite(sc->r_norm)) {
-      sc->claimed = claimed;
-      sc->active = 0;
-      sc->cycle_end = 1;
-      // back substitution H y = g for the i x i upper triangle
-      const int m = sc->i;
-      for (int q = m - 1; q >= 0; --q) {
-        double t = sc->g[q];
-        for (int c = q + 1; c < m; ++c) t -= sc->H[q * K + c] * sc->y[c];
-        sc->y[q] = t / sc->H[q * K + q];
-      }
-      for (int q = 0; q < m; ++q) sc->coef[q] = sc->y[q] / sc->nu[q];
-    }
+    arnoldi_finalize(sc, j, sqrt(tot[0]));
   }
 }
 
@@ -336,7 +346,8 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
         row_ijk((int)r, S.nx, S.ny, i, j, k);
         const double rv = S.b[r] - stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
         S.r[r] = rv;
-        S.V[r] = rv;
+        if (S.a32) S.Vf[r] = (float)rv;
+        else S.V[r] = rv;
         pr = fma(rv, rv, pr);
       }
     }
@@ -357,11 +368,157 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
     if (sc->iters >= sc->maxit) { sc->status = 2; sc->active = 0; return; }
     if (sc->claimed && rt >= sc->real_old) { sc->status = 3; sc->active = 0; return; }
     sc->real_old = rt;
+    sc->cyc_eps = fmax(sc->eps, sc->cyc_rtol * rt);
     sc->i = 0;
     sc->claimed = 0;
     sc->nu[0] = rt;
     sc->g[0] = rt;
     sc->active = 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 Arnoldi cycles (a32 systems, flexible form only). The same three steps
+// on an FP32 basis: the operator is the FP32 copy, products and per-thread
+// sums are FP32, sums across threads and blocks and every scalar are FP64.
+// A cycle stops once its estimate fell by cyc_rtol; the restart computes the
+// true residual in FP64, so the solve still meets the FP64 tolerance.
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active || !S.a32) return;
+  const int j = sc->i, nd = j + 1;
+  __shared__ double sacc[(kMaxKdim + 1) * kWarps];
+  for (int t = threadIdx.x; t < nd * kWarps; t += blockDim.x) sacc[t] = 0.0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float *zj = S.Z + (long)j * S.ldv;
+  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+    float wv[kRowsPerThread];
+#pragma unroll
+    for (int t = 0; t < kRowsPerThread; ++t) {
+      const long r = t0 + t * kThreads + threadIdx.x;
+      wv[t] = 0.0f;
+      if (r < S.n) {
+        int i, jj, k;
+        row_ijk((int)r, S.nx, S.ny, i, jj, k);
+        const float w = stencil7_row_f(S.Af, S.n, zj, (int)r, i, jj, k, S.nx, S.ny, S.nz);
+        S.wf[r] = w;
+        wv[t] = w;
+      }
+    }
+    for (int kk = 0; kk < nd; ++kk) {
+      const float *vk = S.Vf + (long)kk * S.ldv;
+      float p = 0.0f;
+#pragma unroll
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) p = fmaf(vk[r], wv[t], p);
+      }
+      p = warp_sum_f(p);
+      if (lane == 0) sacc[kk * kWarps + warp] += (double)p;
+    }
+  }
+  if (!block_partials_and_last(sacc, nd, S.part, &sc->ticket)) return;
+  __shared__ double tot[kMaxKdim + 1];
+  reduce_partials(S.part, gridDim.x, nd, tot);
+  __syncthreads();
+  for (int kk = threadIdx.x; kk < nd; kk += blockDim.x) {
+    const double h = tot[kk] / sc->nu[kk];
+    sc->h1[kk] = h;
+    sc->coef[kk] = h / sc->nu[kk];
+  }
+  if (threadIdx.x == 0) sc->ticket = 0;
+}
+
+__global__ void __launch_bounds__(kThreads) k_arnoldi_orth32(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active || !S.a32) return;
+  const int j = sc->i, nd = j + 1;
+  __shared__ double sacc[(kMaxKdim + 1) * kWarps];
+  __shared__ float cf[kMaxKdim + 1];
+  for (int t = threadIdx.x; t < nd * kWarps; t += blockDim.x) sacc[t] = 0.0;
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = (float)sc->coef[t];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+    float wv[kRowsPerThread];
+#pragma unroll
+    for (int t = 0; t < kRowsPerThread; ++t) {
+      const long r = t0 + t * kThreads + threadIdx.x;
+      wv[t] = 0.0f;
+      if (r < S.n) {
+        float w = S.wf[r];
+        for (int kk = 0; kk < nd; ++kk) w = fmaf(-cf[kk], S.Vf[(long)kk * S.ldv + r], w);
+        S.wf[r] = w;
+        wv[t] = w;
+      }
+    }
+    for (int kk = 0; kk < nd; ++kk) {
+      float p = 0.0f;
+#pragma unroll
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) p = fmaf(S.Vf[(long)kk * S.ldv + r], wv[t], p);
+      }
+      p = warp_sum_f(p);
+      if (lane == 0) sacc[kk * kWarps + warp] += (double)p;
+    }
+  }
+  if (!block_partials_and_last(sacc, nd, S.part, &sc->ticket)) return;
+  __shared__ double tot[kMaxKdim + 1];
+  reduce_partials(S.part, gridDim.x, nd, tot);
+  __syncthreads();
+  for (int kk = threadIdx.x; kk < nd; kk += blockDim.x) {
+    const double h2 = tot[kk] / sc->nu[kk];
+    sc->coef[kk] = h2 / sc->nu[kk];
+    sc->H[kk * kMaxKdim + j] = sc->h1[kk] + h2;
+  }
+  if (threadIdx.x == 0) sc->ticket = 0;
+}
+
+__global__ void __launch_bounds__(kThreads) k_arnoldi_next32(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active || !S.a32) return;
+  const int j = sc->i, nd = j + 1;
+  __shared__ float cf[kMaxKdim + 1];
+  __shared__ double sacc[kWarps];
+  for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = (float)sc->coef[t];
+  if (threadIdx.x < kWarps) sacc[threadIdx.x] = 0.0;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *vn = S.Vf + (long)nd * S.ldv;
+  const bool store = nd < sc->kdim;
+  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+    double p = 0.0;
+#pragma unroll
+    for (int t = 0; t < kRowsPerThread; ++t) {
+      const long r = t0 + t * kThreads + threadIdx.x;
+      if (r < S.n) {
+        float w = S.wf[r];
+        for (int kk = 0; kk < nd; ++kk) w = fmaf(-cf[kk], S.Vf[(long)kk * S.ldv + r], w);
+        if (store) vn[r] = w;
+        p = fma((double)w, (double)w, p);
+      }
+    }
+    p = warp_sum(p);
+    if (lane == 0) sacc[warp] += p;
+  }
+  if (!block_partials_and_last(sacc, 1, S.part, &sc->ticket)) return;
+  __shared__ double tot[1];
+  reduce_partials(S.part, gridDim.x, 1, tot);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sc->ticket = 0;
+    arnoldi_finalize(sc, j, sqrt(tot[0]));
   }
 }
 
@@ -374,9 +531,10 @@ __global__ void __launch_bounds__(kThreads) k_jacobi32_first(KSys *sys, int to_z
   const int j = sc->i;
   const double inv_nu = 1.0 / sc->nu[j];
   const double *vj = S.V + (long)j * S.ldv;
+  const float *vjf = S.Vf + (long)j * S.ldv;
   float *out = to_z ? S.Z + (long)j * S.ldv : S.zf;
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x)
-    out[r] = (float)(vj[r] * inv_nu) * S.invdf[r];
+    out[r] = (float)((S.a32 ? (double)vjf[r] : vj[r]) * inv_nu) * S.invdf[r];
 }
 
 __global__ void __launch_bounds__(kThreads) k_jacobi32_sweep(KSys *sys, int src_is_zf, int to_z) {
@@ -386,13 +544,14 @@ __global__ void __launch_bounds__(kThreads) k_jacobi32_sweep(KSys *sys, int src_
   const int j = sc->i;
   const double inv_nu = 1.0 / sc->nu[j];
   const double *vj = S.V + (long)j * S.ldv;
+  const float *vjf = S.Vf + (long)j * S.ldv;
   const float *src = src_is_zf ? S.zf : S.zf2;
   float *dst = to_z ? S.Z + (long)j * S.ldv : (src_is_zf ? S.zf2 : S.zf);
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
     int i, jj, k;
     row_ijk((int)r, S.nx, S.ny, i, jj, k);
     const float az = stencil7_row_f(S.Af, S.n, src, (int)r, i, jj, k, S.nx, S.ny, S.nz);
-    const float v = (float)(vj[r] * inv_nu);
+    const float v = (float)((S.a32 ? (double)vjf[r] : vj[r]) * inv_nu);
     dst[r] = fmaf(S.invdf[r], v - az, src[r]);
   }
 }
@@ -448,8 +607,16 @@ void Krylov::configure(int nsys_, const KSysHost *hs) {
     const KSysHost &h = hs[s];
     Slot &sl = slot[s];
     sl.host = h;
-    sl.V.alloc((size_t)(h.kdim + 1) * h.n);
-    sl.w.alloc(h.n);
+    if (h.a32 && h.pc != 2) throw Error(IBM_ERR_ARG, "Krylov: FP32 cycles need the flexible form");
+    if (h.a32) {
+      sl.V.release(); sl.w.release();
+      sl.Vf.alloc((size_t)(h.kdim + 1) * h.n);
+      sl.wf.alloc(h.n);
+    } else {
+      sl.Vf.release(); sl.wf.release();
+      sl.V.alloc((size_t)(h.kdim + 1) * h.n);
+      sl.w.alloc(h.n);
+    }
     sl.r.alloc(h.n);
     if (h.pc == 1) { sl.z.alloc(h.n); sl.z2.alloc(h.n); }
     if (h.pc == 2) {
@@ -491,6 +658,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     k.Z = slot[s].Z.p;
     k.w = slot[s].w.p; k.r = slot[s].r.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;
     k.zf = slot[s].zf.p; k.zf2 = slot[s].zf2.p;
+    k.Vf = slot[s].Vf.p; k.wf = slot[s].wf.p; k.a32 = h.a32;
     k.x = x[s]; k.b = b[s];
     k.part = slot[s].part.p;
     k.nblk = nblk;
@@ -505,6 +673,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     init[s].kdim = slot[s].host.kdim;
     init[s].maxit = slot[s].host.maxit;
     init[s].tol = slot[s].host.tol;
+    init[s].cyc_rtol = slot[s].host.a32 ? slot[s].host.cycle_rtol : 0.0;
   }
   IBM_CUDA_TRY(cudaMemcpyAsync(scal.p, init, sizeof(KScal) * nsys, cudaMemcpyHostToDevice, st));
   IBM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -574,23 +743,33 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
       pc.apply(pc.ctx, st, s, in, out, &scal.p[s].active);
     } else if (h.pc == 2 && h.pc_cb) {
       VecRef in;
-      in.base = slot[s].V.p; in.ld = h.n; in.idx = &scal.p[s].i; in.nu = scal.p[s].nu;
+      if (h.a32) in.basef = slot[s].Vf.p;
+      else in.base = slot[s].V.p;
+      in.ld = h.n; in.idx = &scal.p[s].i; in.nu = scal.p[s].nu;
       OutRef out;
       out.f = slot[s].Z.p; out.ld = h.n; out.idx = &scal.p[s].i;
       pc.apply(pc.ctx, st, s, in, out, &scal.p[s].active);
     }
   }
   int inner_sweeps = 0;
-  double r32 = 0.0, bsp = 0.0, bor = 0.0;
+  bool any64 = false, any32 = false;
+  double r32 = 0.0, bsp = 0.0, bor = 0.0, bsp32 = 0.0, bor32 = 0.0;
   for (int s = 0; s < nsys; ++s) {
     if (!((mask >> s) & 1u)) continue;
+    const bool a32 = slot[s].host.a32 != 0;
+    (a32 ? any32 : any64) = true;
     if (slot[s].host.pc == 2 && !slot[s].host.pc_cb && (!fl || fl[s].active))
       inner_sweeps = std::max(inner_sweeps, std::max(1, slot[s].host.inner_sweeps));
     if (!fl || !fl[s].active) continue;
     const double j1 = fl[s].i + 1.0;
-    if (slot[s].host.pc == 2 && !slot[s].host.pc_cb) r32 += rows(s);
-    bsp += rows(s) * ((slot[s].host.pc == 2 ? 68.0 : 72.0) + 8.0 * j1);
-    bor += rows(s) * (16.0 + 8.0 * j1);
+    if (slot[s].host.pc == 2 && !slot[s].host.pc_cb) r32 += rows(s) * (a32 ? 0.75 : 1.0);
+    if (a32) {
+      bsp32 += rows(s) * (36.0 + 4.0 * j1);
+      bor32 += rows(s) * (8.0 + 4.0 * j1);
+    } else {
+      bsp += rows(s) * ((slot[s].host.pc == 2 ? 68.0 : 72.0) + 8.0 * j1);
+      bor += rows(s) * (16.0 + 8.0 * j1);
+    }
   }
   if (inner_sweeps > 0) {
     if (inner_sweeps == 1) {
@@ -609,16 +788,30 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
       }
     }
   }
-  {
-    LaunchScope ls(K_GM_SPMV, st, bsp);
-    k_arnoldi_spmv<<<grid, kThreads, 0, st>>>(dev);
+  if (any64) {
+    {
+      LaunchScope ls(K_GM_SPMV, st, bsp);
+      k_arnoldi_spmv<<<grid, kThreads, 0, st>>>(dev);
+    }
+    {
+      LaunchScope ls(K_GM_ORTH, st, bor);
+      k_arnoldi_orth<<<grid, kThreads, 0, st>>>(dev);
+    }
+    LaunchScope ls(K_GM_NEXT, st, bor);
+    k_arnoldi_next<<<grid, kThreads, 0, st>>>(dev);
   }
-  {
-    LaunchScope ls(K_GM_ORTH, st, bor);
-    k_arnoldi_orth<<<grid, kThreads, 0, st>>>(dev);
+  if (any32) {
+    {
+      LaunchScope ls(K_GM_SPMV, st, bsp32);
+      k_arnoldi_spmv32<<<grid, kThreads, 0, st>>>(dev);
+    }
+    {
+      LaunchScope ls(K_GM_ORTH, st, bor32);
+      k_arnoldi_orth32<<<grid, kThreads, 0, st>>>(dev);
+    }
+    LaunchScope ls(K_GM_NEXT, st, bor32);
+    k_arnoldi_next32<<<grid, kThreads, 0, st>>>(dev);
   }
-  LaunchScope ls(K_GM_NEXT, st, bor);
-  k_arnoldi_next<<<grid, kThreads, 0, st>>>(dev);
 }
 
 void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, const Precond &pc,

@@ -8,6 +8,7 @@ namespace ibm {
 // optionally scaled by 1 / nu[*idx] (the unnormalised Krylov basis).
 struct VecRef {
   const double *base = nullptr;
+  const float *basef = nullptr;  // FP32 source (used instead of base when set)
   long ld = 0;
   const int *idx = nullptr;
   const double *nu = nullptr;
@@ -36,6 +37,11 @@ struct KSysHost {
   int inner_sweeps = 1;
   int kdim = 50, maxit = 250;
   double tol = 1e-8;
+  // pc 2 only: Arnoldi cycles in FP32 (FP32 basis, FP32 operator and dot
+  // products per thread, FP64 scalars); each cycle stops once its estimate
+  // fell by cycle_rtol and the restart recomputes the true residual in FP64.
+  int a32 = 0;
+  double cycle_rtol = 0.0;
 };
 
 struct KResult {
@@ -70,7 +76,7 @@ class Krylov {
   struct Slot {
     KSysHost host;
     DBuf<double> V, w, r, z, z2, part;
-    DBuf<float> Z, zf, zf2;
+    DBuf<float> Z, zf, zf2, Vf, wf;
   };
   void read_flags(cudaStream_t st);
   // Launch sequences shared by the host-driven and the graph form. With

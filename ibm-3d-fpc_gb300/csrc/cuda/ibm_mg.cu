@@ -238,8 +238,10 @@ __global__ void k_load_input(T *bv, long n, VecRef in, const double *winv, const
   const long off = in.idx ? (long)(*in.idx) * in.ld : 0;
   const double sc = in.nu ? 1.0 / in.nu[in.idx ? *in.idx : 0] : 1.0;
   const double *src = in.base + off;
+  const float *srcf = in.basef ? in.basef + off : nullptr;
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
-    double v = in.nu ? src[r] * sc : src[r];
+    const double a = srcf ? (double)srcf[r] : src[r];
+    double v = in.nu ? a * sc : a;
     if (winv) v = v * winv[r];
     bv[r] = (T)v;
   }

@@ -76,9 +76,13 @@ typedef struct ibm_solver_params {
   int mg_coarse_max;     /* coarsen until a level has at most this many points (dense solve there) */
   int mg_max_levels;
   int use_zero_initial_guess; /* -use-zero-initial-guess (momentum) */
-  int precision;         /* 0: FP64 throughout; 1: FP32 preconditioners inside FP64 flexible GMRES */
+  int precision;         /* 0: FP64 throughout; 1: FP32 preconditioners inside FP64 flexible GMRES;
+                            2: as 1 with the Arnoldi cycles in FP32 (FP32 basis and operator copy,
+                            FP64 scalars), each cycle stopping after a 1e-5 reduction and the
+                            FP64 restart measuring the true residual (mixed-precision iterative
+                            refinement): same FP64 tolerance, far fewer FP64 operations */
   int use_graph;         /* 1: replay the step as a CUDA graph */
-  int vel_inner_sweeps;  /* precision 1: FP32 Jacobi sweeps per momentum preconditioner application */
+  int vel_inner_sweeps;  /* precision 1, 2: FP32 Jacobi sweeps per momentum preconditioner application */
   double mg_group_ratio; /* between relaxed levels, coarsen every direction whose spacing is within
                             this factor of the smallest (0: one direction per relaxed level) */
   int mg_options;        /* bit 0: points with no coupling along the coarsening direction
@@ -162,7 +166,7 @@ int ibm_apply_operator(ibm_ctx *ctx, int field, const double *x, double *y);
 
 /* z = M r: one application of the field's preconditioner from a zero guess,
  * as the solver applies it (HYPRE_StructPFMGSolve / HYPRE_StructJacobiSolve
- * with maxit 1, main.cu:182, 212-218). precision 1 applies the FP32 form. */
+ * with maxit 1, main.cu:182, 212-218). precision 1 or 2 applies the FP32 form. */
 int ibm_apply_preconditioner(ibm_ctx *ctx, int field, const double *r, double *z);
 
 /* The last right-hand side (which = 0) or solution (which = 1) of a field's

@@ -136,7 +136,7 @@ def test_multigrid_vcycle_matches_oracle(ibm, pyoracle, case48, rap, relax, grou
     assert rel_err(s32.apply_preconditioner(ibm.FIELD_P, r), zo) <= 1e-4
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_graph_step_matches_stream_step(ibm, case48, precision):
     """The captured step (one graph launch, GMRES loops on the device) gives
     the same fields and iteration counts as the host-driven step."""
@@ -177,19 +177,38 @@ def test_benchmark_channel_160x32x32(ibm, pyoracle):
         assert rel_err(a, b) <= REL_TOL, name
 
 
-def test_mixed_precision_error(ibm, pyoracle, case48):
-    """FP32 preconditioners inside FP64 flexible GMRES at 1e-8: velocity
-    within 1e-6 of the FP64 oracle."""
-    s = ibm.Solver(case48, ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, precision=1))
+@pytest.mark.parametrize("precision", [1, 2])
+def test_mixed_precision_error(ibm, pyoracle, case48, precision):
+    """FP32 preconditioners inside FP64 flexible GMRES (precision 1), and FP32
+    Arnoldi cycles with FP64 restarts (precision 2), at 1e-8: velocity within
+    1e-6 of the FP64 oracle."""
+    s = ibm.Solver(case48, ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, precision=precision))
     orc = pyoracle.Oracle(case48, vel_tol=1e-13, p_tol=1e-13)
     for step in range(1, 11):
         st = s.step(min(1.0, step / 5.0))
         orc.step(min(1.0, step / 5.0))
         assert st.status == ibm.IBM_OK
+        assert st.p.rel_res <= 1e-8 and st.u.rel_res <= 1e-8  # true FP64 residuals
     gu, gv, gw, gp = s.fields()
     ou, ov, ow, op = orc.fields()
     vel_err = max(np.abs(gu - ou).max(), np.abs(gv - ov).max(), np.abs(gw - ow).max()) / np.abs(ou).max()
     assert vel_err <= 1e-6
+
+
+def test_fp32_cycles_reach_tight_tolerance(ibm, pyoracle, case48):
+    """precision 2 restarts its FP32 cycles from FP64 true residuals, so it
+    reaches tolerances far below FP32 resolution: 1e-12 on every solve."""
+    s = ibm.Solver(case48, ibm.solver_params(vel_tol=1e-12, p_tol=1e-12, precision=2, vel_maxit=500,
+                                             p_maxit=500))
+    orc = pyoracle.Oracle(case48, vel_tol=1e-13, p_tol=1e-13)
+    for step in range(1, 4):
+        st = s.step(min(1.0, step / 2.0))
+        orc.step(min(1.0, step / 2.0))
+        assert st.status == ibm.IBM_OK
+        for f in "uvwp":
+            assert getattr(st, f).rel_res <= 1e-12, f
+    for a, b, name in zip(s.fields(), orc.fields(), "uvwp"):
+        assert rel_err(a, b) <= 1e-9, name
 
 
 def test_not_converged_is_a_warning(ibm, case32):
