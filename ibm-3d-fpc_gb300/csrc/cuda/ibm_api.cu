@@ -514,6 +514,25 @@ int ibm_set_masks(ibm_ctx *c, const uint8_t *active_u, const uint8_t *active_v, 
           const long f = ((long)k * ny + j) * nx + i;
           if (!aw[f - (long)nx * ny]) zw.push_back((int)f);
         }
+    // faces the BC cleanup writes: the diagnostics recompute q there
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j) {
+        fu[((long)k * ny + j) * (nx + 1)] |= kBcSet;
+        fu[((long)k * ny + j) * (nx + 1) + nx] |= kBcSet;
+      }
+    for (int k = 0; k < nz; ++k)
+      for (int i = 0; i < nx; ++i) {
+        fv[((long)k * (ny + 1)) * nx + i] |= kBcSet;
+        fv[((long)k * (ny + 1) + ny) * nx + i] |= kBcSet;
+      }
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        fw[(long)j * nx + i] |= kBcSet;
+        fw[((long)nz * ny + j) * nx + i] |= kBcSet;
+      }
+    for (int f : zu) fu[f] |= kBcSet;
+    for (int f : zv) fv[f] |= kBcSet;
+    for (int f : zw) fw[f] |= kBcSet;
     upload(c->fu, fu, c->st); upload(c->fv, fv, c->st); upload(c->fw, fw, c->st); upload(c->fc, fc, c->st);
     upload(c->zl_u, zu, c->st); upload(c->zl_v, zv, c->st); upload(c->zl_w, zw, c->st);
     c->masks_set = true;

@@ -10,6 +10,7 @@ namespace ibm {
 constexpr uint8_t kActive = 1;   // active_{u,v,w} at the face itself
 constexpr uint8_t kQFace = 2;    // id_q > 0: part of the projection vector q
 constexpr uint8_t kRhsRow = 4;   // id > 0 && active: a solved (non-identity) momentum row
+constexpr uint8_t kBcSet = 8;    // the BC cleanup overwrites this face (boundary plane or zero list)
 // Cell flag bit.
 constexpr uint8_t kFluid = 1;    // fluid_p && id_p > 0
 

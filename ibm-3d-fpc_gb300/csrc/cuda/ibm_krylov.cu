@@ -383,6 +383,8 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
 // sums are FP32, sums across threads and blocks and every scalar are FP64.
 // A cycle stops once its estimate fell by cyc_rtol; the restart computes the
 // true residual in FP64, so the solve still meets the FP64 tolerance.
+constexpr int kChunk32 = 8;  // basis vectors whose dot products a thread keeps in registers
+
 __device__ __forceinline__ float warp_sum_f(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -399,6 +401,34 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float *zj = S.Z + (long)j * S.ldv;
+  if (nd <= kChunk32) {
+    // short basis: every dot product of the thread stays in a register
+    // across the whole sweep, one warp reduction per dot at the end
+    float acc[kChunk32];
+#pragma unroll
+    for (int kk = 0; kk < kChunk32; ++kk) acc[kk] = 0.0f;
+    for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+#pragma unroll
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) {
+          int i, jj, k;
+          row_ijk((int)r, S.nx, S.ny, i, jj, k);
+          const float w = stencil7_row_f(S.Af, S.n, zj, (int)r, i, jj, k, S.nx, S.ny, S.nz);
+          S.wf[r] = w;
+#pragma unroll
+          for (int kk = 0; kk < kChunk32; ++kk)
+            if (kk < nd) acc[kk] = fmaf(S.Vf[(long)kk * S.ldv + r], w, acc[kk]);
+        }
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < kChunk32; ++kk) {
+      if (kk >= nd) break;
+      const float p = warp_sum_f(acc[kk]);
+      if (lane == 0) sacc[kk * kWarps + warp] = (double)p;
+    }
+  } else
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
     float wv[kRowsPerThread];
 #pragma unroll
@@ -448,6 +478,36 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_orth32(KSys *sys) {
   for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = (float)sc->coef[t];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (nd <= kChunk32) {
+    // short basis: each basis value is loaded once for the update and the dots
+    float acc[kChunk32];
+#pragma unroll
+    for (int kk = 0; kk < kChunk32; ++kk) acc[kk] = 0.0f;
+    for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+#pragma unroll
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) {
+          float v[kChunk32];
+#pragma unroll
+          for (int kk = 0; kk < kChunk32; ++kk) v[kk] = kk < nd ? S.Vf[(long)kk * S.ldv + r] : 0.0f;
+          float w = S.wf[r];
+#pragma unroll
+          for (int kk = 0; kk < kChunk32; ++kk)
+            if (kk < nd) w = fmaf(-cf[kk], v[kk], w);
+          S.wf[r] = w;
+#pragma unroll
+          for (int kk = 0; kk < kChunk32; ++kk) acc[kk] = fmaf(v[kk], w, acc[kk]);
+        }
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < kChunk32; ++kk) {
+      if (kk >= nd) break;
+      const float p = warp_sum_f(acc[kk]);
+      if (lane == 0) sacc[kk * kWarps + warp] = (double)p;
+    }
+  } else
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
     float wv[kRowsPerThread];
 #pragma unroll
@@ -497,21 +557,30 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next32(KSys *sys) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float *vn = S.Vf + (long)nd * S.ldv;
   const bool store = nd < sc->kdim;
+  double pt = 0.0;
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
-    double p = 0.0;
 #pragma unroll
     for (int t = 0; t < kRowsPerThread; ++t) {
       const long r = t0 + t * kThreads + threadIdx.x;
       if (r < S.n) {
         float w = S.wf[r];
-        for (int kk = 0; kk < nd; ++kk) w = fmaf(-cf[kk], S.Vf[(long)kk * S.ldv + r], w);
+        if (nd <= kChunk32) {
+          float v[kChunk32];
+#pragma unroll
+          for (int kk = 0; kk < kChunk32; ++kk) v[kk] = kk < nd ? S.Vf[(long)kk * S.ldv + r] : 0.0f;
+#pragma unroll
+          for (int kk = 0; kk < kChunk32; ++kk)
+            if (kk < nd) w = fmaf(-cf[kk], v[kk], w);
+        } else {
+          for (int kk = 0; kk < nd; ++kk) w = fmaf(-cf[kk], S.Vf[(long)kk * S.ldv + r], w);
+        }
         if (store) vn[r] = w;
-        p = fma((double)w, (double)w, p);
+        pt = fma((double)w, (double)w, pt);
       }
     }
-    p = warp_sum(p);
-    if (lane == 0) sacc[warp] += p;
   }
+  pt = warp_sum(pt);
+  if (lane == 0) sacc[warp] = pt;
   if (!block_partials_and_last(sacc, 1, S.part, &sc->ticket)) return;
   __shared__ double tot[1];
   reduce_partials(S.part, gridDim.x, 1, tot);

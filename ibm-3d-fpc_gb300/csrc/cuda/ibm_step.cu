@@ -36,12 +36,31 @@ __device__ __forceinline__ double ld_w(const double *w, const Dims &d, int i, in
   return (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k > d.nz) ? fb : w[W3(d, i, j, k)];
 }
 
+// x / b correctly rounded for a divisor known in advance, without a division:
+// rb = RN(1/b) is computed once on the host, q0 = RN(x rb) is within an ulp of
+// x / b, and one correction with the exact remainder r = x - b q0 (a single
+// FMA) gives RN(x / b) (Markstein, IBM J. Res. Dev. 34(1), 1990; the final
+// step of the IA-64 division sequences). A zero remainder keeps q0, which
+// also keeps the sign of a zero quotient; a non-finite q0 is returned as is.
+// Equal to IEEE division whenever x / b and x rb are normal numbers. A
+// division by the grid spacing this way costs 3 FP64 operations instead of
+// the dozen or so of an IEEE division, and the convection kernel is bound by
+// the FP64 pipe on GB300.
+struct KnownDiv {
+  double b, rb;
+};
+__device__ __forceinline__ double div_known(double x, KnownDiv k) {
+  const double q0 = __dmul_rn(x, k.rb);
+  const double r = fma(-q0, k.b, x);
+  return (r == 0.0 || !isfinite(r)) ? q0 : fma(r, k.rb, q0);
+}
+
 // Centred advective term, separately rounded operations in the reference's order.
-__device__ __forceinline__ double advect(double c, double dm, double dp, double tdx, double a2, double em, double ep,
-                                         double tdy, double a3, double fm, double fp, double tdz) {
-  const double t1 = __ddiv_rn(__dmul_rn(c, __dsub_rn(dp, dm)), tdx);
-  const double t2 = __ddiv_rn(__dmul_rn(a2, __dsub_rn(ep, em)), tdy);
-  const double t3 = __ddiv_rn(__dmul_rn(a3, __dsub_rn(fp, fm)), tdz);
+__device__ __forceinline__ double advect(double c, double dm, double dp, KnownDiv tdx, double a2, double em, double ep,
+                                         KnownDiv tdy, double a3, double fm, double fp, KnownDiv tdz) {
+  const double t1 = div_known(__dmul_rn(c, __dsub_rn(dp, dm)), tdx);
+  const double t2 = div_known(__dmul_rn(a2, __dsub_rn(ep, em)), tdy);
+  const double t3 = div_known(__dmul_rn(a3, __dsub_rn(fp, fm)), tdz);
   return __dadd_rn(__dadd_rn(t1, t2), t3);
 }
 __device__ __forceinline__ double avg4(double a, double b, double c, double d) {
@@ -98,7 +117,8 @@ struct RhsArgs {
   const double *sc[3], *bc[3];
   double *b[3], *x0[3];
   long nb[3];
-  double a, rho, tdx, tdy, tdz;
+  double a, rho;
+  KnownDiv tdx, tdy, tdz;  // 2 dx, 2 dy, 2 dz
   int zero_guess;
 };
 
@@ -370,20 +390,60 @@ struct DiagArgs {
   int np_active;
 };
 
-// Corrected q value of a face (recomputed: the stored field has had the BC applied).
-__device__ __forceinline__ double q_face(const DiagArgs &A, const double *qt, const uint8_t *fl, const double *G,
-                                         long NF, long f, double pl, double pr) {
-  if (!(fl[f] & kQFace)) return 0.0;
+// Corrected q value of a face: the projected field holds it (k_project
+// writes exactly this value), except on the faces the BC cleanup rewrote
+// afterwards, where it is recomputed the same way.
+__device__ __forceinline__ double q_face(const DiagArgs &A, const double *qt, const double *qn, const uint8_t *fl,
+                                         const double *G, long NF, long f, double pl, double pr) {
+  const uint8_t m = fl[f];
+  if (!(m & kQFace)) return 0.0;
+  if (!(m & kBcSet)) return qn[f];
   return fma(-A.factor, grad_face(G[f], pl, G[NF + f], pr), qt[f]);
 }
 
-__global__ void __launch_bounds__(kThreads) k_diagnostics(DiagArgs A) {
+// |x| as an ordered integer key: for non-NaN doubles the bit pattern without
+// its sign orders like the magnitude, so the maxima run on the integer pipe
+// (the FP64 pipe is the scarce one). NaN counts as 0, as fmax would ignore it.
+__device__ __forceinline__ unsigned long long mag_key(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+  return b > 0x7FF0000000000000ull ? 0ull : b;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
+// The six corrected values of a cell next to a face the BC rewrote (rare:
+// kept out of line so the common path keeps few registers).
+__device__ __noinline__ void boundary_q(const DiagArgs &A, long c, int i, int j, int k, double &qw, double &qe,
+                                        double &qs, double &qn, double &qb, double &qt) {
+  const Dims &d = A.d;
+  const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
+             NW = (long)d.nx * d.ny * (d.nz + 1);
+  const long plane = (long)d.nx * d.ny;
+  auto ph = [&](long cc) { return (A.fc[cc] & kFluid) ? A.phi[cc] : 0.0; };
+  const double pc = ph(c);
+  const double pxm = i > 0 ? ph(c - 1) : 0.0, pxp = i < d.nx - 1 ? ph(c + 1) : 0.0;
+  const double pym = j > 0 ? ph(c - d.nx) : 0.0, pyp = j < d.ny - 1 ? ph(c + d.nx) : 0.0;
+  const double pzm = k > 0 ? ph(c - plane) : 0.0, pzp = k < d.nz - 1 ? ph(c + plane) : 0.0;
+  qw = q_face(A, A.ut, A.u, A.fu, A.Gu, NU, U3(d, i, j, k), pxm, pc);
+  qe = q_face(A, A.ut, A.u, A.fu, A.Gu, NU, U3(d, i + 1, j, k), pc, pxp);
+  qs = q_face(A, A.vt, A.v, A.fv, A.Gv, NV, V3(d, i, j, k), pym, pc);
+  qn = q_face(A, A.vt, A.v, A.fv, A.Gv, NV, V3(d, i, j + 1, k), pc, pyp);
+  qb = q_face(A, A.wt, A.w, A.fw, A.Gw, NW, W3(d, i, j, k), pzm, pc);
+  qt = q_face(A, A.wt, A.w, A.fw, A.Gw, NW, W3(d, i, j, k + 1), pc, pzp);
+}
+
+__global__ void __launch_bounds__(kThreads, 4) k_diagnostics(DiagArgs A) {
   const Dims &d = A.d;
   const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
              NW = (long)d.nx * d.ny * (d.nz + 1), NP = (long)d.nx * d.ny * d.nz;
-  const long plane = (long)d.nx * d.ny;
-  double div2 = 0.0, um = 0.0, vm = 0.0, wm = 0.0;
-  auto ph = [&](long c) { return (A.fc[c] & kFluid) ? A.phi[c] : 0.0; };
+  double div2 = 0.0;
+  unsigned long long um = 0, vm = 0, wm = 0;
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < NP + NU + NV + NW; t += (long)gridDim.x * blockDim.x) {
     if (t < NP) {
       const long c = t;
@@ -391,38 +451,54 @@ __global__ void __launch_bounds__(kThreads) k_diagnostics(DiagArgs A) {
       const int i = (int)(c % d.nx);
       const long q = c / d.nx;
       const int j = (int)(q % d.ny), k = (int)(q / d.ny);
-      const double pc = ph(c);
-      const double pxm = i > 0 ? ph(c - 1) : 0.0, pxp = i < d.nx - 1 ? ph(c + 1) : 0.0;
-      const double pym = j > 0 ? ph(c - d.nx) : 0.0, pyp = j < d.ny - 1 ? ph(c + d.nx) : 0.0;
-      const double pzm = k > 0 ? ph(c - plane) : 0.0, pzp = k < d.nz - 1 ? ph(c + plane) : 0.0;
-      const double s = div_cell(A.Dc, NP, c,
-                                q_face(A, A.ut, A.fu, A.Gu, NU, U3(d, i, j, k), pxm, pc),
-                                q_face(A, A.ut, A.fu, A.Gu, NU, U3(d, i + 1, j, k), pc, pxp),
-                                q_face(A, A.vt, A.fv, A.Gv, NV, V3(d, i, j, k), pym, pc),
-                                q_face(A, A.vt, A.fv, A.Gv, NV, V3(d, i, j + 1, k), pc, pyp),
-                                q_face(A, A.wt, A.fw, A.Gw, NW, W3(d, i, j, k), pzm, pc),
-                                q_face(A, A.wt, A.fw, A.Gw, NW, W3(d, i, j, k + 1), pc, pzp));
+      const long fw_ = U3(d, i, j, k), fe = U3(d, i + 1, j, k), fs = V3(d, i, j, k), fn = V3(d, i, j + 1, k),
+                 fb = W3(d, i, j, k), ft = W3(d, i, j, k + 1);
+      double qw, qe, qs, qn, qb, qt;
+      if (!((A.fu[fw_] | A.fu[fe] | A.fv[fs] | A.fv[fn] | A.fw[fb] | A.fw[ft]) & kBcSet)) {
+        // interior cell: the six corrected values are the projected field
+        qw = (A.fu[fw_] & kQFace) ? A.u[fw_] : 0.0;
+        qe = (A.fu[fe] & kQFace) ? A.u[fe] : 0.0;
+        qs = (A.fv[fs] & kQFace) ? A.v[fs] : 0.0;
+        qn = (A.fv[fn] & kQFace) ? A.v[fn] : 0.0;
+        qb = (A.fw[fb] & kQFace) ? A.w[fb] : 0.0;
+        qt = (A.fw[ft] & kQFace) ? A.w[ft] : 0.0;
+      } else {
+        boundary_q(A, c, i, j, k, qw, qe, qs, qn, qb, qt);
+      }
+      const double s = div_cell(A.Dc, NP, c, qw, qe, qs, qn, qb, qt);
       const double dv = __dadd_rn(s, __dmul_rn(*A.ramp, A.div_bc[c]));
       div2 = __dadd_rn(div2, __dmul_rn(dv, dv));
     } else if (t < NP + NU) {
-      um = fmax(um, fabs(A.u[t - NP]));
+      const unsigned long long m = mag_key(A.u[t - NP]);
+      um = m > um ? m : um;
     } else if (t < NP + NU + NV) {
-      vm = fmax(vm, fabs(A.v[t - NP - NU]));
+      const unsigned long long m = mag_key(A.v[t - NP - NU]);
+      vm = m > vm ? m : vm;
     } else {
-      wm = fmax(wm, fabs(A.w[t - NP - NU - NV]));
+      const unsigned long long m = mag_key(A.w[t - NP - NU - NV]);
+      wm = m > wm ? m : wm;
     }
   }
-  __shared__ double s[4][kWarps];
+  __shared__ double s_div[kWarps];
+  __shared__ unsigned long long s_max[3][kWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   div2 = warp_sum(div2);
-  um = warp_max(um); vm = warp_max(vm); wm = warp_max(wm);
-  if (lane == 0) { s[0][warp] = div2; s[1][warp] = um; s[2][warp] = vm; s[3][warp] = wm; }
+  um = warp_max_u64(um); vm = warp_max_u64(vm); wm = warp_max_u64(wm);
+  if (lane == 0) { s_div[warp] = div2; s_max[0][warp] = um; s_max[1][warp] = vm; s_max[2][warp] = wm; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0, c = 0.0, e = 0.0;
-    for (int q = 0; q < kWarps; ++q) { a += s[0][q]; b = fmax(b, s[1][q]); c = fmax(c, s[2][q]); e = fmax(e, s[3][q]); }
-    A.part[4 * blockIdx.x + 0] = a; A.part[4 * blockIdx.x + 1] = b;
-    A.part[4 * blockIdx.x + 2] = c; A.part[4 * blockIdx.x + 3] = e;
+    double a = 0.0;
+    unsigned long long b = 0, c = 0, e = 0;
+    for (int q = 0; q < kWarps; ++q) {
+      a += s_div[q];
+      b = s_max[0][q] > b ? s_max[0][q] : b;
+      c = s_max[1][q] > c ? s_max[1][q] : c;
+      e = s_max[2][q] > e ? s_max[2][q] : e;
+    }
+    A.part[4 * blockIdx.x + 0] = a;
+    A.part[4 * blockIdx.x + 1] = __longlong_as_double((long long)b);
+    A.part[4 * blockIdx.x + 2] = __longlong_as_double((long long)c);
+    A.part[4 * blockIdx.x + 3] = __longlong_as_double((long long)e);
   }
   __threadfence();
   __syncthreads();
@@ -481,7 +557,9 @@ void launch_momentum_rhs(ibm_ctx *c) {
   A.nb[0] = c->g.bu.n; A.nb[1] = c->g.bv.n; A.nb[2] = c->g.bw.n;
   A.a = c->g.rho / c->g.dt;
   A.rho = c->g.rho;
-  A.tdx = 2 * c->g.dx; A.tdy = 2 * c->g.dy; A.tdz = 2 * c->g.dz;
+  A.tdx = {2 * c->g.dx, 1.0 / (2 * c->g.dx)};
+  A.tdy = {2 * c->g.dy, 1.0 / (2 * c->g.dy)};
+  A.tdz = {2 * c->g.dz, 1.0 / (2 * c->g.dz)};
   A.zero_guess = c->prm.use_zero_initial_guess != 0;
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW), nbox = (double)(A.nb[0] + A.nb[1] + A.nb[2]);
   LaunchScope ls(K_RHS, c->st, 8.0 * faces + 9.0 * c->g.NP + nbox * (1 + 16 + 32));
