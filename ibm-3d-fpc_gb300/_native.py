@@ -51,7 +51,8 @@ class SolverParams(C.Structure):
                 ("mg_nu1", C.c_int), ("mg_nu2", C.c_int), ("mg_omega", C.c_double),
                 ("mg_coarse_max", C.c_int), ("mg_max_levels", C.c_int),
                 ("use_zero_initial_guess", C.c_int), ("precision", C.c_int), ("use_graph", C.c_int),
-                ("vel_inner_sweeps", C.c_int), ("mg_group_ratio", C.c_double), ("mg_options", C.c_int)]
+                ("vel_inner_sweeps", C.c_int), ("mg_group_ratio", C.c_double), ("mg_options", C.c_int),
+                ("mg_nu_coarse", C.c_int)]
 
 
 class SolveStats(C.Structure):

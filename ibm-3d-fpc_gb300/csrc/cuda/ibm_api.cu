@@ -236,6 +236,7 @@ void ensure_solvers(ibm_ctx *c) {
     mp.cycles = std::max(1, p.p_pc_maxit);
     mp.group_ratio = p.mg_group_ratio;
     mp.options = p.mg_options;
+    mp.nu_coarse = p.mg_nu_coarse;
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
     const double *winv = ((p.mg_options & 2) && c->p_sym) ? c->p_winv.p : nullptr;
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
@@ -348,6 +349,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->use_zero_initial_guess = 1; p->precision = 0; p->use_graph = 0; p->vel_inner_sweeps = 3;
   p->mg_group_ratio = 0.0;
   p->mg_options = 3;
+  p->mg_nu_coarse = 0;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -704,7 +706,7 @@ int ibm_set_solver_params(ibm_ctx *c, const ibm_solver_params *p) {
       throw Error(IBM_ERR_ARG, "bad tolerance or iteration limit");
     if (p->precision < 0 || p->precision > 2) throw Error(IBM_ERR_ARG, "precision must be 0, 1 or 2");
     if (p->p_pc != 0 && p->p_pc != 1) throw Error(IBM_ERR_ARG, "p_pc must be 0 or 1");
-    if (p->mg_nu1 < 0 || p->mg_nu2 < 0 || p->mg_coarse_max < 1 || p->mg_max_levels < 1)
+    if (p->mg_nu1 < 0 || p->mg_nu2 < 0 || p->mg_nu_coarse < 0 || p->mg_coarse_max < 1 || p->mg_max_levels < 1)
       throw Error(IBM_ERR_ARG, "bad multigrid parameters");
     // switching between the graph and the host-driven step keeps the solvers
     ibm_solver_params a = c->prm, b = *p;

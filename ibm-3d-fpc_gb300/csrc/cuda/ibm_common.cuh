@@ -80,10 +80,33 @@ struct DBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
+// Division by an invariant divisor d >= 1 through a multiply-high (Granlund
+// and Montgomery, "Division by invariant integers using multiplication",
+// PLDI 1994): with s = ceil(log2 d) and m = floor(2^32 (2^s - d) / d) + 1,
+// n / d = (mulhi(n, m) + n) >> s for every 32-bit n.
+struct FastDiv {
+  unsigned m = 1, s = 0;
+};
+inline FastDiv make_fastdiv(unsigned d) {
+  FastDiv f;
+  unsigned s = 0;
+  while ((1ull << s) < d) ++s;
+  f.s = s;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  return f;
+}
+
 struct Box {
   int nx = 0, ny = 0, nz = 0, n = 0;
+  FastDiv dx, dy;  // division by nx and by ny
 };
-inline Box make_box(int nx, int ny, int nz) { return Box{nx, ny, nz, nx * ny * nz}; }
+inline Box make_box(int nx, int ny, int nz) {
+  Box b;
+  b.nx = nx; b.ny = ny; b.nz = nz; b.n = nx * ny * nz;
+  b.dx = make_fastdiv((unsigned)(nx > 0 ? nx : 1));
+  b.dy = make_fastdiv((unsigned)(ny > 0 ? ny : 1));
+  return b;
+}
 
 // 7-point operator on a solve box: coefficient planes [7][n] (C,-x,+x,-y,+y,-z,+z).
 struct Op7 {
@@ -121,6 +144,7 @@ struct KScal {
 // Device view of one linear system for the Krylov kernels.
 struct KSys {
   int nx, ny, nz, n;
+  FastDiv fdx, fdy;     // division by nx and by ny
   const double *A;      // operator applied in the Arnoldi step ([7][n])
   const double *Ar;     // operator of the true residual ([7][n])
   const double *invd;   // inverse diagonal (Jacobi solution update)
@@ -162,6 +186,17 @@ __device__ __forceinline__ double warp_max(double v) {
 }
 
 // Flat row -> (i, j, k) on a box.
+__device__ __forceinline__ unsigned fast_div(unsigned n, FastDiv f) {
+  return (unsigned)(((unsigned long long)__umulhi(n, f.m) + n) >> f.s);
+}
+// Flat row -> (i, j, k) on a box without hardware-emulated divisions.
+__device__ __forceinline__ void box_ijk(long r, const Box &b, int &i, int &j, int &k) {
+  const unsigned q = fast_div((unsigned)r, b.dx);
+  i = (int)((unsigned)r - q * (unsigned)b.nx);
+  const unsigned kk = fast_div(q, b.dy);
+  j = (int)(q - kk * (unsigned)b.ny);
+  k = (int)kk;
+}
 __device__ __forceinline__ void row_ijk(int r, int nx, int ny, int &i, int &j, int &k) {
   const unsigned plane = (unsigned)nx * (unsigned)ny;
   k = (int)((unsigned)r / plane);

@@ -25,6 +25,15 @@ namespace {
 
 constexpr int kLd = kMaxKdim + 2;  // stride of block partials
 
+// Flat row -> (i, j, k) of a system's box (invariant-divisor division).
+__device__ __forceinline__ void sys_ijk(long r, const KSys &S, int &i, int &j, int &k) {
+  const unsigned q = fast_div((unsigned)r, S.fdx);
+  i = (int)((unsigned)r - q * (unsigned)S.nx);
+  const unsigned kk = fast_div(q, S.fdy);
+  j = (int)(q - kk * (unsigned)S.ny);
+  k = (int)kk;
+}
+
 // Sum block partials of `nd` dot products in block order; one warp per dot.
 __device__ void reduce_partials(const double *part, int nblk, int nd, double *out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -69,7 +78,7 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
       const long r = t0 + t * kThreads + threadIdx.x;
       if (r < S.n) {
         int i, j, k;
-        row_ijk((int)r, S.nx, S.ny, i, j, k);
+        sys_ijk(r, S, i, j, k);
         const double ax = stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
         const double bv = S.b[r];
         const double rv = bv - ax;
@@ -174,7 +183,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
       wv[t] = 0.0;
       if (r < S.n) {
         int i, jj, k;
-        row_ijk((int)r, S.nx, S.ny, i, jj, k);
+        sys_ijk(r, S, i, jj, k);
         double w;
         if (S.pc == 0) w = stencil7_row(S.A, S.n, vj, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
         else if (S.pc == 1) w = stencil7_row(S.A, S.n, S.z, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
@@ -343,7 +352,7 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
       const long r = t0 + t * kThreads + threadIdx.x;
       if (r < S.n) {
         int i, j, k;
-        row_ijk((int)r, S.nx, S.ny, i, j, k);
+        sys_ijk(r, S, i, j, k);
         const double rv = S.b[r] - stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
         S.r[r] = rv;
         if (S.a32) S.Vf[r] = (float)rv;
@@ -413,7 +422,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
         const long r = t0 + t * kThreads + threadIdx.x;
         if (r < S.n) {
           int i, jj, k;
-          row_ijk((int)r, S.nx, S.ny, i, jj, k);
+          sys_ijk(r, S, i, jj, k);
           const float w = stencil7_row_f(S.Af, S.n, zj, (int)r, i, jj, k, S.nx, S.ny, S.nz);
           S.wf[r] = w;
 #pragma unroll
@@ -437,7 +446,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
       wv[t] = 0.0f;
       if (r < S.n) {
         int i, jj, k;
-        row_ijk((int)r, S.nx, S.ny, i, jj, k);
+        sys_ijk(r, S, i, jj, k);
         const float w = stencil7_row_f(S.Af, S.n, zj, (int)r, i, jj, k, S.nx, S.ny, S.nz);
         S.wf[r] = w;
         wv[t] = w;
@@ -618,7 +627,7 @@ __global__ void __launch_bounds__(kThreads) k_jacobi32_sweep(KSys *sys, int src_
   float *dst = to_z ? S.Z + (long)j * S.ldv : (src_is_zf ? S.zf2 : S.zf);
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
     int i, jj, k;
-    row_ijk((int)r, S.nx, S.ny, i, jj, k);
+    sys_ijk(r, S, i, jj, k);
     const float az = stencil7_row_f(S.Af, S.n, src, (int)r, i, jj, k, S.nx, S.ny, S.nz);
     const float v = (float)((S.a32 ? (double)vjf[r] : vj[r]) * inv_nu);
     dst[r] = fmaf(S.invdf[r], v - az, src[r]);
@@ -722,6 +731,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     const KSysHost &h = slot[s].host;
     KSys &k = hsys[s];
     k.nx = h.nx; k.ny = h.ny; k.nz = h.nz; k.n = ((mask >> s) & 1u) ? h.n : 0;
+    k.fdx = make_fastdiv((unsigned)h.nx); k.fdy = make_fastdiv((unsigned)h.ny);
     k.A = h.A; k.Ar = h.Ar; k.invd = h.invd; k.Af = h.Af; k.invdf = h.invdf;
     k.V = slot[s].V.p; k.ldv = h.n;
     k.Z = slot[s].Z.p;

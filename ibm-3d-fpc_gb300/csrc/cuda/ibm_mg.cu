@@ -113,7 +113,7 @@ __global__ void k_interp_weights(const double *A, int ns, Box b, int d, const un
     double wm = 0.0, wp = 0.0;
     if (aware && coupled[r] && cm == 0.0 && cp == 0.0) {
       int idx[3];
-      row_ijk((int)r, b.nx, b.ny, idx[0], idx[1], idx[2]);
+      box_ijk(r, b, idx[0], idx[1], idx[2]);
       const int nd = d == 0 ? b.nx : d == 1 ? b.ny : b.nz;
       const int lo = idx[d] > 0 && coupled[r - stride];
       const int hi = idx[d] < nd - 1 && coupled[r + stride];
@@ -143,7 +143,7 @@ __global__ void k_rap(const double *Af, int ns, Box fb, const double *pm, const 
                       double *Ac) {
   for (long I = (long)blockIdx.x * blockDim.x + threadIdx.x; I < cb.n; I += (long)gridDim.x * blockDim.x) {
     int ci[3];
-    row_ijk((int)I, cb.nx, cb.ny, ci[0], ci[1], ci[2]);
+    box_ijk(I, cb, ci[0], ci[1], ci[2]);
     double ac[27];
 #pragma unroll
     for (int s = 0; s < 27; ++s) ac[s] = 0.0;
@@ -270,7 +270,7 @@ __global__ void k_relax_jacobi(const T *A, const T *wd, const T *b, const T *x, 
   if (gate_off(gate)) return;
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < bx.n; r += (long)gridDim.x * blockDim.x) {
     int i, j, k;
-    row_ijk((int)r, bx.nx, bx.ny, i, j, k);
+    box_ijk(r, bx, i, j, k);
     const T ax = apply_row<T, NS>(A, bx.n, x, (int)r, i, j, k, bx.nx, bx.ny, bx.nz);
     t[r] = fmat<T>(wd[r], b[r] - ax, x[r]);
   }
@@ -285,7 +285,7 @@ __global__ void k_relax_color(const T *A, const T *invd, const T *b, const T *x,
   if (gate_off(gate)) return;
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < bx.n; r += (long)gridDim.x * blockDim.x) {
     int i, j, k;
-    row_ijk((int)r, bx.nx, bx.ny, i, j, k);
+    box_ijk(r, bx, i, j, k);
     if (((i + j + k) & 1) != color) { t[r] = zero_x ? T(0) : x[r]; continue; }
     if (zero_x) { t[r] = invd[r] * b[r]; continue; }
     const T ax = apply_row<T, NS>(A, bx.n, x, (int)r, i, j, k, bx.nx, bx.ny, bx.nz);
@@ -298,14 +298,15 @@ __global__ void k_relax_color(const T *A, const T *invd, const T *b, const T *x,
 // pair index m numbers the points of either colour; planes [c][q][m] hold, for
 // the colour-c point of pair m, q = 0 the inverse diagonal and q = 1..6 the
 // couplings -x,+x,-y,+y,-z,+z. A colour phase streams only its own half.
-__device__ __forceinline__ long rb_row(long m, int color, int nx, int ny, int &i, int &j, int &k) {
-  const long q = 2 * m;
-  const long line = q / nx;
-  j = (int)(line % ny);
-  k = (int)(line / ny);
-  const long r = q + ((j + k + color) & 1);
-  i = (int)(r - line * nx);
-  return r;
+__device__ __forceinline__ long rb_row(long m, int color, const Box &b, int &i, int &j, int &k) {
+  const unsigned q = 2u * (unsigned)m;
+  const unsigned line = fast_div(q, b.dx);
+  const unsigned kk = fast_div(line, b.dy);
+  j = (int)(line - kk * (unsigned)b.ny);
+  k = (int)kk;
+  const unsigned r = q + ((j + k + color) & 1);
+  i = (int)(r - line * (unsigned)b.nx);
+  return (long)r;
 }
 
 template <class T>
@@ -315,7 +316,7 @@ __global__ void k_split_colors(const T *A, const T *invd, Box bx, T *R) {
     const int c = (int)(t / h);
     const long m = t - c * h;
     int i, j, k;
-    const long r = rb_row(m, c, bx.nx, bx.ny, i, j, k);
+    const long r = rb_row(m, c, bx, i, j, k);
     T *o = R + (long)c * 7 * h + m;
     o[0] = invd[r];
     for (int s = 1; s < 7; ++s) o[(long)s * h] = A[(long)s * bx.n + r];
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb(const T *__restrict__ R, 
   const T *__restrict__ P = R + (long)color * 7 * h;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
-    const long r = rb_row(m, color, nx, ny, i, j, k);
+    const long r = rb_row(m, color, bx, i, j, k);
     const T xw = i > 0 ? x[r - 1] : T(0);
     const T xe = i < nx - 1 ? x[r + 1] : T(0);
     const T xs = j > 0 ? x[r - sy] : T(0);
@@ -365,7 +366,7 @@ __global__ void k_split_colors27(const T *A, const T *invd, Box bx, T *R) {
     const int c = (int)(t / h);
     const long m = t - c * h;
     int i, j, k;
-    const long r = rb_row(m, c, bx.nx, bx.ny, i, j, k);
+    const long r = rb_row(m, c, bx, i, j, k);
     T *o = R + (long)c * 28 * h + m;
     for (int s = 0; s < 27; ++s) o[(long)s * h] = A[(long)s * bx.n + r];
     o[27L * h] = invd[r];
@@ -382,7 +383,7 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb27(const T *__restrict__ R
   const T *__restrict__ P = R + (long)color * 28 * h;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
-    const long r = rb_row(m, color, nx, ny, i, j, k);
+    const long r = rb_row(m, color, bx, i, j, k);
     if (zero_x) {
       t[r] = P[27 * h + m] * b[r];
       t[r ^ 1] = T(0);
@@ -408,7 +409,7 @@ __global__ void k_relax_rb_zero(const T *__restrict__ R, const T *__restrict__ b
   const long h = bx.n / 2;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
-    const long r = rb_row(m, 0, bx.nx, bx.ny, i, j, k);
+    const long r = rb_row(m, 0, bx, i, j, k);
     x[r] = R[m] * b[r];
     x[r ^ 1] = T(0);
   }
@@ -419,7 +420,7 @@ __global__ void k_residual(const T *A, const T *b, const T *x, T *res, Box bx, c
   if (gate_off(gate)) return;
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < bx.n; r += (long)gridDim.x * blockDim.x) {
     int i, j, k;
-    row_ijk((int)r, bx.nx, bx.ny, i, j, k);
+    box_ijk(r, bx, i, j, k);
     res[r] = b[r] - apply_row<T, NS>(A, bx.n, x, (int)r, i, j, k, bx.nx, bx.ny, bx.nz);
   }
 }
@@ -430,7 +431,7 @@ __global__ void k_restrict(const T *res, const T *pm, const T *pp, Box fb, int d
   const int fn[3] = {fb.nx, fb.ny, fb.nz};
   for (long I = (long)blockIdx.x * blockDim.x + threadIdx.x; I < cb.n; I += (long)gridDim.x * blockDim.x) {
     int ci[3];
-    row_ijk((int)I, cb.nx, cb.ny, ci[0], ci[1], ci[2]);
+    box_ijk(I, cb, ci[0], ci[1], ci[2]);
     T acc = T(0);
     for (int fo = -1; fo <= 1; ++fo) {
       int f[3] = {ci[0], ci[1], ci[2]};
@@ -451,7 +452,7 @@ __global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb,
   const int cn[3] = {cb.nx, cb.ny, cb.nz};
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < fb.n; r += (long)gridDim.x * blockDim.x) {
     int f[3];
-    row_ijk((int)r, fb.nx, fb.ny, f[0], f[1], f[2]);
+    box_ijk(r, fb, f[0], f[1], f[2]);
     T corr;
     if ((f[d] & 1) == 0) {
       int c[3] = {f[0], f[1], f[2]};
@@ -639,11 +640,8 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
       k_coupled<<<grid_for(n), kThreads, 0, st>>>(F.A, F.ns, n, coupled.p);
       k_interp_weights<<<grid_for(n), kThreads, 0, st>>>(F.A, F.ns, F.b, d, coupled.p, aware, F.pm.p, F.pp.p);
     }
-    Box cb = F.b;
-    if (d == 0) cb.nx = (F.b.nx + 1) / 2;
-    if (d == 1) cb.ny = (F.b.ny + 1) / 2;
-    if (d == 2) cb.nz = (F.b.nz + 1) / 2;
-    cb.n = cb.nx * cb.ny * cb.nz;
+    const Box cb = make_box(d == 0 ? (F.b.nx + 1) / 2 : F.b.nx, d == 1 ? (F.b.ny + 1) / 2 : F.b.ny,
+                            d == 2 ? (F.b.nz + 1) / 2 : F.b.nz);
     L.emplace_back();
     MgLevelT<double> &Fr = L[l];  // re-fetch after emplace
     MgLevelT<double> &C = L[l + 1];
@@ -768,7 +766,10 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   };
   // Inside a coarsening group (F.relax == 0) the level only passes the
   // right-hand side down and the correction up.
-  const int nu1 = F.relax ? p.nu1 : 0, nu2 = F.relax ? p.nu2 : 0;
+  // sweeps: the finest level takes nu1 / nu2, coarser relaxed levels nu_coarse
+  // each way when it is set
+  const int c1 = (l > 0 && p.nu_coarse > 0) ? p.nu_coarse : p.nu1, c2 = (l > 0 && p.nu_coarse > 0) ? p.nu_coarse : p.nu2;
+  const int nu1 = F.relax ? c1 : 0, nu2 = F.relax ? c2 : 0;
   for (int s = 0; s < nu1; ++s) relax(s == 0);
   const T *res = F.bv.p;  // residual of a zero initial guess is b
   if (nu1 > 0) {

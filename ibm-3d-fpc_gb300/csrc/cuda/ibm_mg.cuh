@@ -13,6 +13,7 @@ struct MgParams {
   int coarse_max = 64;
   int max_levels = 40;
   int cycles = 1;       // V-cycles per application
+  int nu_coarse = 0;    // sweeps each way on the coarser relaxed levels (0: nu1 / nu2)
   double group_ratio = 0.0;  // see ibm_solver_params.mg_group_ratio
   int options = 3;      // see ibm_solver_params.mg_options
 };

@@ -30,13 +30,13 @@ def main() -> int:
     ap.add_argument("ny", type=int)
     ap.add_argument("nz", type=int)
     ap.add_argument("--repeat", type=int, default=4)
-    ap.add_argument("--precision", type=int, default=1)
+    ap.add_argument("--precision", type=int, default=2)
     a = ap.parse_args()
     sys.path.insert(0, os.path.dirname(HERE))
     ibm = importlib.import_module(os.path.basename(HERE))
     case = ibm.Case(ibm.channel_params(a.nx, a.ny, a.nz, Um=2.25, dt=2e-4))
     prm = ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, vel_kdim=8, p_kdim=8, p_pc_rap_type=0, p_pc_relax_type=2,
-                            mg_nu1=2, mg_nu2=2, mg_omega=1.0, mg_group_ratio=1.5, mg_options=3,
+                            mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_omega=1.0, mg_group_ratio=1.5, mg_options=3,
                             precision=a.precision, use_graph=0)
     s = ibm.Solver(case, prm)
     if a.mode == "pc":

@@ -91,6 +91,7 @@ typedef struct ibm_solver_params {
                             bit 1: when Ap = W S with W diagonal and S symmetric (the cut-cell
                             divergence scales rows by 1 / open fraction), build the hierarchy on
                             S and apply it to W^-1 r. 0 = PFMG's plain rules. Default 3. */
+  int mg_nu_coarse;      /* sweeps each way on the relaxed levels below the finest (0: mg_nu1 / mg_nu2) */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {

@@ -684,7 +684,9 @@ static void mg_cycle(oracle *o, int l, const double *b, double *x) {
     }
     return;
   }
-  const int nu1 = L->relax ? o->prm.mg_nu1 : 0, nu2 = L->relax ? o->prm.mg_nu2 : 0;
+  const int c1 = (l > 0 && o->prm.mg_nu_coarse > 0) ? o->prm.mg_nu_coarse : o->prm.mg_nu1;
+  const int c2 = (l > 0 && o->prm.mg_nu_coarse > 0) ? o->prm.mg_nu_coarse : o->prm.mg_nu2;
+  const int nu1 = L->relax ? c1 : 0, nu2 = L->relax ? c2 : 0;
   for (int s = 0; s < nu1; ++s) mg_relax(o, L, b, x, s == 0);
   if (nu1 == 0) memset(x, 0, sizeof(double) * (size_t)N);
   double *ax = L->rv;

@@ -43,6 +43,7 @@ typedef struct oracle_params {
                           (plain operator-dependent weights give them 0);
                           bit 1: hierarchy of S = W^-1 Ap, where Ap = W S with W diagonal
                           and S symmetric (found from the couplings), applied to W^-1 r */
+  int mg_nu_coarse;    /* sweeps each way on relaxed levels below the finest (0: mg_nu1 / mg_nu2) */
 } oracle_params;
 
 typedef struct oracle_inputs {

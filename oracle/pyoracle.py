@@ -33,7 +33,8 @@ class OracleParams(C.Structure):
                 ("p_tol", C.c_double), ("p_maxit", C.c_int), ("p_kdim", C.c_int),
                 ("p_pc", C.c_int), ("mg_rap", C.c_int), ("mg_relax", C.c_int), ("mg_nu1", C.c_int),
                 ("mg_nu2", C.c_int), ("mg_omega", C.c_double), ("mg_coarse_max", C.c_int), ("mg_max_levels", C.c_int),
-                ("mg_group_ratio", C.c_double), ("mg_options", C.c_int)]
+                ("mg_group_ratio", C.c_double), ("mg_options", C.c_int),
+                ("mg_nu_coarse", C.c_int)]
 
 
 _IN_FIELDS = ["Au", "Av", "Aw", "Ap", "active_u", "active_v", "active_w", "fluid_p", "active_qu", "active_qv",
@@ -97,14 +98,15 @@ class Oracle:
 
     def __init__(self, case, *, vel_tol=1e-13, vel_maxit=500, vel_kdim=50, vel_jacobi_iters=1, p_tol=1e-13,
                  p_maxit=500, p_kdim=50, p_pc=1, mg_rap=1, mg_relax=1, mg_nu1=1, mg_nu2=1, mg_omega=2.0 / 3.0,
-                 mg_coarse_max=64, mg_max_levels=40, mg_group_ratio=0.0, mg_options=3, use_zero_initial_guess=1):
+                 mg_coarse_max=64, mg_max_levels=40, mg_group_ratio=0.0, mg_options=3, mg_nu_coarse=0,
+                 use_zero_initial_guess=1):
         self.L = lib()
         cp = case.params
         self.shape = (cp.nx, cp.ny, cp.nz)
         self.prm = OracleParams(cp.nx, cp.ny, cp.nz, cp.Lx, cp.Ly, cp.Lz, cp.rho, cp.nu, cp.dt,
                                 use_zero_initial_guess, vel_tol, vel_maxit, vel_kdim, vel_jacobi_iters, p_tol,
                                 p_maxit, p_kdim, p_pc, mg_rap, mg_relax, mg_nu1, mg_nu2, mg_omega, mg_coarse_max,
-                                mg_max_levels, mg_group_ratio, mg_options)
+                                mg_max_levels, mg_group_ratio, mg_options, mg_nu_coarse)
         names = {"Au": "Au_vals", "Av": "Av_vals", "Aw": "Aw_vals", "Ap": "Ap_vals"}
         self._keep = {n: np.ascontiguousarray(case.array(names.get(n, n))) for n in _IN_FIELDS}
         self.inp = OracleInputs(*[_p(self._keep[n]) for n in _IN_FIELDS])

@@ -118,16 +118,20 @@ def test_multistep_parity(ibm, pyoracle, case48, rap, relax):
         assert rel_err(a, b) <= REL_TOL, name
 
 
-@pytest.mark.parametrize("rap,relax,group,options", [(1, 1, 0.0, 3), (0, 1, 0.0, 3), (1, 2, 0.0, 3), (0, 2, 1.5, 3),
-                                                     (1, 2, 1.5, 3), (1, 2, 1.5, 0), (0, 2, 1.5, 1), (1, 1, 0.0, 2)])
-def test_multigrid_vcycle_matches_oracle(ibm, pyoracle, case48, rap, relax, group, options):
+@pytest.mark.parametrize("rap,relax,group,options,nu", [(1, 1, 0.0, 3, (1, 0)), (0, 1, 0.0, 3, (1, 0)),
+                                                        (1, 2, 0.0, 3, (1, 0)), (0, 2, 1.5, 3, (1, 0)),
+                                                        (1, 2, 1.5, 3, (1, 0)), (1, 2, 1.5, 0, (1, 0)),
+                                                        (0, 2, 1.5, 1, (1, 0)), (1, 1, 0.0, 2, (1, 0)),
+                                                        (0, 2, 1.5, 3, (3, 2)), (0, 2, 0.0, 3, (2, 1))])
+def test_multigrid_vcycle_matches_oracle(ibm, pyoracle, case48, rap, relax, group, options, nu):
     """One V-cycle of the device multigrid equals the oracle's (same levels,
     coarse operators, smoothers, relaxed and unrelaxed levels); FP64 to
     round-off, the FP32 hierarchy to single precision."""
     omega = 1.0 if relax == 2 else 2.0 / 3.0
-    kw = dict(p_pc_rap_type=rap, p_pc_relax_type=relax, mg_group_ratio=group, mg_omega=omega, mg_options=options)
+    kw = dict(p_pc_rap_type=rap, p_pc_relax_type=relax, mg_group_ratio=group, mg_omega=omega, mg_options=options,
+              mg_nu1=nu[0], mg_nu2=nu[0], mg_nu_coarse=nu[1])
     orc = pyoracle.Oracle(case48, mg_rap=rap, mg_relax=relax, mg_group_ratio=group, mg_omega=omega,
-                          mg_options=options)
+                          mg_options=options, mg_nu1=nu[0], mg_nu2=nu[0], mg_nu_coarse=nu[1])
     r = np.random.default_rng(11).standard_normal(orc.box_sizes()[3])
     zo = orc.mg_vcycle(r)
     s64 = ibm.Solver(case48, ibm.solver_params(**kw))
