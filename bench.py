@@ -94,7 +94,7 @@ def solver_params(ibm, precision, graph=0):
     return ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, vel_maxit=250, p_maxit=250, vel_kdim=50, p_kdim=50,
                              p_pc=1, p_pc_rap_type=0, p_pc_relax_type=2, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_omega=1.0,
                              mg_group_ratio=1.5, mg_coarse_max=64, mg_options=3, precision=precision,
-                             vel_inner_sweeps=3, use_graph=graph)
+                             vel_inner_sweeps=2, use_graph=graph)
 
 
 class ClockSampler:
@@ -390,7 +390,7 @@ def main():
                       "l2": "inputs larger than L2 (operators + fields + Krylov bases, tens of GB resident)",
                       "pressure_pc": "semicoarsening MG (grouped, symmetrized, cut-cell-aware interpolation), "
                                      "Galerkin 27-point coarse levels, two-colour sweeps 3+3 (finest) / 2+2 (coarser), FP32",
-                      "momentum_pc": "FP32 Jacobi sweeps"},
+                      "momentum_pc": "2 FP32 Jacobi sweeps"},
            "phase_ms": phase_means(step_stats), "iterations_mean": iters_mean(step_stats),
            "solve_gbs": solve_gbs, "kernel_ms_per_step": kernel_ms, "kernel_gbs": kernel_gbs,
            "gpu_launches": int(launches),

@@ -763,8 +763,9 @@ int ibm_step(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
     if (c->prm.use_graph) {
       // The whole step as one graph launch; the GMRES loops run on the device.
       if (!c->graph_ready || !c->graph_bound) {
-        c->kmom.bind(st, bm, xm, ~0u);
-        c->kp.bind(st, bp, xp, ~0u);
+        const bool zg = c->prm.use_zero_initial_guess != 0;
+        c->kmom.bind(st, bm, xm, ~0u, zg);
+        c->kp.bind(st, bp, xp, ~0u, zg);
         c->graph_bound = true;
       }
       if (!c->graph_ready) build_step_graph(c, none, mgp);
@@ -792,7 +793,7 @@ int ibm_step(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
       IBM_CUDA_TRY(cudaEventRecord(c->ev[1], st));
       {
         PhaseScope ph(PH_MOM);
-        c->kmom.solve(st, bm, xm, none, rm);
+        c->kmom.solve(st, bm, xm, none, rm, ~0u, c->prm.use_zero_initial_guess != 0);
       }
       IBM_CUDA_TRY(cudaEventRecord(c->ev[2], st));
       {
@@ -803,7 +804,7 @@ int ibm_step(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
       IBM_CUDA_TRY(cudaEventRecord(c->ev[5], st));
       {
         PhaseScope ph(PH_P);
-        c->kp.solve(st, bp, xp, mgp, rp);
+        c->kp.solve(st, bp, xp, mgp, rp, ~0u, c->prm.use_zero_initial_guess != 0);
       }
       IBM_CUDA_TRY(cudaEventRecord(c->ev[3], st));
       {
@@ -869,6 +870,7 @@ int ibm_solve(ibm_ctx *c, int field, const double *b, double *x, ibm_solve_stats
       mgp.ctx = c;
       mgp.apply = mg_apply_cb;
       c->kp.solve(c->st, bp, xp, mgp, r);
+      c->graph_bound = false;
     }
     IBM_CUDA_TRY(cudaMemcpyAsync(x, c->xb[field].p, sizeof(double) * n, cudaMemcpyDefault, c->st));
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));

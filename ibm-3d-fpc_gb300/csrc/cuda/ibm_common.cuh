@@ -159,6 +159,7 @@ struct KSys {
   double *part;         // block partial sums [nblk][kMaxKdim + 2]
   float *Vf, *wf;       // FP32 basis and work vector of the FP32 Arnoldi cycles (a32)
   int a32;              // Arnoldi cycles in FP32 (basis, operator, dots per thread), restarts in FP64
+  int x_zero;           // the initial guess is zero: the first residual is b
   int nblk;
   int pc;               // 0 Jacobi folded into A, 1 explicit z (multigrid), 2 flexible FP32 z
   int pc_cb;            // pc 2: preconditioner supplied by a callback (else FP32 Jacobi sweeps)

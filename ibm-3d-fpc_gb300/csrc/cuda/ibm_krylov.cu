@@ -79,7 +79,8 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
       if (r < S.n) {
         int i, j, k;
         sys_ijk(r, S, i, j, k);
-        const double ax = stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+        // with finite coefficients A 0 is +0 in every row, so b - 0 equals b - A x bit for bit
+        const double ax = S.x_zero ? 0.0 : stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
         const double bv = S.b[r];
         const double rv = bv - ax;
         S.r[r] = rv;
@@ -723,8 +724,9 @@ Krylov::~Krylov() {
   if (hflags) cudaFreeHost(hflags);
 }
 
-void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask) {
+void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask, bool x_zero) {
   bound_mask = mask;
+  bound_x_zero = x_zero;
   KSys hsys[kMaxSys];
   memset(hsys, 0, sizeof(hsys));
   for (int s = 0; s < nsys; ++s) {
@@ -738,6 +740,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     k.w = slot[s].w.p; k.r = slot[s].r.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;
     k.zf = slot[s].zf.p; k.zf2 = slot[s].zf2.p;
     k.Vf = slot[s].Vf.p; k.wf = slot[s].wf.p; k.a32 = h.a32;
+    k.x_zero = x_zero ? 1 : 0;
     k.x = x[s]; k.b = b[s];
     k.part = slot[s].part.p;
     k.nblk = nblk;
@@ -894,13 +897,13 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
 }
 
 void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, const Precond &pc,
-                   KResult *res, unsigned mask) {
-  bind(st, b, x, mask);
+                   KResult *res, unsigned mask, bool x_zero) {
+  bind(st, b, x, mask, x_zero);
   const dim3 grid(nblk, nsys);
   double all_rows = 0.0;
   for (int s = 0; s < nsys; ++s) all_rows += ((mask >> s) & 1u) ? (double)slot[s].host.n : 0.0;
   {
-    LaunchScope ls(K_GM_INIT, st, 88.0 * all_rows);
+    LaunchScope ls(K_GM_INIT, st, (x_zero ? 24.0 : 88.0) * all_rows);
     k_init<<<grid, kThreads, 0, st>>>(dsys.p, nsys);
   }
   for (long guard = 0;; ++guard) {

@@ -56,8 +56,9 @@ class Krylov {
   ~Krylov();
   void configure(int nsys, const KSysHost *systems);
   // mask: bit s set = solve system s (the others are skipped).
+  // x_zero: the caller guarantees x = 0 on entry (the first residual is b).
   void solve(cudaStream_t st, const double *const *b, double *const *x, const Precond &pc, KResult *res,
-             unsigned mask = ~0u);
+             unsigned mask = ~0u, bool x_zero = false);
   size_t bytes() const;
 
   // Graph form. bind() fixes the vectors (outside any capture); enqueue_graph()
@@ -68,7 +69,7 @@ class Krylov {
   // numbers of cycle-end / Arnoldi bodies run in loops[0] / loops[1].
   // Returns the launches recorded outside the loop and per body kind.
   struct GraphCounts { long long fixed = 0, end_body = 0, arnoldi_body = 0, loop = 0; };
-  void bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask);
+  void bind(cudaStream_t st, const double *const *b, double *const *x, unsigned mask, bool x_zero = false);
   GraphCounts enqueue_graph(cudaStream_t st, const cudaStream_t body_st[2], const Precond &pc, KFlags *host_flags,
                             unsigned long long *loops);
 
@@ -85,6 +86,7 @@ class Krylov {
   void launch_cycle_end(cudaStream_t st, const Precond &pc, const KFlags *flags, unsigned mask);
   void launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *flags, unsigned mask);
   unsigned bound_mask = ~0u;
+  bool bound_x_zero = false;
   int nsys = 0;
   int nblk = 0;
   Slot slot[kMaxSys];
