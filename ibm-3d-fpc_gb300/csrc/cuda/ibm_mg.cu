@@ -317,9 +317,10 @@ __global__ void k_split_colors(const T *A, const T *invd, Box bx, T *R) {
     const long m = t - c * h;
     int i, j, k;
     const long r = rb_row(m, c, bx, i, j, k);
-    T *o = R + (long)c * 7 * h + m;
+    T *o = R + (long)c * 8 * h + m;
     o[0] = invd[r];
     for (int s = 1; s < 7; ++s) o[(long)s * h] = A[(long)s * bx.n + r];
+    o[7L * h] = A[r];
   }
 }
 
@@ -333,7 +334,7 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb(const T *__restrict__ R, 
   const long h = bx.n / 2;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
   const long sy = nx, sz = (long)nx * ny;
-  const T *__restrict__ P = R + (long)color * 7 * h;
+  const T *__restrict__ P = R + (long)color * 8 * h;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
     const long r = rb_row(m, color, bx, i, j, k);
@@ -374,7 +375,7 @@ __global__ void k_split_colors27(const T *A, const T *invd, Box bx, T *R) {
 }
 
 template <class T>
-__global__ void __launch_bounds__(kThreads) k_relax_rb27(const T *__restrict__ R, const T *__restrict__ b,
+__global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(const T *__restrict__ R, const T *__restrict__ b,
                                                          const T *__restrict__ x, T *__restrict__ t, Box bx,
                                                          int color, int zero_x, const int *gate) {
   if (gate_off(gate)) return;
@@ -399,6 +400,41 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb27(const T *__restrict__ R
     }
     t[r] = fmat<T>(P[27 * h + m], b[r] - acc, x[r]);
     t[r ^ 1] = x[r ^ 1];
+  }
+}
+
+// Residual after a two-colour sweep that ended with colour 1: the colour-1
+// points were just solved exactly against their colour-0 neighbours, so their
+// residual is zero up to rounding and is written as 0; colour-0 points take
+// b - A x with the colour-split coefficients (centre first, as apply_row).
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_residual_rb(const T *__restrict__ R, const T *__restrict__ b,
+                                                          const T *__restrict__ x, T *__restrict__ res, Box bx,
+                                                          const int *gate) {
+  if (gate_off(gate)) return;
+  const long h = bx.n / 2;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const long sy = nx, sz = (long)nx * ny;
+  for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const long r = rb_row(m, 0, bx, i, j, k);
+    const T xc = x[r];
+    const T xw = i > 0 ? x[r - 1] : T(0);
+    const T xe = i < nx - 1 ? x[r + 1] : T(0);
+    const T xs = j > 0 ? x[r - sy] : T(0);
+    const T xn = j < ny - 1 ? x[r + sy] : T(0);
+    const T xb = k > 0 ? x[r - sz] : T(0);
+    const T xt = k < nz - 1 ? x[r + sz] : T(0);
+    T acc = T(0);
+    acc = fmat<T>(R[7 * h + m], xc, acc);
+    acc = fmat<T>(R[h + m], xw, acc);
+    acc = fmat<T>(R[2 * h + m], xe, acc);
+    acc = fmat<T>(R[3 * h + m], xs, acc);
+    acc = fmat<T>(R[4 * h + m], xn, acc);
+    acc = fmat<T>(R[5 * h + m], xb, acc);
+    acc = fmat<T>(R[6 * h + m], xt, acc);
+    res[r] = b[r] - acc;
+    res[r ^ 1] = T(0);
   }
 }
 
@@ -552,7 +588,7 @@ static void split_colors(cudaStream_t st, MgLevelT<T> &F, const MgParams &prm) {
   if (prm.relax != 2 || (F.b.nx & 1) || F.b.n < 2) return;
   LaunchScope ls(K_SETUP, st, 0.0);
   if (F.ns == 7) {
-    F.rb.alloc((size_t)7 * F.b.n);
+    F.rb.alloc((size_t)8 * F.b.n);
     k_split_colors<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, F.rb.p);
   } else {
     F.rb27.alloc((size_t)28 * F.b.n);
@@ -772,7 +808,11 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   const int nu1 = F.relax ? c1 : 0, nu2 = F.relax ? c2 : 0;
   for (int s = 0; s < nu1; ++s) relax(s == 0);
   const T *res = F.bv.p;  // residual of a zero initial guess is b
-  if (nu1 > 0) {
+  if (nu1 > 0 && p.relax == 2 && F.rb.p) {
+    LaunchScope ls(K_MG_RESID, st, T_ * n * 6.5);
+    k_residual_rb<T><<<grid_for(n / 2), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.r.p, F.b, gate);
+    res = F.r.p;
+  } else if (nu1 > 0) {
     LaunchScope ls(K_MG_RESID, st, T_ * n * (F.ns + 3.0));
     if (F.ns == 7) k_residual<T, 7><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
     else k_residual<T, 27><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
