@@ -287,7 +287,8 @@ def profile_pass(solver, plib, Prof, ibm):
     p.use_graph = 0
     solver.set_params(p)
     per_class, per_bytes, per_launch = {}, {}, {}
-    for k in range(21):  # every kernel class of the step (setup excluded)
+    n_classes = next(k for k in range(64) if plib.ibm_kernel_name(k).decode() == "setup")
+    for k in range(n_classes):  # every kernel class of the step (setup excluded)
         plib.ibm_profile_reset(solver._ctx)
         plib.ibm_profile_time_kernel(solver._ctx, k)
         solver.step(1.0)
@@ -306,7 +307,7 @@ def profile_pass(solver, plib, Prof, ibm):
     # algorithmic bytes of the class / its CUDA-event time
     kernel_gbs = {names[k]: round(per_bytes[k] / (per_class[k] * 1e-3) / 1e9, 1)
                   for k in per_class if per_launch[k] > 0 and per_class[k] > 0}
-    return dom, names[dom], pr, st, kernel_ms, kernel_gbs, 21 + 2
+    return dom, names[dom], pr, st, kernel_ms, kernel_gbs, n_classes + 2
 
 
 def main():

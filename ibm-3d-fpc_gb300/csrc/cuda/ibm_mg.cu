@@ -293,11 +293,13 @@ __global__ void k_relax_color(const T *A, const T *invd, const T *b, const T *x,
   }
 }
 
-// Colour-split coefficients of a 7-point level with an even nx. Rows 2m and
-// 2m+1 lie on one x line and have opposite colours (parity of i+j+k), so the
-// pair index m numbers the points of either colour; planes [c][q][m] hold, for
-// the colour-c point of pair m, q = 0 the inverse diagonal and q = 1..6 the
-// couplings -x,+x,-y,+y,-z,+z. A colour phase streams only its own half.
+// Colour-split coefficients of levels with an even nx. Rows 2m and 2m+1 lie on
+// one x line and have opposite colours (parity of i+j+k), so the pair index m
+// numbers the points of either colour. Each point keeps one contiguous record
+// (array of structures, so a warp reads one contiguous block per phase and a
+// thread loads its record with 16-byte vector loads):
+//   7-point levels:  [c][m][8]  = inverse diagonal, couplings -x,+x,-y,+y,-z,+z, diagonal
+//   27-point levels: [c][m][28] = the 27 coefficients (27-point slot order), inverse diagonal
 __device__ __forceinline__ long rb_row(long m, int color, const Box &b, int &i, int &j, int &k) {
   const unsigned q = 2u * (unsigned)m;
   const unsigned line = fast_div(q, b.dx);
@@ -309,6 +311,18 @@ __device__ __forceinline__ long rb_row(long m, int color, const Box &b, int &i, 
   return (long)r;
 }
 
+// Vector loads of a record of N values of T (N * sizeof(T) a multiple of 16).
+template <class T, int N>
+__device__ __forceinline__ void load_rec(const T *__restrict__ p, T (&v)[N]) {
+  static_assert((N * sizeof(T)) % 16 == 0, "records are whole 16-byte units");
+  const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+  for (int u = 0; u < (int)(N * sizeof(T) / 16); ++u) {
+    const float4 f = __ldg(q + u);
+    memcpy(reinterpret_cast<char *>(v) + 16 * u, &f, 16);
+  }
+}
+
 template <class T>
 __global__ void k_split_colors(const T *A, const T *invd, Box bx, T *R) {
   const long h = bx.n / 2;
@@ -317,10 +331,10 @@ __global__ void k_split_colors(const T *A, const T *invd, Box bx, T *R) {
     const long m = t - c * h;
     int i, j, k;
     const long r = rb_row(m, c, bx, i, j, k);
-    T *o = R + (long)c * 8 * h + m;
+    T *o = R + ((long)c * h + m) * 8;
     o[0] = invd[r];
-    for (int s = 1; s < 7; ++s) o[(long)s * h] = A[(long)s * bx.n + r];
-    o[7L * h] = A[r];
+    for (int s = 1; s < 7; ++s) o[s] = A[(long)s * bx.n + r];
+    o[7] = A[r];
   }
 }
 
@@ -334,10 +348,12 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb(const T *__restrict__ R, 
   const long h = bx.n / 2;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
   const long sy = nx, sz = (long)nx * ny;
-  const T *__restrict__ P = R + (long)color * 8 * h;
+  const T *__restrict__ P = R + (long)color * h * 8;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
     const long r = rb_row(m, color, bx, i, j, k);
+    T c[8];
+    load_rec<T, 8>(P + m * 8, c);
     const T xw = i > 0 ? x[r - 1] : T(0);
     const T xe = i < nx - 1 ? x[r + 1] : T(0);
     const T xs = j > 0 ? x[r - sy] : T(0);
@@ -345,21 +361,20 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb(const T *__restrict__ R, 
     const T xb = k > 0 ? x[r - sz] : T(0);
     const T xt = k < nz - 1 ? x[r + sz] : T(0);
     T acc = T(0);
-    acc = fmat<T>(P[h + m], xw, acc);
-    acc = fmat<T>(P[2 * h + m], xe, acc);
-    acc = fmat<T>(P[3 * h + m], xs, acc);
-    acc = fmat<T>(P[4 * h + m], xn, acc);
-    acc = fmat<T>(P[5 * h + m], xb, acc);
-    acc = fmat<T>(P[6 * h + m], xt, acc);
-    x[r] = P[m] * (b[r] - acc);
+    acc = fmat<T>(c[1], xw, acc);
+    acc = fmat<T>(c[2], xe, acc);
+    acc = fmat<T>(c[3], xs, acc);
+    acc = fmat<T>(c[4], xn, acc);
+    acc = fmat<T>(c[5], xb, acc);
+    acc = fmat<T>(c[6], xt, acc);
+    x[r] = c[0] * (b[r] - acc);
   }
 }
 
-// 27-point levels (even nx): planes [c][q][m] hold the 27 coefficients of the
-// colour-c point of pair m (q = 27-point slot) and, at q = 27, its inverse
-// diagonal. Diagonal neighbours share a colour, so a phase cannot update in
-// place: it writes every point of the pair to the other buffer (the own-colour
-// point relaxed, the other copied), with the same arithmetic as k_relax_color.
+// 27-point levels: diagonal neighbours share a colour, so a phase cannot
+// update in place: it writes every point of the pair to the other buffer (the
+// own-colour point relaxed, the other copied), with the same arithmetic as
+// k_relax_color.
 template <class T>
 __global__ void k_split_colors27(const T *A, const T *invd, Box bx, T *R) {
   const long h = bx.n / 2;
@@ -368,9 +383,9 @@ __global__ void k_split_colors27(const T *A, const T *invd, Box bx, T *R) {
     const long m = t - c * h;
     int i, j, k;
     const long r = rb_row(m, c, bx, i, j, k);
-    T *o = R + (long)c * 28 * h + m;
-    for (int s = 0; s < 27; ++s) o[(long)s * h] = A[(long)s * bx.n + r];
-    o[27L * h] = invd[r];
+    T *o = R + ((long)c * h + m) * 28;
+    for (int s = 0; s < 27; ++s) o[s] = A[(long)s * bx.n + r];
+    o[27] = invd[r];
   }
 }
 
@@ -381,24 +396,35 @@ __global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(const T *__restrict_
   if (gate_off(gate)) return;
   const long h = bx.n / 2;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
-  const T *__restrict__ P = R + (long)color * 28 * h;
+  const T *__restrict__ P = R + (long)color * h * 28;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
     const long r = rb_row(m, color, bx, i, j, k);
     if (zero_x) {
-      t[r] = P[27 * h + m] * b[r];
+      t[r] = P[m * 28 + 27] * b[r];
       t[r ^ 1] = T(0);
       continue;
     }
+    // FP32 records come in with vector loads; FP64 ones (twice the registers)
+    // are read one value at a time
+    T c[sizeof(T) == 4 ? 28 : 1];
+    if constexpr (sizeof(T) == 4) load_rec<T, 28>(P + m * 28, c);
+    const T *__restrict__ pr = P + m * 28;
     T acc = T(0);
 #pragma unroll
     for (int s = 0; s < 27; ++s) {
       const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
       const bool in = ii >= 0 && ii < nx && jj >= 0 && jj < ny && kk >= 0 && kk < nz;
       const T xv = in ? x[((long)kk * ny + jj) * nx + ii] : T(0);
-      acc = fmat<T>(P[(long)s * h + m], xv, acc);
+      T cs;
+      if constexpr (sizeof(T) == 4) cs = c[s];
+      else cs = pr[s];
+      acc = fmat<T>(cs, xv, acc);
     }
-    t[r] = fmat<T>(P[27 * h + m], b[r] - acc, x[r]);
+    T cd;
+    if constexpr (sizeof(T) == 4) cd = c[27];
+    else cd = pr[27];
+    t[r] = fmat<T>(cd, b[r] - acc, x[r]);
     t[r ^ 1] = x[r ^ 1];
   }
 }
@@ -418,6 +444,8 @@ __global__ void __launch_bounds__(kThreads) k_residual_rb(const T *__restrict__ 
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
     const long r = rb_row(m, 0, bx, i, j, k);
+    T c[8];
+    load_rec<T, 8>(R + m * 8, c);
     const T xc = x[r];
     const T xw = i > 0 ? x[r - 1] : T(0);
     const T xe = i < nx - 1 ? x[r + 1] : T(0);
@@ -426,13 +454,13 @@ __global__ void __launch_bounds__(kThreads) k_residual_rb(const T *__restrict__ 
     const T xb = k > 0 ? x[r - sz] : T(0);
     const T xt = k < nz - 1 ? x[r + sz] : T(0);
     T acc = T(0);
-    acc = fmat<T>(R[7 * h + m], xc, acc);
-    acc = fmat<T>(R[h + m], xw, acc);
-    acc = fmat<T>(R[2 * h + m], xe, acc);
-    acc = fmat<T>(R[3 * h + m], xs, acc);
-    acc = fmat<T>(R[4 * h + m], xn, acc);
-    acc = fmat<T>(R[5 * h + m], xb, acc);
-    acc = fmat<T>(R[6 * h + m], xt, acc);
+    acc = fmat<T>(c[7], xc, acc);
+    acc = fmat<T>(c[1], xw, acc);
+    acc = fmat<T>(c[2], xe, acc);
+    acc = fmat<T>(c[3], xs, acc);
+    acc = fmat<T>(c[4], xn, acc);
+    acc = fmat<T>(c[5], xb, acc);
+    acc = fmat<T>(c[6], xt, acc);
     res[r] = b[r] - acc;
     res[r ^ 1] = T(0);
   }
@@ -446,7 +474,7 @@ __global__ void k_relax_rb_zero(const T *__restrict__ R, const T *__restrict__ b
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
     const long r = rb_row(m, 0, bx, i, j, k);
-    x[r] = R[m] * b[r];
+    x[r] = R[m * 8] * b[r];
     x[r ^ 1] = T(0);
   }
 }
@@ -478,6 +506,91 @@ __global__ void k_restrict(const T *res, const T *pm, const T *pp, Box fb, int d
       acc = fmat<T>(rw, res[fr], acc);
     }
     bc[I] = acc;
+  }
+}
+
+// Restriction / interpolation along y or z on FP32 levels whose nx is a
+// multiple of 4: four consecutive x points share everything but their x, so a
+// thread moves them with 16-byte loads. Same operations as k_restrict /
+// k_prolong, lane by lane.
+__global__ void k_restrict_yz4(const float *__restrict__ res, const float *__restrict__ pm,
+                               const float *__restrict__ pp, Box fb, int d, float *__restrict__ bc, Box cb,
+                               const int *gate) {
+  if (gate_off(gate)) return;
+  const long n4 = cb.n / 4;
+  const long plane_f = (long)fb.nx * fb.ny;
+  const int nfd = d == 1 ? fb.ny : fb.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n4; t += (long)gridDim.x * blockDim.x) {
+    int i, J, k;
+    box_ijk(4 * t, cb, i, J, k);
+    const int cd = d == 1 ? J : k;
+    // fine index of (i, 2cd + fo) along d
+    auto fidx = [&](int fo) {
+      const int y = d == 1 ? 2 * cd + fo : J, z = d == 2 ? 2 * cd + fo : k;
+      return (long)z * plane_f + (long)y * fb.nx + i;
+    };
+    const bool lo = 2 * cd - 1 >= 0, hi = 2 * cd + 1 < nfd;
+    const float4 rm = *reinterpret_cast<const float4 *>(res + fidx(0));
+    float4 rl = make_float4(0.f, 0.f, 0.f, 0.f), rh = rl, wl = rl, wh = rl;
+    if (lo) {
+      rl = *reinterpret_cast<const float4 *>(res + fidx(-1));
+      wl = *reinterpret_cast<const float4 *>(pp + fidx(-1));
+    }
+    if (hi) {
+      rh = *reinterpret_cast<const float4 *>(res + fidx(1));
+      wh = *reinterpret_cast<const float4 *>(pm + fidx(1));
+    }
+    auto one = [&](float a_rl, float a_wl, float a_rm, float a_rh, float a_wh) {
+      float acc = 0.0f;
+      if (lo) acc = fmaf(a_wl, a_rl, acc);
+      acc = fmaf(1.0f, a_rm, acc);
+      if (hi) acc = fmaf(a_wh, a_rh, acc);
+      return acc;
+    };
+    float4 o;
+    o.x = one(rl.x, wl.x, rm.x, rh.x, wh.x);
+    o.y = one(rl.y, wl.y, rm.y, rh.y, wh.y);
+    o.z = one(rl.z, wl.z, rm.z, rh.z, wh.z);
+    o.w = one(rl.w, wl.w, rm.w, rh.w, wh.w);
+    *reinterpret_cast<float4 *>(bc + 4 * t) = o;
+  }
+}
+
+__global__ void k_prolong_yz4(const float *__restrict__ xc, Box cb, const float *__restrict__ pm,
+                              const float *__restrict__ pp, Box fb, int d, float *x, int accumulate,
+                              const int *gate) {
+  if (gate_off(gate)) return;
+  const long n4 = fb.n / 4;
+  const long plane_c = (long)cb.nx * cb.ny;
+  const int ncd = d == 1 ? cb.ny : cb.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n4; t += (long)gridDim.x * blockDim.x) {
+    int i, y, k;
+    box_ijk(4 * t, fb, i, y, k);
+    const int fd = d == 1 ? y : k;
+    auto cidx = [&](int c) {
+      const int yy = d == 1 ? c : y, zz = d == 2 ? c : k;
+      return (long)zz * plane_c + (long)yy * cb.nx + i;
+    };
+    float4 corr;
+    if ((fd & 1) == 0) {
+      corr = *reinterpret_cast<const float4 *>(xc + cidx(fd / 2));
+    } else {
+      const float4 x0 = *reinterpret_cast<const float4 *>(xc + cidx((fd - 1) / 2));
+      float4 x1 = make_float4(0.f, 0.f, 0.f, 0.f);
+      if ((fd + 1) / 2 < ncd) x1 = *reinterpret_cast<const float4 *>(xc + cidx((fd + 1) / 2));
+      const float4 a = *reinterpret_cast<const float4 *>(pp + 4 * t);
+      const float4 b = *reinterpret_cast<const float4 *>(pm + 4 * t);
+      corr.x = fmaf(a.x, x1.x, b.x * x0.x);
+      corr.y = fmaf(a.y, x1.y, b.y * x0.y);
+      corr.z = fmaf(a.z, x1.z, b.z * x0.z);
+      corr.w = fmaf(a.w, x1.w, b.w * x0.w);
+    }
+    float4 *xo = reinterpret_cast<float4 *>(x + 4 * t);
+    if (accumulate) {
+      const float4 xv = *xo;
+      corr.x = xv.x + corr.x; corr.y = xv.y + corr.y; corr.z = xv.z + corr.z; corr.w = xv.w + corr.w;
+    }
+    *xo = corr;
   }
 }
 
@@ -530,6 +643,11 @@ int grid_for(long n) {
   if (b > cap) b = cap;
   return (int)std::max(1L, b);
 }
+
+// One thread per element for the V-cycle's streaming kernels: every block
+// retires after one element per thread, so the GPU keeps many independent
+// loads in flight without a serial loop per thread.
+int grid_all(long n) { return (int)std::max(1L, std::min((n + kThreads - 1) / kThreads, 1L << 30)); }
 
 // Gauss-Jordan inverse with partial pivoting of the assembled coarsest operator.
 void dense_inverse(const std::vector<double> &A, int ns, const Box &b, std::vector<double> &inv) {
@@ -769,17 +887,17 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   auto relax = [&](bool zero) {
     if (p.relax == 2 && F.rb.p) {
       {
-        LaunchScope ls(K_MG_RELAX, st, zero ? 2.5 * T_ * n : 5.0 * T_ * n);
-        if (zero) k_relax_rb_zero<T><<<grid_for(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, gate);
-        else k_relax_rb<T><<<grid_for(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 0, gate);
+        LaunchScope ls(K_MG_RELAX_FINE, st, zero ? 2.5 * T_ * n : 5.0 * T_ * n);
+        if (zero) k_relax_rb_zero<T><<<grid_all(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, gate);
+        else k_relax_rb<T><<<grid_all(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 0, gate);
       }
-      LaunchScope ls(K_MG_RELAX, st, 5.0 * T_ * n);
-      k_relax_rb<T><<<grid_for(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 1, gate);
+      LaunchScope ls(K_MG_RELAX_FINE, st, 5.0 * T_ * n);
+      k_relax_rb<T><<<grid_all(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 1, gate);
     } else if (p.relax == 2 && F.rb27.p) {
       for (int color = 0; color < 2; ++color) {
         const bool z = zero && color == 0;
         LaunchScope ls(K_MG_RELAX, st, z ? 2.5 * T_ * n : T_ * n * (14.0 + 3.0));
-        k_relax_rb27<T><<<grid_for(h), kThreads, 0, st>>>(F.rb27.p, F.bv.p, cur, oth, F.b, color, z, gate);
+        k_relax_rb27<T><<<grid_all(h), kThreads, 0, st>>>(F.rb27.p, F.bv.p, cur, oth, F.b, color, z, gate);
         std::swap(cur, oth);
       }
     } else if (p.relax == 2) {
@@ -810,23 +928,37 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   const T *res = F.bv.p;  // residual of a zero initial guess is b
   if (nu1 > 0 && p.relax == 2 && F.rb.p) {
     LaunchScope ls(K_MG_RESID, st, T_ * n * 6.5);
-    k_residual_rb<T><<<grid_for(n / 2), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.r.p, F.b, gate);
+    k_residual_rb<T><<<grid_all(n / 2), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.r.p, F.b, gate);
     res = F.r.p;
   } else if (nu1 > 0) {
     LaunchScope ls(K_MG_RESID, st, T_ * n * (F.ns + 3.0));
-    if (F.ns == 7) k_residual<T, 7><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
-    else k_residual<T, 27><<<g, kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
+    if (F.ns == 7) k_residual<T, 7><<<grid_all(n), kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
+    else k_residual<T, 27><<<grid_all(n), kThreads, 0, st>>>(F.A, F.bv.p, cur, F.r.p, F.b, gate);
     res = F.r.p;
   }
   MgLevelT<T> &C = L[l + 1];
   {
     LaunchScope ls(K_MG_RESTRICT, st, T_ * (3.0 * n + C.b.n));
-    k_restrict<T><<<grid_for(C.b.n), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
+    if constexpr (sizeof(T) == 4) {
+      if (F.cdir != 0 && F.b.nx % 4 == 0)
+        k_restrict_yz4<<<grid_all(C.b.n / 4), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
+      else
+        k_restrict<T><<<grid_all(C.b.n), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
+    } else {
+      k_restrict<T><<<grid_all(C.b.n), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
+    }
   }
   T *xc = vcycle<T>(st, L, l + 1, p, gate);
   {
     LaunchScope ls(K_MG_PROLONG, st, T_ * ((nu1 > 0 ? 4.0 : 3.0) * n + C.b.n));
-    k_prolong<T><<<g, kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, nu1 > 0, gate);
+    if constexpr (sizeof(T) == 4) {
+      if (F.cdir != 0 && F.b.nx % 4 == 0)
+        k_prolong_yz4<<<grid_all(n / 4), kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, nu1 > 0, gate);
+      else
+        k_prolong<T><<<grid_all(n), kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, nu1 > 0, gate);
+    } else {
+      k_prolong<T><<<grid_all(n), kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, nu1 > 0, gate);
+    }
   }
   for (int s = 0; s < nu2; ++s) relax(false);
   return cur;
