@@ -318,7 +318,9 @@ __device__ __forceinline__ void load_rec(const T *__restrict__ p, T (&v)[N]) {
   const float4 *q = reinterpret_cast<const float4 *>(p);
 #pragma unroll
   for (int u = 0; u < (int)(N * sizeof(T) / 16); ++u) {
-    const float4 f = __ldg(q + u);
+    // streamed once per phase: evict-first, so the solution and right-hand
+    // side of the level stay in L2 across the phases
+    const float4 f = __ldcs(q + u);
     memcpy(reinterpret_cast<char *>(v) + 16 * u, &f, 16);
   }
 }
