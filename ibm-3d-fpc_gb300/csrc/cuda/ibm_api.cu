@@ -109,6 +109,11 @@ __global__ void k_op_jacobi(const double *c, const double *invd, double *cj, Box
   }
 }
 
+__global__ void k_to_float(const double *src, float *dst, long n) {
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+    dst[t] = (float)src[t];
+}
+
 __global__ void k_spmv7(const double *c, Box b, const double *x, double *y) {
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < b.n; r += (long)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -213,7 +218,7 @@ void ensure_solvers(ibm_ctx *c) {
     h.nx = o.b.nx; h.ny = o.b.ny; h.nz = o.b.nz; h.n = o.b.n;
     h.Ar = o.c.p;
     h.invd = o.invd.p;
-    h.Af = o.cf.p; h.invdf = o.invdf.p;
+    h.Af = o.cf.p; h.invdf = o.invdf.p; h.Ajf = o.cjf.p;
     h.kdim = p.vel_kdim; h.maxit = p.vel_maxit; h.tol = p.vel_tol;
     if (mixed) {
       h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps);
@@ -449,6 +454,11 @@ int ibm_set_operator(ibm_ctx *c, int field, const double *vals7, int nbx, int nb
       LaunchScope ls(K_SETUP, c->st, 0.0, 2);
       k_op_planes<<<grid1d(n), kThreads, 0, c->st>>>(tmp.p, n, o.c.p, o.invd.p, o.cf.p, o.invdf.p);
       k_op_jacobi<<<grid1d(n), kThreads, 0, c->st>>>(o.c.p, o.invd.p, o.cj.p, b);
+    }
+    o.cjf.alloc((size_t)7 * n);
+    {
+      LaunchScope ls(K_SETUP, c->st, 0.0);
+      k_to_float<<<grid1d(7 * n), kThreads, 0, c->st>>>(o.cj.p, o.cjf.p, 7 * n);
     }
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
     IBM_CUDA_TRY(cudaGetLastError());

@@ -116,6 +116,7 @@ struct Op7 {
   DBuf<double> invd;   // 1 / C
   DBuf<double> cj;     // C * invd(neighbour): the right-Jacobi-preconditioned operator
   DBuf<float> cf;      // FP32 coefficients (mixed precision)
+  DBuf<float> cjf;     // FP32 copy of cj (two Jacobi sweeps in one pass)
   DBuf<float> invdf;
 };
 
@@ -149,6 +150,7 @@ struct KSys {
   const double *Ar;     // operator of the true residual ([7][n])
   const double *invd;   // inverse diagonal (Jacobi solution update)
   const float *Af;      // FP32 operator (inner FP32 sweeps)
+  const float *Ajf;     // FP32 right-Jacobi-scaled operator (cj)
   const float *invdf;
   double *V;            // basis, vector k at V + k*ldv
   long ldv;

@@ -601,6 +601,39 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next32(KSys *sys) {
   }
 }
 
+// Two FP32 Jacobi sweeps from zero in one pass (momentum preconditioner of
+// the flexible form): z = D^-1 (2v - A D^-1 v) = D^-1 (v - sum over the
+// couplings of (A D^-1)_s v_s), with v = V_j / nu_j; A D^-1 is stored (cjf), so
+// the pass reads v, the six scaled couplings and D^-1 once.
+template <class VT>
+__device__ __forceinline__ void jacobi_two_rows(const KSys &S, const VT *__restrict__ vj, float inv_nu,
+                                                float *__restrict__ out) {
+  const long n = S.n, sy = S.nx, sz = (long)S.nx * S.ny;
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    int i, jj, k;
+    sys_ijk(r, S, i, jj, k);
+    float acc = (float)vj[r] * inv_nu;
+    if (i > 0) acc = fmaf(-S.Ajf[n + r], (float)vj[r - 1] * inv_nu, acc);
+    if (i < S.nx - 1) acc = fmaf(-S.Ajf[2 * n + r], (float)vj[r + 1] * inv_nu, acc);
+    if (jj > 0) acc = fmaf(-S.Ajf[3 * n + r], (float)vj[r - sy] * inv_nu, acc);
+    if (jj < S.ny - 1) acc = fmaf(-S.Ajf[4 * n + r], (float)vj[r + sy] * inv_nu, acc);
+    if (k > 0) acc = fmaf(-S.Ajf[5 * n + r], (float)vj[r - sz] * inv_nu, acc);
+    if (k < S.nz - 1) acc = fmaf(-S.Ajf[6 * n + r], (float)vj[r + sz] * inv_nu, acc);
+    out[r] = S.invdf[r] * acc;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_jacobi32_two(KSys *sys) {
+  KSys &S = sys[blockIdx.y];
+  KScal *sc = S.s;
+  if (!sc->active || S.pc != 2 || S.pc_cb) return;
+  const int j = sc->i;
+  const float inv_nu = (float)(1.0 / sc->nu[j]);
+  float *out = S.Z + (long)j * S.ldv;
+  if (S.a32) jacobi_two_rows<float>(S, S.Vf + (long)j * S.ldv, inv_nu, out);
+  else jacobi_two_rows<double>(S, S.V + (long)j * S.ldv, inv_nu, out);
+}
+
 // FP32 inner preconditioner for the flexible form: zf = D^-1 v (v = V_j / nu_j),
 // then `sweeps-1` Jacobi sweeps zf <- zf + D^-1 (v - A zf); result to Z_j.
 __global__ void __launch_bounds__(kThreads) k_jacobi32_first(KSys *sys, int to_z) {
@@ -734,7 +767,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     KSys &k = hsys[s];
     k.nx = h.nx; k.ny = h.ny; k.nz = h.nz; k.n = ((mask >> s) & 1u) ? h.n : 0;
     k.fdx = make_fastdiv((unsigned)h.nx); k.fdy = make_fastdiv((unsigned)h.ny);
-    k.A = h.A; k.Ar = h.Ar; k.invd = h.invd; k.Af = h.Af; k.invdf = h.invdf;
+    k.A = h.A; k.Ar = h.Ar; k.invd = h.invd; k.Af = h.Af; k.invdf = h.invdf; k.Ajf = h.Ajf;
     k.V = slot[s].V.p; k.ldv = h.n;
     k.Z = slot[s].Z.p;
     k.w = slot[s].w.p; k.r = slot[s].r.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;
@@ -854,7 +887,10 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
     }
   }
   if (inner_sweeps > 0) {
-    if (inner_sweeps == 1) {
+    if (inner_sweeps == 2) {
+      LaunchScope ls(K_GM_JAC32, st, 36.0 * r32);
+      k_jacobi32_two<<<gridu, kThreads, 0, st>>>(dev);
+    } else if (inner_sweeps == 1) {
       LaunchScope ls(K_GM_JAC32, st, 16.0 * r32);
       k_jacobi32_first<<<gridu, kThreads, 0, st>>>(dev, 1);
     } else {

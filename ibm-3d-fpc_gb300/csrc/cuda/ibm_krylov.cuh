@@ -32,6 +32,7 @@ struct KSysHost {
   const double *Ar = nullptr;   // operator of the true residual
   const double *invd = nullptr;
   const float *Af = nullptr, *invdf = nullptr;
+  const float *Ajf = nullptr;   // FP32 A D^-1 (pc 2 with two internal Jacobi sweeps)
   int pc = 0;                   // 0 folded Jacobi, 1 explicit FP64 callback, 2 flexible FP32
   int pc_cb = 0;                // pc 2: 1 = callback, 0 = internal FP32 Jacobi sweeps
   int inner_sweeps = 1;
