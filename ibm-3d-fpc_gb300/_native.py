@@ -52,7 +52,7 @@ class SolverParams(C.Structure):
                 ("mg_coarse_max", C.c_int), ("mg_max_levels", C.c_int),
                 ("use_zero_initial_guess", C.c_int), ("precision", C.c_int), ("use_graph", C.c_int),
                 ("vel_inner_sweeps", C.c_int), ("mg_group_ratio", C.c_double), ("mg_options", C.c_int),
-                ("mg_nu_coarse", C.c_int)]
+                ("mg_nu_coarse", C.c_int), ("cycle_rtol32", C.c_double)]
 
 
 class SolveStats(C.Structure):

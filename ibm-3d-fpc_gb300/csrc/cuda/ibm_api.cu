@@ -199,11 +199,6 @@ void require_inputs(ibm_ctx *c) {
   if (!c->csr_set) throw Error(IBM_ERR_STATE, "projection operators not set");
 }
 
-// precision 2: each FP32 Arnoldi cycle stops once its residual estimate fell
-// by this factor (about what an FP32 basis resolves); the FP64 restart then
-// measures the true residual.
-constexpr double kCycleRtol32 = 1e-5;
-
 void ensure_solvers(ibm_ctx *c) {
   if (c->solvers_ready && c->solvers_precision == c->prm.precision) return;
   const ibm_solver_params &p = c->prm;
@@ -222,7 +217,7 @@ void ensure_solvers(ibm_ctx *c) {
     h.kdim = p.vel_kdim; h.maxit = p.vel_maxit; h.tol = p.vel_tol;
     if (mixed) {
       h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps);
-      h.a32 = a32; h.cycle_rtol = kCycleRtol32;
+      h.a32 = a32; h.cycle_rtol = p.cycle_rtol32;
     }
     else { h.pc = 0; h.A = o.cj.p; }
   }
@@ -245,12 +240,12 @@ void ensure_solvers(ibm_ctx *c) {
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
     const double *winv = ((p.mg_options & 2) && c->p_sym) ? c->p_winv.p : nullptr;
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
-    if (mixed) { hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; hp.a32 = a32; hp.cycle_rtol = kCycleRtol32; }
+    if (mixed) { hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32; }
     else { hp.pc = 1; hp.A = op.c.p; }
   } else {
     if (mixed) {
       hp.pc = 2; hp.pc_cb = 0; hp.A = op.c.p; hp.inner_sweeps = 1;
-      hp.a32 = a32; hp.cycle_rtol = kCycleRtol32;
+      hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32;
     }
     else { hp.pc = 0; hp.A = op.cj.p; }
   }
@@ -355,6 +350,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->mg_group_ratio = 0.0;
   p->mg_options = 3;
   p->mg_nu_coarse = 0;
+  p->cycle_rtol32 = 1e-5;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -715,6 +711,7 @@ int ibm_set_solver_params(ibm_ctx *c, const ibm_solver_params *p) {
     if (p->vel_maxit < 0 || p->p_maxit < 0 || !(p->vel_tol >= 0) || !(p->p_tol >= 0))
       throw Error(IBM_ERR_ARG, "bad tolerance or iteration limit");
     if (p->precision < 0 || p->precision > 2) throw Error(IBM_ERR_ARG, "precision must be 0, 1 or 2");
+    if (!(p->cycle_rtol32 > 0.0 && p->cycle_rtol32 < 1.0)) throw Error(IBM_ERR_ARG, "cycle_rtol32 must be in (0, 1)");
     if (p->p_pc != 0 && p->p_pc != 1) throw Error(IBM_ERR_ARG, "p_pc must be 0 or 1");
     if (p->mg_nu1 < 0 || p->mg_nu2 < 0 || p->mg_nu_coarse < 0 || p->mg_coarse_max < 1 || p->mg_max_levels < 1)
       throw Error(IBM_ERR_ARG, "bad multigrid parameters");

@@ -78,7 +78,7 @@ typedef struct ibm_solver_params {
   int use_zero_initial_guess; /* -use-zero-initial-guess (momentum) */
   int precision;         /* 0: FP64 throughout; 1: FP32 preconditioners inside FP64 flexible GMRES;
                             2: as 1 with the Arnoldi cycles in FP32 (FP32 basis and operator copy,
-                            FP64 scalars), each cycle stopping after a 1e-5 reduction and the
+                            FP64 scalars), each cycle stopping after a cycle_rtol32 reduction and the
                             FP64 restart measuring the true residual (mixed-precision iterative
                             refinement): same FP64 tolerance, far fewer FP64 operations */
   int use_graph;         /* 1: replay the step as a CUDA graph */
@@ -92,6 +92,9 @@ typedef struct ibm_solver_params {
                             divergence scales rows by 1 / open fraction), build the hierarchy on
                             S and apply it to W^-1 r. 0 = PFMG's plain rules. Default 3. */
   int mg_nu_coarse;      /* sweeps each way on the relaxed levels below the finest (0: mg_nu1 / mg_nu2) */
+  double cycle_rtol32;   /* precision 2: an FP32 Arnoldi cycle stops once its residual estimate fell by
+                            this factor (default 1e-5, about what an FP32 basis resolves); the FP64
+                            restart then measures the true residual */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {
