@@ -162,6 +162,7 @@ struct KSys {
   float *Vf, *wf;       // FP32 basis and work vector of the FP32 Arnoldi cycles (a32)
   int a32;              // Arnoldi cycles in FP32 (basis, operator, dots per thread), restarts in FP64
   int x_zero;           // the initial guess is zero: the first residual is b
+  int vec4;             // n % 4 == 0: FP32 vectors and planes are 16-byte aligned in blocks of 4 rows
   int nblk;
   int pc;               // 0 Jacobi folded into A, 1 explicit z (multigrid), 2 flexible FP32 z
   int pc_cb;            // pc 2: preconditioner supplied by a callback (else FP32 Jacobi sweeps)

@@ -395,6 +395,10 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
 // true residual in FP64, so the solve still meets the FP64 tolerance.
 constexpr int kChunk32 = 8;  // basis vectors whose dot products a thread keeps in registers
 
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ float f4(const float4 &v, int q) { return q == 0 ? v.x : q == 1 ? v.y : q == 2 ? v.z : v.w; }
+
 __device__ __forceinline__ float warp_sum_f(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -411,6 +415,54 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float *zj = S.Z + (long)j * S.ldv;
+  if (nd <= kChunk32 && S.vec4) {
+    // four consecutive rows per thread: coefficient planes, w and the basis
+    // move as 16-byte vectors; the stencil of each row is stencil7_row_f's
+    float acc[kChunk32];
+#pragma unroll
+    for (int kk = 0; kk < kChunk32; ++kk) acc[kk] = 0.0f;
+    const long n = S.n, sy = S.nx, sz = (long)S.nx * S.ny;
+    for (long t0 = (long)blockIdx.x * kTile; t0 < n; t0 += (long)gridDim.x * kTile) {
+      const long r0 = t0 + 4 * threadIdx.x;
+      if (r0 >= n) continue;
+      float4 cp[7];
+#pragma unroll
+      for (int q = 0; q < 7; ++q) cp[q] = __ldcs(reinterpret_cast<const float4 *>(S.Af + (long)q * n + r0));
+      float w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const long r = r0 + q;
+        int i, jj, k;
+        sys_ijk(r, S, i, jj, k);
+        float a = 0.0f;
+        a = fmaf(f4(cp[0], q), zj[r], a);
+        a = fmaf(f4(cp[1], q), i > 0 ? zj[r - 1] : 0.0f, a);
+        a = fmaf(f4(cp[2], q), i < S.nx - 1 ? zj[r + 1] : 0.0f, a);
+        a = fmaf(f4(cp[3], q), jj > 0 ? zj[r - sy] : 0.0f, a);
+        a = fmaf(f4(cp[4], q), jj < S.ny - 1 ? zj[r + sy] : 0.0f, a);
+        a = fmaf(f4(cp[5], q), k > 0 ? zj[r - sz] : 0.0f, a);
+        a = fmaf(f4(cp[6], q), k < S.nz - 1 ? zj[r + sz] : 0.0f, a);
+        w[q] = a;
+      }
+      st4(S.wf + r0, make_float4(w[0], w[1], w[2], w[3]));
+#pragma unroll
+      for (int kk = 0; kk < kChunk32; ++kk) {
+        if (kk < nd) {
+          const float4 v = ld4(S.Vf + (long)kk * S.ldv + r0);
+          acc[kk] = fmaf(v.x, w[0], acc[kk]);
+          acc[kk] = fmaf(v.y, w[1], acc[kk]);
+          acc[kk] = fmaf(v.z, w[2], acc[kk]);
+          acc[kk] = fmaf(v.w, w[3], acc[kk]);
+        }
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < kChunk32; ++kk) {
+      if (kk >= nd) break;
+      const float p = warp_sum_f(acc[kk]);
+      if (lane == 0) sacc[kk * kWarps + warp] = (double)p;
+    }
+  } else
   if (nd <= kChunk32) {
     // short basis: every dot product of the thread stays in a register
     // across the whole sweep, one warp reduction per dot at the end
@@ -488,6 +540,43 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_orth32(KSys *sys) {
   for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = (float)sc->coef[t];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (nd <= kChunk32 && S.vec4) {
+    float acc[kChunk32];
+#pragma unroll
+    for (int kk = 0; kk < kChunk32; ++kk) acc[kk] = 0.0f;
+    for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+      const long r0 = t0 + 4 * threadIdx.x;
+      if (r0 >= S.n) continue;
+      float4 v[kChunk32];
+#pragma unroll
+      for (int kk = 0; kk < kChunk32; ++kk)
+        v[kk] = kk < nd ? ld4(S.Vf + (long)kk * S.ldv + r0) : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 w = ld4(S.wf + r0);
+#pragma unroll
+      for (int kk = 0; kk < kChunk32; ++kk) {
+        if (kk < nd) {
+          w.x = fmaf(-cf[kk], v[kk].x, w.x);
+          w.y = fmaf(-cf[kk], v[kk].y, w.y);
+          w.z = fmaf(-cf[kk], v[kk].z, w.z);
+          w.w = fmaf(-cf[kk], v[kk].w, w.w);
+        }
+      }
+      st4(S.wf + r0, w);
+#pragma unroll
+      for (int kk = 0; kk < kChunk32; ++kk) {
+        acc[kk] = fmaf(v[kk].x, w.x, acc[kk]);
+        acc[kk] = fmaf(v[kk].y, w.y, acc[kk]);
+        acc[kk] = fmaf(v[kk].z, w.z, acc[kk]);
+        acc[kk] = fmaf(v[kk].w, w.w, acc[kk]);
+      }
+    }
+#pragma unroll
+    for (int kk = 0; kk < kChunk32; ++kk) {
+      if (kk >= nd) break;
+      const float p = warp_sum_f(acc[kk]);
+      if (lane == 0) sacc[kk * kWarps + warp] = (double)p;
+    }
+  } else
   if (nd <= kChunk32) {
     // short basis: each basis value is loaded once for the update and the dots
     float acc[kChunk32];
@@ -568,6 +657,28 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next32(KSys *sys) {
   float *vn = S.Vf + (long)nd * S.ldv;
   const bool store = nd < sc->kdim;
   double pt = 0.0;
+  if (nd <= kChunk32 && S.vec4) {
+    for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+      const long r0 = t0 + 4 * threadIdx.x;
+      if (r0 >= S.n) continue;
+      float4 w = ld4(S.wf + r0);
+#pragma unroll
+      for (int kk = 0; kk < kChunk32; ++kk) {
+        if (kk < nd) {
+          const float4 v = ld4(S.Vf + (long)kk * S.ldv + r0);
+          w.x = fmaf(-cf[kk], v.x, w.x);
+          w.y = fmaf(-cf[kk], v.y, w.y);
+          w.z = fmaf(-cf[kk], v.z, w.z);
+          w.w = fmaf(-cf[kk], v.w, w.w);
+        }
+      }
+      if (store) st4(vn + r0, w);
+      pt = fma((double)w.x, (double)w.x, pt);
+      pt = fma((double)w.y, (double)w.y, pt);
+      pt = fma((double)w.z, (double)w.z, pt);
+      pt = fma((double)w.w, (double)w.w, pt);
+    }
+  } else
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
 #pragma unroll
     for (int t = 0; t < kRowsPerThread; ++t) {
@@ -774,6 +885,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     k.zf = slot[s].zf.p; k.zf2 = slot[s].zf2.p;
     k.Vf = slot[s].Vf.p; k.wf = slot[s].wf.p; k.a32 = h.a32;
     k.x_zero = x_zero ? 1 : 0;
+    k.vec4 = (h.n % 4 == 0) ? 1 : 0;
     k.x = x[s]; k.b = b[s];
     k.part = slot[s].part.p;
     k.nblk = nblk;
