@@ -317,6 +317,20 @@ __global__ void __launch_bounds__(kThreads) k_cycle_update(KSys *sys) {
   __shared__ double cf[kMaxKdim + 1];
   for (int t = threadIdx.x; t < m; t += blockDim.x) cf[t] = S.pc == 2 ? sc->y[t] : sc->coef[t];
   __syncthreads();
+  if (S.a32) {
+    // FP32 cycles: the correction sum Z y is formed in FP32 (its rounding is
+    // far below what the cycle resolved; the restart measures the true
+    // residual of the FP64 x) and added to x in FP64
+    __shared__ float cf32[kMaxKdim + 1];
+    for (int t = threadIdx.x; t < m; t += blockDim.x) cf32[t] = (float)cf[t];
+    __syncthreads();
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
+      float acc = 0.0f;
+      for (int kk = 0; kk < m; ++kk) acc = fmaf(cf32[kk], S.Z[(long)kk * S.ldv + r], acc);
+      S.x[r] = S.x[r] + (double)acc;
+    }
+    return;
+  }
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
     double acc = 0.0;
     if (S.pc == 2) {
@@ -734,6 +748,35 @@ __device__ __forceinline__ void jacobi_two_rows(const KSys &S, const VT *__restr
   }
 }
 
+// The same, four consecutive rows per thread with 16-byte loads of the
+// coefficient planes and stores of z (FP32 basis, n % 4 == 0).
+__device__ __forceinline__ void jacobi_two_rows4(const KSys &S, const float *__restrict__ vj, float inv_nu,
+                                                 float *__restrict__ out) {
+  const long n = S.n, sy = S.nx, sz = (long)S.nx * S.ny;
+  for (long r0 = 4 * ((long)blockIdx.x * blockDim.x + threadIdx.x); r0 < n; r0 += 4L * gridDim.x * blockDim.x) {
+    float4 cp[7];
+#pragma unroll
+    for (int q = 1; q < 7; ++q) cp[q] = __ldcs(reinterpret_cast<const float4 *>(S.Ajf + (long)q * n + r0));
+    const float4 id = __ldcs(reinterpret_cast<const float4 *>(S.invdf + r0));
+    float z[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const long r = r0 + q;
+      int i, jj, k;
+      sys_ijk(r, S, i, jj, k);
+      float acc = vj[r] * inv_nu;
+      if (i > 0) acc = fmaf(-f4(cp[1], q), vj[r - 1] * inv_nu, acc);
+      if (i < S.nx - 1) acc = fmaf(-f4(cp[2], q), vj[r + 1] * inv_nu, acc);
+      if (jj > 0) acc = fmaf(-f4(cp[3], q), vj[r - sy] * inv_nu, acc);
+      if (jj < S.ny - 1) acc = fmaf(-f4(cp[4], q), vj[r + sy] * inv_nu, acc);
+      if (k > 0) acc = fmaf(-f4(cp[5], q), vj[r - sz] * inv_nu, acc);
+      if (k < S.nz - 1) acc = fmaf(-f4(cp[6], q), vj[r + sz] * inv_nu, acc);
+      z[q] = f4(id, q) * acc;
+    }
+    *reinterpret_cast<float4 *>(out + r0) = make_float4(z[0], z[1], z[2], z[3]);
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_jacobi32_two(KSys *sys) {
   KSys &S = sys[blockIdx.y];
   KScal *sc = S.s;
@@ -741,7 +784,8 @@ __global__ void __launch_bounds__(kThreads) k_jacobi32_two(KSys *sys) {
   const int j = sc->i;
   const float inv_nu = (float)(1.0 / sc->nu[j]);
   float *out = S.Z + (long)j * S.ldv;
-  if (S.a32) jacobi_two_rows<float>(S, S.Vf + (long)j * S.ldv, inv_nu, out);
+  if (S.a32 && S.vec4) jacobi_two_rows4(S, S.Vf + (long)j * S.ldv, inv_nu, out);
+  else if (S.a32) jacobi_two_rows<float>(S, S.Vf + (long)j * S.ldv, inv_nu, out);
   else jacobi_two_rows<double>(S, S.V + (long)j * S.ldv, inv_nu, out);
 }
 

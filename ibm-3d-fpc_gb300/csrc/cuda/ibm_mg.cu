@@ -247,6 +247,24 @@ __global__ void k_load_input(T *bv, long n, VecRef in, const double *winv, const
   }
 }
 
+// FP32 hierarchy fed from an FP32 basis: four rows per thread, scale and
+// symmetrizer applied in FP32 (n % 4 == 0, 16-byte aligned source).
+__global__ void k_load_input_f4(float *bv, long n, VecRef in, const float *winvf, const int *gate) {
+  if (gate_off(gate)) return;
+  const long off = in.idx ? (long)(*in.idx) * in.ld : 0;
+  const float sc = in.nu ? (float)(1.0 / in.nu[in.idx ? *in.idx : 0]) : 1.0f;
+  const float *srcf = in.basef + off;
+  for (long r0 = 4 * ((long)blockIdx.x * blockDim.x + threadIdx.x); r0 < n; r0 += 4L * gridDim.x * blockDim.x) {
+    float4 a = *reinterpret_cast<const float4 *>(srcf + r0);
+    a.x *= sc; a.y *= sc; a.z *= sc; a.w *= sc;
+    if (winvf) {
+      const float4 w = *reinterpret_cast<const float4 *>(winvf + r0);
+      a.x *= w.x; a.y *= w.y; a.z *= w.z; a.w *= w.w;
+    }
+    *reinterpret_cast<float4 *>(bv + r0) = a;
+  }
+}
+
 template <class T>
 __global__ void k_store_output(const T *x, long n, OutRef out, const int *gate) {
   if (gate_off(gate)) return;
@@ -833,6 +851,12 @@ void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const flo
                       const MgParams &p, bool fp64, bool fp32, const double *winv) {
   prm = p;
   winv_ = winv;
+  winvf_.release();
+  if (winv) {
+    winvf_.alloc(b.n);
+    LaunchScope ls(K_SETUP, st, 0.0);
+    k_convert<float><<<grid_for(b.n), kThreads, 0, st>>>(winv, winvf_.p, b.n);
+  }
   (void)fp64;
   build<double>(st, L64, b, A7, h);
   L32.clear();
@@ -973,8 +997,13 @@ void Multigrid::apply(cudaStream_t st, const VecRef &in, const OutRef &out, cons
     if (L32.empty()) throw Error(IBM_ERR_STATE, "multigrid: FP32 hierarchy not built");
     MgLevelT<float> &F = L32[0];
     {
-      LaunchScope ls(K_MG_LOAD, st, (winv_ ? 20.0 : 12.0) * F.b.n);
-      k_load_input<float><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, winv_, gate);
+      if (in.basef && F.b.n % 4 == 0 && (in.ld % 4) == 0) {
+        LaunchScope ls(K_MG_LOAD, st, (winv_ ? 12.0 : 8.0) * F.b.n);
+        k_load_input_f4<<<grid_all(F.b.n / 4), kThreads, 0, st>>>(F.bv.p, F.b.n, in, winvf_.p, gate);
+      } else {
+        LaunchScope ls(K_MG_LOAD, st, (winv_ ? 20.0 : 12.0) * F.b.n);
+        k_load_input<float><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, winv_, gate);
+      }
     }
     float *x = vcycle<float>(st, L32, 0, prm, gate);
     LaunchScope ls(K_MG_STORE, st, (4.0 + ob) * F.b.n);

@@ -55,6 +55,7 @@ class Multigrid {
   std::vector<MgLevelT<double>> L64;
   std::vector<MgLevelT<float>> L32;
   const double *winv_ = nullptr;
+  DBuf<float> winvf_;   // FP32 copy of winv_ for the FP32 hierarchy
 };
 
 }  // namespace ibm
