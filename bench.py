@@ -213,6 +213,34 @@ def traffic_for(kernel_name, launch_bytes):
         return None
 
 
+# The reference's solver configuration on the CPU oracle: GMRES + Jacobi for
+# the momentum systems, GMRES + PFMG-style multigrid with its plain rules
+# (weighted-Jacobi relaxation, non-Galerkin 7-point coarse operators, one
+# direction per level), tolerances of the benchmark workload.
+REFERENCE_ORACLE = dict(vel_tol=1e-8, p_tol=1e-8, mg_rap=1, mg_relax=1, mg_omega=2.0 / 3.0, mg_group_ratio=0.0,
+                        mg_options=0)
+
+
+def workload_name(nx, ny, nz):
+    return (f"full timestep {nx}x{ny}x{nz} channel (cylinder D=0.1 at (0.5,0.2)), Um=2.25, nu=1e-3, "
+            f"dt=2e-4, seeded parabolic + 1e-3 N(0,1) initial field")
+
+
+def reduce_max_ms(ms, ws, device):
+    """Max of a per-rank time over all ranks (the slowest replica sets the pace)."""
+    if ws <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(steps, ms_max, ws):
+    """Whole-job steps/s of ws independent replicas that each ran `steps`."""
+    return ws * steps / (ms_max / 1e3)
+
+
 def cpu_baseline(ibm, nx, ny, nz, steps=1):
     """The CPU oracle on a z-slab of the workload (same x-y plane, nz = 8),
     all host threads, scaled to the full grid by the cell count."""
@@ -221,7 +249,7 @@ def cpu_baseline(ibm, nx, ny, nz, steps=1):
     pyoracle.build(with_reference=False)
     nzs = min(CPU_SAMPLE_NZ, nz)
     case = ibm.Case(case_params(ibm, nx, ny, nzs))
-    orc = pyoracle.Oracle(case, vel_tol=1e-8, p_tol=1e-8, mg_rap=1, mg_relax=2, mg_omega=1.0, mg_group_ratio=1.5)
+    orc = pyoracle.Oracle(case, **REFERENCE_ORACLE)
     orc.set_fields(*initial_state(case))
     orc.step(1.0)
     t0 = time.perf_counter()
@@ -230,8 +258,8 @@ def cpu_baseline(ibm, nx, ny, nz, steps=1):
     dt = (time.perf_counter() - t0) / steps
     scale = nz / float(nzs)
     return {"value": 1.0 / (dt * scale), "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{steps} timestep(s) of a {nx}x{ny}x{nzs} z-slab of the same channel, "
-                      f"{dt:.2f} s each, scaled by the cell count ({scale:g}x)"}
+            "sample": f"{steps} timestep(s) of a {nx}x{ny}x{nzs} z-slab of the same channel with the "
+                      f"reference's solver configuration, {dt:.2f} s each, scaled by the cell count ({scale:g}x)"}
 
 
 def reference_arm(args):
@@ -244,7 +272,7 @@ def reference_arm(args):
     pyoracle.build(with_reference=False)
     nzs = min(CPU_SAMPLE_NZ, args.nz)
     case = ibm.Case(case_params(ibm, args.nx, args.ny, nzs))
-    orc = pyoracle.Oracle(case, vel_tol=1e-8, p_tol=1e-8, mg_rap=1, mg_relax=2, mg_omega=1.0, mg_group_ratio=1.5)
+    orc = pyoracle.Oracle(case, **REFERENCE_ORACLE)
     orc.set_fields(*initial_state(case))
     for _ in range(args.warmup):
         orc.step(1.0)
@@ -255,12 +283,15 @@ def reference_arm(args):
     scale = args.nz / float(nzs)
     value = 1.0 / (dt * scale)
     sample = (f"each step: one timestep of a {args.nx}x{args.ny}x{nzs} z-slab of the channel on the CPU "
-              f"oracle (FP64 GMRES + semicoarsening multigrid), scaled by the cell count ({scale:g}x)")
+              f"oracle with the reference's solver configuration (FP64 GMRES + Jacobi, GMRES + PFMG-rule "
+              f"multigrid), scaled by the cell count ({scale:g}x)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * scale * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"full timestep {args.nx}x{args.ny}x{args.nz} channel, Um=2.25, dt=2e-4",
-                       "grid": [args.nx, args.ny, args.nz]},
+            "config": {"workload": workload_name(args.nx, args.ny, args.nz),
+                       "grid": [args.nx, args.ny, args.nz], "parallelism": f"replicas x{ws} (rank 0 runs)",
+                       "solver": "CPU oracle, reference configuration: FP64 GMRES + Jacobi (momentum), "
+                                 "FP64 GMRES + PFMG-rule multigrid (pressure), tol 1e-8"},
             "cpu_baseline": {"value": value, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -349,14 +380,10 @@ def main():
         torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
-    ms = ev0.elapsed_time(ev1)
+    ms = reduce_max_ms(ev0.elapsed_time(ev1), ws, "cuda")
     launches = mixed.launches() - l0
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     ms_per_step = ms / args.steps
-    value = ws * args.steps / (ms / 1e3)
+    value = replica_throughput(args.steps, ms, ws)
 
     # roofline and solve bandwidth from the host-driven pass
     dom, kname, prof, pst, kernel_ms, kernel_gbs, n_prof = profile_pass(mixed, plib, Prof, ibm)
@@ -381,11 +408,10 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
-           "config": {"workload": f"full timestep {nx}x{ny}x{nz} channel (cylinder D=0.1 at (0.5,0.2)), Um=2.25, "
-                                  f"nu=1e-3, dt=2e-4, "
-                                  + ("FP32 Arnoldi cycles with FP64 restarts (FGMRES iterative refinement)"
-                                     if args.precision == 2 else "mixed FP32-preconditioned FP64 FGMRES")
-                                  + ", true FP64 residual tol 1e-8, graph-captured step",
+           "config": {"workload": workload_name(nx, ny, nz),
+                      "solver": ("FP32 Arnoldi cycles with FP64 restarts (FGMRES iterative refinement)"
+                                 if args.precision == 2 else "mixed FP32-preconditioned FP64 FGMRES")
+                                + ", true FP64 residual tol 1e-8, graph-captured step",
                       "precision": args.precision,
                       "grid": [nx, ny, nz], "parallelism": f"replicas x{ws}",
                       "l2": "inputs larger than L2 (operators + fields + Krylov bases, tens of GB resident)",
@@ -408,11 +434,11 @@ def main():
         st64 = [fp64.step(1.0) for _ in range(args.steps)]
         e1.record(s64)
         torch.cuda.synchronize()
-        ms64 = e0.elapsed_time(e1)
+        ms64 = reduce_max_ms(e0.elapsed_time(e1), ws, "cuda")
         f64 = fp64.fields()
         vel_err = max(float(np.abs(a - b).max()) for a, b in zip(mixed_fields[:3], f64[:3])) / float(np.abs(f64[0]).max())
         p_err = float(np.abs(mixed_fields[3] - f64[3]).max() / max(np.abs(f64[3]).max(), 1e-300))
-        out["fp64_plain"] = {"value": ws * args.steps / (ms64 / 1e3), "ms_per_step": ms64 / args.steps,
+        out["fp64_plain"] = {"value": replica_throughput(args.steps, ms64, ws), "ms_per_step": ms64 / args.steps,
                              "phase_ms": phase_means(st64), "iterations_mean": iters_mean(st64),
                              "form": "FP64 throughout, host-driven step"}
         out["speedup_vs_fp64"] = out["fp64_plain"]["ms_per_step"] / ms_per_step
@@ -436,9 +462,10 @@ def main():
             mixed._check(lib.ibm_set_fields(mixed._ctx, *[ptr(t) for t in pinned]))
             mixed.step(1.0)
             mixed._check(lib.ibm_get_fields(mixed._ctx, *[ptr(t) for t in outs]))
-        dt = time.perf_counter() - t0
+        dt_ms = reduce_max_ms((time.perf_counter() - t0) * 1e3, ws, "cuda")
         nbytes = sum(t.numel() * 8 for t in pinned)
-        out["e2e"] = {"value": ws * args.steps / dt, "unit": "steps/s", "h2d_bytes_per_step": nbytes + 8,
+        out["e2e"] = {"value": replica_throughput(args.steps, dt_ms, ws), "unit": "steps/s",
+                      "h2d_bytes_per_step": nbytes + 8,
                       "d2h_bytes_per_step": nbytes + 4 * 40 + 56}
     out["roofline"] = roofline
     out["clocks"] = clk.summary()

@@ -155,7 +155,7 @@ struct KSys {
   double *V;            // basis, vector k at V + k*ldv
   long ldv;
   float *Z;             // flexible basis (FP32), vector k at Z + k*ldv
-  double *w, *x, *r, *z, *z2;
+  double *w, *x, *z, *z2;
   const double *b;
   float *zf, *zf2;      // FP32 work for the inner sweeps
   double *part;         // block partial sums [nblk][kMaxKdim + 2]

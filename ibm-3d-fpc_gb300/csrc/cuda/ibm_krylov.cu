@@ -83,7 +83,6 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
         const double ax = S.x_zero ? 0.0 : stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
         const double bv = S.b[r];
         const double rv = bv - ax;
-        S.r[r] = rv;
         if (S.a32) S.Vf[r] = (float)rv;
         else S.V[r] = rv;
         pb = fma(bv, bv, pb);
@@ -369,7 +368,6 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
         int i, j, k;
         sys_ijk(r, S, i, j, k);
         const double rv = S.b[r] - stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
-        S.r[r] = rv;
         if (S.a32) S.Vf[r] = (float)rv;
         else S.V[r] = rv;
         pr = fma(rv, rv, pr);
@@ -884,7 +882,6 @@ void Krylov::configure(int nsys_, const KSysHost *hs) {
       sl.V.alloc((size_t)(h.kdim + 1) * h.n);
       sl.w.alloc(h.n);
     }
-    sl.r.alloc(h.n);
     if (h.pc == 1) { sl.z.alloc(h.n); sl.z2.alloc(h.n); }
     if (h.pc == 2) {
       sl.Z.alloc((size_t)h.kdim * h.n);
@@ -902,7 +899,7 @@ size_t Krylov::bytes() const {
   size_t b = 0;
   for (int s = 0; s < nsys; ++s) {
     const Slot &sl = slot[s];
-    b += sl.V.bytes() + sl.w.bytes() + sl.r.bytes() + sl.z.bytes() + sl.z2.bytes() + sl.part.bytes() +
+    b += sl.V.bytes() + sl.w.bytes() + sl.z.bytes() + sl.z2.bytes() + sl.part.bytes() +
          sl.Z.bytes() + sl.zf.bytes() + sl.zf2.bytes();
   }
   return b;
@@ -925,7 +922,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     k.A = h.A; k.Ar = h.Ar; k.invd = h.invd; k.Af = h.Af; k.invdf = h.invdf; k.Ajf = h.Ajf;
     k.V = slot[s].V.p; k.ldv = h.n;
     k.Z = slot[s].Z.p;
-    k.w = slot[s].w.p; k.r = slot[s].r.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;
+    k.w = slot[s].w.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;
     k.zf = slot[s].zf.p; k.zf2 = slot[s].zf2.p;
     k.Vf = slot[s].Vf.p; k.wf = slot[s].wf.p; k.a32 = h.a32;
     k.x_zero = x_zero ? 1 : 0;
@@ -1095,7 +1092,7 @@ void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, co
   double all_rows = 0.0;
   for (int s = 0; s < nsys; ++s) all_rows += ((mask >> s) & 1u) ? (double)slot[s].host.n : 0.0;
   {
-    LaunchScope ls(K_GM_INIT, st, (x_zero ? 24.0 : 88.0) * all_rows);
+    LaunchScope ls(K_GM_INIT, st, (x_zero ? 16.0 : 80.0) * all_rows);
     k_init<<<grid, kThreads, 0, st>>>(dsys.p, nsys);
   }
   for (long guard = 0;; ++guard) {

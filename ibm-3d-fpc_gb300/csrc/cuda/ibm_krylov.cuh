@@ -77,7 +77,7 @@ class Krylov {
  private:
   struct Slot {
     KSysHost host;
-    DBuf<double> V, w, r, z, z2, part;
+    DBuf<double> V, w, z, z2, part;
     DBuf<float> Z, zf, zf2, Vf, wf;
   };
   void read_flags(cudaStream_t st);
