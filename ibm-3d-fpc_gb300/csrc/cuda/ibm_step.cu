@@ -52,7 +52,21 @@ struct KnownDiv {
 __device__ __forceinline__ double div_known(double x, KnownDiv k) {
   const double q0 = __dmul_rn(x, k.rb);
   const double r = fma(-q0, k.b, x);
-  return (r == 0.0 || !isfinite(r)) ? q0 : fma(r, k.rb, q0);
+  // r == 0 or r not finite, tested on the bits (integer pipe; FP64 compares
+  // would take FP64 issue slots, the scarce resource of this kernel)
+  const unsigned long long rb = (unsigned long long)__double_as_longlong(r);
+  const bool keep = (rb << 1) == 0ull || (rb & 0x7FF0000000000000ull) == 0x7FF0000000000000ull;
+  return keep ? q0 : fma(r, k.rb, q0);
+}
+
+// 0.25 x, exactly: for |x| >= 2^-1020 the product only lowers the exponent
+// by two, done on the bits; zeros, subnormal-range and non-finite values take
+// the FP64 multiply (same result either way).
+__device__ __forceinline__ double quarter(double x) {
+  const long long b = __double_as_longlong(x);
+  const long long e = b & 0x7FF0000000000000LL;
+  if (e > (2LL << 52) && e != 0x7FF0000000000000LL) return __longlong_as_double(b - (2LL << 52));
+  return __dmul_rn(0.25, x);
 }
 
 // Centred advective term, separately rounded operations in the reference's order.
@@ -64,7 +78,7 @@ __device__ __forceinline__ double advect(double c, double dm, double dp, KnownDi
   return __dadd_rn(__dadd_rn(t1, t2), t3);
 }
 __device__ __forceinline__ double avg4(double a, double b, double c, double d) {
-  return __dmul_rn(0.25, __dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d));
+  return quarter(__dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d));
 }
 // ((rho/dt) u - rho conv - gp + bc) * scale, each operation rounded.
 __device__ __forceinline__ double mom_rhs(double a, double rho, double uc, double conv, double gp, double bc,

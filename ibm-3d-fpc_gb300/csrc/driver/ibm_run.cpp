@@ -24,6 +24,8 @@ struct Options {
   ibm_solver_params sp;
   int checkpoint_every = 0;
   std::string checkpoint_prefix = "ibm_state";
+  std::string restart;      // checkpoint file to resume from (its step + 1 is the first step run)
+  std::string case_cache;   // case cache file (ibm_case_build_cached)
 };
 
 bool arg(int &a, int argc, char **argv, const char *name) { return !std::strcmp(argv[a], name) && a + 1 < argc; }
@@ -74,6 +76,8 @@ void parse(int argc, char **argv, Options &o) {
     else if (arg(a, argc, argv, "-vel-inner-sweeps")) o.sp.vel_inner_sweeps = std::atoi(argv[++a]);
     else if (arg(a, argc, argv, "-checkpoint-every")) o.checkpoint_every = std::atoi(argv[++a]);
     else if (arg(a, argc, argv, "-checkpoint")) o.checkpoint_prefix = argv[++a];
+    else if (arg(a, argc, argv, "-restart")) o.restart = argv[++a];
+    else if (arg(a, argc, argv, "-case-cache")) o.case_cache = argv[++a];
   }
 }
 
@@ -99,7 +103,8 @@ int main(int argc, char **argv) {
 
   const auto t_setup0 = std::chrono::steady_clock::now();
   ibm_case *cs = nullptr;
-  if (ibm_case_build(&o.cp, &cs) != 0) {
+  if (o.case_cache.empty() ? ibm_case_build(&o.cp, &cs) != 0
+                           : ibm_case_build_cached(&o.cp, o.case_cache.c_str(), &cs) != 0) {
     std::fprintf(stderr, "case setup failed (bad parameters)\n");
     return 1;
   }
@@ -136,6 +141,25 @@ int main(int argc, char **argv) {
   const double *uin = arr<double>(cs, "uin");
   for (int k = 0; k < nz; ++k)
     for (int j = 0; j < ny; ++j) u[((size_t)k * ny + j) * (nx + 1)] = uin[(size_t)j + (size_t)ny * k];
+  int first_step = 1;
+  if (!o.restart.empty()) {
+    // checkpoint layout: int nx, ny, nz, step; double ramp; u, v, w, p
+    std::FILE *f = std::fopen(o.restart.c_str(), "rb");
+    int hdr[4] = {0, 0, 0, 0};
+    double ramp0 = 0.0;
+    bool ok = f && std::fread(hdr, sizeof(int), 4, f) == 4 && std::fread(&ramp0, sizeof(double), 1, f) == 1 &&
+              hdr[0] == nx && hdr[1] == ny && hdr[2] == nz && hdr[3] >= 0 &&
+              std::fread(u.data(), sizeof(double), u.size(), f) == u.size() &&
+              std::fread(v.data(), sizeof(double), v.size(), f) == v.size() &&
+              std::fread(w.data(), sizeof(double), w.size(), f) == w.size() &&
+              std::fread(p.data(), sizeof(double), p.size(), f) == p.size();
+    if (f) std::fclose(f);
+    if (!ok) {
+      std::fprintf(stderr, "restart: %s is not a checkpoint of a %d x %d x %d grid\n", o.restart.c_str(), nx, ny, nz);
+      return 1;
+    }
+    first_step = hdr[3] + 1;
+  }
   if (ibm_set_fields(ctx, u.data(), v.data(), w.data(), p.data())) return fail("ibm_set_fields", ctx);
   const double setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_setup0).count();
 
@@ -159,7 +183,7 @@ int main(int argc, char **argv) {
   double t_rhs = 0, t_mom = 0, t_p = 0, t_total = 0;
   const auto t0 = std::chrono::steady_clock::now();
   int rc_final = 0;
-  for (int step = 1; step <= o.nsteps; ++step) {
+  for (int step = first_step; step <= o.nsteps; ++step) {
     const double ramp = std::min(1.0, (double)step / (double)o.inlet_ramp_steps);
     ibm_step_stats st;
     const int rc = ibm_step(ctx, ramp, &st);
@@ -195,7 +219,7 @@ int main(int argc, char **argv) {
   std::printf("momentum solve time    : %.6e s\n", t_mom * 1e-3);
   std::printf("pressure solve time    : %.6e s\n", t_p * 1e-3);
   std::printf("total wall time        : %.6e s\n", wall);
-  std::printf("steps/s                : %.3f\n", o.nsteps / std::max(wall, 1e-12));
+  std::printf("steps/s                : %.3f\n", (o.nsteps - first_step + 1) / std::max(wall, 1e-12));
   std::printf("kernel launches        : %lld\n", ibm_kernel_launches(ctx));
   std::printf("============================================================\n");
   ibm_destroy(ctx);
