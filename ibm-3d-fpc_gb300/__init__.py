@@ -220,10 +220,19 @@ class Solver:
         return out
 
 
+def force_coefficients(force, params: CaseParams):
+    """Drag and lift coefficients of the benchmark channel (Schaefer and Turek
+    1996, 3D case with a full-height cylinder): c = 2 F / (rho U^2 D H) with
+    the mean inflow velocity U = 4 Um / 9, D = 2 Rcirc, H = Lz."""
+    u_mean = 4.0 * params.Um / 9.0
+    scale = 2.0 / (params.rho * u_mean * u_mean * 2.0 * params.Rcirc * params.Lz)
+    return force[0] * scale, force[1] * scale
+
+
 def stats_dict(st: StepStats) -> dict:
     d = {"ramp": st.ramp, "div_l2": st.div_l2, "umax": st.umax, "vmax": st.vmax, "wmax": st.wmax,
          "status": st.status, "t_total_ms": st.t_total_ms, "t_rhs_ms": st.t_rhs_ms, "t_mom_ms": st.t_mom_ms,
-         "t_p_ms": st.t_p_ms, "t_proj_ms": st.t_proj_ms}
+         "t_p_ms": st.t_p_ms, "t_proj_ms": st.t_proj_ms, "force": tuple(st.force)}
     for f in ("u", "v", "w", "p"):
         s = getattr(st, f)
         d[f"its_{f}"] = s.iters

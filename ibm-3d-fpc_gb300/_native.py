@@ -52,7 +52,7 @@ class SolverParams(C.Structure):
                 ("mg_coarse_max", C.c_int), ("mg_max_levels", C.c_int),
                 ("use_zero_initial_guess", C.c_int), ("precision", C.c_int), ("use_graph", C.c_int),
                 ("vel_inner_sweeps", C.c_int), ("mg_group_ratio", C.c_double), ("mg_options", C.c_int),
-                ("mg_nu_coarse", C.c_int), ("cycle_rtol32", C.c_double)]
+                ("mg_nu_coarse", C.c_int), ("cycle_rtol32", C.c_double), ("compute_forces", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -64,7 +64,8 @@ class StepStats(C.Structure):
                 ("p", SolveStats), ("div_l2", C.c_double), ("umax", C.c_double),
                 ("vmax", C.c_double), ("wmax", C.c_double),
                 ("t_rhs_ms", C.c_double), ("t_mom_ms", C.c_double), ("t_p_ms", C.c_double),
-                ("t_proj_ms", C.c_double), ("t_total_ms", C.c_double), ("status", C.c_int)]
+                ("t_proj_ms", C.c_double), ("t_total_ms", C.c_double), ("status", C.c_int),
+                ("force", C.c_double * 3)]
 
 
 _host = None

@@ -351,6 +351,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->mg_options = 3;
   p->mg_nu_coarse = 0;
   p->cycle_rtol32 = 1e-5;
+  p->compute_forces = 0;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -833,6 +834,8 @@ int ibm_step(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
       fill_solve(stats->p, rp[0]);
       stats->div_l2 = std::sqrt(dg.div2 / std::max(1, c->np_active));
       stats->umax = dg.umax; stats->vmax = dg.vmax; stats->wmax = dg.wmax;
+      if (c->prm.compute_forces)
+        for (int q = 0; q < 3; ++q) stats->force[q] = dg.force[q];
       float ms;
       cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); stats->t_rhs_ms = ms;
       cudaEventElapsedTime(&ms, c->ev[2], c->ev[5]); stats->t_rhs_ms += ms;

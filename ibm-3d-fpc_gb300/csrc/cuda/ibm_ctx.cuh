@@ -19,6 +19,9 @@ struct StepDiag {                // written by the diagnostics kernel
   int nonfinite_mom, nonfinite_p;
   unsigned ticket;
   int pad;
+  double force[3];               // force of the fluid on the body (k_forces)
+  unsigned fticket;
+  int pad2;
 };
 
 struct Geometry {

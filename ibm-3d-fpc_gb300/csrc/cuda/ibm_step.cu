@@ -605,6 +605,122 @@ void launch_pressure_rhs(ibm_ctx *c) {
   k_pressure_rhs<<<blocks_for(c->g.NP), kThreads, 0, c->st>>>(A);
 }
 
+// ------------------------------------------------------------------ forces
+// Force of the fluid on the body (the reference computes none), from the
+// end-of-step fields on the staircase of solid cells (non-fluid cells):
+//  - pressure: a fluid cell next to a solid cell pushes the body with p times
+//    the shared face's area, along the direction from the fluid cell into it;
+//  - shear: a face velocity between two fluid cells whose two neighbours
+//    across a coordinate direction are solid sees a no-slip wall half a cell
+//    away: stress 2 rho nu u / h on the face's area in that direction.
+// Each cell adds its own terms in a fixed order (pressure x, y, z; then the
+// u, v, w faces on its lower side); blocks sum in a fixed order.
+struct ForceArgs {
+  Dims d;
+  const double *u, *v, *w, *p;
+  const uint8_t *fc;
+  double dx, dy, dz, rho_nu2;   // rho_nu2 = 2 rho nu
+  double *part;
+  StepDiag *dg;
+};
+
+__device__ __forceinline__ void cell_force(const ForceArgs &A, long c, double f[3]) {
+  const Dims &d = A.d;
+  const int i = (int)(c % d.nx);
+  const long q = c / d.nx;
+  const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+  const long sy = d.nx, sz = (long)d.nx * d.ny;
+  auto solid = [&](int ii, int jj, int kk) {
+    return ii >= 0 && ii < d.nx && jj >= 0 && jj < d.ny && kk >= 0 && kk < d.nz &&
+           !(A.fc[((long)kk * d.ny + jj) * d.nx + ii] & kFluid);
+  };
+  auto fluid = [&](int ii, int jj, int kk) { return (A.fc[((long)kk * d.ny + jj) * d.nx + ii] & kFluid) != 0; };
+  const double ax = A.dy * A.dz, ay = A.dx * A.dz, az = A.dx * A.dy;
+  const double pc = A.p[c];
+  if (solid(i + 1, j, k)) f[0] += pc * ax;
+  if (solid(i - 1, j, k)) f[0] -= pc * ax;
+  if (solid(i, j + 1, k)) f[1] += pc * ay;
+  if (solid(i, j - 1, k)) f[1] -= pc * ay;
+  if (solid(i, j, k + 1)) f[2] += pc * az;
+  if (solid(i, j, k - 1)) f[2] -= pc * az;
+  (void)sy; (void)sz;
+  // u face on the lower x side, between cells i-1 and i
+  if (i > 0 && fluid(i - 1, j, k)) {
+    const double uf = A.u[U3(d, i, j, k)];
+    const double t = A.rho_nu2 * uf;
+    if (solid(i - 1, j + 1, k) && solid(i, j + 1, k)) f[0] += t * A.dx * A.dz / A.dy;
+    if (solid(i - 1, j - 1, k) && solid(i, j - 1, k)) f[0] += t * A.dx * A.dz / A.dy;
+    if (solid(i - 1, j, k + 1) && solid(i, j, k + 1)) f[0] += t * A.dx * A.dy / A.dz;
+    if (solid(i - 1, j, k - 1) && solid(i, j, k - 1)) f[0] += t * A.dx * A.dy / A.dz;
+  }
+  if (j > 0 && fluid(i, j - 1, k)) {
+    const double vf = A.v[V3(d, i, j, k)];
+    const double t = A.rho_nu2 * vf;
+    if (solid(i + 1, j - 1, k) && solid(i + 1, j, k)) f[1] += t * A.dy * A.dz / A.dx;
+    if (solid(i - 1, j - 1, k) && solid(i - 1, j, k)) f[1] += t * A.dy * A.dz / A.dx;
+    if (solid(i, j - 1, k + 1) && solid(i, j, k + 1)) f[1] += t * A.dx * A.dy / A.dz;
+    if (solid(i, j - 1, k - 1) && solid(i, j, k - 1)) f[1] += t * A.dx * A.dy / A.dz;
+  }
+  if (k > 0 && fluid(i, j, k - 1)) {
+    const double wf = A.w[W3(d, i, j, k)];
+    const double t = A.rho_nu2 * wf;
+    if (solid(i + 1, j, k - 1) && solid(i + 1, j, k)) f[2] += t * A.dz * A.dy / A.dx;
+    if (solid(i - 1, j, k - 1) && solid(i - 1, j, k)) f[2] += t * A.dz * A.dy / A.dx;
+    if (solid(i, j + 1, k - 1) && solid(i, j + 1, k)) f[2] += t * A.dz * A.dx / A.dy;
+    if (solid(i, j - 1, k - 1) && solid(i, j - 1, k)) f[2] += t * A.dz * A.dx / A.dy;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_forces(ForceArgs A) {
+  const long NP = (long)A.d.nx * A.d.ny * A.d.nz;
+  double f[3] = {0.0, 0.0, 0.0};
+  for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < NP; c += (long)gridDim.x * blockDim.x)
+    if (A.fc[c] & kFluid) cell_force(A, c, f);
+  __shared__ double s[3][kWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int q = 0; q < 3; ++q) {
+    const double t = warp_sum(f[q]);
+    if (lane == 0) s[q][warp] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 3; ++q) {
+      double a = 0.0;
+      for (int w = 0; w < kWarps; ++w) a += s[q][w];
+      A.part[3 * blockIdx.x + q] = a;
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  __shared__ int last;
+  if (threadIdx.x == 0) last = (atomicAdd(&A.dg->fticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 3; ++q) {
+      double a = 0.0;
+      for (int b = 0; b < (int)gridDim.x; ++b) a += A.part[3 * b + q];
+      A.dg->force[q] = a;
+    }
+    A.dg->fticket = 0;
+  }
+}
+
+void launch_forces(ibm_ctx *c) {
+  ForceArgs A;
+  A.d = dims_of(c);
+  A.u = c->u.p; A.v = c->v.p; A.w = c->w.p; A.p = c->p.p;
+  A.fc = c->fc.p;
+  A.dx = c->g.dx; A.dy = c->g.dy; A.dz = c->g.dz;
+  A.rho_nu2 = 2.0 * c->g.rho * c->g.nu;
+  A.part = c->part.p;
+  A.dg = c->diag.p;
+  const int nb = std::min(blocks_for(c->g.NP), 1024);
+  LaunchScope ls(K_DIAG, c->st, 4.0 * 8.0 * c->g.NP + 7.0 * c->g.NP);
+  k_forces<<<nb, kThreads, 0, c->st>>>(A);
+}
+
 void launch_projection(ibm_ctx *c) {
   ProjArgs A;
   A.d = dims_of(c);
@@ -632,8 +748,11 @@ void launch_projection(ibm_ctx *c) {
   D.part = c->part.p;
   D.dg = c->diag.p;
   D.np_active = c->np_active;
-  LaunchScope ls(K_DIAG, c->st, 33.0 * faces + 65.0 * c->g.NP);
-  k_diagnostics<<<nb, kThreads, 0, c->st>>>(D);
+  {
+    LaunchScope ls(K_DIAG, c->st, 33.0 * faces + 65.0 * c->g.NP);
+    k_diagnostics<<<nb, kThreads, 0, c->st>>>(D);
+  }
+  if (c->prm.compute_forces) launch_forces(c);
 }
 
 }  // namespace ibm

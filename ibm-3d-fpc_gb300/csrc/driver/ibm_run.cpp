@@ -77,6 +77,7 @@ void parse(int argc, char **argv, Options &o) {
     else if (arg(a, argc, argv, "-checkpoint-every")) o.checkpoint_every = std::atoi(argv[++a]);
     else if (arg(a, argc, argv, "-checkpoint")) o.checkpoint_prefix = argv[++a];
     else if (arg(a, argc, argv, "-restart")) o.restart = argv[++a];
+    else if (arg(a, argc, argv, "-forces")) o.sp.compute_forces = std::atoi(argv[++a]);
     else if (arg(a, argc, argv, "-case-cache")) o.case_cache = argv[++a];
   }
 }
@@ -193,10 +194,17 @@ int main(int argc, char **argv) {
       break;
     }
     t_rhs += st.t_rhs_ms; t_mom += st.t_mom_ms; t_p += st.t_p_ms; t_total += st.t_total_ms;
-    if (step == 1 || step == o.nsteps || (o.print_every > 0 && step % o.print_every == 0))
-      std::printf("%4d  %.6f  %.6e  %.6e  %.6e  %.6e  (%d,%d,%d,%d)  (%.3e,%.3e,%.3e,%.3e)\n", step, ramp, st.umax,
+    if (step == 1 || step == o.nsteps || (o.print_every > 0 && step % o.print_every == 0)) {
+      std::printf("%4d  %.6f  %.6e  %.6e  %.6e  %.6e  (%d,%d,%d,%d)  (%.3e,%.3e,%.3e,%.3e)", step, ramp, st.umax,
                   st.vmax, st.wmax, st.div_l2, st.u.iters, st.v.iters, st.w.iters, st.p.iters, st.u.rel_res,
                   st.v.rel_res, st.w.rel_res, st.p.rel_res);
+      if (o.sp.compute_forces) {
+        // drag / lift coefficients of the benchmark channel: 2 F / (rho U^2 D H), U = 4 Um / 9
+        const double um = 4.0 * o.cp.Um / 9.0, sc = 2.0 / (o.cp.rho * um * um * 2.0 * o.cp.Rcirc * o.cp.Lz);
+        std::printf("  cD %.5f cL %.5f", st.force[0] * sc, st.force[1] * sc);
+      }
+      std::printf("\n");
+    }
     if (o.checkpoint_every > 0 && step % o.checkpoint_every == 0) {
       ibm_get_fields(ctx, u.data(), v.data(), w.data(), p.data());
       const std::string fn = o.checkpoint_prefix + "_" + std::to_string(step) + ".bin";

@@ -95,6 +95,7 @@ typedef struct ibm_solver_params {
   double cycle_rtol32;   /* precision 2: an FP32 Arnoldi cycle stops once its residual estimate fell by
                             this factor (default 1e-5, about what an FP32 basis resolves); the FP64
                             restart then measures the true residual */
+  int compute_forces;    /* 1: fill ibm_step_stats.force each step (one extra kernel); default 0 */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {
@@ -110,6 +111,12 @@ typedef struct ibm_step_stats {
   double div_l2, umax, vmax, wmax;
   double t_rhs_ms, t_mom_ms, t_p_ms, t_proj_ms, t_total_ms;
   int status;
+  /* Force of the fluid on the body (x, y, z) from the end-of-step fields when
+   * ibm_solver_params.compute_forces is set (the reference computes none):
+   * pressure on the faces shared by fluid and non-fluid cells, and wall shear
+   * 2 rho nu u / h on face velocities whose neighbours across a direction are
+   * non-fluid (a staircase of the body, first order in h). Else 0. */
+  double force[3];
 } ibm_step_stats;
 
 typedef struct ibm_ctx ibm_ctx;

@@ -982,7 +982,61 @@ void oracle_projection(oracle *o, const double *ut, const double *vt, const doub
   for (long f = 0; f < NV; ++f) vm = fmax(vm, fabs(o->v[f]));
   for (long f = 0; f < NW; ++f) wm = fmax(wm, fabs(o->w[f]));
   st->umax = um; st->vmax = vm; st->wmax = wm;
+  oracle_forces(o, st->force);
   free(phi); free(gphi); free(q); free(dv); free(uin);
+}
+
+/* Force of the fluid on the body from the end-of-step fields on the staircase
+ * of non-fluid cells (the reference computes none; the library's k_forces
+ * uses the same definition): pressure p times the shared face area on every
+ * fluid/non-fluid cell pair, towards the non-fluid cell; wall shear
+ * 2 rho nu u / h times the face area on every face velocity between two fluid
+ * cells whose two neighbours across a direction are non-fluid. */
+static int o_fluid(const oracle *o, int i, int j, int k) {
+  const long c = ((long)k * o->ny + j) * o->nx + i;
+  return o->in.fluid_p[c] && o->in.id_p[c] > 0;
+}
+static int o_solid(const oracle *o, int i, int j, int k) {
+  return i >= 0 && i < o->nx && j >= 0 && j < o->ny && k >= 0 && k < o->nz && !o_fluid(o, i, j, k);
+}
+void oracle_forces(const oracle *o, double f[3]) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const double dx = o->dx, dy = o->dy, dz = o->dz, t2 = 2.0 * o->prm.rho * o->prm.nu;
+  const double ax = dy * dz, ay = dx * dz, az = dx * dy;
+  f[0] = f[1] = f[2] = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        if (!o_fluid(o, i, j, k)) continue;
+        const double pc = o->p[((long)k * ny + j) * nx + i];
+        if (o_solid(o, i + 1, j, k)) f[0] += pc * ax;
+        if (o_solid(o, i - 1, j, k)) f[0] -= pc * ax;
+        if (o_solid(o, i, j + 1, k)) f[1] += pc * ay;
+        if (o_solid(o, i, j - 1, k)) f[1] -= pc * ay;
+        if (o_solid(o, i, j, k + 1)) f[2] += pc * az;
+        if (o_solid(o, i, j, k - 1)) f[2] -= pc * az;
+        if (i > 0 && o_fluid(o, i - 1, j, k)) {
+          const double t = t2 * o->u[((long)k * ny + j) * (nx + 1) + i];
+          if (o_solid(o, i - 1, j + 1, k) && o_solid(o, i, j + 1, k)) f[0] += t * dx * dz / dy;
+          if (o_solid(o, i - 1, j - 1, k) && o_solid(o, i, j - 1, k)) f[0] += t * dx * dz / dy;
+          if (o_solid(o, i - 1, j, k + 1) && o_solid(o, i, j, k + 1)) f[0] += t * dx * dy / dz;
+          if (o_solid(o, i - 1, j, k - 1) && o_solid(o, i, j, k - 1)) f[0] += t * dx * dy / dz;
+        }
+        if (j > 0 && o_fluid(o, i, j - 1, k)) {
+          const double t = t2 * o->v[((long)k * (ny + 1) + j) * nx + i];
+          if (o_solid(o, i + 1, j - 1, k) && o_solid(o, i + 1, j, k)) f[1] += t * dy * dz / dx;
+          if (o_solid(o, i - 1, j - 1, k) && o_solid(o, i - 1, j, k)) f[1] += t * dy * dz / dx;
+          if (o_solid(o, i, j - 1, k + 1) && o_solid(o, i, j, k + 1)) f[1] += t * dx * dy / dz;
+          if (o_solid(o, i, j - 1, k - 1) && o_solid(o, i, j, k - 1)) f[1] += t * dx * dy / dz;
+        }
+        if (k > 0 && o_fluid(o, i, j, k - 1)) {
+          const double t = t2 * o->w[((long)k * ny + j) * nx + i];
+          if (o_solid(o, i + 1, j, k - 1) && o_solid(o, i + 1, j, k)) f[2] += t * dz * dy / dx;
+          if (o_solid(o, i - 1, j, k - 1) && o_solid(o, i - 1, j, k)) f[2] += t * dz * dy / dx;
+          if (o_solid(o, i, j + 1, k - 1) && o_solid(o, i, j + 1, k)) f[2] += t * dz * dx / dy;
+          if (o_solid(o, i, j - 1, k - 1) && o_solid(o, i, j - 1, k)) f[2] += t * dz * dx / dy;
+        }
+      }
 }
 
 static int all_finite(const double *x, long n) {

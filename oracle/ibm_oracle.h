@@ -62,6 +62,7 @@ typedef struct oracle_step_stats {
   oracle_solve_stats u, v, w, p;
   double div_l2, umax, vmax, wmax;
   int status;
+  double force[3];   /* force of the fluid on the body, staircase definition (see oracle_forces) */
 } oracle_step_stats;
 
 typedef struct oracle oracle;
@@ -72,6 +73,8 @@ void oracle_destroy(oracle *o);
 void oracle_set_fields(oracle *o, const double *u, const double *v, const double *w, const double *p);
 void oracle_get_fields(const oracle *o, double *u, double *v, double *w, double *p);
 int oracle_step(oracle *o, double ramp, oracle_step_stats *st);
+/* Force of the fluid on the body from the current fields (the step fills st->force). */
+void oracle_forces(const oracle *o, double f[3]);
 
 /* Pieces of the step, for kernel-level checks. */
 void oracle_bc_cleanup(const oracle *o, double *u, double *v, double *w, const double *uin_step);

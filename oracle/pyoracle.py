@@ -53,7 +53,8 @@ class OSolve(C.Structure):
 
 class OStep(C.Structure):
     _fields_ = [("u", OSolve), ("v", OSolve), ("w", OSolve), ("p", OSolve), ("div_l2", C.c_double),
-                ("umax", C.c_double), ("vmax", C.c_double), ("wmax", C.c_double), ("status", C.c_int)]
+                ("umax", C.c_double), ("vmax", C.c_double), ("wmax", C.c_double), ("status", C.c_int),
+                ("force", C.c_double * 3)]
 
 
 _lib = None
@@ -72,6 +73,7 @@ def lib() -> C.CDLL:
         L.oracle_set_fields.argtypes = [vp, vp, vp, vp, vp]
         L.oracle_get_fields.argtypes = [vp, vp, vp, vp, vp]
         L.oracle_step.argtypes = [vp, d, C.POINTER(OStep)]
+        L.oracle_forces.argtypes = [vp, vp]
         L.oracle_bc_cleanup.argtypes = [vp, vp, vp, vp, vp]
         L.oracle_convection.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.oracle_momentum_rhs.argtypes = [vp] + [vp] * 7
@@ -134,6 +136,12 @@ class Oracle:
     def fields(self):
         out = [np.empty(n) for n in self.sizes()]
         self.L.oracle_get_fields(self.h, *[_p(x) for x in out])
+        return out
+
+    def forces(self):
+        """Force of the fluid on the body from the current fields."""
+        out = np.zeros(3)
+        self.L.oracle_forces(self.h, _p(out))
         return out
 
     def step(self, ramp: float) -> OStep:

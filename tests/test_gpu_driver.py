@@ -42,7 +42,7 @@ def test_restart_reproduces_uninterrupted_run(tmp_path):
     resumed = tmp_path / "resumed"
     resumed.mkdir()
     log = _run(resumed, "-checkpoint", "b", "-restart", str(full / "a_3.bin"), "-case-cache", str(tmp_path / "case.bin"))
-    steps = [int(l.split()[0]) for l in log.splitlines() if l[:4].strip().isdigit() and len(l.split()) > 8]
+    steps = [int(l.split()[0]) for l in log.splitlines() if l[:4].strip().isdigit() and l.count("(") == 2]
     assert steps and steps[0] == 4  # the resumed run starts after the checkpoint
     h6a, fa = _fields(full / "a_6.bin")
     h6b, fb = _fields(resumed / "b_6.bin")

@@ -215,6 +215,22 @@ def test_fp32_cycles_reach_tight_tolerance(ibm, pyoracle, case48):
         assert rel_err(a, b) <= 1e-9, name
 
 
+def test_forces_match_oracle(ibm, pyoracle, case48):
+    """Body force (staircase pressure + wall shear) of the device step equals
+    the oracle's on the same fields; off by default."""
+    s = ibm.Solver(case48, tight(ibm, compute_forces=1))
+    orc = pyoracle.Oracle(case48, vel_tol=1e-13, p_tol=1e-13)
+    for step in range(1, 5):
+        st = s.step(min(1.0, step / 2.0))
+        so = orc.step(min(1.0, step / 2.0))
+    fo = np.array(so.force)
+    fg = np.array(st.force)
+    assert np.abs(fg - fo).max() <= 1e-9 * np.abs(fo).max()
+    assert fo[0] > 0  # the flow drags the cylinder downstream
+    s.set_params(tight(ibm, compute_forces=0))
+    assert tuple(s.step(1.0).force) == (0.0, 0.0, 0.0)
+
+
 def test_not_converged_is_a_warning(ibm, case32):
     s = ibm.Solver(case32, ibm.solver_params(vel_tol=1e-14, p_tol=1e-14, vel_maxit=1, p_maxit=1))
     st = s.step(1.0)

@@ -278,3 +278,23 @@ def test_step_properties(case32, pyoracle):
     assert np.all(v.reshape(nz, ny + 1, nx)[:, [0, ny], :] == 0)
     assert np.all(w.reshape(nz + 1, ny, nx)[[0, nz], :, :] == 0)
     assert np.all(p.reshape(-1)[case32.array("fluid_p") == 0] == 0)
+
+
+def test_forces_of_a_closed_body(case32, pyoracle):
+    """Staircase force definition: a uniform pressure on a closed body and
+    still fluid give no net force; the pressure force is linear in p."""
+    orc = pyoracle.Oracle(case32)
+    nx, ny, nz = case32.shape
+    fl = (case32.array("fluid_p") > 0) & (case32.array("id_p") > 0)
+    zu, zv, zw = np.zeros((nx + 1) * ny * nz), np.zeros(nx * (ny + 1) * nz), np.zeros(nx * ny * (nz + 1))
+    orc.set_fields(zu, zv, zw, np.where(fl, 3.0, 0.0))
+    assert np.abs(orc.forces()).max() <= 1e-12
+    rng = np.random.default_rng(4)
+    p1, p2 = rng.standard_normal(nx * ny * nz) * fl, rng.standard_normal(nx * ny * nz) * fl
+    orc.set_fields(zu, zv, zw, p1)
+    f1 = orc.forces()
+    orc.set_fields(zu, zv, zw, p2)
+    f2 = orc.forces()
+    orc.set_fields(zu, zv, zw, 2.0 * p1 + p2)
+    assert np.allclose(orc.forces(), 2.0 * f1 + f2, rtol=1e-12, atol=1e-14)
+    assert np.abs(f1).max() > 0
