@@ -33,7 +33,7 @@ def pyoracle():
 
 def gpu_available() -> bool:
     try:
-        import torch  # noqa: F401  (only to ask the driver whether a GPU exists)
+        import torch  # noqa: F401  (only to ask the CUDA driver whether a GPU exists)
         return torch.cuda.is_available()
     except Exception:
         return False
