@@ -208,6 +208,15 @@ class Solver:
     def launches(self) -> int:
         return int(self._lib.ibm_kernel_launches(self._ctx))
 
+    def profile_reset(self) -> None:
+        self._check(self._lib.ibm_profile_reset(self._ctx))
+
+    def profile(self) -> "_native.Profile":
+        """Launch accounting since the last profile_reset (ibm_profile)."""
+        p = _native.Profile()
+        self._check(self._lib.ibm_profile_get(self._ctx, C.byref(p)))
+        return p
+
     def run(self, nsteps: int, ramp_steps: int = 200, start: int = 1, callback=None):
         """The reference's step loop (main.cu:249-251): ramp = min(1, step/ramp_steps)."""
         out = []
@@ -218,6 +227,18 @@ class Solver:
             if callback:
                 callback(step, st)
         return out
+
+
+def kernel_names() -> list:
+    """Names of the kernel classes of ibm_profile, in index order."""
+    lib = _native.gpu()
+    out = []
+    for k in range(64):
+        name = lib.ibm_kernel_name(k).decode()
+        out.append(name)
+        if name == "setup":
+            return out
+    return out
 
 
 def force_coefficients(force, params: CaseParams):

@@ -52,7 +52,15 @@ class SolverParams(C.Structure):
                 ("mg_coarse_max", C.c_int), ("mg_max_levels", C.c_int),
                 ("use_zero_initial_guess", C.c_int), ("precision", C.c_int), ("use_graph", C.c_int),
                 ("vel_inner_sweeps", C.c_int), ("mg_group_ratio", C.c_double), ("mg_options", C.c_int),
-                ("mg_nu_coarse", C.c_int), ("cycle_rtol32", C.c_double), ("compute_forces", C.c_int)]
+                ("mg_nu_coarse", C.c_int), ("cycle_rtol32", C.c_double), ("compute_forces", C.c_int),
+                ("row_classes", C.c_int), ("mg_octets", C.c_int)]
+
+
+class Profile(C.Structure):
+    """ibm_profile: per kernel class launches, algorithmic bytes, timed ms."""
+    _fields_ = [("nkernels", C.c_int), ("launches", C.c_longlong * 32), ("bytes", C.c_double * 32),
+                ("time_ms", C.c_double * 32), ("timed_launches", C.c_longlong * 32),
+                ("phase_bytes", C.c_double * 5)]
 
 
 class SolveStats(C.Structure):
@@ -125,6 +133,7 @@ def gpu() -> C.CDLL:
         lib.ibm_apply_preconditioner.argtypes = [vp, i, vp, vp]
         lib.ibm_profile_reset.argtypes = [vp]
         lib.ibm_profile_time_kernel.argtypes = [vp, i]
+        lib.ibm_profile_get.argtypes = [vp, P(Profile)]
         lib.ibm_kernel_name.argtypes = [i]
         lib.ibm_kernel_name.restype = C.c_char_p
         lib.ibm_synchronize.argtypes = [vp]

@@ -97,6 +97,12 @@ __global__ void k_op_planes(const double *vals, long n, double *c, double *invd,
   }
 }
 
+// Planes [7][n] -> row-major [n][7].
+__global__ void k_planes_to_rows(const double *c, long n, double *rows) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    for (int s = 0; s < 7; ++s) rows[7 * r + s] = c[(long)s * n + r];
+}
+
 // Right-Jacobi-scaled operator: cj_s(r) = c_s(r) * invd(neighbour_s(r)).
 __global__ void k_op_jacobi(const double *c, const double *invd, double *cj, Box b) {
   const long n = b.n, sy = b.nx, sz = (long)b.nx * b.ny;
@@ -112,6 +118,27 @@ __global__ void k_op_jacobi(const double *c, const double *invd, double *cj, Box
 __global__ void k_to_float(const double *src, float *dst, long n) {
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
     dst[t] = (float)src[t];
+}
+
+// Class rows [K][7] -> [K][8] (slot 7 zero) and their FP32 copies.
+__global__ void k_pad_rows(const double *rows7, int K, double *rows8, float *rows8f) {
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < 8L * K; e += (long)gridDim.x * blockDim.x) {
+    const long c = e / 8;
+    const int s = (int)(e - 8 * c);
+    const double v = s < 7 ? rows7[7 * c + s] : 0.0;
+    rows8[e] = v;
+    rows8f[e] = (float)v;
+  }
+}
+
+// FP32 Jacobi records {invdf, cjf_1..cjf_6, 0} per row.
+__global__ void k_jacobi_records(const float *cjf, const float *invdf, long n, float *rec) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+    float *o = rec + 8 * r;
+    o[0] = invdf[r];
+    for (int s = 1; s < 7; ++s) o[s] = cjf[(long)s * n + r];
+    o[7] = 0.0f;
+  }
 }
 
 __global__ void k_spmv7(const double *c, Box b, const double *x, double *y) {
@@ -199,6 +226,41 @@ void require_inputs(ibm_ctx *c) {
   if (!c->csr_set) throw Error(IBM_ERR_STATE, "projection operators not set");
 }
 
+// Record classes of an operator's rows and Jacobi records, built once per
+// set of coefficients (they stay empty where the rows do not repeat enough).
+void ensure_classes(ibm_ctx *c, Op7 &o) {
+  if (o.cls_tried) return;
+  o.cls_tried = true;
+  const long n = o.b.n;
+  DBuf<double> rows;  // row-major [n][7] copy of the planes
+  rows.alloc((size_t)7 * n);
+  {
+    LaunchScope ls(K_SETUP, c->st, 0.0);
+    k_planes_to_rows<<<grid1d(n), kThreads, 0, c->st>>>(o.c.p, n, rows.p);
+  }
+  if (build_classes<double>(c->st, rows.p, 7, n, o.cls)) {
+    o.tab.alloc((size_t)8 * o.cls.K);
+    o.tabf.alloc((size_t)8 * o.cls.K);
+    LaunchScope ls(K_SETUP, c->st, 0.0);
+    k_pad_rows<<<grid1d(8L * o.cls.K), kThreads, 0, c->st>>>(o.cls.tab.p, o.cls.K, o.tab.p, o.tabf.p);
+  }
+  rows.release();
+  DBuf<float> jrec;
+  jrec.alloc((size_t)8 * n);
+  {
+    LaunchScope ls(K_SETUP, c->st, 0.0);
+    k_jacobi_records<<<grid1d(n), kThreads, 0, c->st>>>(o.cjf.p, o.invdf.p, n, jrec.p);
+  }
+  build_classes<float>(c->st, jrec.p, 8, n, o.clsj);
+  IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+}
+
+// Points a system at its operator's classes.
+void use_classes(const Op7 &o, KSysHost &h) {
+  if (o.cls.ok()) { h.cls = o.cls.code.p; h.tab = o.tab.p; h.tabf = o.tabf.p; }
+  if (o.clsj.ok()) { h.clsj = o.clsj.code.p; h.tabj = o.clsj.tab.p; }
+}
+
 void ensure_solvers(ibm_ctx *c) {
   if (c->solvers_ready && c->solvers_precision == c->prm.precision) return;
   const ibm_solver_params &p = c->prm;
@@ -220,6 +282,10 @@ void ensure_solvers(ibm_ctx *c) {
       h.a32 = a32; h.cycle_rtol = p.cycle_rtol32;
     }
     else { h.pc = 0; h.A = o.cj.p; }
+    if (p.row_classes) {
+      ensure_classes(c, c->op[f]);
+      use_classes(o, h);
+    }
   }
   c->kmom.configure(3, hs);
   const Op7 &op = c->op[3];
@@ -237,6 +303,8 @@ void ensure_solvers(ibm_ctx *c) {
     mp.group_ratio = p.mg_group_ratio;
     mp.options = p.mg_options;
     mp.nu_coarse = p.mg_nu_coarse;
+    mp.classes = p.row_classes ? 1 : 0;
+    mp.octets = p.mg_octets ? 1 : 0;
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
     const double *winv = ((p.mg_options & 2) && c->p_sym) ? c->p_winv.p : nullptr;
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
@@ -248,6 +316,10 @@ void ensure_solvers(ibm_ctx *c) {
       hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32;
     }
     else { hp.pc = 0; hp.A = op.cj.p; }
+  }
+  if (p.row_classes) {
+    ensure_classes(c, c->op[3]);
+    use_classes(op, hp);
   }
   c->kp.configure(1, &hp);
   c->solvers_ready = true;
@@ -352,6 +424,8 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->mg_nu_coarse = 0;
   p->cycle_rtol32 = 1e-5;
   p->compute_forces = 0;
+  p->row_classes = 1;
+  p->mg_octets = 1;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -441,6 +515,11 @@ int ibm_set_operator(ibm_ctx *c, int field, const double *vals7, int nbx, int nb
       throw Error(IBM_ERR_ARG, "ibm_set_operator: box does not match the field's solve box");
     Op7 &o = c->op[field];
     o.b = b;
+    o.cls_tried = false;
+    o.cls = Classes<double>();
+    o.clsj = Classes<float>();
+    o.tab.release();
+    o.tabf.release();
     const long n = b.n;
     DBuf<double> tmp;
     tmp.alloc((size_t)7 * n);

@@ -80,6 +80,24 @@ struct DBuf {
   size_t bytes() const { return n * sizeof(T); }
 };
 
+// Record classes (ibm_classes.cu) -------------------------------------------
+// The distinct records of an array of nrec records of W values: record t
+// equals tab[code[t]] bit for bit.
+constexpr int kMaxClasses = 65535;
+template <class T>
+struct Classes {
+  DBuf<uint16_t> code;  // class of each record
+  DBuf<T> tab;          // [K][W] distinct records, first-seen order
+  int K = 0, W = 0;
+  bool ok() const { return code.p != nullptr; }
+  size_t bytes() const { return code.bytes() + tab.bytes(); }
+};
+// Fills c for the records rec[t * W .. t * W + W) (device memory, t < nrec).
+// Returns false and leaves c empty when there are more than kMaxClasses
+// distinct records. Synchronises the stream.
+template <class T>
+bool build_classes(cudaStream_t st, const T *rec, int W, long nrec, Classes<T> &c);
+
 // Division by an invariant divisor d >= 1 through a multiply-high (Granlund
 // and Montgomery, "Division by invariant integers using multiplication",
 // PLDI 1994): with s = ceil(log2 d) and m = floor(2^32 (2^s - d) / d) + 1,
@@ -118,6 +136,12 @@ struct Op7 {
   DBuf<float> cf;      // FP32 coefficients (mixed precision)
   DBuf<float> cjf;     // FP32 copy of cj (two Jacobi sweeps in one pass)
   DBuf<float> invdf;
+  // Record classes of the rows (empty when there are too many distinct rows):
+  Classes<double> cls;  // classes of the supplied rows (W 7)
+  DBuf<double> tab;     // [K][8] the distinct rows, slot 7 zero
+  DBuf<float> tabf;     // [K][8] their FP32 copies (the rows of cf)
+  Classes<float> clsj;  // classes of the FP32 Jacobi records {invdf, cjf_1..cjf_6, 0} (W 8)
+  bool cls_tried = false;  // classes built (or found too many) for the current coefficients
 };
 
 // Per-system GMRES scalars kept on the device (no host round trip per iteration).
@@ -167,6 +191,12 @@ struct KSys {
   int pc;               // 0 Jacobi folded into A, 1 explicit z (multigrid), 2 flexible FP32 z
   int pc_cb;            // pc 2: preconditioner supplied by a callback (else FP32 Jacobi sweeps)
   KScal *s;
+  // Record classes (null cls / clsj: the planes above are read instead)
+  const uint16_t *cls;  // class of each row of Ar (and of Af, its FP32 copy)
+  const double *tab;    // [K][8] rows of Ar
+  const float *tabf;    // [K][8] rows of Af
+  const uint16_t *clsj; // class of each FP32 Jacobi record
+  const float *tabj;    // [K][8] {invdf, Ajf_1..Ajf_6, 0}
 };
 
 // Host-side mirror of what the loop needs from each system after a step.
@@ -210,35 +240,46 @@ __device__ __forceinline__ void row_ijk(int r, int nx, int ny, int &i, int &j, i
 }
 
 // y_r = sum_s c_s x_{r+off_s}, fused multiply-add chain in slot order
-// C,-x,+x,-y,+y,-z,+z; neighbours outside the box contribute 0.
+// C,-x,+x,-y,+y,-z,+z; neighbours outside the box contribute 0. Slot s of the
+// row is c0[s * cs]: planes [7][n] give c0 = c + r, cs = n; a class table
+// row gives cs = 1.
+template <class T, class X>
+__device__ __forceinline__ double stencil7_at(const T *__restrict__ c0, long cs, const X *__restrict__ x, int r,
+                                              int i, int j, int k, int nx, int ny, int nz) {
+  const long sy = nx, sz = (long)nx * ny;
+  double acc = 0.0;
+  acc = fma((double)c0[0], (double)x[r], acc);
+  acc = fma((double)c0[cs], i > 0 ? (double)x[r - 1] : 0.0, acc);
+  acc = fma((double)c0[2 * cs], i < nx - 1 ? (double)x[r + 1] : 0.0, acc);
+  acc = fma((double)c0[3 * cs], j > 0 ? (double)x[r - sy] : 0.0, acc);
+  acc = fma((double)c0[4 * cs], j < ny - 1 ? (double)x[r + sy] : 0.0, acc);
+  acc = fma((double)c0[5 * cs], k > 0 ? (double)x[r - sz] : 0.0, acc);
+  acc = fma((double)c0[6 * cs], k < nz - 1 ? (double)x[r + sz] : 0.0, acc);
+  return acc;
+}
 template <class T, class X>
 __device__ __forceinline__ double stencil7_row(const T *__restrict__ c, long n, const X *__restrict__ x, int r,
                                                int i, int j, int k, int nx, int ny, int nz) {
-  const long sy = nx, sz = (long)nx * ny;
-  double acc = 0.0;
-  acc = fma((double)c[r], (double)x[r], acc);
-  acc = fma((double)c[n + r], i > 0 ? (double)x[r - 1] : 0.0, acc);
-  acc = fma((double)c[2 * n + r], i < nx - 1 ? (double)x[r + 1] : 0.0, acc);
-  acc = fma((double)c[3 * n + r], j > 0 ? (double)x[r - sy] : 0.0, acc);
-  acc = fma((double)c[4 * n + r], j < ny - 1 ? (double)x[r + sy] : 0.0, acc);
-  acc = fma((double)c[5 * n + r], k > 0 ? (double)x[r - sz] : 0.0, acc);
-  acc = fma((double)c[6 * n + r], k < nz - 1 ? (double)x[r + sz] : 0.0, acc);
-  return acc;
+  return stencil7_at(c + r, n, x, r, i, j, k, nx, ny, nz);
 }
 
 // FP32 variant.
-__device__ __forceinline__ float stencil7_row_f(const float *__restrict__ c, long n, const float *__restrict__ x,
-                                                int r, int i, int j, int k, int nx, int ny, int nz) {
+__device__ __forceinline__ float stencil7_at_f(const float *__restrict__ c0, long cs, const float *__restrict__ x,
+                                               int r, int i, int j, int k, int nx, int ny, int nz) {
   const long sy = nx, sz = (long)nx * ny;
   float acc = 0.0f;
-  acc = fmaf(c[r], x[r], acc);
-  acc = fmaf(c[n + r], i > 0 ? x[r - 1] : 0.0f, acc);
-  acc = fmaf(c[2 * n + r], i < nx - 1 ? x[r + 1] : 0.0f, acc);
-  acc = fmaf(c[3 * n + r], j > 0 ? x[r - sy] : 0.0f, acc);
-  acc = fmaf(c[4 * n + r], j < ny - 1 ? x[r + sy] : 0.0f, acc);
-  acc = fmaf(c[5 * n + r], k > 0 ? x[r - sz] : 0.0f, acc);
-  acc = fmaf(c[6 * n + r], k < nz - 1 ? x[r + sz] : 0.0f, acc);
+  acc = fmaf(c0[0], x[r], acc);
+  acc = fmaf(c0[cs], i > 0 ? x[r - 1] : 0.0f, acc);
+  acc = fmaf(c0[2 * cs], i < nx - 1 ? x[r + 1] : 0.0f, acc);
+  acc = fmaf(c0[3 * cs], j > 0 ? x[r - sy] : 0.0f, acc);
+  acc = fmaf(c0[4 * cs], j < ny - 1 ? x[r + sy] : 0.0f, acc);
+  acc = fmaf(c0[5 * cs], k > 0 ? x[r - sz] : 0.0f, acc);
+  acc = fmaf(c0[6 * cs], k < nz - 1 ? x[r + sz] : 0.0f, acc);
   return acc;
+}
+__device__ __forceinline__ float stencil7_row_f(const float *__restrict__ c, long n, const float *__restrict__ x,
+                                                int r, int i, int j, int k, int nx, int ny, int nz) {
+  return stencil7_at_f(c + r, n, x, r, i, j, k, nx, ny, nz);
 }
 
 // Grid size for persistent grid-stride kernels: a multiple of the SM count.

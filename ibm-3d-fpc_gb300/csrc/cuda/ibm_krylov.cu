@@ -34,6 +34,26 @@ __device__ __forceinline__ void sys_ijk(long r, const KSys &S, int &i, int &j, i
   k = (int)kk;
 }
 
+// Slot 0 of row r of Ar and the distance between its slots: the row of the
+// row's class, or the planes.
+__device__ __forceinline__ const double *ar_row(const KSys &S, long r, long &cs) {
+  if (S.cls) { cs = 1; return S.tab + 8 * (long)S.cls[r]; }
+  cs = S.n;
+  return S.Ar + r;
+}
+// The same for the Arnoldi operator A (classed only when A is Ar).
+__device__ __forceinline__ const double *a_row(const KSys &S, long r, long &cs) {
+  if (S.cls && S.A == S.Ar) { cs = 1; return S.tab + 8 * (long)S.cls[r]; }
+  cs = S.n;
+  return S.A + r;
+}
+// ... and for Af, the FP32 copy of Ar.
+__device__ __forceinline__ const float *af_row(const KSys &S, long r, long &cs) {
+  if (S.cls) { cs = 1; return S.tabf + 8 * (long)S.cls[r]; }
+  cs = S.n;
+  return S.Af + r;
+}
+
 // Sum block partials of `nd` dot products in block order; one warp per dot.
 __device__ void reduce_partials(const double *part, int nblk, int nd, double *out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -80,7 +100,12 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
         int i, j, k;
         sys_ijk(r, S, i, j, k);
         // with finite coefficients A 0 is +0 in every row, so b - 0 equals b - A x bit for bit
-        const double ax = S.x_zero ? 0.0 : stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+        double ax = 0.0;
+        if (!S.x_zero) {
+          long cs;
+          const double *c0 = ar_row(S, r, cs);
+          ax = stencil7_at(c0, cs, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+        }
         const double bv = S.b[r];
         const double rv = bv - ax;
         if (S.a32) S.Vf[r] = (float)rv;
@@ -185,9 +210,11 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
         int i, jj, k;
         sys_ijk(r, S, i, jj, k);
         double w;
-        if (S.pc == 0) w = stencil7_row(S.A, S.n, vj, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
-        else if (S.pc == 1) w = stencil7_row(S.A, S.n, S.z, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
-        else w = stencil7_row(S.A, S.n, S.Z + (long)j * S.ldv, (int)r, i, jj, k, S.nx, S.ny, S.nz);
+        long cs;
+        const double *c0 = a_row(S, r, cs);
+        if (S.pc == 0) w = stencil7_at(c0, cs, vj, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
+        else if (S.pc == 1) w = stencil7_at(c0, cs, S.z, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
+        else w = stencil7_at(c0, cs, S.Z + (long)j * S.ldv, (int)r, i, jj, k, S.nx, S.ny, S.nz);
         S.w[r] = w;
         wv[t] = w;
       }
@@ -367,7 +394,9 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
       if (r < S.n) {
         int i, j, k;
         sys_ijk(r, S, i, j, k);
-        const double rv = S.b[r] - stencil7_row(S.Ar, S.n, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+        long cs;
+        const double *c0 = ar_row(S, r, cs);
+        const double rv = S.b[r] - stencil7_at(c0, cs, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
         if (S.a32) S.Vf[r] = (float)rv;
         else S.V[r] = rv;
         pr = fma(rv, rv, pr);
@@ -438,8 +467,16 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
       const long r0 = t0 + 4 * threadIdx.x;
       if (r0 >= n) continue;
       float4 cp[7];
+      if (S.cls) {
+        const ushort4 c4 = __ldcs(reinterpret_cast<const ushort4 *>(S.cls + r0));
+        const float *t0 = S.tabf + 8 * (long)c4.x, *t1 = S.tabf + 8 * (long)c4.y;
+        const float *t2 = S.tabf + 8 * (long)c4.z, *t3 = S.tabf + 8 * (long)c4.w;
 #pragma unroll
-      for (int q = 0; q < 7; ++q) cp[q] = __ldcs(reinterpret_cast<const float4 *>(S.Af + (long)q * n + r0));
+        for (int q = 0; q < 7; ++q) cp[q] = make_float4(__ldg(t0 + q), __ldg(t1 + q), __ldg(t2 + q), __ldg(t3 + q));
+      } else {
+#pragma unroll
+        for (int q = 0; q < 7; ++q) cp[q] = __ldcs(reinterpret_cast<const float4 *>(S.Af + (long)q * n + r0));
+      }
       float w[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -488,7 +525,9 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
         if (r < S.n) {
           int i, jj, k;
           sys_ijk(r, S, i, jj, k);
-          const float w = stencil7_row_f(S.Af, S.n, zj, (int)r, i, jj, k, S.nx, S.ny, S.nz);
+          long cs;
+          const float *c0 = af_row(S, r, cs);
+          const float w = stencil7_at_f(c0, cs, zj, (int)r, i, jj, k, S.nx, S.ny, S.nz);
           S.wf[r] = w;
 #pragma unroll
           for (int kk = 0; kk < kChunk32; ++kk)
@@ -512,7 +551,9 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
       if (r < S.n) {
         int i, jj, k;
         sys_ijk(r, S, i, jj, k);
-        const float w = stencil7_row_f(S.Af, S.n, zj, (int)r, i, jj, k, S.nx, S.ny, S.nz);
+        long cs;
+        const float *c0 = af_row(S, r, cs);
+        const float w = stencil7_at_f(c0, cs, zj, (int)r, i, jj, k, S.nx, S.ny, S.nz);
         S.wf[r] = w;
         wv[t] = w;
       }
@@ -735,14 +776,19 @@ __device__ __forceinline__ void jacobi_two_rows(const KSys &S, const VT *__restr
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
     int i, jj, k;
     sys_ijk(r, S, i, jj, k);
+    // slot s (1..6) of the scaled couplings at cj[s * cs], D^-1 at id
+    const float *cj, *id;
+    long cs;
+    if (S.clsj) { cj = S.tabj + 8 * (long)S.clsj[r]; cs = 1; id = cj; }
+    else { cj = S.Ajf + r; cs = n; id = S.invdf + r; }
     float acc = (float)vj[r] * inv_nu;
-    if (i > 0) acc = fmaf(-S.Ajf[n + r], (float)vj[r - 1] * inv_nu, acc);
-    if (i < S.nx - 1) acc = fmaf(-S.Ajf[2 * n + r], (float)vj[r + 1] * inv_nu, acc);
-    if (jj > 0) acc = fmaf(-S.Ajf[3 * n + r], (float)vj[r - sy] * inv_nu, acc);
-    if (jj < S.ny - 1) acc = fmaf(-S.Ajf[4 * n + r], (float)vj[r + sy] * inv_nu, acc);
-    if (k > 0) acc = fmaf(-S.Ajf[5 * n + r], (float)vj[r - sz] * inv_nu, acc);
-    if (k < S.nz - 1) acc = fmaf(-S.Ajf[6 * n + r], (float)vj[r + sz] * inv_nu, acc);
-    out[r] = S.invdf[r] * acc;
+    if (i > 0) acc = fmaf(-cj[cs], (float)vj[r - 1] * inv_nu, acc);
+    if (i < S.nx - 1) acc = fmaf(-cj[2 * cs], (float)vj[r + 1] * inv_nu, acc);
+    if (jj > 0) acc = fmaf(-cj[3 * cs], (float)vj[r - sy] * inv_nu, acc);
+    if (jj < S.ny - 1) acc = fmaf(-cj[4 * cs], (float)vj[r + sy] * inv_nu, acc);
+    if (k > 0) acc = fmaf(-cj[5 * cs], (float)vj[r - sz] * inv_nu, acc);
+    if (k < S.nz - 1) acc = fmaf(-cj[6 * cs], (float)vj[r + sz] * inv_nu, acc);
+    out[r] = *id * acc;
   }
 }
 
@@ -753,9 +799,20 @@ __device__ __forceinline__ void jacobi_two_rows4(const KSys &S, const float *__r
   const long n = S.n, sy = S.nx, sz = (long)S.nx * S.ny;
   for (long r0 = 4 * ((long)blockIdx.x * blockDim.x + threadIdx.x); r0 < n; r0 += 4L * gridDim.x * blockDim.x) {
     float4 cp[7];
+    float4 id;
+    if (S.clsj) {
+      // class records {invdf, Ajf_1..Ajf_6, 0}: slot 0 is D^-1
+      const ushort4 c4 = __ldcs(reinterpret_cast<const ushort4 *>(S.clsj + r0));
+      const float *t0 = S.tabj + 8 * (long)c4.x, *t1 = S.tabj + 8 * (long)c4.y;
+      const float *t2 = S.tabj + 8 * (long)c4.z, *t3 = S.tabj + 8 * (long)c4.w;
 #pragma unroll
-    for (int q = 1; q < 7; ++q) cp[q] = __ldcs(reinterpret_cast<const float4 *>(S.Ajf + (long)q * n + r0));
-    const float4 id = __ldcs(reinterpret_cast<const float4 *>(S.invdf + r0));
+      for (int q = 0; q < 7; ++q) cp[q] = make_float4(__ldg(t0 + q), __ldg(t1 + q), __ldg(t2 + q), __ldg(t3 + q));
+      id = cp[0];
+    } else {
+#pragma unroll
+      for (int q = 1; q < 7; ++q) cp[q] = __ldcs(reinterpret_cast<const float4 *>(S.Ajf + (long)q * n + r0));
+      id = __ldcs(reinterpret_cast<const float4 *>(S.invdf + r0));
+    }
     float z[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -815,7 +872,9 @@ __global__ void __launch_bounds__(kThreads) k_jacobi32_sweep(KSys *sys, int src_
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
     int i, jj, k;
     sys_ijk(r, S, i, jj, k);
-    const float az = stencil7_row_f(S.Af, S.n, src, (int)r, i, jj, k, S.nx, S.ny, S.nz);
+    long cs;
+    const float *c0 = af_row(S, r, cs);
+    const float az = stencil7_at_f(c0, cs, src, (int)r, i, jj, k, S.nx, S.ny, S.nz);
     const float v = (float)((S.a32 ? (double)vjf[r] : vj[r]) * inv_nu);
     dst[r] = fmaf(S.invdf[r], v - az, src[r]);
   }
@@ -920,6 +979,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     k.nx = h.nx; k.ny = h.ny; k.nz = h.nz; k.n = ((mask >> s) & 1u) ? h.n : 0;
     k.fdx = make_fastdiv((unsigned)h.nx); k.fdy = make_fastdiv((unsigned)h.ny);
     k.A = h.A; k.Ar = h.Ar; k.invd = h.invd; k.Af = h.Af; k.invdf = h.invdf; k.Ajf = h.Ajf;
+    k.cls = h.cls; k.tab = h.tab; k.tabf = h.tabf; k.clsj = h.clsj; k.tabj = h.tabj;
     k.V = slot[s].V.p; k.ldv = h.n;
     k.Z = slot[s].Z.p;
     k.w = slot[s].w.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;
@@ -970,7 +1030,8 @@ void Krylov::launch_cycle_end(cudaStream_t st, const Precond &pc, const KFlags *
       if (!fl[s].cycle_end) continue;
       const int m = fl[s].i, pcm = slot[s].host.pc;
       bu += rows(s) * (pcm == 2 ? 4.0 * m + 16.0 : pcm == 1 ? 8.0 * m + 8.0 : 8.0 * m + 24.0);
-      br += 88.0 * rows(s);
+      // a classed row is its 2-byte class instead of 7 FP64 coefficients
+      br += (slot[s].host.cls ? 34.0 : 88.0) * rows(s);
       if (pcm == 1) ba += 24.0 * rows(s);
     }
   }
@@ -1021,7 +1082,7 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
   }
   int inner_sweeps = 0;
   bool any64 = false, any32 = false;
-  double r32 = 0.0, bsp = 0.0, bor = 0.0, bsp32 = 0.0, bor32 = 0.0;
+  double r32 = 0.0, j32two = 0.0, bsp = 0.0, bor = 0.0, bsp32 = 0.0, bor32 = 0.0;
   for (int s = 0; s < nsys; ++s) {
     if (!((mask >> s) & 1u)) continue;
     const bool a32 = slot[s].host.a32 != 0;
@@ -1030,18 +1091,25 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
       inner_sweeps = std::max(inner_sweeps, std::max(1, slot[s].host.inner_sweeps));
     if (!fl || !fl[s].active) continue;
     const double j1 = fl[s].i + 1.0;
-    if (slot[s].host.pc == 2 && !slot[s].host.pc_cb) r32 += rows(s) * (a32 ? 0.75 : 1.0);
+    const KSysHost &h = slot[s].host;
+    // coefficient bytes of a row: 7 values, or a 2-byte class
+    const double c64 = (h.cls && h.A == h.Ar) ? 2.0 : 56.0, c32 = h.cls ? 2.0 : 28.0;
+    if (h.pc == 2 && !h.pc_cb) {
+      r32 += rows(s) * (a32 ? 0.75 : 1.0);
+      // two sweeps in one pass: v, z and a 2-byte class instead of 7 FP32 values
+      j32two += rows(s) * (h.clsj ? (a32 ? 10.0 : 14.0) : (a32 ? 27.0 : 36.0));
+    }
     if (a32) {
-      bsp32 += rows(s) * (36.0 + 4.0 * j1);
+      bsp32 += rows(s) * (c32 + 8.0 + 4.0 * j1);
       bor32 += rows(s) * (8.0 + 4.0 * j1);
     } else {
-      bsp += rows(s) * ((slot[s].host.pc == 2 ? 68.0 : 72.0) + 8.0 * j1);
+      bsp += rows(s) * ((h.pc == 2 ? 12.0 : 16.0) + c64 + 8.0 * j1);
       bor += rows(s) * (16.0 + 8.0 * j1);
     }
   }
   if (inner_sweeps > 0) {
     if (inner_sweeps == 2) {
-      LaunchScope ls(K_GM_JAC32, st, 36.0 * r32);
+      LaunchScope ls(K_GM_JAC32, st, j32two);
       k_jacobi32_two<<<gridu, kThreads, 0, st>>>(dev);
     } else if (inner_sweeps == 1) {
       LaunchScope ls(K_GM_JAC32, st, 16.0 * r32);
@@ -1089,10 +1157,11 @@ void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, co
                    KResult *res, unsigned mask, bool x_zero) {
   bind(st, b, x, mask, x_zero);
   const dim3 grid(nblk, nsys);
-  double all_rows = 0.0;
-  for (int s = 0; s < nsys; ++s) all_rows += ((mask >> s) & 1u) ? (double)slot[s].host.n : 0.0;
+  double init_bytes = 0.0;
+  for (int s = 0; s < nsys; ++s)
+    if ((mask >> s) & 1u) init_bytes += (x_zero ? 16.0 : slot[s].host.cls ? 26.0 : 80.0) * slot[s].host.n;
   {
-    LaunchScope ls(K_GM_INIT, st, (x_zero ? 16.0 : 80.0) * all_rows);
+    LaunchScope ls(K_GM_INIT, st, init_bytes);
     k_init<<<grid, kThreads, 0, st>>>(dsys.p, nsys);
   }
   for (long guard = 0;; ++guard) {

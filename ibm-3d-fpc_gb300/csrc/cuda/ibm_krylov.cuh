@@ -43,6 +43,12 @@ struct KSysHost {
   // fell by cycle_rtol and the restart recomputes the true residual in FP64.
   int a32 = 0;
   double cycle_rtol = 0.0;
+  // record classes of the operator rows and of the Jacobi records (optional)
+  const uint16_t *cls = nullptr;
+  const double *tab = nullptr;
+  const float *tabf = nullptr;
+  const uint16_t *clsj = nullptr;
+  const float *tabj = nullptr;
 };
 
 struct KResult {

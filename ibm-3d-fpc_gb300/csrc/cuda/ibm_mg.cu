@@ -343,6 +343,34 @@ __device__ __forceinline__ void load_rec(const T *__restrict__ p, T (&v)[N]) {
   }
 }
 
+// Where a level's colour-split records live: the records themselves, or a
+// 2-byte class per record and the table of distinct records (record classes,
+// ibm_classes.cu). The table is small and read through the read-only cache;
+// the per-record data streams.
+template <class T, int W>
+struct Recs {
+  const T *R = nullptr;            // [c][m][W]
+  const uint16_t *code = nullptr;  // [c][m] when classed
+  const T *tab = nullptr;          // [K][W]
+};
+template <class T, int W>
+__device__ __forceinline__ void load_recs(const Recs<T, W> &s, long idx, T (&v)[W]) {
+  if (s.code) {
+    const float4 *q = reinterpret_cast<const float4 *>(s.tab + (long)__ldcs(s.code + idx) * W);
+#pragma unroll
+    for (int u = 0; u < (int)(W * sizeof(T) / 16); ++u) {
+      const float4 f = __ldg(q + u);
+      memcpy(reinterpret_cast<char *>(v) + 16 * u, &f, 16);
+    }
+  } else {
+    load_rec<T, W>(s.R + idx * W, v);
+  }
+}
+template <class T, int W>
+__device__ __forceinline__ const T *rec_ptr(const Recs<T, W> &s, long idx) {
+  return s.code ? s.tab + (long)__ldcs(s.code + idx) * W : s.R + idx * W;
+}
+
 template <class T>
 __global__ void k_split_colors(const T *A, const T *invd, Box bx, T *R) {
   const long h = bx.n / 2;
@@ -362,18 +390,17 @@ __global__ void k_split_colors(const T *A, const T *invd, Box bx, T *R) {
 // other colour's points). Points of one colour are not coupled to each other
 // in a 7-point stencil, so the phase reads only values it does not write.
 template <class T>
-__global__ void __launch_bounds__(kThreads) k_relax_rb(const T *__restrict__ R, const T *__restrict__ b, T *x,
+__global__ void __launch_bounds__(kThreads) k_relax_rb(Recs<T, 8> R, const T *__restrict__ b, T *x,
                                                        Box bx, int color, const int *gate) {
   if (gate_off(gate)) return;
   const long h = bx.n / 2;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
   const long sy = nx, sz = (long)nx * ny;
-  const T *__restrict__ P = R + (long)color * h * 8;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
     const long r = rb_row(m, color, bx, i, j, k);
     T c[8];
-    load_rec<T, 8>(P + m * 8, c);
+    load_recs<T, 8>(R, (long)color * h + m, c);
     const T xw = i > 0 ? x[r - 1] : T(0);
     const T xe = i < nx - 1 ? x[r + 1] : T(0);
     const T xs = j > 0 ? x[r - sy] : T(0);
@@ -410,26 +437,26 @@ __global__ void k_split_colors27(const T *A, const T *invd, Box bx, T *R) {
 }
 
 template <class T>
-__global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(const T *__restrict__ R, const T *__restrict__ b,
+__global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(Recs<T, 28> R, const T *__restrict__ b,
                                                          const T *__restrict__ x, T *__restrict__ t, Box bx,
                                                          int color, int zero_x, const int *gate) {
   if (gate_off(gate)) return;
   const long h = bx.n / 2;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
-  const T *__restrict__ P = R + (long)color * h * 28;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
     const long r = rb_row(m, color, bx, i, j, k);
+    const long idx = (long)color * h + m;
     if (zero_x) {
-      t[r] = P[m * 28 + 27] * b[r];
+      t[r] = rec_ptr<T, 28>(R, idx)[27] * b[r];
       t[r ^ 1] = T(0);
       continue;
     }
     // FP32 records come in with vector loads; FP64 ones (twice the registers)
     // are read one value at a time
     T c[sizeof(T) == 4 ? 28 : 1];
-    if constexpr (sizeof(T) == 4) load_rec<T, 28>(P + m * 28, c);
-    const T *__restrict__ pr = P + m * 28;
+    if constexpr (sizeof(T) == 4) load_recs<T, 28>(R, idx, c);
+    const T *__restrict__ pr = sizeof(T) == 4 ? nullptr : rec_ptr<T, 28>(R, idx);
     T acc = T(0);
 #pragma unroll
     for (int s = 0; s < 27; ++s) {
@@ -449,12 +476,45 @@ __global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(const T *__restrict_
   }
 }
 
+// Residual of a 27-point level from its colour-split records: every point
+// (both colours; same-colour points are coupled), b - A x in apply_row's slot
+// order, so the result equals k_residual<T, 27> bit for bit.
+template <class T>
+__global__ void __launch_bounds__(kThreads, 4) k_residual_rb27(Recs<T, 28> R, const T *__restrict__ b,
+                                                            const T *__restrict__ x, T *__restrict__ res, Box bx,
+                                                            const int *gate) {
+  if (gate_off(gate)) return;
+  const long h = bx.n / 2;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < 2 * h; t += (long)gridDim.x * blockDim.x) {
+    const int color = t >= h;
+    const long m = t - color * h;
+    int i, j, k;
+    const long r = rb_row(m, color, bx, i, j, k);
+    T c[sizeof(T) == 4 ? 28 : 1];
+    if constexpr (sizeof(T) == 4) load_recs<T, 28>(R, t, c);
+    const T *__restrict__ pr = sizeof(T) == 4 ? nullptr : rec_ptr<T, 28>(R, t);
+    T acc = T(0);
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+      const int ii = i + s % 3 - 1, jj = j + (s / 3) % 3 - 1, kk = k + s / 9 - 1;
+      const bool in = ii >= 0 && ii < nx && jj >= 0 && jj < ny && kk >= 0 && kk < nz;
+      const T xv = in ? x[((long)kk * ny + jj) * nx + ii] : T(0);
+      T cs;
+      if constexpr (sizeof(T) == 4) cs = c[s];
+      else cs = pr[s];
+      acc = fmat<T>(cs, xv, acc);
+    }
+    res[r] = b[r] - acc;
+  }
+}
+
 // Residual after a two-colour sweep that ended with colour 1: the colour-1
 // points were just solved exactly against their colour-0 neighbours, so their
 // residual is zero up to rounding and is written as 0; colour-0 points take
 // b - A x with the colour-split coefficients (centre first, as apply_row).
 template <class T>
-__global__ void __launch_bounds__(kThreads) k_residual_rb(const T *__restrict__ R, const T *__restrict__ b,
+__global__ void __launch_bounds__(kThreads) k_residual_rb(Recs<T, 8> R, const T *__restrict__ b,
                                                           const T *__restrict__ x, T *__restrict__ res, Box bx,
                                                           const int *gate) {
   if (gate_off(gate)) return;
@@ -465,7 +525,7 @@ __global__ void __launch_bounds__(kThreads) k_residual_rb(const T *__restrict__ 
     int i, j, k;
     const long r = rb_row(m, 0, bx, i, j, k);
     T c[8];
-    load_rec<T, 8>(R + m * 8, c);
+    load_recs<T, 8>(R, m, c);
     const T xc = x[r];
     const T xw = i > 0 ? x[r - 1] : T(0);
     const T xe = i < nx - 1 ? x[r + 1] : T(0);
@@ -486,15 +546,185 @@ __global__ void __launch_bounds__(kThreads) k_residual_rb(const T *__restrict__ 
   }
 }
 
+// Octet form of the FP32 in-place phases (nx a multiple of 8): a thread takes
+// eight consecutive points of a line, four of each colour, and issues every
+// load it needs (the four records, b and the x values of its own and the four
+// neighbouring lines, as 16-byte vectors) before it computes. One point per
+// thread leaves the phase latency-bound on its dependent loads; the octet
+// gives each thread about twenty independent loads in flight. Per point the
+// arithmetic is k_relax_rb's / k_residual_rb's, in the same order.
+__device__ __forceinline__ void load8f(const float *__restrict__ p, float (&v)[8]) {
+  const float4 a = *reinterpret_cast<const float4 *>(p), c = *reinterpret_cast<const float4 *>(p + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = c.x; v[5] = c.y; v[6] = c.z; v[7] = c.w;
+}
+__device__ __forceinline__ void store8f(float *p, const float (&v)[8]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  *reinterpret_cast<float4 *>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
+}
+// The four records of the octet's points of one colour (record indices m0..m0+3).
+__device__ __forceinline__ void load_recs4(const Recs<float, 8> &s, long m0, float (&c)[4][8]) {
+  if (s.code) {
+    const ushort4 k4 = __ldcs(reinterpret_cast<const ushort4 *>(s.code + m0));
+    const unsigned short ks[4] = {k4.x, k4.y, k4.z, k4.w};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const float4 *q = reinterpret_cast<const float4 *>(s.tab + 8 * (long)ks[t]);
+      const float4 a = __ldg(q), e = __ldg(q + 1);
+      c[t][0] = a.x; c[t][1] = a.y; c[t][2] = a.z; c[t][3] = a.w;
+      c[t][4] = e.x; c[t][5] = e.y; c[t][6] = e.z; c[t][7] = e.w;
+    }
+  } else {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) load_rec<float, 8>(s.R + (m0 + t) * 8, c[t]);
+  }
+}
+
+struct Octet {
+  long r0;      // first point (a multiple of 8)
+  int i0, j, k;
+};
+__device__ __forceinline__ Octet octet_at(long q, const Box &bx) {
+  Octet o;
+  o.r0 = 8 * q;
+  const unsigned line = fast_div((unsigned)o.r0, bx.dx);
+  o.i0 = (int)((unsigned)o.r0 - line * (unsigned)bx.nx);
+  const unsigned kk = fast_div(line, bx.dy);
+  o.j = (int)(line - kk * (unsigned)bx.ny);
+  o.k = (int)kk;
+  return o;
+}
+
+// x values the octet's points of parity P (local index l = P + 2t) read:
+// centre line with its two outside neighbours, and the four neighbour lines.
+struct OctetX {
+  float xc[8], xs[8], xn[8], xb[8], xt[8];
+  float xl, xr;
+};
+__device__ __forceinline__ void load_octet_x(const float *x, const Octet &o, const Box &bx, OctetX &v) {
+  const long sy = bx.nx, sz = (long)bx.nx * bx.ny;
+  load8f(x + o.r0, v.xc);
+#pragma unroll
+  for (int l = 0; l < 8; ++l) v.xs[l] = v.xn[l] = v.xb[l] = v.xt[l] = 0.0f;
+  if (o.j > 0) load8f(x + o.r0 - sy, v.xs);
+  if (o.j < bx.ny - 1) load8f(x + o.r0 + sy, v.xn);
+  if (o.k > 0) load8f(x + o.r0 - sz, v.xb);
+  if (o.k < bx.nz - 1) load8f(x + o.r0 + sz, v.xt);
+  v.xl = o.i0 > 0 ? x[o.r0 - 1] : 0.0f;
+  v.xr = o.i0 + 8 < bx.nx ? x[o.r0 + 8] : 0.0f;
+}
+
+// Relaxed values of the octet's four points of parity P.
+template <int P>
+__device__ __forceinline__ void relax_octet(const float (&c)[4][8], const float (&bb)[8], const OctetX &v,
+                                            float (&out)[4]) {
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int l = P + 2 * t;
+    const float xw = l == 0 ? v.xl : v.xc[l == 0 ? 0 : l - 1];
+    const float xe = l == 7 ? v.xr : v.xc[l == 7 ? 7 : l + 1];
+    float acc = 0.0f;
+    acc = fmaf(c[t][1], xw, acc);
+    acc = fmaf(c[t][2], xe, acc);
+    acc = fmaf(c[t][3], v.xs[l], acc);
+    acc = fmaf(c[t][4], v.xn[l], acc);
+    acc = fmaf(c[t][5], v.xb[l], acc);
+    acc = fmaf(c[t][6], v.xt[l], acc);
+    out[t] = c[t][0] * (bb[l] - acc);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_relax_rb_oct(Recs<float, 8> R, const float *__restrict__ b, float *x,
+                                                           Box bx, int color, int zero_x, const int *gate) {
+  if (gate_off(gate)) return;
+  const long h = bx.n / 2, n8 = bx.n / 8;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n8; q += (long)gridDim.x * blockDim.x) {
+    const Octet o = octet_at(q, bx);
+    const int p = (o.j + o.k + color) & 1;  // the phase's points are l = p + 2t
+    const long m0 = (long)color * h + o.r0 / 2;
+    float c[4][8], bb[8];
+    load_recs4(R, m0, c);
+    load8f(b + o.r0, bb);
+    if (zero_x) {
+      // colour 0 from a zero guess: invd b on the phase's points, 0 on the others
+      float v[8];
+#pragma unroll
+      for (int l = 0; l < 8; ++l) v[l] = 0.0f;
+      if (p == 0) {
+#pragma unroll
+        for (int t = 0; t < 4; ++t) v[2 * t] = c[t][0] * bb[2 * t];
+      } else {
+#pragma unroll
+        for (int t = 0; t < 4; ++t) v[2 * t + 1] = c[t][0] * bb[2 * t + 1];
+      }
+      store8f(x + o.r0, v);
+      continue;
+    }
+    OctetX v;
+    load_octet_x(x, o, bx, v);
+    float out[4];
+    if (p == 0) {
+      relax_octet<0>(c, bb, v, out);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) x[o.r0 + 2 * t] = out[t];
+    } else {
+      relax_octet<1>(c, bb, v, out);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) x[o.r0 + 2 * t + 1] = out[t];
+    }
+  }
+}
+
+// Residual after a sweep that ended with colour 1 (k_residual_rb), octet form.
+template <int P>
+__device__ __forceinline__ void resid_octet(const float (&c)[4][8], const float (&bb)[8], const OctetX &v,
+                                            float (&res)[8]) {
+#pragma unroll
+  for (int l = 0; l < 8; ++l) res[l] = 0.0f;
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int l = P + 2 * t;
+    const float xw = l == 0 ? v.xl : v.xc[l == 0 ? 0 : l - 1];
+    const float xe = l == 7 ? v.xr : v.xc[l == 7 ? 7 : l + 1];
+    float acc = 0.0f;
+    acc = fmaf(c[t][7], v.xc[l], acc);
+    acc = fmaf(c[t][1], xw, acc);
+    acc = fmaf(c[t][2], xe, acc);
+    acc = fmaf(c[t][3], v.xs[l], acc);
+    acc = fmaf(c[t][4], v.xn[l], acc);
+    acc = fmaf(c[t][5], v.xb[l], acc);
+    acc = fmaf(c[t][6], v.xt[l], acc);
+    res[l] = bb[l] - acc;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_residual_rb_oct(Recs<float, 8> R, const float *__restrict__ b,
+                                                              const float *__restrict__ x, float *__restrict__ res,
+                                                              Box bx, const int *gate) {
+  if (gate_off(gate)) return;
+  const long n8 = bx.n / 8;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n8; q += (long)gridDim.x * blockDim.x) {
+    const Octet o = octet_at(q, bx);
+    const int p = (o.j + o.k) & 1;  // colour-0 points
+    float c[4][8], bb[8], rr[8];
+    load_recs4(R, o.r0 / 2, c);
+    load8f(b + o.r0, bb);
+    OctetX v;
+    load_octet_x(x, o, bx, v);
+    if (p == 0) resid_octet<0>(c, bb, v, rr);
+    else resid_octet<1>(c, bb, v, rr);
+    store8f(res + o.r0, rr);
+  }
+}
+
 // First phase from a zero guess: colour-0 points take invd b, colour-1 points 0.
 template <class T>
-__global__ void k_relax_rb_zero(const T *__restrict__ R, const T *__restrict__ b, T *x, Box bx, const int *gate) {
+__global__ void k_relax_rb_zero(Recs<T, 8> R, const T *__restrict__ b, T *x, Box bx, const int *gate) {
   if (gate_off(gate)) return;
   const long h = bx.n / 2;
   for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
     int i, j, k;
     const long r = rb_row(m, 0, bx, i, j, k);
-    x[r] = R[m * 8] * b[r];
+    x[r] = rec_ptr<T, 8>(R, m)[0] * b[r];
     x[r ^ 1] = T(0);
   }
 }
@@ -721,17 +951,28 @@ void dense_inverse(const std::vector<double> &A, int ns, const Box &b, std::vect
 // ---------------------------------------------------------------- host side
 // Colour-split copy of a relaxed 7-point level with an even nx (the fine
 // level), used by the in-place two-colour relaxation.
+// With record classes on, the records are replaced by their classes when
+// there are at most kMaxClasses distinct ones.
 template <class T>
 static void split_colors(cudaStream_t st, MgLevelT<T> &F, const MgParams &prm) {
   if (prm.relax != 2 || (F.b.nx & 1) || F.b.n < 2) return;
-  LaunchScope ls(K_SETUP, st, 0.0);
-  if (F.ns == 7) {
-    F.rb.alloc((size_t)8 * F.b.n);
-    k_split_colors<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, F.rb.p);
-  } else {
-    F.rb27.alloc((size_t)28 * F.b.n);
-    k_split_colors27<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, F.rb27.p);
+  DBuf<T> &R = F.ns == 7 ? F.rb : F.rb27;
+  const int W = F.ns == 7 ? 8 : 28;
+  R.alloc((size_t)W * F.b.n);
+  {
+    LaunchScope ls(K_SETUP, st, 0.0);
+    if (F.ns == 7) k_split_colors<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, R.p);
+    else k_split_colors27<T><<<grid_for(F.b.n), kThreads, 0, st>>>(F.A, F.invd.p, F.b, R.p);
   }
+  if (prm.classes && build_classes<T>(st, R.p, W, F.b.n, F.rbc)) R.release();
+}
+
+template <class T, int W>
+static Recs<T, W> recs_of(const DBuf<T> &plain, const Classes<T> &c) {
+  Recs<T, W> r;
+  if (c.ok() && c.W == W) { r.code = c.code.p; r.tab = c.tab.p; }
+  else r.R = plain.p;
+  return r;
 }
 
 template <>
@@ -910,20 +1151,42 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   T *cur = F.x.p, *oth = F.t.p;
   const double sweep_bytes = T_ * n * (F.ns + 4.0);
   const long h = n / 2;
+  // Colour-split records, plain or classed. Algorithmic bytes of a phase: the
+  // records of its colour, b of its colour, x of the other colour read and
+  // the phase's writes of x.
+  const Recs<T, 8> R7 = recs_of<T, 8>(F.rb, F.rbc);
+  const Recs<T, 28> R27 = recs_of<T, 28>(F.rb27, F.rbc);
+  const bool rb7 = R7.R || R7.code, rb27 = R27.R || R27.code;
+  const bool oct = F.b.nx % 8 == 0 && p.octets;  // octet kernels (FP32)
+  const double rec7 = R7.code ? 2.0 : 8.0 * T_, rec27 = R27.code ? 2.0 : 28.0 * T_;
   auto relax = [&](bool zero) {
-    if (p.relax == 2 && F.rb.p) {
-      {
-        LaunchScope ls(K_MG_RELAX_FINE, st, zero ? 2.5 * T_ * n : 5.0 * T_ * n);
-        if (zero) k_relax_rb_zero<T><<<grid_all(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, gate);
-        else k_relax_rb<T><<<grid_all(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 0, gate);
+    if constexpr (sizeof(T) == 4) {
+      if (p.relax == 2 && rb7 && oct) {
+        {
+          LaunchScope ls(K_MG_RELAX_FINE, st, zero ? 0.5 * n * (R7.code ? 2.0 : T_) + 1.5 * T_ * n
+                                                   : 0.5 * n * rec7 + 1.5 * T_ * n);
+          k_relax_rb_oct<<<grid_all(n / 8), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, 0, zero, gate);
+        }
+        LaunchScope ls(K_MG_RELAX_FINE, st, 0.5 * n * rec7 + 1.5 * T_ * n);
+        k_relax_rb_oct<<<grid_all(n / 8), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, 1, 0, gate);
+        return;
       }
-      LaunchScope ls(K_MG_RELAX_FINE, st, 5.0 * T_ * n);
-      k_relax_rb<T><<<grid_all(h), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.b, 1, gate);
-    } else if (p.relax == 2 && F.rb27.p) {
+    }
+    if (p.relax == 2 && rb7) {
+      {
+        LaunchScope ls(K_MG_RELAX_FINE, st, zero ? 0.5 * n * (R7.code ? 2.0 : T_) + 1.5 * T_ * n
+                                                 : 0.5 * n * rec7 + 1.5 * T_ * n);
+        if (zero) k_relax_rb_zero<T><<<grid_all(h), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, gate);
+        else k_relax_rb<T><<<grid_all(h), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, 0, gate);
+      }
+      LaunchScope ls(K_MG_RELAX_FINE, st, 0.5 * n * rec7 + 1.5 * T_ * n);
+      k_relax_rb<T><<<grid_all(h), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, 1, gate);
+    } else if (p.relax == 2 && rb27) {
       for (int color = 0; color < 2; ++color) {
         const bool z = zero && color == 0;
-        LaunchScope ls(K_MG_RELAX, st, z ? 2.5 * T_ * n : T_ * n * (14.0 + 3.0));
-        k_relax_rb27<T><<<grid_all(h), kThreads, 0, st>>>(F.rb27.p, F.bv.p, cur, oth, F.b, color, z, gate);
+        LaunchScope ls(K_MG_RELAX, st, z ? 0.5 * n * (R27.code ? 2.0 : T_) + 1.5 * T_ * n
+                                         : 0.5 * n * rec27 + 2.5 * T_ * n);
+        k_relax_rb27<T><<<grid_all(h), kThreads, 0, st>>>(R27, F.bv.p, cur, oth, F.b, color, z, gate);
         std::swap(cur, oth);
       }
     } else if (p.relax == 2) {
@@ -952,9 +1215,20 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   const int nu1 = F.relax ? c1 : 0, nu2 = F.relax ? c2 : 0;
   for (int s = 0; s < nu1; ++s) relax(s == 0);
   const T *res = F.bv.p;  // residual of a zero initial guess is b
-  if (nu1 > 0 && p.relax == 2 && F.rb.p) {
-    LaunchScope ls(K_MG_RESID, st, T_ * n * 6.5);
-    k_residual_rb<T><<<grid_all(n / 2), kThreads, 0, st>>>(F.rb.p, F.bv.p, cur, F.r.p, F.b, gate);
+  if (nu1 > 0 && p.relax == 2 && rb7) {
+    LaunchScope ls(K_MG_RESID, st, 0.5 * n * rec7 + 2.5 * T_ * n);
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+      if (oct) {
+        k_residual_rb_oct<<<grid_all(n / 8), kThreads, 0, st>>>(R7, F.bv.p, cur, F.r.p, F.b, gate);
+        done = true;
+      }
+    }
+    if (!done) k_residual_rb<T><<<grid_all(n / 2), kThreads, 0, st>>>(R7, F.bv.p, cur, F.r.p, F.b, gate);
+    res = F.r.p;
+  } else if (nu1 > 0 && p.relax == 2 && rb27) {
+    LaunchScope ls(K_MG_RESID, st, n * rec27 + 3.0 * T_ * n);
+    k_residual_rb27<T><<<grid_all(n), kThreads, 0, st>>>(R27, F.bv.p, cur, F.r.p, F.b, gate);
     res = F.r.p;
   } else if (nu1 > 0) {
     LaunchScope ls(K_MG_RESID, st, T_ * n * (F.ns + 3.0));
@@ -1042,8 +1316,8 @@ void Multigrid::level_coef27(cudaStream_t st, int l, double *host_out) const {
 
 size_t Multigrid::bytes() const {
   size_t b = 0;
-  for (const auto &F : L64) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes() + F.rb27.bytes();
-  for (const auto &F : L32) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes() + F.rb27.bytes();
+  for (const auto &F : L64) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes() + F.rb27.bytes() + F.rbc.bytes();
+  for (const auto &F : L32) b += F.Aown.bytes() + F.wd.bytes() + F.invd.bytes() + F.pm.bytes() + F.pp.bytes() + F.x.bytes() + F.bv.bytes() + F.r.bytes() + F.t.bytes() + F.dense.bytes() + F.rb.bytes() + F.rb27.bytes() + F.rbc.bytes();
   return b;
 }
 

@@ -16,6 +16,8 @@ struct MgParams {
   int nu_coarse = 0;    // sweeps each way on the coarser relaxed levels (0: nu1 / nu2)
   double group_ratio = 0.0;  // see ibm_solver_params.mg_group_ratio
   int options = 3;      // see ibm_solver_params.mg_options
+  int classes = 1;      // colour-split records as record classes where they repeat (ibm_classes.cu)
+  int octets = 1;       // FP32 7-point phases eight points per thread (nx % 8 == 0)
 };
 
 template <class T>
@@ -28,6 +30,7 @@ struct MgLevelT {
   DBuf<T> Aown, wd, invd, pm, pp, x, bv, r, t, dense;
   DBuf<T> rb;           // colour-split coefficients for the in-place two-colour relaxation (7-point, even nx)
   DBuf<T> rb27;         // colour-split 27-point coefficients + inverse diagonal (two-colour relaxation)
+  Classes<T> rbc;       // the classes of rb or rb27 (W 8 or 28); the plain records are then released
 };
 
 class Multigrid {

@@ -96,6 +96,12 @@ typedef struct ibm_solver_params {
                             this factor (default 1e-5, about what an FP32 basis resolves); the FP64
                             restart then measures the true residual */
   int compute_forces;    /* 1: fill ibm_step_stats.force each step (one extra kernel); default 0 */
+  int row_classes;       /* 1 (default): where an operator repeats few distinct rows (every fluid cell
+                            away from walls and bodies has the same ones), kernels read a 2-byte class
+                            per row and the row from a table of the distinct rows; results are bitwise
+                            those of the plain layout. 0: plain layout */
+  int mg_octets;         /* 1 (default): FP32 two-colour phases of 7-point levels with nx % 8 == 0 take
+                            eight points per thread (same arithmetic, bitwise equal results) */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {

@@ -1,0 +1,85 @@
+"""Record classes (row_classes = 1, the default) against the plain layout.
+
+Kernels that read a 2-byte class per row and the row from the table of
+distinct rows compute with the same values in the same order as the kernels
+that read the rows themselves, so every result must be bitwise equal. The
+algorithmic bytes the library books for the class-reading kernels show that
+the classes were in use.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
+
+
+@pytest.fixture(scope="module")
+def case48(ibm):
+    return ibm.Case(ibm.channel_params(48, 16, 16, Um=1.0, dt=1e-3))
+
+
+def bench_like(ibm, **kw):
+    base = dict(vel_tol=1e-10, p_tol=1e-10, p_pc_rap_type=0, p_pc_relax_type=2, mg_nu1=3, mg_nu2=3,
+                mg_nu_coarse=2, mg_omega=1.0, mg_group_ratio=1.5, mg_options=3)
+    base.update(kw)
+    return ibm.solver_params(**base)
+
+
+def relax_fine_bytes_per_launch(ibm, solver, r):
+    k = ibm.kernel_names().index("mg_relax_fine")
+    solver.profile_reset()
+    solver.apply_preconditioner(ibm.FIELD_P, r)
+    prof = solver.profile()
+    assert prof.launches[k] > 0
+    return prof.bytes[k] / prof.launches[k]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("rap", [0, 1])
+def test_vcycle_bitwise_with_classes(ibm, case48, precision, rap):
+    r = np.random.default_rng(5).standard_normal(case48.shape[0] * case48.shape[1] * case48.shape[2])
+    a = ibm.Solver(case48, bench_like(ibm, precision=precision, p_pc_rap_type=rap, row_classes=0))
+    b = ibm.Solver(case48, bench_like(ibm, precision=precision, p_pc_rap_type=rap, row_classes=1))
+    za = a.apply_preconditioner(ibm.FIELD_P, r)
+    zb = b.apply_preconditioner(ibm.FIELD_P, r)
+    assert bits_equal(za, zb)
+    # classed records book 2 bytes per record instead of 8 values
+    assert relax_fine_bytes_per_launch(ibm, b, r) < 0.6 * relax_fine_bytes_per_launch(ibm, a, r)
+
+
+@pytest.mark.parametrize("classes", [0, 1])
+def test_vcycle_octets_bitwise(ibm, case48, classes):
+    """Eight points per thread (FP32 phases and residual of the finest level)
+    against one point per thread."""
+    r = np.random.default_rng(8).standard_normal(case48.shape[0] * case48.shape[1] * case48.shape[2])
+    z = [ibm.Solver(case48, bench_like(ibm, precision=1, row_classes=classes, mg_octets=o))
+         .apply_preconditioner(ibm.FIELD_P, r) for o in (0, 1)]
+    assert bits_equal(z[0], z[1])
+
+
+@pytest.mark.parametrize("precision,graph", [(0, 0), (1, 0), (2, 0), (2, 1)])
+def test_steps_bitwise_with_classes(ibm, case48, precision, graph):
+    a = ibm.Solver(case48, bench_like(ibm, precision=precision, use_graph=graph, row_classes=0))
+    b = ibm.Solver(case48, bench_like(ibm, precision=precision, use_graph=graph, row_classes=1))
+    for step in range(1, 6):
+        ramp = min(1.0, step / 3.0)
+        sa = a.step(ramp)
+        sb = b.step(ramp)
+        assert sa.status == sb.status == ibm.IBM_OK
+        for f in "uvwp":
+            assert getattr(sa, f).iters == getattr(sb, f).iters, f
+    for x, y, name in zip(a.fields(), b.fields(), "uvwp"):
+        assert bits_equal(x, y), name
+    if graph == 0:
+        # the true residuals read 2-byte classes instead of 7 FP64 coefficients
+        k = ibm.kernel_names().index("gmres_residual")
+        per = []
+        for s in (a, b):
+            s.profile_reset()
+            s.step(1.0)
+            prof = s.profile()
+            per.append(prof.bytes[k] / max(prof.launches[k], 1))
+        assert per[1] < 0.5 * per[0]
