@@ -304,7 +304,7 @@ void ensure_solvers(ibm_ctx *c) {
     mp.options = p.mg_options;
     mp.nu_coarse = p.mg_nu_coarse;
     mp.classes = p.row_classes ? 1 : 0;
-    mp.octets = p.mg_octets ? 1 : 0;
+    mp.quads = p.mg_quads ? 1 : 0;
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
     const double *winv = ((p.mg_options & 2) && c->p_sym) ? c->p_winv.p : nullptr;
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
@@ -425,7 +425,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->cycle_rtol32 = 1e-5;
   p->compute_forces = 0;
   p->row_classes = 1;
-  p->mg_octets = 1;
+  p->mg_quads = 1;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -963,6 +963,7 @@ int ibm_solve(ibm_ctx *c, int field, const double *b, double *x, ibm_solve_stats
     }
     IBM_CUDA_TRY(cudaMemcpyAsync(x, c->xb[field].p, sizeof(double) * n, cudaMemcpyDefault, c->st));
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->prof.drain();
     if (stats) fill_solve(*stats, r[0]);
     if (r[0].nonfinite) { c->err = "non-finite solve output"; return (int)IBM_ERR_NONFINITE; }
     return solve_status(r[0]);
@@ -1007,7 +1008,8 @@ int ibm_apply_preconditioner(ibm_ctx *c, int field, const double *r, double *z) 
         c->mg.apply(c->st, in, out, nullptr, true);
         std::vector<float> hz(b.n);
         IBM_CUDA_TRY(cudaMemcpyAsync(hz.data(), zf.p, sizeof(float) * b.n, cudaMemcpyDeviceToHost, c->st));
-        IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+            IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+            c->prof.drain();
         std::vector<double> zd(hz.begin(), hz.end());
         IBM_CUDA_TRY(cudaMemcpy(z, zd.data(), sizeof(double) * b.n, cudaMemcpyDefault));
         return IBM_OK;
@@ -1023,6 +1025,7 @@ int ibm_apply_preconditioner(ibm_ctx *c, int field, const double *r, double *z) 
     }
     IBM_CUDA_TRY(cudaMemcpyAsync(z, dz.p, sizeof(double) * b.n, cudaMemcpyDefault, c->st));
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    c->prof.drain();
     return IBM_OK;
   });
 }

@@ -546,173 +546,153 @@ __global__ void __launch_bounds__(kThreads) k_residual_rb(Recs<T, 8> R, const T 
   }
 }
 
-// Octet form of the FP32 in-place phases (nx a multiple of 8): a thread takes
-// eight consecutive points of a line, four of each colour, and issues every
-// load it needs (the four records, b and the x values of its own and the four
-// neighbouring lines, as 16-byte vectors) before it computes. One point per
-// thread leaves the phase latency-bound on its dependent loads; the octet
-// gives each thread about twenty independent loads in flight. Per point the
-// arithmetic is k_relax_rb's / k_residual_rb's, in the same order.
-__device__ __forceinline__ void load8f(const float *__restrict__ p, float (&v)[8]) {
-  const float4 a = *reinterpret_cast<const float4 *>(p), c = *reinterpret_cast<const float4 *>(p + 4);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = c.x; v[5] = c.y; v[6] = c.z; v[7] = c.w;
-}
-__device__ __forceinline__ void store8f(float *p, const float (&v)[8]) {
-  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
-  *reinterpret_cast<float4 *>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
-}
-// The four records of the octet's points of one colour (record indices m0..m0+3).
-__device__ __forceinline__ void load_recs4(const Recs<float, 8> &s, long m0, float (&c)[4][8]) {
-  if (s.code) {
-    const ushort4 k4 = __ldcs(reinterpret_cast<const ushort4 *>(s.code + m0));
-    const unsigned short ks[4] = {k4.x, k4.y, k4.z, k4.w};
+// Quartet form of the FP32 in-place phases (nx a multiple of 4): a thread
+// takes four consecutive points of a line, two of each colour, and issues its
+// loads (two records, b and the x values of its own and the four neighbouring
+// lines as 16-byte vectors) before it computes. One point per thread leaves a
+// phase latency-bound on its dependent loads; the quad puts about a dozen
+// independent loads in flight per thread at 60 registers (four blocks per SM).
+// Per point the arithmetic is k_relax_rb's, in the same order.
+// The two records of a quad's points of one colour (record indices m0, m0+1).
+__device__ __forceinline__ void load_quad_recs(const Recs<float, 8> &R, long m0, float (&c)[2][8]) {
+  if (R.code) {
+    const ushort2 k2 = __ldcs(reinterpret_cast<const ushort2 *>(R.code + m0));
+    const unsigned short ks[2] = {k2.x, k2.y};
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-      const float4 *q = reinterpret_cast<const float4 *>(s.tab + 8 * (long)ks[t]);
-      const float4 a = __ldg(q), e = __ldg(q + 1);
-      c[t][0] = a.x; c[t][1] = a.y; c[t][2] = a.z; c[t][3] = a.w;
-      c[t][4] = e.x; c[t][5] = e.y; c[t][6] = e.z; c[t][7] = e.w;
+    for (int t = 0; t < 2; ++t) {
+      const float4 *qq = reinterpret_cast<const float4 *>(R.tab + 8 * (long)ks[t]);
+      const float4 u = __ldg(qq), w = __ldg(qq + 1);
+      c[t][0] = u.x; c[t][1] = u.y; c[t][2] = u.z; c[t][3] = u.w;
+      c[t][4] = w.x; c[t][5] = w.y; c[t][6] = w.z; c[t][7] = w.w;
     }
   } else {
 #pragma unroll
-    for (int t = 0; t < 4; ++t) load_rec<float, 8>(s.R + (m0 + t) * 8, c[t]);
+    for (int t = 0; t < 2; ++t) load_rec<float, 8>(R.R + (m0 + t) * 8, c[t]);
   }
 }
 
-struct Octet {
-  long r0;      // first point (a multiple of 8)
-  int i0, j, k;
-};
-__device__ __forceinline__ Octet octet_at(long q, const Box &bx) {
-  Octet o;
-  o.r0 = 8 * q;
-  const unsigned line = fast_div((unsigned)o.r0, bx.dx);
-  o.i0 = (int)((unsigned)o.r0 - line * (unsigned)bx.nx);
-  const unsigned kk = fast_div(line, bx.dy);
-  o.j = (int)(line - kk * (unsigned)bx.ny);
-  o.k = (int)kk;
-  return o;
-}
-
-// x values the octet's points of parity P (local index l = P + 2t) read:
-// centre line with its two outside neighbours, and the four neighbour lines.
-struct OctetX {
-  float xc[8], xs[8], xn[8], xb[8], xt[8];
-  float xl, xr;
-};
-__device__ __forceinline__ void load_octet_x(const float *x, const Octet &o, const Box &bx, OctetX &v) {
-  const long sy = bx.nx, sz = (long)bx.nx * bx.ny;
-  load8f(x + o.r0, v.xc);
-#pragma unroll
-  for (int l = 0; l < 8; ++l) v.xs[l] = v.xn[l] = v.xb[l] = v.xt[l] = 0.0f;
-  if (o.j > 0) load8f(x + o.r0 - sy, v.xs);
-  if (o.j < bx.ny - 1) load8f(x + o.r0 + sy, v.xn);
-  if (o.k > 0) load8f(x + o.r0 - sz, v.xb);
-  if (o.k < bx.nz - 1) load8f(x + o.r0 + sz, v.xt);
-  v.xl = o.i0 > 0 ? x[o.r0 - 1] : 0.0f;
-  v.xr = o.i0 + 8 < bx.nx ? x[o.r0 + 8] : 0.0f;
-}
-
-// Relaxed values of the octet's four points of parity P.
 template <int P>
-__device__ __forceinline__ void relax_octet(const float (&c)[4][8], const float (&bb)[8], const OctetX &v,
-                                            float (&out)[4]) {
+__device__ __forceinline__ void relax_quad(const float (&c)[2][8], const float4 &bq, const float4 &xc,
+                                           const float4 &xs, const float4 &xn, const float4 &xb, const float4 &xt,
+                                           float xl, float xr, float (&out)[2]) {
+  const float cc[4] = {xc.x, xc.y, xc.z, xc.w}, ss[4] = {xs.x, xs.y, xs.z, xs.w}, nn[4] = {xn.x, xn.y, xn.z, xn.w};
+  const float bo[4] = {xb.x, xb.y, xb.z, xb.w}, tt[4] = {xt.x, xt.y, xt.z, xt.w}, bb[4] = {bq.x, bq.y, bq.z, bq.w};
 #pragma unroll
-  for (int t = 0; t < 4; ++t) {
+  for (int t = 0; t < 2; ++t) {
     const int l = P + 2 * t;
-    const float xw = l == 0 ? v.xl : v.xc[l == 0 ? 0 : l - 1];
-    const float xe = l == 7 ? v.xr : v.xc[l == 7 ? 7 : l + 1];
+    const float xw = l == 0 ? xl : cc[l == 0 ? 0 : l - 1];
+    const float xe = l == 3 ? xr : cc[l == 3 ? 3 : l + 1];
     float acc = 0.0f;
     acc = fmaf(c[t][1], xw, acc);
     acc = fmaf(c[t][2], xe, acc);
-    acc = fmaf(c[t][3], v.xs[l], acc);
-    acc = fmaf(c[t][4], v.xn[l], acc);
-    acc = fmaf(c[t][5], v.xb[l], acc);
-    acc = fmaf(c[t][6], v.xt[l], acc);
+    acc = fmaf(c[t][3], ss[l], acc);
+    acc = fmaf(c[t][4], nn[l], acc);
+    acc = fmaf(c[t][5], bo[l], acc);
+    acc = fmaf(c[t][6], tt[l], acc);
     out[t] = c[t][0] * (bb[l] - acc);
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_relax_rb_oct(Recs<float, 8> R, const float *__restrict__ b, float *x,
-                                                           Box bx, int color, int zero_x, const int *gate) {
+__global__ void __launch_bounds__(kThreads) k_relax_rb_quad(Recs<float, 8> R, const float *__restrict__ b, float *x,
+                                                            Box bx, int color, int zero_x, const int *gate) {
   if (gate_off(gate)) return;
-  const long h = bx.n / 2, n8 = bx.n / 8;
-  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n8; q += (long)gridDim.x * blockDim.x) {
-    const Octet o = octet_at(q, bx);
-    const int p = (o.j + o.k + color) & 1;  // the phase's points are l = p + 2t
-    const long m0 = (long)color * h + o.r0 / 2;
-    float c[4][8], bb[8];
-    load_recs4(R, m0, c);
-    load8f(b + o.r0, bb);
+  const long h = bx.n / 2, n4 = bx.n / 4;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const long sy = nx, sz = (long)nx * ny;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+    const long r0 = 4 * q;
+    const unsigned line = fast_div((unsigned)r0, bx.dx);
+    const int i0 = (int)((unsigned)r0 - line * (unsigned)nx);
+    const unsigned kk = fast_div(line, bx.dy);
+    const int j = (int)(line - kk * (unsigned)ny), k = (int)kk;
+    const int p = (j + k + color) & 1;
+    const long m0 = (long)color * h + r0 / 2;
+    float c[2][8];
+    load_quad_recs(R, m0, c);
+    const float4 bq = *reinterpret_cast<const float4 *>(b + r0);
     if (zero_x) {
-      // colour 0 from a zero guess: invd b on the phase's points, 0 on the others
-      float v[8];
-#pragma unroll
-      for (int l = 0; l < 8; ++l) v[l] = 0.0f;
-      if (p == 0) {
-#pragma unroll
-        for (int t = 0; t < 4; ++t) v[2 * t] = c[t][0] * bb[2 * t];
-      } else {
-#pragma unroll
-        for (int t = 0; t < 4; ++t) v[2 * t + 1] = c[t][0] * bb[2 * t + 1];
-      }
-      store8f(x + o.r0, v);
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (p == 0) { v.x = c[0][0] * bq.x; v.z = c[1][0] * bq.z; }
+      else { v.y = c[0][0] * bq.y; v.w = c[1][0] * bq.w; }
+      *reinterpret_cast<float4 *>(x + r0) = v;
       continue;
     }
-    OctetX v;
-    load_octet_x(x, o, bx, v);
-    float out[4];
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 xc = *reinterpret_cast<const float4 *>(x + r0);
+    const float4 xs = j > 0 ? *reinterpret_cast<const float4 *>(x + r0 - sy) : z4;
+    const float4 xn = j < ny - 1 ? *reinterpret_cast<const float4 *>(x + r0 + sy) : z4;
+    const float4 xb = k > 0 ? *reinterpret_cast<const float4 *>(x + r0 - sz) : z4;
+    const float4 xt = k < nz - 1 ? *reinterpret_cast<const float4 *>(x + r0 + sz) : z4;
+    const float xl = i0 > 0 ? x[r0 - 1] : 0.0f;
+    const float xr = i0 + 4 < nx ? x[r0 + 4] : 0.0f;
+    float out[2];
     if (p == 0) {
-      relax_octet<0>(c, bb, v, out);
-#pragma unroll
-      for (int t = 0; t < 4; ++t) x[o.r0 + 2 * t] = out[t];
+      relax_quad<0>(c, bq, xc, xs, xn, xb, xt, xl, xr, out);
+      x[r0] = out[0];
+      x[r0 + 2] = out[1];
     } else {
-      relax_octet<1>(c, bb, v, out);
-#pragma unroll
-      for (int t = 0; t < 4; ++t) x[o.r0 + 2 * t + 1] = out[t];
+      relax_quad<1>(c, bq, xc, xs, xn, xb, xt, xl, xr, out);
+      x[r0 + 1] = out[0];
+      x[r0 + 3] = out[1];
     }
   }
 }
 
-// Residual after a sweep that ended with colour 1 (k_residual_rb), octet form.
+// Residual after a sweep that ended with colour 1 (k_residual_rb), quartet
+// form: colour-0 points b - A x in k_residual_rb's order, colour-1 points 0.
 template <int P>
-__device__ __forceinline__ void resid_octet(const float (&c)[4][8], const float (&bb)[8], const OctetX &v,
-                                            float (&res)[8]) {
+__device__ __forceinline__ void resid_quad(const float (&c)[2][8], const float4 &bq, const float4 &xc,
+                                           const float4 &xs, const float4 &xn, const float4 &xb, const float4 &xt,
+                                           float xl, float xr, float (&res)[4]) {
+  const float cc[4] = {xc.x, xc.y, xc.z, xc.w}, ss[4] = {xs.x, xs.y, xs.z, xs.w}, nn[4] = {xn.x, xn.y, xn.z, xn.w};
+  const float bo[4] = {xb.x, xb.y, xb.z, xb.w}, tt[4] = {xt.x, xt.y, xt.z, xt.w}, bb[4] = {bq.x, bq.y, bq.z, bq.w};
 #pragma unroll
-  for (int l = 0; l < 8; ++l) res[l] = 0.0f;
+  for (int l = 0; l < 4; ++l) res[l] = 0.0f;
 #pragma unroll
-  for (int t = 0; t < 4; ++t) {
+  for (int t = 0; t < 2; ++t) {
     const int l = P + 2 * t;
-    const float xw = l == 0 ? v.xl : v.xc[l == 0 ? 0 : l - 1];
-    const float xe = l == 7 ? v.xr : v.xc[l == 7 ? 7 : l + 1];
+    const float xw = l == 0 ? xl : cc[l == 0 ? 0 : l - 1];
+    const float xe = l == 3 ? xr : cc[l == 3 ? 3 : l + 1];
     float acc = 0.0f;
-    acc = fmaf(c[t][7], v.xc[l], acc);
+    acc = fmaf(c[t][7], cc[l], acc);
     acc = fmaf(c[t][1], xw, acc);
     acc = fmaf(c[t][2], xe, acc);
-    acc = fmaf(c[t][3], v.xs[l], acc);
-    acc = fmaf(c[t][4], v.xn[l], acc);
-    acc = fmaf(c[t][5], v.xb[l], acc);
-    acc = fmaf(c[t][6], v.xt[l], acc);
+    acc = fmaf(c[t][3], ss[l], acc);
+    acc = fmaf(c[t][4], nn[l], acc);
+    acc = fmaf(c[t][5], bo[l], acc);
+    acc = fmaf(c[t][6], tt[l], acc);
     res[l] = bb[l] - acc;
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_residual_rb_oct(Recs<float, 8> R, const float *__restrict__ b,
-                                                              const float *__restrict__ x, float *__restrict__ res,
-                                                              Box bx, const int *gate) {
+__global__ void __launch_bounds__(kThreads) k_residual_rb_quad(Recs<float, 8> R, const float *__restrict__ b,
+                                                               const float *__restrict__ x, float *__restrict__ res,
+                                                               Box bx, const int *gate) {
   if (gate_off(gate)) return;
-  const long n8 = bx.n / 8;
-  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n8; q += (long)gridDim.x * blockDim.x) {
-    const Octet o = octet_at(q, bx);
-    const int p = (o.j + o.k) & 1;  // colour-0 points
-    float c[4][8], bb[8], rr[8];
-    load_recs4(R, o.r0 / 2, c);
-    load8f(b + o.r0, bb);
-    OctetX v;
-    load_octet_x(x, o, bx, v);
-    if (p == 0) resid_octet<0>(c, bb, v, rr);
-    else resid_octet<1>(c, bb, v, rr);
-    store8f(res + o.r0, rr);
+  const long n4 = bx.n / 4;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const long sy = nx, sz = (long)nx * ny;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+    const long r0 = 4 * q;
+    const unsigned line = fast_div((unsigned)r0, bx.dx);
+    const int i0 = (int)((unsigned)r0 - line * (unsigned)nx);
+    const unsigned kk = fast_div(line, bx.dy);
+    const int j = (int)(line - kk * (unsigned)ny), k = (int)kk;
+    float c[2][8];
+    load_quad_recs(R, r0 / 2, c);
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 bq = *reinterpret_cast<const float4 *>(b + r0);
+    const float4 xc = *reinterpret_cast<const float4 *>(x + r0);
+    const float4 xs = j > 0 ? *reinterpret_cast<const float4 *>(x + r0 - sy) : z4;
+    const float4 xn = j < ny - 1 ? *reinterpret_cast<const float4 *>(x + r0 + sy) : z4;
+    const float4 xb = k > 0 ? *reinterpret_cast<const float4 *>(x + r0 - sz) : z4;
+    const float4 xt = k < nz - 1 ? *reinterpret_cast<const float4 *>(x + r0 + sz) : z4;
+    const float xl = i0 > 0 ? x[r0 - 1] : 0.0f;
+    const float xr = i0 + 4 < nx ? x[r0 + 4] : 0.0f;
+    float rr[4];
+    if (((j + k) & 1) == 0) resid_quad<0>(c, bq, xc, xs, xn, xb, xt, xl, xr, rr);
+    else resid_quad<1>(c, bq, xc, xs, xn, xb, xt, xl, xr, rr);
+    *reinterpret_cast<float4 *>(res + r0) = make_float4(rr[0], rr[1], rr[2], rr[3]);
   }
 }
 
@@ -1157,18 +1137,17 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   const Recs<T, 8> R7 = recs_of<T, 8>(F.rb, F.rbc);
   const Recs<T, 28> R27 = recs_of<T, 28>(F.rb27, F.rbc);
   const bool rb7 = R7.R || R7.code, rb27 = R27.R || R27.code;
-  const bool oct = F.b.nx % 8 == 0 && p.octets;  // octet kernels (FP32)
+  const bool quad = F.b.nx % 4 == 0 && p.quads;  // quartet kernels (FP32)
   const double rec7 = R7.code ? 2.0 : 8.0 * T_, rec27 = R27.code ? 2.0 : 28.0 * T_;
   auto relax = [&](bool zero) {
     if constexpr (sizeof(T) == 4) {
-      if (p.relax == 2 && rb7 && oct) {
-        {
-          LaunchScope ls(K_MG_RELAX_FINE, st, zero ? 0.5 * n * (R7.code ? 2.0 : T_) + 1.5 * T_ * n
-                                                   : 0.5 * n * rec7 + 1.5 * T_ * n);
-          k_relax_rb_oct<<<grid_all(n / 8), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, 0, zero, gate);
+      if (p.relax == 2 && rb7 && quad) {
+        for (int color = 0; color < 2; ++color) {
+          const bool z = zero && color == 0;
+          LaunchScope ls(K_MG_RELAX_FINE, st, z ? 0.5 * n * (R7.code ? 2.0 : T_) + 1.5 * T_ * n
+                                                : 0.5 * n * rec7 + 1.5 * T_ * n);
+          k_relax_rb_quad<<<grid_all(n / 4), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, color, z, gate);
         }
-        LaunchScope ls(K_MG_RELAX_FINE, st, 0.5 * n * rec7 + 1.5 * T_ * n);
-        k_relax_rb_oct<<<grid_all(n / 8), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, 1, 0, gate);
         return;
       }
     }
@@ -1219,8 +1198,8 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
     LaunchScope ls(K_MG_RESID, st, 0.5 * n * rec7 + 2.5 * T_ * n);
     bool done = false;
     if constexpr (sizeof(T) == 4) {
-      if (oct) {
-        k_residual_rb_oct<<<grid_all(n / 8), kThreads, 0, st>>>(R7, F.bv.p, cur, F.r.p, F.b, gate);
+      if (quad) {
+        k_residual_rb_quad<<<grid_all(n / 4), kThreads, 0, st>>>(R7, F.bv.p, cur, F.r.p, F.b, gate);
         done = true;
       }
     }

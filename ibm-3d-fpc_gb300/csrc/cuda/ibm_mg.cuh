@@ -17,7 +17,7 @@ struct MgParams {
   double group_ratio = 0.0;  // see ibm_solver_params.mg_group_ratio
   int options = 3;      // see ibm_solver_params.mg_options
   int classes = 1;      // colour-split records as record classes where they repeat (ibm_classes.cu)
-  int octets = 1;       // FP32 7-point phases eight points per thread (nx % 8 == 0)
+  int quads = 1;        // FP32 7-point phases and residual four points per thread (nx % 4 == 0)
 };
 
 template <class T>

@@ -100,8 +100,8 @@ typedef struct ibm_solver_params {
                             away from walls and bodies has the same ones), kernels read a 2-byte class
                             per row and the row from a table of the distinct rows; results are bitwise
                             those of the plain layout. 0: plain layout */
-  int mg_octets;         /* 1 (default): FP32 two-colour phases of 7-point levels with nx % 8 == 0 take
-                            eight points per thread (same arithmetic, bitwise equal results) */
+  int mg_quads;          /* 1 (default): FP32 two-colour phases and residual of 7-point levels with
+                            nx % 4 == 0 take four points per thread (same arithmetic, bitwise equal) */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {

@@ -51,12 +51,14 @@ def test_vcycle_bitwise_with_classes(ibm, case48, precision, rap):
 
 
 @pytest.mark.parametrize("classes", [0, 1])
-def test_vcycle_octets_bitwise(ibm, case48, classes):
-    """Eight points per thread (FP32 phases and residual of the finest level)
-    against one point per thread."""
-    r = np.random.default_rng(8).standard_normal(case48.shape[0] * case48.shape[1] * case48.shape[2])
-    z = [ibm.Solver(case48, bench_like(ibm, precision=1, row_classes=classes, mg_octets=o))
-         .apply_preconditioner(ibm.FIELD_P, r) for o in (0, 1)]
+@pytest.mark.parametrize("shape", [(48, 16, 16), (36, 10, 7)])
+def test_vcycle_quads_bitwise(ibm, classes, shape):
+    """Four points per thread (FP32 phases and residual of 7-point levels)
+    against one point per thread, including odd line and plane counts."""
+    case = ibm.Case(ibm.channel_params(*shape, Um=1.0, dt=1e-3))
+    r = np.random.default_rng(8).standard_normal(shape[0] * shape[1] * shape[2])
+    z = [ibm.Solver(case, bench_like(ibm, precision=1, row_classes=classes, mg_quads=q))
+         .apply_preconditioner(ibm.FIELD_P, r) for q in (0, 1)]
     assert bits_equal(z[0], z[1])
 
 
