@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mg-coarse-max", type=int, default=640,
+                    help="multigrid: largest level solved directly (dense inverse)")
     ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
                     help="mixed form: 1 = FP32 preconditioners in FP64 GMRES, 2 = also FP32 Arnoldi cycles")
     return ap.parse_args()
@@ -90,10 +92,10 @@ def initial_state(case, seed=2026):
     return u, v, w, p
 
 
-def solver_params(ibm, precision, graph=0):
+def solver_params(ibm, precision, graph=0, coarse_max=640):
     return ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, vel_maxit=250, p_maxit=250, vel_kdim=50, p_kdim=50,
                              p_pc=1, p_pc_rap_type=0, p_pc_relax_type=2, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_omega=1.0,
-                             mg_group_ratio=1.5, mg_coarse_max=64, mg_options=3, precision=precision,
+                             mg_group_ratio=1.5, mg_coarse_max=coarse_max, mg_options=3, precision=precision,
                              vel_inner_sweeps=2, use_graph=graph)
 
 
@@ -359,7 +361,7 @@ def main():
     t_setup = time.perf_counter()
     case = ibm.Case(case_params(ibm, nx, ny, nz))
     state = initial_state(case)
-    mixed = ibm.Solver(case, solver_params(ibm, args.precision, graph=1), device=local)
+    mixed = ibm.Solver(case, solver_params(ibm, args.precision, graph=1, coarse_max=args.mg_coarse_max), device=local)
     mixed.set_fields(*state)
     setup_s = time.perf_counter() - t_setup
 

@@ -476,6 +476,69 @@ __global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(Recs<T, 28> R, const
   }
 }
 
+// Quartet form of the FP32 27-point phase (nx a multiple of 4): a thread
+// takes four consecutive points of a line, loads the 9 x 6 window of x values
+// their stencils touch (16-byte loads plus the two edge values per line, 0
+// outside the box) and writes the pair's four outputs with one 16-byte store:
+// the phase colour's points relaxed, the others copied. Per point the
+// arithmetic is k_relax_rb27's, in the same slot order.
+__global__ void __launch_bounds__(kThreads) k_relax_rb27_quad(Recs<float, 28> R, const float *__restrict__ b,
+                                                              const float *__restrict__ x, float *__restrict__ t,
+                                                              Box bx, int color, int zero_x, const int *gate) {
+  if (gate_off(gate)) return;
+  const long h = bx.n / 2, n4 = bx.n / 4;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+    const long r0 = 4 * q;
+    const unsigned line = fast_div((unsigned)r0, bx.dx);
+    const int i0 = (int)((unsigned)r0 - line * (unsigned)nx);
+    const unsigned kk = fast_div(line, bx.dy);
+    const int j = (int)(line - kk * (unsigned)ny), k = (int)kk;
+    const int p = (j + k + color) & 1;  // the phase's points are l = p, p + 2
+    const long m0 = (long)color * h + r0 / 2;
+    const float4 bq = *reinterpret_cast<const float4 *>(b + r0);
+    const float bb[4] = {bq.x, bq.y, bq.z, bq.w};
+    if (zero_x) {
+      float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int u = 0; u < 2; ++u) o[p + 2 * u] = rec_ptr<float, 28>(R, m0 + u)[27] * bb[p + 2 * u];
+      *reinterpret_cast<float4 *>(t + r0) = make_float4(o[0], o[1], o[2], o[3]);
+      continue;
+    }
+    // w[L][c]: line L = (dj + 1) + 3 (dk + 1), column i0 - 1 + c
+    float w[9][6];
+#pragma unroll
+    for (int L = 0; L < 9; ++L) {
+      const int jj = j + L % 3 - 1, kz = k + L / 3 - 1;
+      if (jj >= 0 && jj < ny && kz >= 0 && kz < nz) {
+        const float *xr = x + ((long)kz * ny + jj) * nx + i0;
+        const float4 v = *reinterpret_cast<const float4 *>(xr);
+        w[L][0] = i0 > 0 ? xr[-1] : 0.0f;
+        w[L][1] = v.x; w[L][2] = v.y; w[L][3] = v.z; w[L][4] = v.w;
+        w[L][5] = i0 + 4 < nx ? xr[4] : 0.0f;
+      } else {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) w[L][c] = 0.0f;
+      }
+    }
+    float o[4] = {w[4][1], w[4][2], w[4][3], w[4][4]};
+    auto relax_at = [&](int l, const float (&c)[28]) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int s = 0; s < 27; ++s) acc = fmaf(c[s], w[s / 3][l + s % 3], acc);
+      return fmaf(c[27], bb[l] - acc, w[4][l + 1]);
+    };
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      float c[28];
+      load_recs<float, 28>(R, m0 + u, c);
+      if (p == 0) o[2 * u] = relax_at(2 * u, c);
+      else o[2 * u + 1] = relax_at(2 * u + 1, c);
+    }
+    *reinterpret_cast<float4 *>(t + r0) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
 // Residual of a 27-point level from its colour-split records: every point
 // (both colours; same-colour points are coupled), b - A x in apply_row's slot
 // order, so the result equals k_residual<T, 27> bit for bit.
@@ -1165,7 +1228,14 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
         const bool z = zero && color == 0;
         LaunchScope ls(K_MG_RELAX, st, z ? 0.5 * n * (R27.code ? 2.0 : T_) + 1.5 * T_ * n
                                          : 0.5 * n * rec27 + 2.5 * T_ * n);
-        k_relax_rb27<T><<<grid_all(h), kThreads, 0, st>>>(R27, F.bv.p, cur, oth, F.b, color, z, gate);
+        bool done = false;
+        if constexpr (sizeof(T) == 4) {
+          if (p.quads && F.b.nx % 4 == 0) {
+            k_relax_rb27_quad<<<grid_all(n / 4), kThreads, 0, st>>>(R27, F.bv.p, cur, oth, F.b, color, z, gate);
+            done = true;
+          }
+        }
+        if (!done) k_relax_rb27<T><<<grid_all(h), kThreads, 0, st>>>(R27, F.bv.p, cur, oth, F.b, color, z, gate);
         std::swap(cur, oth);
       }
     } else if (p.relax == 2) {
