@@ -99,21 +99,22 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
       if (r < S.n) {
         int i, j, k;
         sys_ijk(r, S, i, j, k);
-        // with finite coefficients A 0 is +0 in every row, so b - 0 equals b - A x bit for bit
-        double ax = 0.0;
+        // with finite coefficients A 0 is +0 in every row, so b - 0 equals b - A x
+        // bit for bit: a zero guess takes r = b and |r| = |b|
+        const double bv = S.b[r];
+        double rv = bv;
         if (!S.x_zero) {
           long cs;
           const double *c0 = ar_row(S, r, cs);
-          ax = stencil7_at(c0, cs, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+          rv = bv - stencil7_at(c0, cs, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+          pr = fma(rv, rv, pr);
         }
-        const double bv = S.b[r];
-        const double rv = bv - ax;
         if (S.a32) S.Vf[r] = (float)rv;
         else S.V[r] = rv;
         pb = fma(bv, bv, pb);
-        pr = fma(rv, rv, pr);
       }
     }
+    if (S.x_zero) pr = pb;
     pb = warp_sum(pb);
     pr = warp_sum(pr);
     if (lane == 0) { sacc[warp] += pb; sacc[kWarps + warp] += pr; }
@@ -709,7 +710,8 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next32(KSys *sys) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float *vn = S.Vf + (long)nd * S.ldv;
   const bool store = nd < sc->kdim;
-  double pt = 0.0;
+  // |w|^2: FP32 per thread (as the dot products of the FP32 cycle), FP64 across threads
+  float pt = 0.0f;
   if (nd <= kChunk32 && S.vec4) {
     for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
       const long r0 = t0 + 4 * threadIdx.x;
@@ -726,10 +728,10 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next32(KSys *sys) {
         }
       }
       if (store) st4(vn + r0, w);
-      pt = fma((double)w.x, (double)w.x, pt);
-      pt = fma((double)w.y, (double)w.y, pt);
-      pt = fma((double)w.z, (double)w.z, pt);
-      pt = fma((double)w.w, (double)w.w, pt);
+      pt = fmaf(w.x, w.x, pt);
+      pt = fmaf(w.y, w.y, pt);
+      pt = fmaf(w.z, w.z, pt);
+      pt = fmaf(w.w, w.w, pt);
     }
   } else
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
@@ -749,12 +751,12 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next32(KSys *sys) {
           for (int kk = 0; kk < nd; ++kk) w = fmaf(-cf[kk], S.Vf[(long)kk * S.ldv + r], w);
         }
         if (store) vn[r] = w;
-        pt = fma((double)w, (double)w, pt);
+        pt = fmaf(w, w, pt);
       }
     }
   }
-  pt = warp_sum(pt);
-  if (lane == 0) sacc[warp] = pt;
+  const double ptd = warp_sum((double)pt);
+  if (lane == 0) sacc[warp] = ptd;
   if (!block_partials_and_last(sacc, 1, S.part, &sc->ticket)) return;
   __shared__ double tot[1];
   reduce_partials(S.part, gridDim.x, 1, tot);

@@ -656,48 +656,54 @@ __device__ __forceinline__ void relax_quad(const float (&c)[2][8], const float4 
   }
 }
 
+// One quad of an FP32 in-place phase: the four points r0 .. r0+3 of line
+// (j, k) from column i0.
+__device__ __forceinline__ void relax_quad_at(const Recs<float, 8> &R, const float *__restrict__ b, float *x,
+                                              const Box &bx, int color, int zero_x, long r0, int i0, int j, int k) {
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const long sy = nx, sz = (long)nx * ny;
+  const int p = (j + k + color) & 1;
+  const long m0 = (long)color * (bx.n / 2) + r0 / 2;
+  float c[2][8];
+  load_quad_recs(R, m0, c);
+  const float4 bq = *reinterpret_cast<const float4 *>(b + r0);
+  if (zero_x) {
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (p == 0) { v.x = c[0][0] * bq.x; v.z = c[1][0] * bq.z; }
+    else { v.y = c[0][0] * bq.y; v.w = c[1][0] * bq.w; }
+    *reinterpret_cast<float4 *>(x + r0) = v;
+    return;
+  }
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 xc = *reinterpret_cast<const float4 *>(x + r0);
+  const float4 xs = j > 0 ? *reinterpret_cast<const float4 *>(x + r0 - sy) : z4;
+  const float4 xn = j < ny - 1 ? *reinterpret_cast<const float4 *>(x + r0 + sy) : z4;
+  const float4 xb = k > 0 ? *reinterpret_cast<const float4 *>(x + r0 - sz) : z4;
+  const float4 xt = k < nz - 1 ? *reinterpret_cast<const float4 *>(x + r0 + sz) : z4;
+  const float xl = i0 > 0 ? x[r0 - 1] : 0.0f;
+  const float xr = i0 + 4 < nx ? x[r0 + 4] : 0.0f;
+  float out[2];
+  if (p == 0) {
+    relax_quad<0>(c, bq, xc, xs, xn, xb, xt, xl, xr, out);
+    x[r0] = out[0];
+    x[r0 + 2] = out[1];
+  } else {
+    relax_quad<1>(c, bq, xc, xs, xn, xb, xt, xl, xr, out);
+    x[r0 + 1] = out[0];
+    x[r0 + 3] = out[1];
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_relax_rb_quad(Recs<float, 8> R, const float *__restrict__ b, float *x,
                                                             Box bx, int color, int zero_x, const int *gate) {
   if (gate_off(gate)) return;
-  const long h = bx.n / 2, n4 = bx.n / 4;
-  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
-  const long sy = nx, sz = (long)nx * ny;
+  const long n4 = bx.n / 4;
   for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
     const long r0 = 4 * q;
     const unsigned line = fast_div((unsigned)r0, bx.dx);
-    const int i0 = (int)((unsigned)r0 - line * (unsigned)nx);
+    const int i0 = (int)((unsigned)r0 - line * (unsigned)bx.nx);
     const unsigned kk = fast_div(line, bx.dy);
-    const int j = (int)(line - kk * (unsigned)ny), k = (int)kk;
-    const int p = (j + k + color) & 1;
-    const long m0 = (long)color * h + r0 / 2;
-    float c[2][8];
-    load_quad_recs(R, m0, c);
-    const float4 bq = *reinterpret_cast<const float4 *>(b + r0);
-    if (zero_x) {
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (p == 0) { v.x = c[0][0] * bq.x; v.z = c[1][0] * bq.z; }
-      else { v.y = c[0][0] * bq.y; v.w = c[1][0] * bq.w; }
-      *reinterpret_cast<float4 *>(x + r0) = v;
-      continue;
-    }
-    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 xc = *reinterpret_cast<const float4 *>(x + r0);
-    const float4 xs = j > 0 ? *reinterpret_cast<const float4 *>(x + r0 - sy) : z4;
-    const float4 xn = j < ny - 1 ? *reinterpret_cast<const float4 *>(x + r0 + sy) : z4;
-    const float4 xb = k > 0 ? *reinterpret_cast<const float4 *>(x + r0 - sz) : z4;
-    const float4 xt = k < nz - 1 ? *reinterpret_cast<const float4 *>(x + r0 + sz) : z4;
-    const float xl = i0 > 0 ? x[r0 - 1] : 0.0f;
-    const float xr = i0 + 4 < nx ? x[r0 + 4] : 0.0f;
-    float out[2];
-    if (p == 0) {
-      relax_quad<0>(c, bq, xc, xs, xn, xb, xt, xl, xr, out);
-      x[r0] = out[0];
-      x[r0 + 2] = out[1];
-    } else {
-      relax_quad<1>(c, bq, xc, xs, xn, xb, xt, xl, xr, out);
-      x[r0 + 1] = out[0];
-      x[r0 + 3] = out[1];
-    }
+    relax_quad_at(R, b, x, bx, color, zero_x, r0, i0, (int)(line - kk * (unsigned)bx.ny), (int)kk);
   }
 }
 
