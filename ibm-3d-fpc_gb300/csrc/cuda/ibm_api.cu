@@ -120,14 +120,18 @@ __global__ void k_to_float(const double *src, float *dst, long n) {
     dst[t] = (float)src[t];
 }
 
-// Class rows [K][7] -> [K][8] (slot 7 zero) and their FP32 copies.
-__global__ void k_pad_rows(const double *rows7, int K, double *rows8, float *rows8f) {
+// Class rows [K][7] -> [K][8] (slot 7 zero), their FP32 copies and their
+// double-float pairs [K][16] (hi = v rounded to FP32, lo = v - hi rounded).
+__global__ void k_pad_rows(const double *rows7, int K, double *rows8, float *rows8f, float *rowsdf) {
   for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < 8L * K; e += (long)gridDim.x * blockDim.x) {
     const long c = e / 8;
     const int s = (int)(e - 8 * c);
     const double v = s < 7 ? rows7[7 * c + s] : 0.0;
     rows8[e] = v;
-    rows8f[e] = (float)v;
+    const float hi = (float)v;
+    rows8f[e] = hi;
+    rowsdf[16 * c + s] = hi;
+    rowsdf[16 * c + 8 + s] = (float)(v - (double)hi);
   }
 }
 
@@ -241,8 +245,9 @@ void ensure_classes(ibm_ctx *c, Op7 &o) {
   if (build_classes<double>(c->st, rows.p, 7, n, o.cls)) {
     o.tab.alloc((size_t)8 * o.cls.K);
     o.tabf.alloc((size_t)8 * o.cls.K);
+    o.tabdf.alloc((size_t)16 * o.cls.K);
     LaunchScope ls(K_SETUP, c->st, 0.0);
-    k_pad_rows<<<grid1d(8L * o.cls.K), kThreads, 0, c->st>>>(o.cls.tab.p, o.cls.K, o.tab.p, o.tabf.p);
+    k_pad_rows<<<grid1d(8L * o.cls.K), kThreads, 0, c->st>>>(o.cls.tab.p, o.cls.K, o.tab.p, o.tabf.p, o.tabdf.p);
   }
   rows.release();
   DBuf<float> jrec;
@@ -257,7 +262,7 @@ void ensure_classes(ibm_ctx *c, Op7 &o) {
 
 // Points a system at its operator's classes.
 void use_classes(const Op7 &o, KSysHost &h) {
-  if (o.cls.ok()) { h.cls = o.cls.code.p; h.tab = o.tab.p; h.tabf = o.tabf.p; }
+  if (o.cls.ok()) { h.cls = o.cls.code.p; h.tab = o.tab.p; h.tabf = o.tabf.p; h.tabdf = o.tabdf.p; }
   if (o.clsj.ok()) { h.clsj = o.clsj.code.p; h.tabj = o.clsj.tab.p; }
 }
 
@@ -279,7 +284,7 @@ void ensure_solvers(ibm_ctx *c) {
     h.kdim = p.vel_kdim; h.maxit = p.vel_maxit; h.tol = p.vel_tol;
     if (mixed) {
       h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps);
-      h.a32 = a32; h.cycle_rtol = p.cycle_rtol32;
+      h.a32 = a32; h.cycle_rtol = p.cycle_rtol32; h.df_residual = p.df_residual;
     }
     else { h.pc = 0; h.A = o.cj.p; }
     if (p.row_classes) {
@@ -308,12 +313,15 @@ void ensure_solvers(ibm_ctx *c) {
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
     const double *winv = ((p.mg_options & 2) && c->p_sym) ? c->p_winv.p : nullptr;
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
-    if (mixed) { hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32; }
+    if (mixed) {
+      hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32;
+      hp.df_residual = p.df_residual;
+    }
     else { hp.pc = 1; hp.A = op.c.p; }
   } else {
     if (mixed) {
       hp.pc = 2; hp.pc_cb = 0; hp.A = op.c.p; hp.inner_sweeps = 1;
-      hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32;
+      hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32; hp.df_residual = p.df_residual;
     }
     else { hp.pc = 0; hp.A = op.cj.p; }
   }
@@ -426,6 +434,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->compute_forces = 0;
   p->row_classes = 1;
   p->mg_quads = 1;
+  p->df_residual = 1;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -520,6 +529,7 @@ int ibm_set_operator(ibm_ctx *c, int field, const double *vals7, int nbx, int nb
     o.clsj = Classes<float>();
     o.tab.release();
     o.tabf.release();
+    o.tabdf.release();
     const long n = b.n;
     DBuf<double> tmp;
     tmp.alloc((size_t)7 * n);

@@ -140,6 +140,7 @@ struct Op7 {
   Classes<double> cls;  // classes of the supplied rows (W 7)
   DBuf<double> tab;     // [K][8] the distinct rows, slot 7 zero
   DBuf<float> tabf;     // [K][8] their FP32 copies (the rows of cf)
+  DBuf<float> tabdf;    // [K][16] the rows as double-float pairs: hi in slots 0-7, lo in 8-15
   Classes<float> clsj;  // classes of the FP32 Jacobi records {invdf, cjf_1..cjf_6, 0} (W 8)
   bool cls_tried = false;  // classes built (or found too many) for the current coefficients
 };
@@ -156,6 +157,7 @@ struct KScal {
   int claimed;        // the Givens estimate reached the tolerance
   unsigned ticket;    // last-block-done counter of the reduction kernels
   int nonfinite;
+  int use64;          // double-float residual too close to call: FP64 residuals for the rest of the solve
   double b_norm, r_norm, eps, real_old;
   double cyc_eps;     // the current cycle also ends when the estimate reaches this
   double cyc_rtol;    // cyc_eps = max(eps, cyc_rtol * true residual at the cycle start)
@@ -197,6 +199,9 @@ struct KSys {
   const float *tabf;    // [K][8] rows of Af
   const uint16_t *clsj; // class of each FP32 Jacobi record
   const float *tabj;    // [K][8] {invdf, Ajf_1..Ajf_6, 0}
+  const float *tabdf;   // [K][16] rows of Ar as double-float pairs
+  int df_resid;         // FP32 cycles with classes: true residuals in double-float (FP32 pipe)
+  float2 *xs;           // df_resid: x as double-float pairs, written with every update of x
 };
 
 // Host-side mirror of what the loop needs from each system after a step.

@@ -18,6 +18,7 @@
 // partials summed in block order by the last block to finish.
 #include "ibm_common.cuh"
 #include "ibm_krylov.cuh"
+#include "ibm_df.cuh"
 
 namespace ibm {
 
@@ -136,6 +137,7 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
     sc->claimed = 0;
     sc->cycle_end = 0;
     sc->nonfinite = !isfinite(rn);
+    sc->use64 = 0;
     if (!isfinite(rn)) { sc->status = 2; sc->active = 0; }
     else if (rn == 0.0 || rn <= sc->eps) { sc->status = 1; sc->active = 0; }
     else if (sc->maxit <= 0) { sc->status = 2; sc->active = 0; }
@@ -354,7 +356,13 @@ __global__ void __launch_bounds__(kThreads) k_cycle_update(KSys *sys) {
     for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
       float acc = 0.0f;
       for (int kk = 0; kk < m; ++kk) acc = fmaf(cf32[kk], S.Z[(long)kk * S.ldv + r], acc);
-      S.x[r] = S.x[r] + (double)acc;
+      const double xn = S.x[r] + (double)acc;
+      S.x[r] = xn;
+      if (S.df_resid) {
+        float h, l;
+        df_split(xn, h, l);
+        S.xs[r] = make_float2(h, l);
+      }
     }
     return;
   }
@@ -378,15 +386,67 @@ __global__ void k_add_z(KSys *sys) {
     S.x[r] = S.x[r] + S.z2[r];
 }
 
+// Relative bound on the double-float residual of one row: |r_df - r| <=
+// kDfRowBound * (|b| + sum_s |c_s x_s|). Per row the seven products carry
+// about 3 * 2^-47 of their size (split of c and of x, rounded cross terms, the
+// dropped lo * lo) and the eight double-float additions 2^-47 of the running
+// sum each, about 2^-43.3 in all; 2^-41 leaves a factor of five.
+constexpr double kDfRowBound = 4.547473508864641e-13;  // 2^-41
+
 // True residual after a cycle; decide converged / stop / restart (V_0 = r).
+// Systems with df_resid compute it in double-float and also the norm M of
+// the per-row bounds; a decision closer to the tolerance than
+// kDfRowBound * M is taken again from an FP64 residual, and the rest of the
+// solve stays in FP64, so convergence is always decided within FP64 rounding.
 __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
   KSys &S = sys[blockIdx.y];
   KScal *sc = S.s;
   if (!sc->cycle_end) return;
-  __shared__ double sacc[kWarps];
-  if (threadIdx.x < kWarps) sacc[threadIdx.x] = 0.0;
+  const bool df = S.df_resid && !sc->use64;
+  __shared__ double sacc[2 * kWarps];
+  if (threadIdx.x < 2 * kWarps) sacc[threadIdx.x] = 0.0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (df) {
+    // r = b - A x in double-float (about 48 bits) on the FP32 pipe, from the
+    // double-float copy of x that the update wrote; |r|^2 and the squared
+    // row bounds summed in FP32 per thread and FP64 across threads
+    const long sy = S.nx, sz = (long)S.nx * S.ny;
+    for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+      float pf = 0.0f, mf = 0.0f;
+#pragma unroll
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) {
+          int i, j, k;
+          sys_ijk(r, S, i, j, k);
+          const float *c = S.tabdf + 16 * (long)S.cls[r];
+          float ah = 0.0f, al = 0.0f, mag = 0.0f;
+          auto add = [&](int s, long q) {
+            const float2 xv = S.xs[q];
+            df_fma(ah, al, c[s], c[8 + s], xv.x, xv.y);
+            mag = fmaf(fabsf(c[s]), fabsf(xv.x), mag);
+          };
+          add(0, r);
+          if (i > 0) add(1, r - 1);
+          if (i < S.nx - 1) add(2, r + 1);
+          if (j > 0) add(3, r - sy);
+          if (j < S.ny - 1) add(4, r + sy);
+          if (k > 0) add(5, r - sz);
+          if (k < S.nz - 1) add(6, r + sz);
+          float bh, bl, rh, rl;
+          df_split(S.b[r], bh, bl);
+          df_sub(bh, bl, ah, al, rh, rl);
+          S.Vf[r] = rh;
+          pf = fmaf(rh, rh, pf);
+          mag = 1.001f * (mag + fabsf(bh));  // the FP32 magnitudes' own rounding
+          mf = fmaf(mag, mag, mf);
+        }
+      }
+      const double pr = warp_sum((double)pf), mr = warp_sum((double)mf);
+      if (lane == 0) { sacc[warp] += pr; sacc[kWarps + warp] += mr; }
+    }
+  } else
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
     double pr = 0.0;
 #pragma unroll
@@ -406,9 +466,9 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
     pr = warp_sum(pr);
     if (lane == 0) sacc[warp] += pr;
   }
-  if (!block_partials_and_last(sacc, 1, S.part, &sc->ticket)) return;
-  __shared__ double tot[1];
-  reduce_partials(S.part, gridDim.x, 1, tot);
+  if (!block_partials_and_last(sacc, 2, S.part, &sc->ticket)) return;
+  __shared__ double tot[2];
+  reduce_partials(S.part, gridDim.x, 2, tot);
   __syncthreads();
   if (threadIdx.x == 0) {
     sc->ticket = 0;
@@ -416,7 +476,20 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
     sc->cycle_end = 0;
     sc->r_norm = rt;
     if (!isfinite(rt)) { sc->nonfinite = 1; sc->status = 2; sc->active = 0; return; }
-    if (rt <= sc->eps) { sc->status = 1; sc->active = 0; return; }
+    if (df) {
+      const double bound = kDfRowBound * sqrt(tot[1]);
+      if (rt + bound <= sc->eps) { sc->status = 1; sc->active = 0; return; }
+      if (rt - bound <= sc->eps) {
+        // too close to call: the next cycle end (no update, i = 0) computes the
+        // FP64 residual of the same x
+        sc->use64 = 1;
+        sc->cycle_end = 1;
+        sc->i = 0;
+        return;
+      }
+    } else if (rt <= sc->eps) {
+      sc->status = 1; sc->active = 0; return;
+    }
     if (sc->iters >= sc->maxit) { sc->status = 2; sc->active = 0; return; }
     if (sc->claimed && rt >= sc->real_old) { sc->status = 3; sc->active = 0; return; }
     sc->real_old = rt;
@@ -944,6 +1017,8 @@ void Krylov::configure(int nsys_, const KSysHost *hs) {
       sl.w.alloc(h.n);
     }
     if (h.pc == 1) { sl.z.alloc(h.n); sl.z2.alloc(h.n); }
+    if (h.a32 && h.cls && h.tabdf && h.df_residual) sl.xs.alloc(h.n);
+    else sl.xs.release();
     if (h.pc == 2) {
       sl.Z.alloc((size_t)h.kdim * h.n);
       if (!h.pc_cb) { sl.zf.alloc(h.n); sl.zf2.alloc(h.n); }
@@ -961,7 +1036,7 @@ size_t Krylov::bytes() const {
   for (int s = 0; s < nsys; ++s) {
     const Slot &sl = slot[s];
     b += sl.V.bytes() + sl.w.bytes() + sl.z.bytes() + sl.z2.bytes() + sl.part.bytes() +
-         sl.Z.bytes() + sl.zf.bytes() + sl.zf2.bytes();
+         sl.Z.bytes() + sl.zf.bytes() + sl.zf2.bytes() + sl.Vf.bytes() + sl.wf.bytes() + sl.xs.bytes();
   }
   return b;
 }
@@ -982,6 +1057,9 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     k.fdx = make_fastdiv((unsigned)h.nx); k.fdy = make_fastdiv((unsigned)h.ny);
     k.A = h.A; k.Ar = h.Ar; k.invd = h.invd; k.Af = h.Af; k.invdf = h.invdf; k.Ajf = h.Ajf;
     k.cls = h.cls; k.tab = h.tab; k.tabf = h.tabf; k.clsj = h.clsj; k.tabj = h.tabj;
+    k.tabdf = h.tabdf;
+    k.df_resid = (h.a32 && h.cls && h.tabdf && h.df_residual) ? 1 : 0;
+    k.xs = slot[s].xs.p;
     k.V = slot[s].V.p; k.ldv = h.n;
     k.Z = slot[s].Z.p;
     k.w = slot[s].w.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;

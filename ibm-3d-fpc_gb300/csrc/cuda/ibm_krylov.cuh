@@ -49,6 +49,8 @@ struct KSysHost {
   const float *tabf = nullptr;
   const uint16_t *clsj = nullptr;
   const float *tabj = nullptr;
+  const float *tabdf = nullptr;  // with a32: true residuals in double-float
+  int df_residual = 1;           // use them when a32 and tabdf are set
 };
 
 struct KResult {
@@ -85,6 +87,7 @@ class Krylov {
     KSysHost host;
     DBuf<double> V, w, z, z2, part;
     DBuf<float> Z, zf, zf2, Vf, wf;
+    DBuf<float2> xs;  // double-float copy of x for the double-float residual
   };
   void read_flags(cudaStream_t st);
   // Launch sequences shared by the host-driven and the graph form. With

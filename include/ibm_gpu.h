@@ -102,6 +102,9 @@ typedef struct ibm_solver_params {
                             those of the plain layout. 0: plain layout */
   int mg_quads;          /* 1 (default): FP32 two-colour phases and residual of 7-point levels with
                             nx % 4 == 0 take four points per thread (same arithmetic, bitwise equal) */
+  int df_residual;       /* precision 2 with row classes, 1 (default): the true residual at each restart
+                            is computed in double-float on the FP32 pipe (about 48 significant bits;
+                            GB300's FP64 rate makes the FP64 stencil the bound there). 0: FP64 */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {

@@ -64,8 +64,9 @@ def test_vcycle_quads_bitwise(ibm, classes, shape):
 
 @pytest.mark.parametrize("precision,graph", [(0, 0), (1, 0), (2, 0), (2, 1)])
 def test_steps_bitwise_with_classes(ibm, case48, precision, graph):
-    a = ibm.Solver(case48, bench_like(ibm, precision=precision, use_graph=graph, row_classes=0))
-    b = ibm.Solver(case48, bench_like(ibm, precision=precision, use_graph=graph, row_classes=1))
+    # the double-float residual (precision 2 with classes) is checked on its own below
+    a = ibm.Solver(case48, bench_like(ibm, precision=precision, use_graph=graph, row_classes=0, df_residual=0))
+    b = ibm.Solver(case48, bench_like(ibm, precision=precision, use_graph=graph, row_classes=1, df_residual=0))
     for step in range(1, 6):
         ramp = min(1.0, step / 3.0)
         sa = a.step(ramp)
@@ -85,3 +86,32 @@ def test_steps_bitwise_with_classes(ibm, case48, precision, graph):
             prof = s.profile()
             per.append(prof.bytes[k] / max(prof.launches[k], 1))
         assert per[1] < 0.5 * per[0]
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+def test_double_float_residual(ibm, case48, graph):
+    """FP32 cycles whose restarts compute the true residual in double-float
+    (about 48 bits on the FP32 pipe) against the FP64 residual: same
+    iteration counts within one, fields within the solve tolerance, and a
+    tight pressure solve still reaches 1e-12."""
+    kw = dict(precision=2, use_graph=graph)
+    a = ibm.Solver(case48, bench_like(ibm, df_residual=0, **kw))
+    b = ibm.Solver(case48, bench_like(ibm, df_residual=1, **kw))
+    for step in range(1, 6):
+        ramp = min(1.0, step / 3.0)
+        sa = a.step(ramp)
+        sb = b.step(ramp)
+        assert sa.status == sb.status == ibm.IBM_OK
+        for f in "uvwp":
+            assert abs(getattr(sa, f).iters - getattr(sb, f).iters) <= 1, f
+    for x, y, name in zip(a.fields(), b.fields(), "uvwp"):
+        assert np.abs(x - y).max() <= 1e-7 * max(np.abs(x).max(), 1e-30), name
+    s = ibm.Solver(case48, bench_like(ibm, precision=2, df_residual=1, p_tol=1e-12, p_maxit=400))
+    rng = np.random.default_rng(4)
+    nx, ny, nz = case48.shape
+    rhs = rng.standard_normal(nx * ny * nz) * case48.array("fluid_p")
+    rhs -= rhs.mean() * case48.array("fluid_p")
+    x, st = s.solve(ibm.FIELD_P, rhs)
+    assert st.status == ibm.IBM_OK
+    r = rhs - s.apply_operator(ibm.FIELD_P, x)
+    assert np.linalg.norm(r) <= 2e-12 * np.linalg.norm(rhs)
