@@ -539,6 +539,55 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb27_quad(Recs<float, 28> R,
   }
 }
 
+// Quartet form of the FP32 27-point residual (nx a multiple of 4): the 9 x 6
+// window of x as in k_relax_rb27_quad, all four points b - A x in
+// k_residual_rb27's slot order, one 16-byte store.
+__global__ void __launch_bounds__(kThreads) k_residual_rb27_quad(Recs<float, 28> R, const float *__restrict__ b,
+                                                                 const float *__restrict__ x,
+                                                                 float *__restrict__ res, Box bx, const int *gate) {
+  if (gate_off(gate)) return;
+  const long h = bx.n / 2, n4 = bx.n / 4;
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+    const long r0 = 4 * q;
+    const unsigned line = fast_div((unsigned)r0, bx.dx);
+    const int i0 = (int)((unsigned)r0 - line * (unsigned)nx);
+    const unsigned kk = fast_div(line, bx.dy);
+    const int j = (int)(line - kk * (unsigned)ny), k = (int)kk;
+    const int p0 = (j + k) & 1;  // colour of the quad's even points (l = 0, 2)
+    float w[9][6];
+#pragma unroll
+    for (int L = 0; L < 9; ++L) {
+      const int jj = j + L % 3 - 1, kz = k + L / 3 - 1;
+      if (jj >= 0 && jj < ny && kz >= 0 && kz < nz) {
+        const float *xr = x + ((long)kz * ny + jj) * nx + i0;
+        const float4 v = *reinterpret_cast<const float4 *>(xr);
+        w[L][0] = i0 > 0 ? xr[-1] : 0.0f;
+        w[L][1] = v.x; w[L][2] = v.y; w[L][3] = v.z; w[L][4] = v.w;
+        w[L][5] = i0 + 4 < nx ? xr[4] : 0.0f;
+      } else {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) w[L][c] = 0.0f;
+      }
+    }
+    const float4 bq = *reinterpret_cast<const float4 *>(b + r0);
+    const float bb[4] = {bq.x, bq.y, bq.z, bq.w};
+    float o[4];
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+      // point l has colour p0 ^ (l & 1); its record is m = (r0 + l) / 2 of that colour
+      const int col = p0 ^ (l & 1);
+      float c[28];
+      load_recs<float, 28>(R, (long)col * h + r0 / 2 + l / 2, c);
+      float acc = 0.0f;
+#pragma unroll
+      for (int s = 0; s < 27; ++s) acc = fmaf(c[s], w[s / 3][l + s % 3], acc);
+      o[l] = bb[l] - acc;
+    }
+    *reinterpret_cast<float4 *>(res + r0) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
 // Residual of a 27-point level from its colour-split records: every point
 // (both colours; same-colour points are coupled), b - A x in apply_row's slot
 // order, so the result equals k_residual<T, 27> bit for bit.
@@ -1283,7 +1332,14 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
     res = F.r.p;
   } else if (nu1 > 0 && p.relax == 2 && rb27) {
     LaunchScope ls(K_MG_RESID, st, n * rec27 + 3.0 * T_ * n);
-    k_residual_rb27<T><<<grid_all(n), kThreads, 0, st>>>(R27, F.bv.p, cur, F.r.p, F.b, gate);
+    bool done = false;
+    if constexpr (sizeof(T) == 4) {
+      if (p.quads && F.b.nx % 4 == 0) {
+        k_residual_rb27_quad<<<grid_all(n / 4), kThreads, 0, st>>>(R27, F.bv.p, cur, F.r.p, F.b, gate);
+        done = true;
+      }
+    }
+    if (!done) k_residual_rb27<T><<<grid_all(n), kThreads, 0, st>>>(R27, F.bv.p, cur, F.r.p, F.b, gate);
     res = F.r.p;
   } else if (nu1 > 0) {
     LaunchScope ls(K_MG_RESID, st, T_ * n * (F.ns + 3.0));
