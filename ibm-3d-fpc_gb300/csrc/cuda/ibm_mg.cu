@@ -942,6 +942,74 @@ __global__ void k_prolong_yz4(const float *__restrict__ xc, Box cb, const float 
   }
 }
 
+// Restriction / interpolation along x on FP32 levels with fine nx = 2 coarse
+// nx and coarse nx a multiple of 4: a thread makes four coarse points from
+// fine points 2i0 - 1 .. 2i0 + 7 (restriction), or four fine points from
+// coarse points i0/2 .. i0/2 + 2 (interpolation), with 16-byte loads. Same
+// operations as k_restrict / k_prolong, point by point.
+__global__ void k_restrict_x4(const float *__restrict__ res, const float *__restrict__ pm,
+                              const float *__restrict__ pp, Box fb, float *__restrict__ bc, Box cb, const int *gate) {
+  if (gate_off(gate)) return;
+  const long n4 = cb.n / 4;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n4; t += (long)gridDim.x * blockDim.x) {
+    const long c0 = 4 * t;
+    const unsigned cline = fast_div((unsigned)c0, cb.dx);
+    const int ci0 = (int)((unsigned)c0 - cline * (unsigned)cb.nx);
+    const long f0 = (long)cline * fb.nx + 2 * ci0;  // fine point 2 ci0 of the same line
+    float rv[9], wl[9], wh[9];  // fine points 2ci0 - 1 + e, e = 0..8
+    {
+      const float4 a = *reinterpret_cast<const float4 *>(res + f0), b4 = *reinterpret_cast<const float4 *>(res + f0 + 4);
+      rv[1] = a.x; rv[2] = a.y; rv[3] = a.z; rv[4] = a.w; rv[5] = b4.x; rv[6] = b4.y; rv[7] = b4.z; rv[8] = b4.w;
+      const float4 p1 = *reinterpret_cast<const float4 *>(pp + f0), p2 = *reinterpret_cast<const float4 *>(pp + f0 + 4);
+      wl[1] = p1.x; wl[2] = p1.y; wl[3] = p1.z; wl[4] = p1.w; wl[5] = p2.x; wl[6] = p2.y; wl[7] = p2.z; wl[8] = p2.w;
+      const float4 m1 = *reinterpret_cast<const float4 *>(pm + f0), m2 = *reinterpret_cast<const float4 *>(pm + f0 + 4);
+      wh[1] = m1.x; wh[2] = m1.y; wh[3] = m1.z; wh[4] = m1.w; wh[5] = m2.x; wh[6] = m2.y; wh[7] = m2.z; wh[8] = m2.w;
+      const bool lo = ci0 > 0;
+      rv[0] = lo ? res[f0 - 1] : 0.0f;
+      wl[0] = lo ? pp[f0 - 1] : 0.0f;
+      wh[0] = 0.0f;
+    }
+    float o[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      // coarse point ci0 + u: fine 2(ci0 + u) - 1, 2(ci0 + u), 2(ci0 + u) + 1 = rv[2u], rv[2u + 1], rv[2u + 2]
+      float acc = 0.0f;
+      if (ci0 + u > 0) acc = fmaf(wl[2 * u], rv[2 * u], acc);
+      acc = fmaf(1.0f, rv[2 * u + 1], acc);
+      acc = fmaf(wh[2 * u + 2], rv[2 * u + 2], acc);  // 2(ci0 + u) + 1 < fine nx always
+      o[u] = acc;
+    }
+    *reinterpret_cast<float4 *>(bc + c0) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
+__global__ void k_prolong_x4(const float *__restrict__ xc, Box cb, const float *__restrict__ pm,
+                             const float *__restrict__ pp, Box fb, float *x, int accumulate, const int *gate) {
+  if (gate_off(gate)) return;
+  const long n4 = fb.n / 4;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n4; t += (long)gridDim.x * blockDim.x) {
+    const long r0 = 4 * t;
+    const unsigned line = fast_div((unsigned)r0, fb.dx);
+    const int i0 = (int)((unsigned)r0 - line * (unsigned)fb.nx);
+    const long cc = (long)line * cb.nx + i0 / 2;  // coarse point i0 / 2 of the same line
+    const float2 c01 = *reinterpret_cast<const float2 *>(xc + cc);
+    const float c2 = i0 / 2 + 2 < cb.nx ? xc[cc + 2] : 0.0f;
+    const float4 a = *reinterpret_cast<const float4 *>(pp + r0), m = *reinterpret_cast<const float4 *>(pm + r0);
+    // fine i0 + 0: even -> c0; i0 + 1: odd between c0, c1; i0 + 2: c1; i0 + 3: between c1, c2
+    float4 corr;
+    corr.x = c01.x;
+    corr.y = fmaf(a.y, c01.y, m.y * c01.x);
+    corr.z = c01.y;
+    corr.w = fmaf(a.w, c2, m.w * c01.y);
+    float4 *xo = reinterpret_cast<float4 *>(x + r0);
+    if (accumulate) {
+      const float4 xv = *xo;
+      corr.x = xv.x + corr.x; corr.y = xv.y + corr.y; corr.z = xv.z + corr.z; corr.w = xv.w + corr.w;
+    }
+    *xo = corr;
+  }
+}
+
 template <class T>
 __global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb, int d, T *x, int accumulate,
                           const int *gate) {
@@ -1353,6 +1421,8 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
     if constexpr (sizeof(T) == 4) {
       if (F.cdir != 0 && F.b.nx % 4 == 0)
         k_restrict_yz4<<<grid_all(C.b.n / 4), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
+      else if (p.quads && F.cdir == 0 && F.b.nx == 2 * C.b.nx && C.b.nx % 4 == 0)
+        k_restrict_x4<<<grid_all(C.b.n / 4), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, C.bv.p, C.b, gate);
       else
         k_restrict<T><<<grid_all(C.b.n), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
     } else {
@@ -1365,6 +1435,8 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
     if constexpr (sizeof(T) == 4) {
       if (F.cdir != 0 && F.b.nx % 4 == 0)
         k_prolong_yz4<<<grid_all(n / 4), kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, nu1 > 0, gate);
+      else if (p.quads && F.cdir == 0 && F.b.nx == 2 * C.b.nx && C.b.nx % 4 == 0)
+        k_prolong_x4<<<grid_all(n / 4), kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, cur, nu1 > 0, gate);
       else
         k_prolong<T><<<grid_all(n), kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, nu1 > 0, gate);
     } else {

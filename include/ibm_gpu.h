@@ -100,8 +100,9 @@ typedef struct ibm_solver_params {
                             away from walls and bodies has the same ones), kernels read a 2-byte class
                             per row and the row from a table of the distinct rows; results are bitwise
                             those of the plain layout. 0: plain layout */
-  int mg_quads;          /* 1 (default): FP32 two-colour phases and residual of 7-point levels with
-                            nx % 4 == 0 take four points per thread (same arithmetic, bitwise equal) */
+  int mg_quads;          /* 1 (default): FP32 levels with nx % 4 == 0 relax (two-colour phases), form
+                            residuals and transfer along x four points per thread (same arithmetic,
+                            bitwise equal results) */
   int df_residual;       /* precision 2 with row classes, 1 (default): the true residual at each restart
                             is computed in double-float on the FP32 pipe (about 48 significant bits;
                             GB300's FP64 rate makes the FP64 stencil the bound there). 0: FP64 */
