@@ -21,7 +21,7 @@ import numpy as np
 from . import _native
 from ._native import CaseCounts, CaseParams, GridDesc, SolverParams, SolveStats, StepStats
 
-__all__ = ["CaseParams", "Case", "Solver", "SolverParams", "StepStats", "channel_params", "solver_params",
+__all__ = ["CaseParams", "Case", "Solver", "Batch", "SolverParams", "StepStats", "channel_params", "solver_params",
            "IBM_OK", "IBM_NOT_CONVERGED", "IBMError", "FIELD_U", "FIELD_V", "FIELD_W", "FIELD_P"]
 
 IBM_OK = 0
@@ -116,15 +116,18 @@ def _ptr(a: np.ndarray) -> C.c_void_p:
 class Solver:
     """One GPU context running the per-timestep hot path (include/ibm_gpu.h)."""
 
-    def __init__(self, case: Case, params: Optional[SolverParams] = None, device: int = 0):
+    def __init__(self, case: Case, params: Optional[SolverParams] = None, device: int = 0, _ctx=None):
         self._lib = _native.gpu()
         self.case = case
-        cp = case.params
-        g = GridDesc(cp.nx, cp.ny, cp.nz, cp.Lx, cp.Ly, cp.Lz, cp.rho, cp.nu, cp.dt, device)
-        self._ctx = C.c_void_p()
-        rc = self._lib.ibm_create(C.byref(g), C.byref(self._ctx))
-        if rc != 0:
-            raise IBMError(rc, self._lib.ibm_last_error(None).decode())
+        self._owned = _ctx is None
+        if _ctx is None:
+            g = grid_desc(case, device)
+            self._ctx = C.c_void_p()
+            rc = self._lib.ibm_create(C.byref(g), C.byref(self._ctx))
+            if rc != 0:
+                raise IBMError(rc, self._lib.ibm_last_error(None).decode())
+        else:
+            self._ctx = C.c_void_p(_ctx)
         nx, ny, nz = case.shape
         a = case.array
         self._check(self._lib.ibm_set_operator(self._ctx, FIELD_U, _ptr(a("Au_vals")), nx - 1, ny, nz))
@@ -146,7 +149,8 @@ class Solver:
 
     def close(self):
         if getattr(self, "_ctx", None):
-            self._lib.ibm_destroy(self._ctx)
+            if self._owned:
+                self._lib.ibm_destroy(self._ctx)
             self._ctx = None
 
     def __del__(self):
@@ -227,6 +231,58 @@ class Solver:
             if callback:
                 callback(step, st)
         return out
+
+
+def grid_desc(case: Case, device: int = 0) -> GridDesc:
+    cp = case.params
+    return GridDesc(cp.nx, cp.ny, cp.nz, cp.Lx, cp.Ly, cp.Lz, cp.rho, cp.nu, cp.dt, device)
+
+
+class Batch:
+    """Independent channels stepped together (ibm_batch_*, include/ibm_gpu.h).
+
+    ``solvers[i]`` is a Solver on instance i's context (inputs, parameters and
+    fields are set per instance); ``step(ramps)`` queues one step of every
+    instance before waiting for any, so instances in graph mode run
+    concurrently on the GPU."""
+
+    def __init__(self, cases, params=None, device: int = 0):
+        self._lib = _native.gpu()
+        n = len(cases)
+        grids = (GridDesc * n)(*[grid_desc(c, device) for c in cases])
+        self._b = C.c_void_p()
+        rc = self._lib.ibm_batch_create(n, grids, C.byref(self._b))
+        if rc != 0:
+            raise IBMError(rc, self._lib.ibm_last_error(None).decode())
+        if params is None or isinstance(params, SolverParams):
+            params = [params] * n
+        self.solvers = [Solver(c, p, device, _ctx=self._lib.ibm_batch_ctx(self._b, i))
+                        for i, (c, p) in enumerate(zip(cases, params))]
+
+    def __len__(self):
+        return len(self.solvers)
+
+    def step(self, ramps) -> list:
+        n = len(self.solvers)
+        if isinstance(ramps, (int, float)):
+            ramps = [float(ramps)] * n
+        r = (C.c_double * n)(*ramps)
+        stats = (StepStats * n)()
+        rc = self._lib.ibm_batch_step(self._b, r, stats)
+        if rc < 0:
+            bad = next(i for i in range(n) if stats[i].status < 0)
+            raise IBMError(rc, f"instance {bad}: " + self._lib.ibm_last_error(self.solvers[bad]._ctx).decode())
+        return list(stats)
+
+    def close(self):
+        for s in getattr(self, "solvers", []):
+            s.close()
+        if getattr(self, "_b", None):
+            self._lib.ibm_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        self.close()
 
 
 def kernel_names() -> list:

@@ -135,6 +135,12 @@ def gpu() -> C.CDLL:
         lib.ibm_profile_reset.argtypes = [vp]
         lib.ibm_profile_time_kernel.argtypes = [vp, i]
         lib.ibm_profile_get.argtypes = [vp, P(Profile)]
+        lib.ibm_batch_create.argtypes = [i, P(GridDesc), P(vp)]
+        lib.ibm_batch_destroy.argtypes = [vp]
+        lib.ibm_batch_size.argtypes = [vp]
+        lib.ibm_batch_ctx.argtypes = [vp, i]
+        lib.ibm_batch_ctx.restype = vp
+        lib.ibm_batch_step.argtypes = [vp, P(d), P(StepStats)]
         lib.ibm_kernel_name.argtypes = [i]
         lib.ibm_kernel_name.restype = C.c_char_p
         lib.ibm_synchronize.argtypes = [vp]

@@ -843,107 +843,179 @@ int ibm_get_fields(ibm_ctx *c, double *u, double *v, double *w, double *p) {
   });
 }
 
+namespace {
+
+// One timestep in two halves so that several contexts can run steps at the
+// same time (ibm_batch_step). step_launch queues the whole step; in graph
+// mode it returns without waiting (one graph launch on the context's
+// stream), in the host-driven mode it runs the step to completion (the GMRES
+// host loop reads flags every iteration). step_collect waits for the
+// context's stream and turns the solver flags and diagnostics into stats.
+void step_launch(ibm_ctx *c, double ramp) {
+  require_inputs(c);
+  ensure_solvers(c);
+  cudaStream_t st = c->st;
+  *c->hramp = ramp;
+  KResult *rm = c->last_rm, *rp = c->last_rp;
+  const double *bm[3] = {c->bb[0].p, c->bb[1].p, c->bb[2].p};
+  double *xm[3] = {c->xb[0].p, c->xb[1].p, c->xb[2].p};
+  const double *bp[1] = {c->bb[3].p};
+  double *xp[1] = {c->xb[3].p};
+  Precond none, mgp;
+  mgp.ctx = c;
+  mgp.apply = mg_apply_cb;
+  c->last_graph = c->prm.use_graph != 0;
+  if (c->prm.use_graph) {
+    // The whole step as one graph launch; the GMRES loops run on the device.
+    if (!c->graph_ready || !c->graph_bound) {
+      const bool zg = c->prm.use_zero_initial_guess != 0;
+      c->kmom.bind(st, bm, xm, ~0u, zg);
+      c->kp.bind(st, bp, xp, ~0u, zg);
+      c->graph_bound = true;
+    }
+    if (!c->graph_ready) build_step_graph(c, none, mgp);
+    IBM_CUDA_TRY(cudaGraphLaunch(c->gexec, st));
+    return;
+  }
+  IBM_CUDA_TRY(cudaMemcpyAsync(c->dramp.p, c->hramp, sizeof(double), cudaMemcpyHostToDevice, st));
+  IBM_CUDA_TRY(cudaMemsetAsync(c->diag.p, 0, sizeof(StepDiag), st));
+  IBM_CUDA_TRY(cudaEventRecord(c->ev[0], st));
+  {
+    PhaseScope ph(PH_RHS);
+    launch_bc(c, c->u.p, c->v.p, c->w.p);
+    launch_momentum_rhs(c);
+  }
+  IBM_CUDA_TRY(cudaEventRecord(c->ev[1], st));
+  {
+    PhaseScope ph(PH_MOM);
+    c->kmom.solve(st, bm, xm, none, rm, ~0u, c->prm.use_zero_initial_guess != 0);
+  }
+  IBM_CUDA_TRY(cudaEventRecord(c->ev[2], st));
+  {
+    PhaseScope ph(PH_RHS);
+    launch_tilde(c);
+    launch_pressure_rhs(c);
+  }
+  IBM_CUDA_TRY(cudaEventRecord(c->ev[5], st));
+  {
+    PhaseScope ph(PH_P);
+    c->kp.solve(st, bp, xp, mgp, rp, ~0u, c->prm.use_zero_initial_guess != 0);
+  }
+  IBM_CUDA_TRY(cudaEventRecord(c->ev[3], st));
+  {
+    PhaseScope ph(PH_PROJ);
+    launch_projection(c);
+  }
+  IBM_CUDA_TRY(cudaEventRecord(c->ev[4], st));
+  IBM_CUDA_TRY(cudaMemcpyAsync(c->hdiag, c->diag.p, sizeof(StepDiag), cudaMemcpyDeviceToHost, st));
+  IBM_CUDA_TRY(cudaStreamSynchronize(st));
+  IBM_CUDA_TRY(cudaGetLastError());
+  c->prof.drain();
+}
+
+int step_collect(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
+  KResult *rm = c->last_rm, *rp = c->last_rp;
+  if (c->last_graph) {
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    IBM_CUDA_TRY(cudaGetLastError());
+    for (int s = 0; s < 4; ++s) {
+      const KFlags &f = c->hflags_graph[s];
+      KResult &r = s < 3 ? rm[s] : rp[0];
+      r.iters = f.iters; r.rel_res = f.rel; r.status = f.status; r.nonfinite = f.nonfinite;
+    }
+    const unsigned long long *lp = c->hloops;
+    c->launches += c->graph_fixed_launches + (long long)lp[0] * c->graph_body_launches[0] +
+                   (long long)lp[1] * c->graph_body_launches[1] + (long long)lp[2] * c->graph_body_launches[2] +
+                   (long long)lp[3] * c->graph_body_launches[3];
+  }
+  int rc = IBM_OK;
+  const StepDiag &dg = *c->hdiag;
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    stats->ramp = ramp;
+    fill_solve(stats->u, rm[0]); fill_solve(stats->v, rm[1]); fill_solve(stats->w, rm[2]);
+    fill_solve(stats->p, rp[0]);
+    stats->div_l2 = std::sqrt(dg.div2 / std::max(1, c->np_active));
+    stats->umax = dg.umax; stats->vmax = dg.vmax; stats->wmax = dg.wmax;
+    if (c->prm.compute_forces)
+      for (int q = 0; q < 3; ++q) stats->force[q] = dg.force[q];
+    float ms;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); stats->t_rhs_ms = ms;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[5]); stats->t_rhs_ms += ms;
+    cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); stats->t_mom_ms = ms;
+    cudaEventElapsedTime(&ms, c->ev[5], c->ev[3]); stats->t_p_ms = ms;
+    cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); stats->t_proj_ms = ms;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); stats->t_total_ms = ms;
+  }
+  for (int f = 0; f < 3; ++f) rc = worst(rc, solve_status(rm[f]));
+  rc = worst(rc, solve_status(rp[0]));
+  const bool bad_mom = dg.nonfinite_mom || rm[0].nonfinite || rm[1].nonfinite || rm[2].nonfinite;
+  const bool bad_p = dg.nonfinite_p || rp[0].nonfinite;
+  if (bad_mom || bad_p) {
+    rc = IBM_ERR_NONFINITE;
+    c->err = bad_mom ? "non-finite momentum solve (main.cu:302-305)" : "non-finite pressure solve (main.cu:333-336)";
+  }
+  if (stats) stats->status = rc;
+  return rc;
+}
+
+
+}  // namespace
+
 int ibm_step(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
   return guarded(c, [&]() {
-    require_inputs(c);
-    ensure_solvers(c);
-    cudaStream_t st = c->st;
-    *c->hramp = ramp;
-    KResult rm[3], rp[1];
-    const double *bm[3] = {c->bb[0].p, c->bb[1].p, c->bb[2].p};
-    double *xm[3] = {c->xb[0].p, c->xb[1].p, c->xb[2].p};
-    const double *bp[1] = {c->bb[3].p};
-    double *xp[1] = {c->xb[3].p};
-    Precond none, mgp;
-    mgp.ctx = c;
-    mgp.apply = mg_apply_cb;
-    if (c->prm.use_graph) {
-      // The whole step as one graph launch; the GMRES loops run on the device.
-      if (!c->graph_ready || !c->graph_bound) {
-        const bool zg = c->prm.use_zero_initial_guess != 0;
-        c->kmom.bind(st, bm, xm, ~0u, zg);
-        c->kp.bind(st, bp, xp, ~0u, zg);
-        c->graph_bound = true;
-      }
-      if (!c->graph_ready) build_step_graph(c, none, mgp);
-      IBM_CUDA_TRY(cudaGraphLaunch(c->gexec, st));
-      IBM_CUDA_TRY(cudaStreamSynchronize(st));
-      IBM_CUDA_TRY(cudaGetLastError());
-      for (int s = 0; s < 4; ++s) {
-        const KFlags &f = c->hflags_graph[s];
-        KResult &r = s < 3 ? rm[s] : rp[0];
-        r.iters = f.iters; r.rel_res = f.rel; r.status = f.status; r.nonfinite = f.nonfinite;
-      }
-      const unsigned long long *lp = c->hloops;
-      c->launches += c->graph_fixed_launches + (long long)lp[0] * c->graph_body_launches[0] +
-                     (long long)lp[1] * c->graph_body_launches[1] + (long long)lp[2] * c->graph_body_launches[2] +
-                     (long long)lp[3] * c->graph_body_launches[3];
-    } else {
-      IBM_CUDA_TRY(cudaMemcpyAsync(c->dramp.p, c->hramp, sizeof(double), cudaMemcpyHostToDevice, st));
-      IBM_CUDA_TRY(cudaMemsetAsync(c->diag.p, 0, sizeof(StepDiag), st));
-      IBM_CUDA_TRY(cudaEventRecord(c->ev[0], st));
-      {
-        PhaseScope ph(PH_RHS);
-        launch_bc(c, c->u.p, c->v.p, c->w.p);
-        launch_momentum_rhs(c);
-      }
-      IBM_CUDA_TRY(cudaEventRecord(c->ev[1], st));
-      {
-        PhaseScope ph(PH_MOM);
-        c->kmom.solve(st, bm, xm, none, rm, ~0u, c->prm.use_zero_initial_guess != 0);
-      }
-      IBM_CUDA_TRY(cudaEventRecord(c->ev[2], st));
-      {
-        PhaseScope ph(PH_RHS);
-        launch_tilde(c);
-        launch_pressure_rhs(c);
-      }
-      IBM_CUDA_TRY(cudaEventRecord(c->ev[5], st));
-      {
-        PhaseScope ph(PH_P);
-        c->kp.solve(st, bp, xp, mgp, rp, ~0u, c->prm.use_zero_initial_guess != 0);
-      }
-      IBM_CUDA_TRY(cudaEventRecord(c->ev[3], st));
-      {
-        PhaseScope ph(PH_PROJ);
-        launch_projection(c);
-      }
-      IBM_CUDA_TRY(cudaEventRecord(c->ev[4], st));
-      IBM_CUDA_TRY(cudaMemcpyAsync(c->hdiag, c->diag.p, sizeof(StepDiag), cudaMemcpyDeviceToHost, st));
-      IBM_CUDA_TRY(cudaStreamSynchronize(st));
-      IBM_CUDA_TRY(cudaGetLastError());
-      c->prof.drain();
-    }
-    int rc = IBM_OK;
-    const StepDiag &dg = *c->hdiag;
-    if (stats) {
-      memset(stats, 0, sizeof(*stats));
-      stats->ramp = ramp;
-      fill_solve(stats->u, rm[0]); fill_solve(stats->v, rm[1]); fill_solve(stats->w, rm[2]);
-      fill_solve(stats->p, rp[0]);
-      stats->div_l2 = std::sqrt(dg.div2 / std::max(1, c->np_active));
-      stats->umax = dg.umax; stats->vmax = dg.vmax; stats->wmax = dg.wmax;
-      if (c->prm.compute_forces)
-        for (int q = 0; q < 3; ++q) stats->force[q] = dg.force[q];
-      float ms;
-      cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); stats->t_rhs_ms = ms;
-      cudaEventElapsedTime(&ms, c->ev[2], c->ev[5]); stats->t_rhs_ms += ms;
-      cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); stats->t_mom_ms = ms;
-      cudaEventElapsedTime(&ms, c->ev[5], c->ev[3]); stats->t_p_ms = ms;
-      cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]); stats->t_proj_ms = ms;
-      cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]); stats->t_total_ms = ms;
-    }
-    for (int f = 0; f < 3; ++f) rc = worst(rc, solve_status(rm[f]));
-    rc = worst(rc, solve_status(rp[0]));
-    const bool bad_mom = dg.nonfinite_mom || rm[0].nonfinite || rm[1].nonfinite || rm[2].nonfinite;
-    const bool bad_p = dg.nonfinite_p || rp[0].nonfinite;
-    if (bad_mom || bad_p) {
-      rc = IBM_ERR_NONFINITE;
-      c->err = bad_mom ? "non-finite momentum solve (main.cu:302-305)" : "non-finite pressure solve (main.cu:333-336)";
-    }
-    if (stats) stats->status = rc;
-    return rc;
+    step_launch(c, ramp);
+    return step_collect(c, ramp, stats);
   });
+}
+
+struct ibm_batch {
+  std::vector<ibm_ctx *> ctx;
+};
+
+int ibm_batch_create(int n, const ibm_grid_desc *grids, ibm_batch **out) {
+  if (n < 1 || !grids || !out) return IBM_ERR_ARG;
+  *out = nullptr;
+  ibm_batch *b = new ibm_batch;
+  for (int i = 0; i < n; ++i) {
+    ibm_ctx *c = nullptr;
+    const int rc = ibm_create(&grids[i], &c);
+    if (rc != IBM_OK) {
+      ibm_batch_destroy(b);
+      return rc;
+    }
+    b->ctx.push_back(c);
+  }
+  *out = b;
+  return IBM_OK;
+}
+
+void ibm_batch_destroy(ibm_batch *b) {
+  if (!b) return;
+  for (ibm_ctx *c : b->ctx) ibm_destroy(c);
+  delete b;
+}
+
+int ibm_batch_size(const ibm_batch *b) { return b ? (int)b->ctx.size() : 0; }
+
+ibm_ctx *ibm_batch_ctx(ibm_batch *b, int i) {
+  return (b && i >= 0 && i < (int)b->ctx.size()) ? b->ctx[(size_t)i] : nullptr;
+}
+
+int ibm_batch_step(ibm_batch *b, const double *ramps, ibm_step_stats *stats) {
+  if (!b || !ramps) return IBM_ERR_ARG;
+  const size_t n = b->ctx.size();
+  std::vector<int> rc(n, IBM_OK);
+  for (size_t i = 0; i < n; ++i) rc[i] = guarded(b->ctx[i], [&]() { step_launch(b->ctx[i], ramps[i]); return IBM_OK; });
+  int worst_rc = IBM_OK;
+  for (size_t i = 0; i < n; ++i) {
+    ibm_step_stats *st = stats ? stats + i : nullptr;
+    if (rc[i] == IBM_OK) rc[i] = guarded(b->ctx[i], [&]() { return step_collect(b->ctx[i], ramps[i], st); });
+    else if (st) { memset(st, 0, sizeof(*st)); st->status = rc[i]; }
+    if (rc[i] < 0) { if (worst_rc >= 0) worst_rc = rc[i]; }
+    else if (worst_rc >= 0) worst_rc = std::max(worst_rc, rc[i]);
+  }
+  return worst_rc;
 }
 
 int ibm_solve(ibm_ctx *c, int field, const double *b, double *x, ibm_solve_stats *stats) {

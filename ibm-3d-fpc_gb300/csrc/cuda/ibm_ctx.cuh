@@ -63,6 +63,9 @@ struct ibm_ctx {
   ibm::DBuf<double> part;        // diagnostics block partials
   ibm::DBuf<ibm::StepDiag> diag;
   ibm::StepDiag *hdiag = nullptr;
+  // results of the step being collected (the halves of ibm_step)
+  ibm::KResult last_rm[3], last_rp[1];
+  bool last_graph = false;
 
   bool solvers_ready = false;
   int solvers_precision = -1;

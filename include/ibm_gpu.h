@@ -216,6 +216,24 @@ int ibm_profile_time_kernel(ibm_ctx *ctx, int kernel);
 int ibm_profile_get(ibm_ctx *ctx, ibm_profile *out);
 const char *ibm_kernel_name(int kernel);
 
+/* Batching extension (independent channels stepped together; the reference
+ * runs one channel per process, main.cu:249-376). Each instance is a full
+ * context with its own stream: set its inputs and parameters with the ibm_*
+ * calls on ibm_batch_ctx(b, i). ibm_batch_step queues one step of every
+ * instance before waiting for any, so instances in graph mode (use_graph)
+ * run concurrently on the GPU; host-driven instances step one after the
+ * other. Each instance's results equal ibm_step's on that context alone. */
+typedef struct ibm_batch ibm_batch;
+int ibm_batch_create(int n, const ibm_grid_desc *grids, ibm_batch **out);
+void ibm_batch_destroy(ibm_batch *b);
+int ibm_batch_size(const ibm_batch *b);
+ibm_ctx *ibm_batch_ctx(ibm_batch *b, int i);
+/* ramps[n]; stats[n] (may be NULL). Returns the worst instance status
+ * (IBM_OK < IBM_NOT_CONVERGED < errors: the first negative code); the
+ * instance's own code is in stats[i].status and its message in
+ * ibm_last_error(ibm_batch_ctx(b, i)). */
+int ibm_batch_step(ibm_batch *b, const double *ramps, ibm_step_stats *stats);
+
 int ibm_synchronize(ibm_ctx *ctx);
 void *ibm_stream(ibm_ctx *ctx);            /* the context's cudaStream_t */
 long long ibm_kernel_launches(ibm_ctx *ctx); /* kernels this context has launched */
