@@ -20,10 +20,15 @@ roofline   : the kernel class with the largest device time in the timed
 cpu_baseline: the CPU oracle (the reference's HYPRE path is not available
              here) on all host cores, on a bounded sample.
 
+ensemble    : a batched ensemble of 32 seeded independent channels (96..256 x
+             16..48 x 16..48) stepped together through ibm_batch_step, in
+             instance-steps/s, beside the same contexts stepped one by one.
+
 --impl reference times the CPU path alone (the oracle port, all cores) on
 bounded samples of the same workload and prints its own line.
 Multi-GPU: the single channel does not shard; N ranks run N replicas
-(weak scaling), timing is the max over ranks.
+(weak scaling), timing is the max over ranks. The ensemble shards its
+instances over the ranks by cell count.
 """
 from __future__ import annotations
 
@@ -57,6 +62,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--ensemble", type=int, default=32, help="instances of the batched ensemble")
     ap.add_argument("--mg-coarse-max", type=int, default=640,
                     help="multigrid: largest level solved directly (dense inverse)")
     ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
@@ -160,6 +167,80 @@ def device_timer(ibm_lib, ctx):
     import torch
     stream = torch.cuda.ExternalStream(ibm_lib.ibm_stream(ctx))
     return stream
+
+
+def ensemble_cases(ibm, n, seed=5):
+    """The batched-ensemble workload: n channels with seeded sizes in
+    {96..256} x {16..48} x {16..48} (multiples of 16), cylinder diameter
+    U(0.06, 0.14) at y U(0.15, 0.26), inflow Um U(0.2, 2.25)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(n):
+        nx = int(rng.integers(6, 17)) * 16
+        ny = int(rng.integers(1, 4)) * 16
+        nz = int(rng.integers(1, 4)) * 16
+        d = float(rng.uniform(0.06, 0.14))
+        yc = float(rng.uniform(0.15, 0.26))
+        um = float(rng.uniform(0.2, 2.25))
+        specs.append((nx, ny, nz, d, yc, um))
+    return specs
+
+
+def shard_by_cells(specs, ws, rank):
+    """Instances of this rank: greedy balance of the cell counts over ranks."""
+    load = [0] * ws
+    mine = []
+    for i in sorted(range(len(specs)), key=lambda i: -specs[i][0] * specs[i][1] * specs[i][2]):
+        r = min(range(ws), key=lambda q: load[q])
+        load[r] += specs[i][0] * specs[i][1] * specs[i][2]
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
+
+
+def ensemble_measure(ibm, args, ws, rank, local, steps, warmup):
+    """Instance-steps/s of the batched ensemble (ibm_batch_step: every
+    instance's graph-captured step queued before any is waited for) and of
+    the same contexts stepped one after the other; instances are sharded over
+    ranks by cell count, the time is the max over ranks."""
+    specs = ensemble_cases(ibm, args.ensemble)
+    mine = shard_by_cells(specs, ws, rank)
+    cases = [ibm.Case(ibm.channel_params(nx, ny, nz, Um=um, Rcirc=d / 2, ycirc=yc, dt=1e-3))
+             for nx, ny, nz, d, yc, um in (specs[i] for i in mine)]
+    prm = solver_params(ibm, args.precision, graph=1, coarse_max=args.mg_coarse_max)
+    batch = ibm.Batch(cases, prm, device=local)
+    for s, c in zip(batch.solvers, cases):
+        s.set_fields(*initial_state(c))
+    for _ in range(warmup):
+        batch.step(1.0)
+    for s in batch.solvers:
+        s.step(1.0)
+    if ws > 1:
+        import torch
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    worst = 0
+    for _ in range(steps):
+        worst = max(worst, max(st.status for st in batch.step(1.0)))
+    t_batch = reduce_max_ms((time.perf_counter() - t0) * 1e3, ws, "cuda")
+    if ws > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for s in batch.solvers:
+            s.step(1.0)
+    t_seq = reduce_max_ms((time.perf_counter() - t0) * 1e3, ws, "cuda")
+    cells = sum(nx * ny * nz for nx, ny, nz, *_ in specs)
+    batch.close()
+    n = len(specs)
+    return {"workload": f"{n} independent channels, seeded sizes {{96..256}}x{{16..48}}x{{16..48}} (multiples of 16), "
+                        "cylinder D U(0.06,0.14) at y U(0.15,0.26), Um U(0.2,2.25), dt 1e-3, same solver settings",
+            "instances": n, "cells": cells, "steps": steps,
+            "instance_steps_per_s": n * steps / (t_batch / 1e3),
+            "cell_steps_per_s": cells * steps / (t_batch / 1e3),
+            "sequential_instance_steps_per_s": n * steps / (t_seq / 1e3),
+            "concurrency_gain": t_seq / t_batch, "worst_status": int(worst),
+            "sharding": f"instances over {ws} rank(s) balanced by cell count, no collective; host wall time, max over ranks"}
 
 
 def run_steps(solver, n):
@@ -471,12 +552,17 @@ def main():
                       "d2h_bytes_per_step": nbytes + 4 * 40 + 56}
     out["roofline"] = roofline
     out["clocks"] = clk.summary()
+    mixed.close()
+    if not args.no_ensemble:
+        try:
+            out["ensemble"] = ensemble_measure(ibm, args, ws, rank, local, steps=min(args.steps, 10), warmup=3)
+        except Exception as e:  # the line must still print
+            out["ensemble"] = {"value": None, "error": str(e)}
     if rank == 0 and not args.no_cpu:
         try:
             out["cpu_baseline"] = cpu_baseline(ibm, nx, ny, nz)
         except Exception as e:  # the line must still print
             out["cpu_baseline"] = {"value": None, "error": str(e)}
-    mixed.close()
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
