@@ -63,3 +63,22 @@ def test_reference_arm_idle_on_other_ranks(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"])
     b.reference_arm(b.parse())
     assert capsys.readouterr().out == ""
+
+
+@pytest.mark.parametrize("ws", [1, 2, 3, 8])
+def test_ensemble_shards_cover_every_instance_once(ws):
+    """The batched ensemble shards by instance: every instance lands on
+    exactly one rank and the cell counts are balanced to within the largest
+    instance."""
+    b = _bench()
+    specs = b.ensemble_cases(None, 32)
+    shards = [b.shard_by_cells(specs, ws, r) for r in range(ws)]
+    flat = sorted(i for s in shards for i in s)
+    assert flat == list(range(len(specs)))
+    cells = [sum(specs[i][0] * specs[i][1] * specs[i][2] for i in s) for s in shards]
+    largest = max(nx * ny * nz for nx, ny, nz, *_ in specs)
+    assert max(cells) - min(cells) <= largest
+    for nx, ny, nz, d, yc, um in specs:
+        assert 96 <= nx <= 256 and 16 <= ny <= 48 and 16 <= nz <= 48
+        assert nx % 16 == ny % 16 == nz % 16 == 0
+        assert 0.06 <= d <= 0.14 and 0.15 <= yc <= 0.26 and 0.2 <= um <= 2.25
