@@ -55,6 +55,22 @@ __device__ __forceinline__ const float *af_row(const KSys &S, long r, long &cs) 
   return S.Af + r;
 }
 
+// Four class-table rows (8 floats each) as four 16-byte pairs, transposed so
+// that cp[s] holds slot s of the four rows.
+__device__ __forceinline__ void load_rows4(const float *__restrict__ tab, ushort4 c4, float4 (&cp)[7]) {
+  const unsigned short ks[4] = {c4.x, c4.y, c4.z, c4.w};
+  float v[4][8];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float4 *p = reinterpret_cast<const float4 *>(tab + 8 * (long)ks[q]);
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    v[q][0] = a.x; v[q][1] = a.y; v[q][2] = a.z; v[q][3] = a.w;
+    v[q][4] = b.x; v[q][5] = b.y; v[q][6] = b.z; v[q][7] = b.w;
+  }
+#pragma unroll
+  for (int s = 0; s < 7; ++s) cp[s] = make_float4(v[0][s], v[1][s], v[2][s], v[3][s]);
+}
+
 // Sum block partials of `nd` dot products in block order; one warp per dot.
 __device__ void reduce_partials(const double *part, int nblk, int nd, double *out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -542,11 +558,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv32(KSys *sys) {
       if (r0 >= n) continue;
       float4 cp[7];
       if (S.cls) {
-        const ushort4 c4 = __ldcs(reinterpret_cast<const ushort4 *>(S.cls + r0));
-        const float *t0 = S.tabf + 8 * (long)c4.x, *t1 = S.tabf + 8 * (long)c4.y;
-        const float *t2 = S.tabf + 8 * (long)c4.z, *t3 = S.tabf + 8 * (long)c4.w;
-#pragma unroll
-        for (int q = 0; q < 7; ++q) cp[q] = make_float4(__ldg(t0 + q), __ldg(t1 + q), __ldg(t2 + q), __ldg(t3 + q));
+        load_rows4(S.tabf, __ldcs(reinterpret_cast<const ushort4 *>(S.cls + r0)), cp);
       } else {
 #pragma unroll
         for (int q = 0; q < 7; ++q) cp[q] = __ldcs(reinterpret_cast<const float4 *>(S.Af + (long)q * n + r0));
@@ -877,11 +889,7 @@ __device__ __forceinline__ void jacobi_two_rows4(const KSys &S, const float *__r
     float4 id;
     if (S.clsj) {
       // class records {invdf, Ajf_1..Ajf_6, 0}: slot 0 is D^-1
-      const ushort4 c4 = __ldcs(reinterpret_cast<const ushort4 *>(S.clsj + r0));
-      const float *t0 = S.tabj + 8 * (long)c4.x, *t1 = S.tabj + 8 * (long)c4.y;
-      const float *t2 = S.tabj + 8 * (long)c4.z, *t3 = S.tabj + 8 * (long)c4.w;
-#pragma unroll
-      for (int q = 0; q < 7; ++q) cp[q] = make_float4(__ldg(t0 + q), __ldg(t1 + q), __ldg(t2 + q), __ldg(t3 + q));
+      load_rows4(S.tabj, __ldcs(reinterpret_cast<const ushort4 *>(S.clsj + r0)), cp);
       id = cp[0];
     } else {
 #pragma unroll
