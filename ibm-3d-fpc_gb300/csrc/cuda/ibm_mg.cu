@@ -708,7 +708,8 @@ __device__ __forceinline__ void relax_quad(const float (&c)[2][8], const float4 
 // One quad of an FP32 in-place phase: the four points r0 .. r0+3 of line
 // (j, k) from column i0.
 __device__ __forceinline__ void relax_quad_at(const Recs<float, 8> &R, const float *__restrict__ b, float *x,
-                                              const Box &bx, int color, int zero_x, long r0, int i0, int j, int k) {
+                                              const Box &bx, int color, int zero_x, long r0, int i0, int j, int k,
+                                              float *zout = nullptr) {
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
   const long sy = nx, sz = (long)nx * ny;
   const int p = (j + k + color) & 1;
@@ -732,14 +733,69 @@ __device__ __forceinline__ void relax_quad_at(const Recs<float, 8> &R, const flo
   const float xl = i0 > 0 ? x[r0 - 1] : 0.0f;
   const float xr = i0 + 4 < nx ? x[r0 + 4] : 0.0f;
   float out[2];
+  float4 q = xc;  // the quad after the phase
   if (p == 0) {
     relax_quad<0>(c, bq, xc, xs, xn, xb, xt, xl, xr, out);
     x[r0] = out[0];
     x[r0 + 2] = out[1];
+    q.x = out[0];
+    q.z = out[1];
   } else {
     relax_quad<1>(c, bq, xc, xs, xn, xb, xt, xl, xr, out);
     x[r0 + 1] = out[0];
     x[r0 + 3] = out[1];
+    q.y = out[0];
+    q.w = out[1];
+  }
+  if (zout) *reinterpret_cast<float4 *>(zout + r0) = q;
+}
+
+// The finest level's first phase from a zero guess with the V-cycle's input
+// load fused in (k_load_input_f4's b = winv * in / nu, then k_relax_rb_quad's
+// zero phase), and its last phase with the output store fused in (the whole
+// quad also written to the preconditioned direction). Same values as the
+// separate kernels.
+__global__ void __launch_bounds__(kThreads) k_relax_rb_quad_in(Recs<float, 8> R, float *bv, float *x, Box bx,
+                                                               VecRef in, const float *winvf, const int *gate) {
+  if (gate_off(gate)) return;
+  const long n4 = bx.n / 4;
+  const long off = in.idx ? (long)(*in.idx) * in.ld : 0;
+  const float sc = in.nu ? (float)(1.0 / in.nu[in.idx ? *in.idx : 0]) : 1.0f;
+  const float *srcf = in.basef + off;
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+    const long r0 = 4 * q;
+    float4 a = *reinterpret_cast<const float4 *>(srcf + r0);
+    a.x *= sc; a.y *= sc; a.z *= sc; a.w *= sc;
+    if (winvf) {
+      const float4 w = *reinterpret_cast<const float4 *>(winvf + r0);
+      a.x *= w.x; a.y *= w.y; a.z *= w.z; a.w *= w.w;
+    }
+    *reinterpret_cast<float4 *>(bv + r0) = a;
+    const unsigned line = fast_div((unsigned)r0, bx.dx);
+    const unsigned kk = fast_div(line, bx.dy);
+    const int j = (int)(line - kk * (unsigned)bx.ny), k = (int)kk;
+    const int p = (j + k) & 1;  // colour-0 points of the quad
+    float c[2][8];
+    load_quad_recs(R, r0 / 2, c);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (p == 0) { v.x = c[0][0] * a.x; v.z = c[1][0] * a.z; }
+    else { v.y = c[0][0] * a.y; v.w = c[1][0] * a.w; }
+    *reinterpret_cast<float4 *>(x + r0) = v;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_relax_rb_quad_out(Recs<float, 8> R, const float *__restrict__ b,
+                                                                float *x, Box bx, int color, OutRef out,
+                                                                const int *gate) {
+  if (gate_off(gate)) return;
+  const long n4 = bx.n / 4;
+  float *z = out.f + (out.idx ? (long)(*out.idx) * out.ld : 0);
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+    const long r0 = 4 * q;
+    const unsigned line = fast_div((unsigned)r0, bx.dx);
+    const int i0 = (int)((unsigned)r0 - line * (unsigned)bx.nx);
+    const unsigned kk = fast_div(line, bx.dy);
+    relax_quad_at(R, b, x, bx, color, 0, r0, i0, (int)(line - kk * (unsigned)bx.ny), (int)kk, z);
   }
 }
 
@@ -1303,7 +1359,10 @@ void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const flo
 // Runs the V-cycle from level l with zero initial guess; returns (through the
 // level's x buffer pointer swap-free scheme) the buffer holding the result.
 template <class T>
-static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgParams &p, const int *gate) {
+// fin / fout (finest level only, may be null): the V-cycle's input load and
+// output store, fused into the first and the last relaxation phases.
+static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgParams &p, const int *gate,
+                 const VecRef *fin = nullptr, const OutRef *fout = nullptr, const float *winvf = nullptr) {
   MgLevelT<T> &F = L[l];
   const long n = F.b.n;
   const double T_ = sizeof(T);
@@ -1325,14 +1384,22 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   const bool rb7 = R7.R || R7.code, rb27 = R27.R || R27.code;
   const bool quad = F.b.nx % 4 == 0 && p.quads;  // quartet kernels (FP32)
   const double rec7 = R7.code ? 2.0 : 8.0 * T_, rec27 = R27.code ? 2.0 : 28.0 * T_;
-  auto relax = [&](bool zero) {
+  auto relax = [&](bool zero, bool last) {
     if constexpr (sizeof(T) == 4) {
       if (p.relax == 2 && rb7 && quad) {
         for (int color = 0; color < 2; ++color) {
           const bool z = zero && color == 0;
-          LaunchScope ls(K_MG_RELAX_FINE, st, z ? 0.5 * n * (R7.code ? 2.0 : T_) + 1.5 * T_ * n
-                                                : 0.5 * n * rec7 + 1.5 * T_ * n);
-          k_relax_rb_quad<<<grid_all(n / 4), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, color, z, gate);
+          if (z && fin) {
+            LaunchScope ls(K_MG_RELAX_FINE, st, 0.5 * n * (R7.code ? 2.0 : T_) + (winvf ? 4.0 : 3.0) * T_ * n);
+            k_relax_rb_quad_in<<<grid_all(n / 4), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, *fin, winvf, gate);
+          } else if (color == 1 && last && fout) {
+            LaunchScope ls(K_MG_RELAX_FINE, st, 0.5 * n * rec7 + 2.5 * T_ * n);
+            k_relax_rb_quad_out<<<grid_all(n / 4), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, 1, *fout, gate);
+          } else {
+            LaunchScope ls(K_MG_RELAX_FINE, st, z ? 0.5 * n * (R7.code ? 2.0 : T_) + 1.5 * T_ * n
+                                                  : 0.5 * n * rec7 + 1.5 * T_ * n);
+            k_relax_rb_quad<<<grid_all(n / 4), kThreads, 0, st>>>(R7, F.bv.p, cur, F.b, color, z, gate);
+          }
         }
         return;
       }
@@ -1385,7 +1452,7 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   // each way when it is set
   const int c1 = (l > 0 && p.nu_coarse > 0) ? p.nu_coarse : p.nu1, c2 = (l > 0 && p.nu_coarse > 0) ? p.nu_coarse : p.nu2;
   const int nu1 = F.relax ? c1 : 0, nu2 = F.relax ? c2 : 0;
-  for (int s = 0; s < nu1; ++s) relax(s == 0);
+  for (int s = 0; s < nu1; ++s) relax(s == 0, false);
   const T *res = F.bv.p;  // residual of a zero initial guess is b
   if (nu1 > 0 && p.relax == 2 && rb7) {
     LaunchScope ls(K_MG_RESID, st, 0.5 * n * rec7 + 2.5 * T_ * n);
@@ -1443,7 +1510,7 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
       k_prolong<T><<<grid_all(n), kThreads, 0, st>>>(xc, C.b, F.pm.p, F.pp.p, F.b, F.cdir, cur, nu1 > 0, gate);
     }
   }
-  for (int s = 0; s < nu2; ++s) relax(false);
+  for (int s = 0; s < nu2; ++s) relax(false, s == nu2 - 1);
   return cur;
 }
 
@@ -1453,6 +1520,15 @@ void Multigrid::apply(cudaStream_t st, const VecRef &in, const OutRef &out, cons
   if (use_fp32) {
     if (L32.empty()) throw Error(IBM_ERR_STATE, "multigrid: FP32 hierarchy not built");
     MgLevelT<float> &F = L32[0];
+    // input load and output store fused into the finest level's first and
+    // last phases when that level relaxes with the quartet kernels
+    const bool fuse = in.basef && out.f && !out.d && F.b.n % 4 == 0 && (in.ld % 4) == 0 && prm.quads &&
+                      prm.relax == 2 && F.relax && F.cdir >= 0 && F.ns == 7 && (F.rb.p || F.rbc.ok()) &&
+                      F.b.nx % 4 == 0 && prm.nu1 > 0 && prm.nu2 > 0;
+    if (fuse) {
+      vcycle<float>(st, L32, 0, prm, gate, &in, &out, winvf_.p);
+      return;
+    }
     {
       if (in.basef && F.b.n % 4 == 0 && (in.ld % 4) == 0) {
         LaunchScope ls(K_MG_LOAD, st, (winv_ ? 12.0 : 8.0) * F.b.n);

@@ -115,3 +115,19 @@ def test_double_float_residual(ibm, case48, graph):
     assert st.status == ibm.IBM_OK
     r = rhs - s.apply_operator(ibm.FIELD_P, x)
     assert np.linalg.norm(r) <= 2e-12 * np.linalg.norm(rhs)
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+def test_steps_bitwise_quads(ibm, case48, graph):
+    """Steps with the quartet kernels (including the finest level's first and
+    last phases with the V-cycle's input load and output store fused in)
+    against one point per thread and separate load / store kernels."""
+    a = ibm.Solver(case48, bench_like(ibm, precision=2, use_graph=graph, mg_quads=0))
+    b = ibm.Solver(case48, bench_like(ibm, precision=2, use_graph=graph, mg_quads=1))
+    for step in range(1, 5):
+        sa = a.step(min(1.0, step / 3.0))
+        sb = b.step(min(1.0, step / 3.0))
+        for f in "uvwp":
+            assert getattr(sa, f).iters == getattr(sb, f).iters, f
+    for x, y, name in zip(a.fields(), b.fields(), "uvwp"):
+        assert bits_equal(x, y), name
