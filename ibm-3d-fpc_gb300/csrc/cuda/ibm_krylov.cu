@@ -108,34 +108,56 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
   if (threadIdx.x < 2 * kWarps) sacc[threadIdx.x] = 0.0;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
-    double pb = 0.0, pr = 0.0;
+  // per-thread sums over all of the thread's rows, one warp reduction at the
+  // end (GB300's FP64 pipe is the bound here: no FP64 work per tile)
+  double pb = 0.0, pr = 0.0;
+  if (S.a32 && S.x_zero) {
+    // r = b: the FP32 basis vector from the bits of b (integer split, one FP32
+    // add: b rounded to FP32), |b|^2 in FP32 per thread; no FP64 instruction
+    float pf = 0.0f;
+    for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
 #pragma unroll
-    for (int t = 0; t < kRowsPerThread; ++t) {
-      const long r = t0 + t * kThreads + threadIdx.x;
-      if (r < S.n) {
-        int i, j, k;
-        sys_ijk(r, S, i, j, k);
-        // with finite coefficients A 0 is +0 in every row, so b - 0 equals b - A x
-        // bit for bit: a zero guess takes r = b and |r| = |b|
-        const double bv = S.b[r];
-        double rv = bv;
-        if (!S.x_zero) {
-          long cs;
-          const double *c0 = ar_row(S, r, cs);
-          rv = bv - stencil7_at(c0, cs, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
-          pr = fma(rv, rv, pr);
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) {
+          float bh, bl;
+          df_split(S.b[r], bh, bl);
+          const float v = __fadd_rn(bh, bl);
+          S.Vf[r] = v;
+          pf = fmaf(v, v, pf);
         }
-        if (S.a32) S.Vf[r] = (float)rv;
-        else S.V[r] = rv;
-        pb = fma(bv, bv, pb);
+      }
+    }
+    pb = pr = (double)pf;
+  } else {
+    for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
+#pragma unroll
+      for (int t = 0; t < kRowsPerThread; ++t) {
+        const long r = t0 + t * kThreads + threadIdx.x;
+        if (r < S.n) {
+          int i, j, k;
+          sys_ijk(r, S, i, j, k);
+          // with finite coefficients A 0 is +0 in every row, so b - 0 equals b - A x
+          // bit for bit: a zero guess takes r = b and |r| = |b|
+          const double bv = S.b[r];
+          double rv = bv;
+          if (!S.x_zero) {
+            long cs;
+            const double *c0 = ar_row(S, r, cs);
+            rv = bv - stencil7_at(c0, cs, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
+            pr = fma(rv, rv, pr);
+          }
+          if (S.a32) S.Vf[r] = (float)rv;
+          else S.V[r] = rv;
+          pb = fma(bv, bv, pb);
+        }
       }
     }
     if (S.x_zero) pr = pb;
-    pb = warp_sum(pb);
-    pr = warp_sum(pr);
-    if (lane == 0) { sacc[warp] += pb; sacc[kWarps + warp] += pr; }
   }
+  pb = warp_sum(pb);
+  pr = warp_sum(pr);
+  if (lane == 0) { sacc[warp] = pb; sacc[kWarps + warp] = pr; }
   if (!block_partials_and_last(sacc, 2, S.part, &sc->ticket)) return;
   __shared__ double tot[2];
   reduce_partials(S.part, gridDim.x, 2, tot);
@@ -327,8 +349,8 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next(KSys *sys) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *vn = S.V + (long)nd * S.ldv;
   const bool store = nd < sc->kdim;  // the last vector of a full cycle is never used
+  double p = 0.0;  // per thread over all its rows
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
-    double p = 0.0;
 #pragma unroll
     for (int t = 0; t < kRowsPerThread; ++t) {
       const long r = t0 + t * kThreads + threadIdx.x;
@@ -339,9 +361,9 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next(KSys *sys) {
         p = fma(w, w, p);
       }
     }
-    p = warp_sum(p);
-    if (lane == 0) sacc[warp] += p;
   }
+  p = warp_sum(p);
+  if (lane == 0) sacc[warp] = p;
   if (!block_partials_and_last(sacc, 1, S.part, &sc->ticket)) return;
   __shared__ double tot[1];
   reduce_partials(S.part, gridDim.x, 1, tot);
@@ -428,8 +450,8 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
     // double-float copy of x that the update wrote; |r|^2 and the squared
     // row bounds summed in FP32 per thread and FP64 across threads
     const long sy = S.nx, sz = (long)S.nx * S.ny;
+    float pf = 0.0f, mf = 0.0f;  // per thread over all its rows
     for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
-      float pf = 0.0f, mf = 0.0f;
 #pragma unroll
       for (int t = 0; t < kRowsPerThread; ++t) {
         const long r = t0 + t * kThreads + threadIdx.x;
@@ -459,12 +481,12 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
           mf = fmaf(mag, mag, mf);
         }
       }
-      const double pr = warp_sum((double)pf), mr = warp_sum((double)mf);
-      if (lane == 0) { sacc[warp] += pr; sacc[kWarps + warp] += mr; }
     }
-  } else
+    const double pr = warp_sum((double)pf), mr = warp_sum((double)mf);
+    if (lane == 0) { sacc[warp] = pr; sacc[kWarps + warp] = mr; }
+  } else {
+  double pr = 0.0;  // per thread over all its rows
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
-    double pr = 0.0;
 #pragma unroll
     for (int t = 0; t < kRowsPerThread; ++t) {
       const long r = t0 + t * kThreads + threadIdx.x;
@@ -479,8 +501,9 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
         pr = fma(rv, rv, pr);
       }
     }
-    pr = warp_sum(pr);
-    if (lane == 0) sacc[warp] += pr;
+  }
+  pr = warp_sum(pr);
+  if (lane == 0) sacc[warp] = pr;
   }
   if (!block_partials_and_last(sacc, 2, S.part, &sc->ticket)) return;
   __shared__ double tot[2];
