@@ -9,6 +9,8 @@
 // written out (fma() where the reference's device code fuses a CSR
 // accumulation, separately rounded operations elsewhere) so the CPU oracle
 // reproduces the results bit for bit.
+#include <cmath>
+
 #include "ibm_ctx.cuh"
 #include "ibm_step.cuh"
 
@@ -16,9 +18,25 @@ namespace ibm {
 
 namespace {
 
+// Division by a grid extent with a multiply-high (Granlund-Montgomery): flat
+// face and cell indices stay below 2^32, and a 64-bit integer division would
+// cost a long instruction sequence per use in kernels whose FP64 work is
+// already the bound.
+struct IDiv {
+  unsigned d;
+  FastDiv f;
+};
+inline IDiv make_idiv(int d) { return IDiv{(unsigned)d, make_fastdiv((unsigned)d)}; }
 struct Dims {
   int nx, ny, nz;
+  IDiv dnx, dnx1, dnxm, dny, dny1, dnym;  // nx, nx + 1, nx - 1, ny, ny + 1, ny - 1
 };
+// q = n / D, returns n - q D.
+__device__ __forceinline__ int udivmod(long n, const IDiv &D, long &q) {
+  const unsigned qq = fast_div((unsigned)n, D.f);
+  q = (long)qq;
+  return (int)((unsigned)n - qq * D.d);
+}
 
 __device__ __forceinline__ long U3(const Dims &d, int i, int j, int k) { return ((long)k * d.ny + j) * (d.nx + 1) + i; }
 __device__ __forceinline__ long V3(const Dims &d, int i, int j, int k) { return ((long)k * (d.ny + 1) + j) * d.nx + i; }
@@ -46,10 +64,33 @@ __device__ __forceinline__ double ld_w(const double *w, const Dims &d, int i, in
 // division by the grid spacing this way costs 3 FP64 operations instead of
 // the dozen or so of an IEEE division, and the convection kernel is bound by
 // the FP64 pipe on GB300.
+//
+// A divisor that is a power of two, b = 2^p2 (the grid spacing when the
+// domain length over the cell count is one, e.g. 2.5 / 640 = 2^-8), needs no
+// correction: x / 2^p2 = x 2^-p2 exactly, so a normal result only moves the
+// exponent (integer pipe), and the other cases (zero, subnormal, infinite,
+// NaN) take one FP64 multiply by the exact 2^-p2.
+constexpr int kNotPow2 = 1 << 20;
 struct KnownDiv {
   double b, rb;
+  int p2;  // b == 2^p2, else kNotPow2
 };
+inline KnownDiv make_known_div(double b) {
+  KnownDiv k;
+  k.b = b;
+  k.rb = 1.0 / b;
+  k.p2 = kNotPow2;
+  int e = 0;
+  if (std::frexp(b, &e) == 0.5 && e - 1 > -1000 && e - 1 < 1000) k.p2 = e - 1;
+  return k;
+}
 __device__ __forceinline__ double div_known(double x, KnownDiv k) {
+  if (k.p2 != kNotPow2) {
+    const long long bits = __double_as_longlong(x);
+    const int e = (int)((bits >> 52) & 0x7FF), ne = e - k.p2;
+    if (e != 0 && e != 0x7FF && ne > 0 && ne < 0x7FF) return __longlong_as_double(bits - (long long)k.p2 * (1LL << 52));
+    return __dmul_rn(x, k.rb);
+  }
   const double q0 = __dmul_rn(x, k.rb);
   const double r = fma(-q0, k.b, x);
   // r == 0 or r not finite, tested on the bits (integer pipe; FP64 compares
@@ -98,12 +139,14 @@ __device__ __forceinline__ double grad_face(double gl, double pl, double gr, dou
 __global__ void k_bc_planes(double *u, double *v, double *w, const double *uin, const double *ramp, Dims d) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < (long)d.ny * d.nz) {
-    const int j = (int)(t % d.ny), k = (int)(t / d.ny);
+    long kq;
+    const int j = udivmod(t, d.dny, kq), k = (int)kq;
     u[U3(d, 0, j, k)] = __dmul_rn(*ramp, uin[t]);
     u[U3(d, d.nx, j, k)] = u[U3(d, d.nx - 1, j, k)];
   }
   if (t < (long)d.nx * d.nz) {
-    const int i = (int)(t % d.nx), k = (int)(t / d.nx);
+    long kq;
+    const int i = udivmod(t, d.dnx, kq), k = (int)kq;
     v[V3(d, i, 0, k)] = 0.0;
     v[V3(d, i, d.ny, k)] = 0.0;
   }
@@ -137,7 +180,7 @@ struct RhsArgs {
 };
 
 // One thread per solve-box row of u, v and w (flat index over the three boxes).
-__global__ void __launch_bounds__(kThreads) k_momentum_rhs(RhsArgs A) {
+__global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
   const Dims &d = A.d;
   const long total = A.nb[0] + A.nb[1] + A.nb[2];
   const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
@@ -146,10 +189,10 @@ __global__ void __launch_bounds__(kThreads) k_momentum_rhs(RhsArgs A) {
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
     if (t < A.nb[0]) {  // u row: face (i+1, j, k) with i in [0, nx-2]
       const long r = t;
-      const int nxu = d.nx - 1;
-      const int i = (int)(r % nxu) + 1;
-      const long q = r / nxu;
-      const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+      long q;
+      const int i = udivmod(r, d.dnxm, q) + 1;
+      long kq;
+      const int j = udivmod(q, d.dny, kq), k = (int)kq;
       const long f = U3(d, i, j, k);
       const uint8_t fl = A.fu[f];
       const double uc = A.u[f];
@@ -177,9 +220,10 @@ __global__ void __launch_bounds__(kThreads) k_momentum_rhs(RhsArgs A) {
       A.x0[0][r] = A.zero_guess ? 0.0 : uc;
     } else if (t < A.nb[0] + A.nb[1]) {  // v row: face (i, j+1, k)
       const long r = t - A.nb[0];
-      const int i = (int)(r % d.nx);
-      const long q = r / d.nx;
-      const int j = (int)(q % (d.ny - 1)) + 1, k = (int)(q / (d.ny - 1));
+      long q;
+      const int i = udivmod(r, d.dnx, q);
+      long kq;
+      const int j = udivmod(q, d.dnym, kq) + 1, k = (int)kq;
       const long f = V3(d, i, j, k);
       const uint8_t fl = A.fv[f];
       const double vc = A.v[f];
@@ -207,9 +251,10 @@ __global__ void __launch_bounds__(kThreads) k_momentum_rhs(RhsArgs A) {
       A.x0[1][r] = A.zero_guess ? 0.0 : vc;
     } else {  // w row: face (i, j, k+1)
       const long r = t - A.nb[0] - A.nb[1];
-      const int i = (int)(r % d.nx);
-      const long q = r / d.nx;
-      const int j = (int)(q % d.ny), k = (int)(q / d.ny) + 1;
+      long q;
+      const int i = udivmod(r, d.dnx, q);
+      long kq;
+      const int j = udivmod(q, d.dny, kq), k = (int)kq + 1;
       const long f = W3(d, i, j, k);
       const uint8_t fl = A.fw[f];
       const double wc = A.w[f];
@@ -250,16 +295,17 @@ __global__ void k_scatter(const double *u, const double *v, const double *w, con
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < NU + NV + NW; t += (long)gridDim.x * blockDim.x) {
     if (t < NU) {
       const long f = t;
-      const int i = (int)(f % (d.nx + 1));
-      const long q = f / (d.nx + 1);
+      long q;
+      const int i = udivmod(f, d.dnx1, q);
       double val = u[f];
       if (i >= 1 && i <= d.nx - 1) { val = xu[q * (d.nx - 1) + (i - 1)]; bad |= !isfinite(val); }
       ut[f] = val;
     } else if (t < NU + NV) {
       const long f = t - NU;
-      const int i = (int)(f % d.nx);
-      const long q = f / d.nx;
-      const int j = (int)(q % (d.ny + 1)), k = (int)(q / (d.ny + 1));
+      long q;
+      const int i = udivmod(f, d.dnx, q);
+      long kq;
+      const int j = udivmod(q, d.dny1, kq), k = (int)kq;
       double val = v[f];
       if (j >= 1 && j <= d.ny - 1) { val = xv[((long)k * (d.ny - 1) + (j - 1)) * d.nx + i]; bad |= !isfinite(val); }
       vt[f] = val;
@@ -307,9 +353,10 @@ __global__ void __launch_bounds__(kThreads) k_pressure_rhs(DivArgs A) {
   for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < NP; c += (long)gridDim.x * blockDim.x) {
     double rhs = 0.0;
     if (A.fc[c] & kFluid) {
-      const int i = (int)(c % d.nx);
-      const long q = c / d.nx;
-      const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+      long q;
+      const int i = udivmod(c, d.dnx, q);
+      long kq;
+      const int j = udivmod(q, d.dny, kq), k = (int)kq;
       const long fw_ = U3(d, i, j, k), fe = U3(d, i + 1, j, k);
       const long fs = V3(d, i, j, k), fn = V3(d, i, j + 1, k);
       const long fb = W3(d, i, j, k), ft = W3(d, i, j, k + 1);
@@ -338,7 +385,7 @@ struct ProjArgs {
 __device__ __forceinline__ double phi_at(const ProjArgs &A, long c) { return (A.fc[c] & kFluid) ? A.phi[c] : 0.0; }
 
 // q = q~ - (dt/rho) G phi on q-faces, other faces keep q~; p += phi on fluid cells.
-__global__ void __launch_bounds__(kThreads) k_project(ProjArgs A) {
+__global__ void __launch_bounds__(kThreads, 4) k_project(ProjArgs A) {
   const Dims &d = A.d;
   const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
              NW = (long)d.nx * d.ny * (d.nz + 1), NP = (long)d.nx * d.ny * d.nz;
@@ -349,9 +396,10 @@ __global__ void __launch_bounds__(kThreads) k_project(ProjArgs A) {
       const long f = t;
       double val = A.ut[f];
       if (A.fu[f] & kQFace) {
-        const int i = (int)(f % (d.nx + 1));
-        const long q = f / (d.nx + 1);
-        const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+        long q;
+        const int i = udivmod(f, d.dnx1, q);
+        long kq;
+      const int j = udivmod(q, d.dny, kq), k = (int)kq;
         const double pl = i > 0 ? phi_at(A, P3(d, i - 1, j, k)) : 0.0;
         const double pr = i < d.nx ? phi_at(A, P3(d, i, j, k)) : 0.0;
         val = fma(nf, grad_face(A.Gu[f], pl, A.Gu[NU + f], pr), val);
@@ -361,9 +409,10 @@ __global__ void __launch_bounds__(kThreads) k_project(ProjArgs A) {
       const long f = t - NU;
       double val = A.vt[f];
       if (A.fv[f] & kQFace) {
-        const int i = (int)(f % d.nx);
-        const long q = f / d.nx;
-        const int j = (int)(q % (d.ny + 1)), k = (int)(q / (d.ny + 1));
+        long q;
+        const int i = udivmod(f, d.dnx, q);
+        long kq;
+      const int j = udivmod(q, d.dny1, kq), k = (int)kq;
         const double pl = j > 0 ? phi_at(A, P3(d, i, j - 1, k)) : 0.0;
         const double pr = j < d.ny ? phi_at(A, P3(d, i, j, k)) : 0.0;
         val = fma(nf, grad_face(A.Gv[f], pl, A.Gv[NV + f], pr), val);
@@ -462,9 +511,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_diagnostics(DiagArgs A) {
     if (t < NP) {
       const long c = t;
       if (!(A.fc[c] & kFluid)) continue;
-      const int i = (int)(c % d.nx);
-      const long q = c / d.nx;
-      const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+      long q;
+      const int i = udivmod(c, d.dnx, q);
+      long kq;
+      const int j = udivmod(q, d.dny, kq), k = (int)kq;
       const long fw_ = U3(d, i, j, k), fe = U3(d, i + 1, j, k), fs = V3(d, i, j, k), fn = V3(d, i, j + 1, k),
                  fb = W3(d, i, j, k), ft = W3(d, i, j, k + 1);
       double qw, qe, qs, qn, qb, qt;
@@ -531,7 +581,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_diagnostics(DiagArgs A) {
   }
 }
 
-Dims dims_of(const ibm_ctx *c) { return Dims{c->g.nx, c->g.ny, c->g.nz}; }
+Dims dims_of(const ibm_ctx *c) {
+  Dims d;
+  d.nx = c->g.nx; d.ny = c->g.ny; d.nz = c->g.nz;
+  d.dnx = make_idiv(d.nx); d.dnx1 = make_idiv(d.nx + 1); d.dnxm = make_idiv(std::max(1, d.nx - 1));
+  d.dny = make_idiv(d.ny); d.dny1 = make_idiv(d.ny + 1); d.dnym = make_idiv(std::max(1, d.ny - 1));
+  return d;
+}
 
 int blocks_for(long n) {
   long b = (n + kThreads - 1) / kThreads;
@@ -571,9 +627,9 @@ void launch_momentum_rhs(ibm_ctx *c) {
   A.nb[0] = c->g.bu.n; A.nb[1] = c->g.bv.n; A.nb[2] = c->g.bw.n;
   A.a = c->g.rho / c->g.dt;
   A.rho = c->g.rho;
-  A.tdx = {2 * c->g.dx, 1.0 / (2 * c->g.dx)};
-  A.tdy = {2 * c->g.dy, 1.0 / (2 * c->g.dy)};
-  A.tdz = {2 * c->g.dz, 1.0 / (2 * c->g.dz)};
+  A.tdx = make_known_div(2 * c->g.dx);
+  A.tdy = make_known_div(2 * c->g.dy);
+  A.tdz = make_known_div(2 * c->g.dz);
   A.zero_guess = c->prm.use_zero_initial_guess != 0;
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW), nbox = (double)(A.nb[0] + A.nb[1] + A.nb[2]);
   LaunchScope ls(K_RHS, c->st, 8.0 * faces + 9.0 * c->g.NP + nbox * (1 + 16 + 32));
@@ -626,9 +682,10 @@ struct ForceArgs {
 
 __device__ __forceinline__ void cell_force(const ForceArgs &A, long c, double f[3]) {
   const Dims &d = A.d;
-  const int i = (int)(c % d.nx);
-  const long q = c / d.nx;
-  const int j = (int)(q % d.ny), k = (int)(q / d.ny);
+  long q;
+  const int i = udivmod(c, d.dnx, q);
+  long kq;
+      const int j = udivmod(q, d.dny, kq), k = (int)kq;
   const long sy = d.nx, sz = (long)d.nx * d.ny;
   auto solid = [&](int ii, int jj, int kk) {
     return ii >= 0 && ii < d.nx && jj >= 0 && jj < d.ny && kk >= 0 && kk < d.nz &&
