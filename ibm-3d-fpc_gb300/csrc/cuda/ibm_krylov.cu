@@ -1032,6 +1032,13 @@ void Krylov::configure(int nsys_, const KSysHost *hs) {
     maxn = std::max(maxn, hs[s].n);
   }
   nblk = persistent_blocks(maxn, 4);
+  // the FP32 SpMV + dots kernel holds 80 registers (three blocks per SM): a
+  // grid of as many blocks as stay resident runs in one wave
+  {
+    int per_sm = 0;
+    IBM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_arnoldi_spmv32, kThreads, 0));
+    nblk_spmv32 = std::max(1, std::min(nblk, std::max(1, per_sm) * sm_count()));
+  }
   const size_t need_part = (size_t)nblk * (kMaxKdim + 2);
   for (int s = 0; s < nsys; ++s) {
     const KSysHost &h = hs[s];
@@ -1253,7 +1260,7 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
   if (any32) {
     {
       LaunchScope ls(K_GM_SPMV, st, bsp32);
-      k_arnoldi_spmv32<<<grid, kThreads, 0, st>>>(dev);
+      k_arnoldi_spmv32<<<dim3(nblk_spmv32, nsys), kThreads, 0, st>>>(dev);
     }
     {
       LaunchScope ls(K_GM_ORTH, st, bor32);

@@ -99,6 +99,7 @@ class Krylov {
   bool bound_x_zero = false;
   int nsys = 0;
   int nblk = 0;
+  int nblk_spmv32 = 0;
   Slot slot[kMaxSys];
   DBuf<KScal> scal;
   DBuf<KSys> dsys;
