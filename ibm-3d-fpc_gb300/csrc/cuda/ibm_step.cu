@@ -801,7 +801,8 @@ void launch_projection(ibm_ctx *c) {
   D.Gu = c->Gu.p; D.Gv = c->Gv.p; D.Gw = c->Gw.p; D.Dc = c->Dc.p; D.div_bc = c->div_bc_cell.p;
   D.factor = A.factor;
   D.ramp = c->dramp.p;
-  const int nb = std::min(blocks_for(c->g.NP + c->g.NU + c->g.NV + c->g.NW), 1024);
+  // one wave: four resident blocks per SM (launch bounds), at most the 1024 partials of c->part
+  const int nb = std::min(std::min(blocks_for(c->g.NP + c->g.NU + c->g.NV + c->g.NW), 4 * sm_count()), 1024);
   D.part = c->part.p;
   D.dg = c->diag.p;
   D.np_active = c->np_active;
