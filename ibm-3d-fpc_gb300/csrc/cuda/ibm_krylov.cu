@@ -25,6 +25,7 @@ namespace ibm {
 namespace {
 
 constexpr int kLd = kMaxKdim + 2;  // stride of block partials
+constexpr int kChunk32 = 8;  // basis vectors whose dot products a thread keeps in registers
 
 // Flat row -> (i, j, k) of a system's box (invariant-divisor division).
 __device__ __forceinline__ void sys_ijk(long r, const KSys &S, int &i, int &j, int &k) {
@@ -391,6 +392,38 @@ __global__ void __launch_bounds__(kThreads) k_cycle_update(KSys *sys) {
     __shared__ float cf32[kMaxKdim + 1];
     for (int t = threadIdx.x; t < m; t += blockDim.x) cf32[t] = (float)cf[t];
     __syncthreads();
+    if (S.vec4 && m <= kChunk32) {
+      // four consecutive rows per thread: 16-byte loads of the directions,
+      // every load of the thread in flight together; same sums row by row
+      for (long r0 = 4 * ((long)blockIdx.x * blockDim.x + threadIdx.x); r0 < S.n;
+           r0 += 4L * gridDim.x * blockDim.x) {
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int kk = 0; kk < kChunk32; ++kk) {
+          if (kk < m) {
+            const float4 z = *reinterpret_cast<const float4 *>(S.Z + (long)kk * S.ldv + r0);
+            acc.x = fmaf(cf32[kk], z.x, acc.x);
+            acc.y = fmaf(cf32[kk], z.y, acc.y);
+            acc.z = fmaf(cf32[kk], z.z, acc.z);
+            acc.w = fmaf(cf32[kk], z.w, acc.w);
+          }
+        }
+        const double2 x01 = *reinterpret_cast<const double2 *>(S.x + r0);
+        const double2 x23 = *reinterpret_cast<const double2 *>(S.x + r0 + 2);
+        const double xn[4] = {x01.x + (double)acc.x, x01.y + (double)acc.y, x23.x + (double)acc.z,
+                              x23.y + (double)acc.w};
+        *reinterpret_cast<double2 *>(S.x + r0) = make_double2(xn[0], xn[1]);
+        *reinterpret_cast<double2 *>(S.x + r0 + 2) = make_double2(xn[2], xn[3]);
+        if (S.df_resid) {
+          float h[4], l[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) df_split(xn[q], h[q], l[q]);
+          *reinterpret_cast<float4 *>(S.xs + r0) = make_float4(h[0], l[0], h[1], l[1]);
+          *reinterpret_cast<float4 *>(S.xs + r0 + 2) = make_float4(h[2], l[2], h[3], l[3]);
+        }
+      }
+      return;
+    }
     for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
       float acc = 0.0f;
       for (int kk = 0; kk < m; ++kk) acc = fmaf(cf32[kk], S.Z[(long)kk * S.ldv + r], acc);
@@ -547,7 +580,6 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
 // sums are FP32, sums across threads and blocks and every scalar are FP64.
 // A cycle stops once its estimate fell by cyc_rtol; the restart computes the
 // true residual in FP64, so the solve still meets the FP64 tolerance.
-constexpr int kChunk32 = 8;  // basis vectors whose dot products a thread keeps in registers
 
 __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 __device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
