@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-pressure-only", action="store_true", help="skip the 512x96x96 pressure-solve measurement")
     ap.add_argument("--ensemble", type=int, default=32, help="instances of the batched ensemble")
-    ap.add_argument("--mg-coarse-max", type=int, default=640,
+    ap.add_argument("--mg-coarse-max", type=int, default=2560,
                     help="multigrid: largest level solved directly (dense inverse)")
     ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
                     help="mixed form: 1 = FP32 preconditioners in FP64 GMRES, 2 = also FP32 Arnoldi cycles")
@@ -100,7 +100,7 @@ def initial_state(case, seed=2026):
     return u, v, w, p
 
 
-def solver_params(ibm, precision, graph=0, coarse_max=640):
+def solver_params(ibm, precision, graph=0, coarse_max=2560):
     return ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, vel_maxit=250, p_maxit=250, vel_kdim=50, p_kdim=50,
                              p_pc=1, p_pc_rap_type=0, p_pc_relax_type=2, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_omega=1.0,
                              mg_group_ratio=1.5, mg_coarse_max=coarse_max, mg_options=3, precision=precision,

@@ -1096,14 +1096,38 @@ __global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb,
 }
 
 // Coarsest level: x = Ainv b (one warp per row).
+// Coarsest level: x = A^-1 b, one warp per row. FP64 hierarchies accumulate
+// in FP64; FP32 ones in FP32 per lane (n / 32 products each) and FP64 across
+// the warp, so a dense level of a few thousand points does not wait on the
+// FP64 pipe.
 template <class T>
 __global__ void k_dense(const T *Ainv, const T *b, T *x, int n, const int *gate) {
   if (gate_off(gate)) return;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int nw = (gridDim.x * blockDim.x) >> 5;
   for (int r = warp; r < n; r += nw) {
-    double acc = 0.0;
-    for (int c = lane; c < n; c += 32) acc = fma((double)Ainv[(long)r * n + c], (double)b[c], acc);
+    double acc;
+    if constexpr (sizeof(T) == 4) {
+      float a = 0.0f;
+      if (n % 128 == 0) {
+        // 16-byte loads: lane l takes columns 4l .. 4l+3 of every 128
+        const float4 *row = reinterpret_cast<const float4 *>(Ainv + (long)r * n);
+        const float4 *bb = reinterpret_cast<const float4 *>(b);
+        for (int c = lane; c < n / 4; c += 32) {
+          const float4 m = row[c], v = bb[c];
+          a = fmaf(m.x, v.x, a);
+          a = fmaf(m.y, v.y, a);
+          a = fmaf(m.z, v.z, a);
+          a = fmaf(m.w, v.w, a);
+        }
+      } else {
+        for (int c = lane; c < n; c += 32) a = fmaf(Ainv[(long)r * n + c], b[c], a);
+      }
+      acc = (double)a;
+    } else {
+      acc = 0.0;
+      for (int c = lane; c < n; c += 32) acc = fma(Ainv[(long)r * n + c], b[c], acc);
+    }
     acc = warp_sum(acc);
     if (lane == 0) x[r] = (T)acc;
   }
