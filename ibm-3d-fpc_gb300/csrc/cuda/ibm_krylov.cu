@@ -1187,7 +1187,7 @@ void Krylov::launch_cycle_end(cudaStream_t st, const Precond &pc, const KFlags *
   }
   {
     LaunchScope ls(K_GM_UPDATE, st, bu);
-    k_cycle_update<<<gridu, kThreads, 0, st>>>(dev);
+    k_cycle_update<<<wave(k_cycle_update), kThreads, 0, st>>>(dev);
   }
   bool cb = false;
   for (int s = 0; s < nsys; ++s) {
@@ -1201,10 +1201,10 @@ void Krylov::launch_cycle_end(cudaStream_t st, const Precond &pc, const KFlags *
   }
   if (cb) {
     LaunchScope ls(K_GM_ADDZ, st, ba);
-    k_add_z<<<gridu, kThreads, 0, st>>>(dev);
+    k_add_z<<<wave(k_add_z), kThreads, 0, st>>>(dev);
   }
   LaunchScope ls(K_GM_RESID, st, br);
-  k_cycle_residual<<<grid, kThreads, 0, st>>>(dev);
+  k_cycle_residual<<<wave(k_cycle_residual), kThreads, 0, st>>>(dev);
 }
 
 void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl, unsigned mask) {
@@ -1260,7 +1260,7 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
   if (inner_sweeps > 0) {
     if (inner_sweeps == 2) {
       LaunchScope ls(K_GM_JAC32, st, j32two);
-      k_jacobi32_two<<<gridu, kThreads, 0, st>>>(dev);
+      k_jacobi32_two<<<wave(k_jacobi32_two), kThreads, 0, st>>>(dev);
     } else if (inner_sweeps == 1) {
       LaunchScope ls(K_GM_JAC32, st, 16.0 * r32);
       k_jacobi32_first<<<gridu, kThreads, 0, st>>>(dev, 1);
@@ -1280,27 +1280,37 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
   if (any64) {
     {
       LaunchScope ls(K_GM_SPMV, st, bsp);
-      k_arnoldi_spmv<<<grid, kThreads, 0, st>>>(dev);
+      k_arnoldi_spmv<<<wave(k_arnoldi_spmv), kThreads, 0, st>>>(dev);
     }
     {
       LaunchScope ls(K_GM_ORTH, st, bor);
-      k_arnoldi_orth<<<grid, kThreads, 0, st>>>(dev);
+      k_arnoldi_orth<<<wave(k_arnoldi_orth), kThreads, 0, st>>>(dev);
     }
     LaunchScope ls(K_GM_NEXT, st, bor);
-    k_arnoldi_next<<<grid, kThreads, 0, st>>>(dev);
+    k_arnoldi_next<<<wave(k_arnoldi_next), kThreads, 0, st>>>(dev);
   }
   if (any32) {
     {
       LaunchScope ls(K_GM_SPMV, st, bsp32);
-      k_arnoldi_spmv32<<<dim3(nblk_spmv32, nsys), kThreads, 0, st>>>(dev);
+      k_arnoldi_spmv32<<<wave(k_arnoldi_spmv32), kThreads, 0, st>>>(dev);
     }
     {
       LaunchScope ls(K_GM_ORTH, st, bor32);
-      k_arnoldi_orth32<<<grid, kThreads, 0, st>>>(dev);
+      k_arnoldi_orth32<<<wave(k_arnoldi_orth32), kThreads, 0, st>>>(dev);
     }
     LaunchScope ls(K_GM_NEXT, st, bor32);
-    k_arnoldi_next32<<<grid, kThreads, 0, st>>>(dev);
+    k_arnoldi_next32<<<wave(k_arnoldi_next32), kThreads, 0, st>>>(dev);
   }
+}
+
+// Grid of a grid-stride Krylov kernel: (x, nsys) with x such that all blocks
+// stay resident (one wave), at most nblk (the size of the partials).
+template <class K>
+dim3 Krylov::wave(K kernel) const {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+  const int x = std::max(1, std::min(nblk, std::max(1, per_sm) * sm_count() / std::max(1, nsys)));
+  return dim3(x, nsys);
 }
 
 void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, const Precond &pc,
@@ -1312,7 +1322,7 @@ void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, co
     if ((mask >> s) & 1u) init_bytes += (x_zero ? 16.0 : slot[s].host.cls ? 26.0 : 80.0) * slot[s].host.n;
   {
     LaunchScope ls(K_GM_INIT, st, init_bytes);
-    k_init<<<grid, kThreads, 0, st>>>(dsys.p, nsys);
+    k_init<<<wave(k_init), kThreads, 0, st>>>(dsys.p, nsys);
   }
   for (long guard = 0;; ++guard) {
     if (guard > 4L * 1000 * 1000) throw Error(IBM_ERR_CUDA, "GMRES host loop did not terminate");
@@ -1387,7 +1397,7 @@ Krylov::GraphCounts Krylov::enqueue_graph(cudaStream_t st, const cudaStream_t bo
   const unsigned mask = bound_mask;
   {
     LaunchScope ls(K_GM_INIT, st, 0.0);
-    k_init<<<grid, kThreads, 0, st>>>(dev, nsys);
+    k_init<<<wave(k_init), kThreads, 0, st>>>(dev, nsys);
   }
   cudaGraphConditionalHandle hw;
   IBM_CUDA_TRY(cudaGraphConditionalHandleCreate(&hw, capture_graph_of(st), 0, 0));

@@ -90,6 +90,8 @@ class Krylov {
     DBuf<float2> xs;  // double-float copy of x for the double-float residual
   };
   void read_flags(cudaStream_t st);
+  template <class K>
+  dim3 wave(K kernel) const;
   // Launch sequences shared by the host-driven and the graph form. With
   // flags == nullptr every launch is recorded (each kernel is gated on the
   // device flags of its system); otherwise only what the flags require.

@@ -595,6 +595,16 @@ int blocks_for(long n) {
   return (int)std::max(1L, std::min(b, cap));
 }
 
+// The same, capped at the blocks that stay resident (one wave of the
+// grid-stride loop).
+template <class K>
+int wave_blocks(K kernel, long n) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0);
+  const long b = (n + kThreads - 1) / kThreads;
+  return (int)std::max(1L, std::min(b, (long)std::max(1, per_sm) * sm_count()));
+}
+
 }  // namespace
 
 // Algorithmic bytes of each launch count every array element the kernel must
@@ -633,7 +643,7 @@ void launch_momentum_rhs(ibm_ctx *c) {
   A.zero_guess = c->prm.use_zero_initial_guess != 0;
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW), nbox = (double)(A.nb[0] + A.nb[1] + A.nb[2]);
   LaunchScope ls(K_RHS, c->st, 8.0 * faces + 9.0 * c->g.NP + nbox * (1 + 16 + 32));
-  k_momentum_rhs<<<blocks_for(A.nb[0] + A.nb[1] + A.nb[2]), kThreads, 0, c->st>>>(A);
+  k_momentum_rhs<<<wave_blocks(k_momentum_rhs, A.nb[0] + A.nb[1] + A.nb[2]), kThreads, 0, c->st>>>(A);
 }
 
 void launch_tilde(ibm_ctx *c) {
@@ -641,7 +651,7 @@ void launch_tilde(ibm_ctx *c) {
   {
     const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
     LaunchScope ls(K_SCATTER, c->st, 16.0 * faces + 8.0 * (c->g.bu.n + c->g.bv.n + c->g.bw.n));
-    k_scatter<<<blocks_for(c->g.NU + c->g.NV + c->g.NW), kThreads, 0, c->st>>>(
+    k_scatter<<<wave_blocks(k_scatter, c->g.NU + c->g.NV + c->g.NW), kThreads, 0, c->st>>>(
         c->u.p, c->v.p, c->w.p, c->xb[0].p, c->xb[1].p, c->xb[2].p, c->ut.p, c->vt.p, c->wt.p, d, c->diag.p);
   }
   launch_bc(c, c->ut.p, c->vt.p, c->wt.p);
@@ -658,7 +668,7 @@ void launch_pressure_rhs(ibm_ctx *c) {
   A.ramp = c->dramp.p;
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
   LaunchScope ls(K_PRHS, c->st, 9.0 * faces + 73.0 * c->g.NP);
-  k_pressure_rhs<<<blocks_for(c->g.NP), kThreads, 0, c->st>>>(A);
+  k_pressure_rhs<<<wave_blocks(k_pressure_rhs, c->g.NP), kThreads, 0, c->st>>>(A);
 }
 
 // ------------------------------------------------------------------ forces
@@ -790,7 +800,7 @@ void launch_projection(ibm_ctx *c) {
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
   {
     LaunchScope ls(K_PROJECT, c->st, 33.0 * faces + 25.0 * c->g.NP);
-    k_project<<<blocks_for(c->g.NU + c->g.NV + c->g.NW + c->g.NP), kThreads, 0, c->st>>>(A);
+    k_project<<<wave_blocks(k_project, c->g.NU + c->g.NV + c->g.NW + c->g.NP), kThreads, 0, c->st>>>(A);
   }
   launch_bc(c, c->u.p, c->v.p, c->w.p);
   DiagArgs D;
