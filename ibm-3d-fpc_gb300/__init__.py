@@ -221,6 +221,93 @@ class Solver:
         self._check(self._lib.ibm_profile_get(self._ctx, C.byref(p)))
         return p
 
+    # ---------------------------------------------------------- adjoint extension
+    def adjoint_setup(self) -> None:
+        """Transposed-operator context and inlet weights (ibm_adjoint_setup)."""
+        beta = np.ascontiguousarray(self.case.array("beta_p"), dtype=np.float64)
+        self._check(self._lib.ibm_adjoint_setup(self._ctx, _ptr(beta)))
+
+    def set_inflow(self, g) -> None:
+        """Inflow profile g[ny*nz] (ibm_set_inflow; needs adjoint_setup)."""
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        self._check(self._lib.ibm_set_inflow(self._ctx, _ptr(g)))
+
+    def step_forward(self, ramp: float) -> StepStats:
+        st = StepStats()
+        self._check(self._lib.ibm_step_forward(self._ctx, C.c_double(ramp), C.byref(st)))
+        return st
+
+    def step_backward(self, ramp: float, weight: float = 0.0) -> StepStats:
+        st = StepStats()
+        self._check(self._lib.ibm_step_backward(self._ctx, C.c_double(ramp), C.c_double(weight), C.byref(st)))
+        return st
+
+    def adjoint_reset(self) -> None:
+        self._check(self._lib.ibm_adjoint_reset(self._ctx))
+
+    def adjoint_set(self, lu=None, lv=None, lw=None, lp=None) -> None:
+        arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (lu, lv, lw, lp)]
+        self._check(self._lib.ibm_adjoint_set(self._ctx, *[None if x is None else _ptr(x) for x in arrs]))
+
+    def adjoint_get(self):
+        """(lambda_u, lambda_v, lambda_w, lambda_p, dJ/dg, dJ/dnu)."""
+        nx, ny, nz = self.case.shape
+        out = [np.empty((nx + 1) * ny * nz), np.empty(nx * (ny + 1) * nz), np.empty(nx * ny * (nz + 1)),
+               np.empty(nx * ny * nz), np.empty(ny * nz), np.empty(1)]
+        self._check(self._lib.ibm_adjoint_get(self._ctx, *[_ptr(x) for x in out]))
+        return out[0], out[1], out[2], out[3], out[4], float(out[5][0])
+
+    def tape_depth(self) -> int:
+        return self._check(self._lib.ibm_adjoint_tape_depth(self._ctx))
+
+    def checkpoint_save(self, slot: int) -> None:
+        self._check(self._lib.ibm_checkpoint_save(self._ctx, slot))
+
+    def checkpoint_load(self, slot: int) -> None:
+        self._check(self._lib.ibm_checkpoint_load(self._ctx, slot))
+
+    def checkpoint_clear(self) -> None:
+        self._check(self._lib.ibm_checkpoint_clear(self._ctx))
+
+    def drag_gradient(self, ramps, window, checkpoint_every: int = 20):
+        """Mean end-of-step drag over the steps in ``window`` (1-based step
+        numbers) of len(ramps) steps from the current fields, and its gradient
+        with respect to the inflow profile and nu: (J, dJ/dg, dJ/dnu).
+
+        Checkpointing with recomputation: the forward sweep saves the state
+        every ``checkpoint_every`` steps; the reverse sweep replays each
+        segment from its checkpoint with ibm_step_forward (the tape holds one
+        segment) and runs ibm_step_backward over it in reverse. The fields
+        are left at the state after the last step."""
+        window = set(window)
+        n = len(ramps)
+        w = 1.0 / len(window)
+        p = self.params
+        if not p.compute_forces:
+            p.compute_forces = 1
+            self.set_params(p)
+        self.adjoint_reset()
+        self.checkpoint_clear()
+        J = 0.0
+        for k in range(1, n + 1):
+            if (k - 1) % checkpoint_every == 0:
+                self.checkpoint_save((k - 1) // checkpoint_every)
+            st = self.step(ramps[k - 1])
+            if k in window:
+                J += w * st.force[0]
+        end = self.fields()
+        for seg in range((n - 1) // checkpoint_every, -1, -1):
+            first = seg * checkpoint_every + 1
+            last = min(n, first + checkpoint_every - 1)
+            self.checkpoint_load(seg)
+            for k in range(first, last + 1):
+                self.step_forward(ramps[k - 1])
+            for k in range(last, first - 1, -1):
+                self.step_backward(ramps[k - 1], w if k in window else 0.0)
+        self.set_fields(*end)
+        *_, dg, dnu = self.adjoint_get()
+        return J, dg, dnu
+
     def run(self, nsteps: int, ramp_steps: int = 200, start: int = 1, callback=None):
         """The reference's step loop (main.cu:249-251): ramp = min(1, step/ramp_steps)."""
         out = []

@@ -149,5 +149,16 @@ def gpu() -> C.CDLL:
         lib.ibm_kernel_launches.argtypes = [vp]
         lib.ibm_kernel_launches.restype = C.c_longlong
         lib.ibm_device_query.argtypes = [i, C.c_char_p, i]
+        lib.ibm_adjoint_setup.argtypes = [vp, vp]
+        lib.ibm_set_inflow.argtypes = [vp, vp]
+        lib.ibm_step_forward.argtypes = [vp, d, P(StepStats)]
+        lib.ibm_step_backward.argtypes = [vp, d, d, P(StepStats)]
+        lib.ibm_adjoint_reset.argtypes = [vp]
+        lib.ibm_adjoint_set.argtypes = [vp, vp, vp, vp, vp]
+        lib.ibm_adjoint_get.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        lib.ibm_adjoint_tape_depth.argtypes = [vp]
+        lib.ibm_checkpoint_save.argtypes = [vp, i]
+        lib.ibm_checkpoint_load.argtypes = [vp, i]
+        lib.ibm_checkpoint_clear.argtypes = [vp]
         _gpu = lib
     return _gpu

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "ibm_adjoint.cuh"
 #include "ibm_ctx.cuh"
 #include "ibm_step.cuh"
 
@@ -502,6 +503,11 @@ void ibm_destroy(ibm_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->adj) {
+    if (c->adj->t) ibm_destroy(c->adj->t);
+    delete c->adj;
+    c->adj = nullptr;
+  }
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
   if (c->hdiag) cudaFreeHost(c->hdiag);
@@ -1168,6 +1174,260 @@ int ibm_device_query(int device, char *buf, int len) {
   if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return IBM_ERR_CUDA;
   if (buf && len > 0) snprintf(buf, (size_t)len, "%s sm_%d%d SMs=%d", p.name, p.major, p.minor, p.multiProcessorCount);
   return IBM_OK;
+}
+
+// ---------------------------------------------------------------- adjoint extension
+namespace {
+
+ibm::AdjState &adj_of(ibm_ctx *c) {
+  if (!c->adj || !c->adj->t) throw Error(IBM_ERR_STATE, "call ibm_adjoint_setup first");
+  return *c->adj;
+}
+
+std::array<DBuf<double>, 4> snapshot(ibm_ctx *c) {
+  std::array<DBuf<double>, 4> s;
+  const double *src[4] = {c->u.p, c->v.p, c->w.p, c->p.p};
+  const long n[4] = {c->g.NU, c->g.NV, c->g.NW, c->g.NP};
+  for (int q = 0; q < 4; ++q) {
+    s[q].alloc(n[q]);
+    IBM_CUDA_TRY(cudaMemcpyAsync(s[q].p, src[q], sizeof(double) * n[q], cudaMemcpyDeviceToDevice, c->st));
+  }
+  return s;
+}
+
+void restore(ibm_ctx *c, const std::array<DBuf<double>, 4> &s) {
+  double *dst[4] = {c->u.p, c->v.p, c->w.p, c->p.p};
+  for (int q = 0; q < 4; ++q)
+    IBM_CUDA_TRY(cudaMemcpyAsync(dst[q], s[q].p, sizeof(double) * s[q].n, cudaMemcpyDeviceToDevice, c->st));
+}
+
+// x = A^-T b on the transposed-operator context t (device vectors, zero
+// initial guess). The caller's stream must have produced b already.
+KResult transposed_solve(ibm_ctx *t, int field, const double *b, double *x) {
+  Scope sc(t);
+  ensure_solvers(t);
+  const long n = field_box(t, field).n;
+  IBM_CUDA_TRY(cudaMemcpyAsync(t->bb[field].p, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, t->st));
+  IBM_CUDA_TRY(cudaMemsetAsync(t->xb[field].p, 0, sizeof(double) * n, t->st));
+  KResult r[3];
+  if (field < 3) {
+    const double *bm[3] = {t->bb[0].p, t->bb[1].p, t->bb[2].p};
+    double *xm[3] = {t->xb[0].p, t->xb[1].p, t->xb[2].p};
+    Precond none;
+    t->kmom.solve(t->st, bm, xm, none, r, 1u << field, true);
+    r[0] = r[field];
+  } else {
+    const double *bp[1] = {t->bb[3].p};
+    double *xp[1] = {t->xb[3].p};
+    Precond mgp;
+    mgp.ctx = t;
+    mgp.apply = mg_apply_cb;
+    t->kp.solve(t->st, bp, xp, mgp, r, ~0u, true);
+  }
+  t->graph_bound = false;
+  IBM_CUDA_TRY(cudaMemcpyAsync(x, t->xb[field].p, sizeof(double) * n, cudaMemcpyDeviceToDevice, t->st));
+  IBM_CUDA_TRY(cudaStreamSynchronize(t->st));
+  t->prof.drain();
+  return r[0];
+}
+
+void sync_transposed_params(ibm_ctx *c) {
+  ibm_ctx *t = c->adj->t;
+  ibm_solver_params p = c->prm;
+  p.use_graph = 0;
+  p.compute_forces = 0;
+  if (memcmp(&p, &t->prm, sizeof(p)) != 0) {
+    const int rc = ibm_set_solver_params(t, &p);
+    if (rc < 0) throw Error(rc, "transposed context: " + t->err);
+  }
+}
+
+}  // namespace
+
+int ibm_adjoint_setup(ibm_ctx *c, const double *beta_p) {
+  return guarded(c, [&]() {
+    if (!beta_p) throw Error(IBM_ERR_ARG, "ibm_adjoint_setup: null beta_p");
+    require_inputs(c);
+    if (!c->adj) c->adj = new ibm::AdjState();
+    ibm::AdjState &a = *c->adj;
+    if (a.t) { ibm_destroy(a.t); a.t = nullptr; }
+    int rc = ibm_create(&c->grid, &a.t);
+    if (rc < 0) throw Error(rc, "transposed context: " + g_create_error);
+    for (int f = 0; f < 4; ++f) {
+      const Box &b = field_box(c, f);
+      DBuf<double> rows;
+      rows.alloc((size_t)7 * b.n);
+      launch_transpose7(c->st, c->op[f].c.p, b, rows.p);
+      IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+      rc = ibm_set_operator(a.t, f, rows.p, b.nx, b.ny, b.nz);
+      if (rc < 0) throw Error(rc, "transposed context: " + a.t->err);
+    }
+    sync_transposed_params(c);
+    const Geometry &g = c->g;
+    const auto beta = to_host(beta_p, (size_t)g.NP);
+    const auto fc = to_host(c->fc.p, (size_t)g.NP);
+    const int nyz = g.ny * g.nz;
+    std::vector<double> bdx(nyz, 0.0), winl(nyz, 0.0);
+    for (int t = 0; t < nyz; ++t) {
+      const long cell = (long)t * g.nx;
+      if (fc[cell] & kFluid) {
+        bdx[t] = beta[cell] * g.dx;
+        winl[t] = 1.0 / bdx[t];
+      }
+    }
+    upload(a.bdx, bdx, c->st);
+    upload(a.winl, winl, c->st);
+    a.lu.alloc(g.NU); a.lv.alloc(g.NV); a.lw.alloc(g.NW); a.lp.alloc(g.NP);
+    a.cu.alloc(g.NU); a.cv.alloc(g.NV); a.cw.alloc(g.NW);
+    a.gu.alloc(g.NU); a.gv.alloc(g.NV); a.gw.alloc(g.NW);
+    a.u1.alloc(g.NU); a.v1.alloc(g.NV); a.w1.alloc(g.NW);
+    for (int f = 0; f < 3; ++f) { a.lx[f].alloc(field_box(c, f).n); a.lb[f].alloc(field_box(c, f).n); }
+    a.rphi.alloc(g.NP); a.mu.alloc(g.NP);
+    a.dg.alloc(nyz); a.acc.alloc(1);
+    a.lu.zero(c->st); a.lv.zero(c->st); a.lw.zero(c->st); a.lp.zero(c->st);
+    a.dg.zero(c->st); a.acc.zero(c->st);
+    a.tape.clear();
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_set_inflow(ibm_ctx *c, const double *g) {
+  return guarded(c, [&]() {
+    ibm::AdjState &a = adj_of(c);
+    if (!g) throw Error(IBM_ERR_ARG, "ibm_set_inflow: null profile");
+    const size_t nyz = (size_t)c->g.ny * c->g.nz;
+    DBuf<double> dg;
+    dg.alloc(nyz);
+    IBM_CUDA_TRY(cudaMemcpyAsync(dg.p, g, sizeof(double) * nyz, cudaMemcpyDefault, c->st));
+    (void)a;
+    adj_set_inflow(c, dg.p);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_step_forward(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
+  return guarded(c, [&]() {
+    ibm::AdjState &a = adj_of(c);
+    require_inputs(c);
+    a.tape.push_back(snapshot(c));
+    step_launch(c, ramp);
+    return step_collect(c, ramp, stats);
+  });
+}
+
+int ibm_step_backward(ibm_ctx *c, double ramp, double weight, ibm_step_stats *stats) {
+  return guarded(c, [&]() {
+    ibm::AdjState &a = adj_of(c);
+    if (a.tape.empty()) throw Error(IBM_ERR_STATE, "ibm_step_backward: no step on the tape (ibm_step_forward)");
+    sync_transposed_params(c);
+    std::array<DBuf<double>, 4> s0 = std::move(a.tape.back());
+    a.tape.pop_back();
+    // recompute the step from its start state: the momentum right-hand sides
+    // and solutions stay in bb / xb, the end-of-step fields in u, v, w, p
+    restore(c, s0);
+    step_launch(c, ramp);
+    int rc = step_collect(c, ramp, stats);
+    if (rc < 0) return rc;
+    // post-BC start velocities: the convection's linearisation point
+    IBM_CUDA_TRY(cudaMemcpyAsync(a.u1.p, s0[0].p, sizeof(double) * c->g.NU, cudaMemcpyDeviceToDevice, c->st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(a.v1.p, s0[1].p, sizeof(double) * c->g.NV, cudaMemcpyDeviceToDevice, c->st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(a.w1.p, s0[2].p, sizeof(double) * c->g.NW, cudaMemcpyDeviceToDevice, c->st));
+    launch_bc(c, a.u1.p, a.v1.p, a.w1.p);
+    // reverse sweep
+    if (weight != 0.0) adj_force(c, weight);
+    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+    adj_projection(c);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    KResult r = transposed_solve(a.t, 3, a.rphi.p, a.mu.p);
+    int worst_rc = solve_status(r);
+    if (r.nonfinite) throw Error(IBM_ERR_NONFINITE, "non-finite transposed pressure solve");
+    adj_divergence(c, ramp);
+    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+    adj_scatter(c);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    for (int f = 0; f < 3; ++f) {
+      r = transposed_solve(a.t, f, a.lx[f].p, a.lb[f].p);
+      worst_rc = worst(worst_rc, solve_status(r));
+      if (r.nonfinite) throw Error(IBM_ERR_NONFINITE, "non-finite transposed momentum solve");
+    }
+    adj_momentum(c);
+    adj_gradient(c);
+    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    IBM_CUDA_TRY(cudaGetLastError());
+    c->prof.drain();
+    return worst(rc, worst_rc);
+  });
+}
+
+int ibm_adjoint_reset(ibm_ctx *c) {
+  return guarded(c, [&]() {
+    ibm::AdjState &a = adj_of(c);
+    a.lu.zero(c->st); a.lv.zero(c->st); a.lw.zero(c->st); a.lp.zero(c->st);
+    a.dg.zero(c->st); a.acc.zero(c->st);
+    a.tape.clear();
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_adjoint_set(ibm_ctx *c, const double *lu, const double *lv, const double *lw, const double *lp) {
+  return guarded(c, [&]() {
+    ibm::AdjState &a = adj_of(c);
+    const double *src[4] = {lu, lv, lw, lp};
+    DBuf<double> *dst[4] = {&a.lu, &a.lv, &a.lw, &a.lp};
+    for (int q = 0; q < 4; ++q) {
+      if (src[q]) IBM_CUDA_TRY(cudaMemcpyAsync(dst[q]->p, src[q], sizeof(double) * dst[q]->n, cudaMemcpyDefault, c->st));
+      else dst[q]->zero(c->st);
+    }
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_adjoint_get(ibm_ctx *c, double *lu, double *lv, double *lw, double *lp, double *dg, double *dnu) {
+  return guarded(c, [&]() {
+    ibm::AdjState &a = adj_of(c);
+    double *dst[6] = {lu, lv, lw, lp, dg, dnu};
+    const DBuf<double> *src[6] = {&a.lu, &a.lv, &a.lw, &a.lp, &a.dg, &a.acc};
+    for (int q = 0; q < 6; ++q)
+      if (dst[q]) IBM_CUDA_TRY(cudaMemcpyAsync(dst[q], src[q]->p, sizeof(double) * src[q]->n, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_adjoint_tape_depth(ibm_ctx *c) {
+  return guarded(c, [&]() { return (int)adj_of(c).tape.size(); });
+}
+
+int ibm_checkpoint_save(ibm_ctx *c, int slot) {
+  return guarded(c, [&]() {
+    ibm::AdjState &a = adj_of(c);
+    a.ckpt[slot] = snapshot(c);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_checkpoint_load(ibm_ctx *c, int slot) {
+  return guarded(c, [&]() {
+    ibm::AdjState &a = adj_of(c);
+    auto it = a.ckpt.find(slot);
+    if (it == a.ckpt.end()) throw Error(IBM_ERR_ARG, "ibm_checkpoint_load: no checkpoint in slot " + std::to_string(slot));
+    restore(c, it->second);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_checkpoint_clear(ibm_ctx *c) {
+  return guarded(c, [&]() {
+    adj_of(c).ckpt.clear();
+    return IBM_OK;
+  });
 }
 
 }  // extern "C"

@@ -31,6 +31,8 @@ struct Geometry {
   double dx, dy, dz, rho, nu, dt;
 };
 
+struct AdjState;  // adjoint extension (ibm_adjoint.cuh)
+
 }  // namespace ibm
 
 struct ibm_ctx {
@@ -87,4 +89,6 @@ struct ibm_ctx {
   unsigned long long *hloops = nullptr;  // pinned copy
   long long graph_fixed_launches = 0;
   long long graph_body_launches[4] = {0, 0, 0, 0};
+  // Adjoint extension: transposed-operator context, lambdas, tape, checkpoints.
+  ibm::AdjState *adj = nullptr;
 };

@@ -234,6 +234,51 @@ ibm_ctx *ibm_batch_ctx(ibm_batch *b, int i);
  * ibm_last_error(ibm_batch_ctx(b, i)). */
 int ibm_batch_step(ibm_batch *b, const double *ramps, ibm_step_stats *stats);
 
+/* Adjoint extension (the reference has none; its inputs are the ones
+ * main.cu:249-376 steps with). The step is s1 = step(s0; g, nu), with
+ *  - g[ny*nz] the inflow profile (y fastest): u at the inlet = ramp g in
+ *    every BC cleanup (main.cu:250-251) and the inlet column's divergence
+ *    lift div_bc = -g / (beta dx) (immersed_operators.hpp:223-228); the
+ *    implicit-diffusion lift rhs_u_bc keeps the reference's unit base
+ *    profile, as the reference builds it (immersed_operators.hpp:26);
+ *  - nu the viscosity, on which the momentum operators, their row scales and
+ *    rhs_u_bc depend (immersed_operators.hpp:1-177, main.cu:98-100).
+ * The objective is a weighted sum over steps of the x force (drag) that
+ * ibm_step_stats.force reports. ibm_step_backward maps the lambda of a
+ * step's end-of-step fields (held in the context) to the lambda of its
+ * step-start fields and accumulates dJ/dg and dJ/dnu; the transposed solves
+ * (A^T y = c for the three momentum operators and the pressure operator)
+ * run on a second context built on the transposed stencils, with the
+ * solver parameters of this one. */
+/* Builds the transposed-operator context and the inlet weights from beta_p
+ * (cell open fractions, nx*ny*nz); clears lambdas, gradients and the tape.
+ * Requires every input of ibm_step; call again after changing an operator. */
+int ibm_adjoint_setup(ibm_ctx *ctx, const double *beta_p);
+/* Sets the inflow profile g (host or device pointer): the inlet values and
+ * the inlet column's divergence lift, computed as the setup computes them
+ * (bitwise the setup's arrays when g is its uin). */
+int ibm_set_inflow(ibm_ctx *ctx, const double *g);
+/* ibm_step that first pushes the step-start fields onto the context's tape
+ * (device memory, one state per step). */
+int ibm_step_forward(ibm_ctx *ctx, double ramp, ibm_step_stats *stats);
+/* Pops the last step-start state, recomputes that step from it (the context
+ * then holds its end-of-step fields; stats are the recomputed step's), adds
+ * weight * dF_x/d(end-of-step fields) to the lambdas, and runs the reverse
+ * sweep. `ramp` must be the step's own. */
+int ibm_step_backward(ibm_ctx *ctx, double ramp, double weight, ibm_step_stats *stats);
+/* Lambdas, dJ/dg and dJ/dnu to zero; tape emptied. */
+int ibm_adjoint_reset(ibm_ctx *ctx);
+/* Lambdas of the state (full MAC arrays and cells; NULL = zero). */
+int ibm_adjoint_set(ibm_ctx *ctx, const double *lu, const double *lv, const double *lw, const double *lp);
+/* Lambdas, dJ/dg[ny*nz] and dJ/dnu[1]; any pointer may be NULL. */
+int ibm_adjoint_get(ibm_ctx *ctx, double *lu, double *lv, double *lw, double *lp, double *dg, double *dnu);
+int ibm_adjoint_tape_depth(ibm_ctx *ctx);
+/* Checkpoints of the state fields in device memory, by slot number, for
+ * checkpointing with recomputation across many steps. */
+int ibm_checkpoint_save(ibm_ctx *ctx, int slot);
+int ibm_checkpoint_load(ibm_ctx *ctx, int slot);
+int ibm_checkpoint_clear(ibm_ctx *ctx);
+
 int ibm_synchronize(ibm_ctx *ctx);
 void *ibm_stream(ibm_ctx *ctx);            /* the context's cudaStream_t */
 long long ibm_kernel_launches(ibm_ctx *ctx); /* kernels this context has launched */

@@ -1085,3 +1085,329 @@ done:
   free(uin); free(bu); free(bv); free(bw); free(bp); free(xu); free(xv); free(xw); free(xp);
   return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* adjoint of one step (the adjoint extension; the reference has none)      */
+/* ------------------------------------------------------------------------ */
+
+static int u_in(const oracle *o, int i, int j, int k) {
+  return !(i < 0 || i > o->nx || j < 0 || j >= o->ny || k < 0 || k >= o->nz);
+}
+static int v_in(const oracle *o, int i, int j, int k) {
+  return !(i < 0 || i >= o->nx || j < 0 || j > o->ny || k < 0 || k >= o->nz);
+}
+static int w_in(const oracle *o, int i, int j, int k) {
+  return !(i < 0 || i >= o->nx || j < 0 || j >= o->ny || k < 0 || k > o->nz);
+}
+
+/* Adjoint of oracle_bc_cleanup with inlet values ramp * g, in reverse order:
+ * the lambdas of the faces the cleanup overwrites become 0, the outlet copy
+ * u[nx] = u[nx-1] hands its lambda to u[nx-1], and the inlet lambdas times
+ * ramp accumulate into dg[j + ny k]. */
+static void bc_adjoint(const oracle *o, double *lu, double *lv, double *lw, double ramp, double *dg) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  for (int k = 1; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        if (!o->in.active_w[W3(o, i, j, k - 1)]) lw[W3(o, i, j, k)] = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 1; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        if (!o->in.active_v[V3(o, i, j, k)]) lv[V3(o, i, j, k)] = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 1; i < nx; ++i)
+        if (!o->in.active_u[U3(o, i, j, k)]) lu[U3(o, i, j, k)] = 0.0;
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) { lw[W3(o, i, j, 0)] = 0.0; lw[W3(o, i, j, nz)] = 0.0; }
+  for (int k = 0; k < nz; ++k)
+    for (int i = 0; i < nx; ++i) { lv[V3(o, i, 0, k)] = 0.0; lv[V3(o, i, ny, k)] = 0.0; }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j) {
+      lu[U3(o, nx - 1, j, k)] += lu[U3(o, nx, j, k)];
+      lu[U3(o, nx, j, k)] = 0.0;
+      if (dg) dg[j + (long)ny * k] += ramp * lu[U3(o, 0, j, k)];
+      lu[U3(o, 0, j, k)] = 0.0;
+    }
+}
+
+/* Scatter helpers of the convection adjoint: add to a neighbour when it lies
+ * inside its array, else to the centre (the forward's fallback) or nowhere
+ * (the averages' zero fallback). */
+static void add_u(const oracle *o, double *lu, int i, int j, int k, double g, long fb) {
+  if (u_in(o, i, j, k)) lu[U3(o, i, j, k)] += g; else if (fb >= 0) lu[fb] += g;
+}
+static void add_v(const oracle *o, double *lv, int i, int j, int k, double g, long fb) {
+  if (v_in(o, i, j, k)) lv[V3(o, i, j, k)] += g; else if (fb >= 0) lv[fb] += g;
+}
+static void add_w(const oracle *o, double *lw, int i, int j, int k, double g, long fb) {
+  if (w_in(o, i, j, k)) lw[W3(o, i, j, k)] += g; else if (fb >= 0) lw[fb] += g;
+}
+
+/* lambda += J^T lc for the centred advective form of oracle_convection,
+ * linearised at (u, v, w); lc is zero where no convection is computed. */
+static void conv_adjoint(const oracle *o, const double *u, const double *v, const double *w, const double *lcu,
+                         const double *lcv, const double *lcw, double *lu, double *lv, double *lw) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const double tdx = 2 * o->dx, tdy = 2 * o->dy, tdz = 2 * o->dz;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 1; i < nx; ++i) {
+        const long f = U3(o, i, j, k);
+        const double g = lcu[f];
+        if (g == 0.0) continue;
+        const double uc = u[f];
+        const double va = 0.25 * (vval(o, v, i - 1, j, k, 0.0) + vval(o, v, i - 1, j + 1, k, 0.0) +
+                                  vval(o, v, i, j, k, 0.0) + vval(o, v, i, j + 1, k, 0.0));
+        const double wa = 0.25 * (wval(o, w, i - 1, j, k, 0.0) + wval(o, w, i - 1, j, k + 1, 0.0) +
+                                  wval(o, w, i, j, k, 0.0) + wval(o, w, i, j, k + 1, 0.0));
+        const double ue = uval(o, u, i + 1, j, k, uc), uw = uval(o, u, i - 1, j, k, uc);
+        const double un = uval(o, u, i, j + 1, k, uc), us = uval(o, u, i, j - 1, k, uc);
+        const double ut = uval(o, u, i, j, k + 1, uc), ub = uval(o, u, i, j, k - 1, uc);
+        const double gx = g / tdx, gy = g / tdy, gz = g / tdz;
+        lu[f] += gx * (ue - uw);
+        add_u(o, lu, i + 1, j, k, gx * uc, f); add_u(o, lu, i - 1, j, k, -gx * uc, f);
+        add_u(o, lu, i, j + 1, k, gy * va, f); add_u(o, lu, i, j - 1, k, -gy * va, f);
+        add_u(o, lu, i, j, k + 1, gz * wa, f); add_u(o, lu, i, j, k - 1, -gz * wa, f);
+        const double cv = 0.25 * gy * (un - us), cw = 0.25 * gz * (ut - ub);
+        add_v(o, lv, i - 1, j, k, cv, -1); add_v(o, lv, i - 1, j + 1, k, cv, -1);
+        add_v(o, lv, i, j, k, cv, -1); add_v(o, lv, i, j + 1, k, cv, -1);
+        add_w(o, lw, i - 1, j, k, cw, -1); add_w(o, lw, i - 1, j, k + 1, cw, -1);
+        add_w(o, lw, i, j, k, cw, -1); add_w(o, lw, i, j, k + 1, cw, -1);
+      }
+  for (int k = 0; k < nz; ++k)
+    for (int j = 1; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const long f = V3(o, i, j, k);
+        const double g = lcv[f];
+        if (g == 0.0) continue;
+        const double vc = v[f];
+        const double ua = 0.25 * (uval(o, u, i, j - 1, k, 0.0) + uval(o, u, i + 1, j - 1, k, 0.0) +
+                                  uval(o, u, i, j, k, 0.0) + uval(o, u, i + 1, j, k, 0.0));
+        const double wa = 0.25 * (wval(o, w, i, j - 1, k, 0.0) + wval(o, w, i, j, k, 0.0) +
+                                  wval(o, w, i, j - 1, k + 1, 0.0) + wval(o, w, i, j, k + 1, 0.0));
+        const double ve = vval(o, v, i + 1, j, k, vc), vw = vval(o, v, i - 1, j, k, vc);
+        const double vn = vval(o, v, i, j + 1, k, vc), vs = vval(o, v, i, j - 1, k, vc);
+        const double vt = vval(o, v, i, j, k + 1, vc), vb = vval(o, v, i, j, k - 1, vc);
+        const double gx = g / tdx, gy = g / tdy, gz = g / tdz;
+        lv[f] += gy * (vn - vs);
+        add_v(o, lv, i + 1, j, k, gx * ua, f); add_v(o, lv, i - 1, j, k, -gx * ua, f);
+        add_v(o, lv, i, j + 1, k, gy * vc, f); add_v(o, lv, i, j - 1, k, -gy * vc, f);
+        add_v(o, lv, i, j, k + 1, gz * wa, f); add_v(o, lv, i, j, k - 1, -gz * wa, f);
+        const double cu = 0.25 * gx * (ve - vw), cw = 0.25 * gz * (vt - vb);
+        add_u(o, lu, i, j - 1, k, cu, -1); add_u(o, lu, i + 1, j - 1, k, cu, -1);
+        add_u(o, lu, i, j, k, cu, -1); add_u(o, lu, i + 1, j, k, cu, -1);
+        add_w(o, lw, i, j - 1, k, cw, -1); add_w(o, lw, i, j, k, cw, -1);
+        add_w(o, lw, i, j - 1, k + 1, cw, -1); add_w(o, lw, i, j, k + 1, cw, -1);
+      }
+  for (int k = 1; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const long f = W3(o, i, j, k);
+        const double g = lcw[f];
+        if (g == 0.0) continue;
+        const double wc = w[f];
+        const double ua = 0.25 * (uval(o, u, i, j, k - 1, 0.0) + uval(o, u, i + 1, j, k - 1, 0.0) +
+                                  uval(o, u, i, j, k, 0.0) + uval(o, u, i + 1, j, k, 0.0));
+        const double va = 0.25 * (vval(o, v, i, j, k - 1, 0.0) + vval(o, v, i, j + 1, k - 1, 0.0) +
+                                  vval(o, v, i, j, k, 0.0) + vval(o, v, i, j + 1, k, 0.0));
+        const double we = wval(o, w, i + 1, j, k, wc), ww = wval(o, w, i - 1, j, k, wc);
+        const double wn = wval(o, w, i, j + 1, k, wc), ws = wval(o, w, i, j - 1, k, wc);
+        const double wt = wval(o, w, i, j, k + 1, wc), wb = wval(o, w, i, j, k - 1, wc);
+        const double gx = g / tdx, gy = g / tdy, gz = g / tdz;
+        lw[f] += gz * (wt - wb);
+        add_w(o, lw, i + 1, j, k, gx * ua, f); add_w(o, lw, i - 1, j, k, -gx * ua, f);
+        add_w(o, lw, i, j + 1, k, gy * va, f); add_w(o, lw, i, j - 1, k, -gy * va, f);
+        add_w(o, lw, i, j, k + 1, gz * wc, f); add_w(o, lw, i, j, k - 1, -gz * wc, f);
+        const double cu = 0.25 * gx * (we - ww), cv = 0.25 * gy * (wn - ws);
+        add_u(o, lu, i, j, k - 1, cu, -1); add_u(o, lu, i + 1, j, k - 1, cu, -1);
+        add_u(o, lu, i, j, k, cu, -1); add_u(o, lu, i + 1, j, k, cu, -1);
+        add_v(o, lv, i, j, k - 1, cv, -1); add_v(o, lv, i, j + 1, k - 1, cv, -1);
+        add_v(o, lv, i, j, k, cv, -1); add_v(o, lv, i, j + 1, k, cv, -1);
+      }
+}
+
+/* lambda += weight dF_x/d(u, p) for the x force of oracle_forces at the
+ * oracle's current fields; *dnu += weight dF_x/dnu (the shear terms are
+ * proportional to nu). */
+static void force_x_adjoint(const oracle *o, double weight, double *lu, double *lp, double *dnu) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const double dx = o->dx, dy = o->dy, dz = o->dz, t2 = 2.0 * o->prm.rho * o->prm.nu;
+  const double ax = dy * dz;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        if (!o_fluid(o, i, j, k)) continue;
+        const long c = ((long)k * ny + j) * nx + i;
+        if (o_solid(o, i + 1, j, k)) lp[c] += weight * ax;
+        if (o_solid(o, i - 1, j, k)) lp[c] -= weight * ax;
+        if (i > 0 && o_fluid(o, i - 1, j, k)) {
+          double s = 0.0;
+          if (o_solid(o, i - 1, j + 1, k) && o_solid(o, i, j + 1, k)) s += dx * dz / dy;
+          if (o_solid(o, i - 1, j - 1, k) && o_solid(o, i, j - 1, k)) s += dx * dz / dy;
+          if (o_solid(o, i - 1, j, k + 1) && o_solid(o, i, j, k + 1)) s += dx * dy / dz;
+          if (o_solid(o, i - 1, j, k - 1) && o_solid(o, i, j, k - 1)) s += dx * dy / dz;
+          const long f = U3(o, i, j, k);
+          lu[f] += weight * t2 * s;
+          *dnu += weight * 2.0 * o->prm.rho * o->u[f] * s;
+        }
+      }
+}
+
+/* z += A^T-like transpose of a 1-based CSR: z[col] += val * y[row]. */
+static void csr_apply_t(const int32_t *rp, const int32_t *col, const double *val, long nrows, const double *y,
+                        double *z) {
+  for (long r = 0; r < nrows; ++r)
+    for (int t = rp[r]; t < rp[r + 1]; ++t) z[col[t]] += val[t] * y[r + 1];
+}
+
+/* Reverse sweep of one step (see ibm_oracle.h). */
+int oracle_step_backward(oracle *o, oracle *ot, double ramp, const double *beta_p, double weight, double *lu,
+                         double *lv, double *lw, double *lp, double *dg, double *dnu) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const long NU = (long)(nx + 1) * ny * nz, NV = (long)nx * (ny + 1) * nz, NW = (long)nx * ny * (nz + 1),
+             NP = (long)nx * ny * nz;
+  const double a = o->prm.rho / o->prm.dt, rho = o->prm.rho, nu = o->prm.nu, factor = o->prm.dt / o->prm.rho;
+  double *u0 = (double *)xcalloc((size_t)NU, 8), *v0 = (double *)xcalloc((size_t)NV, 8),
+         *w0 = (double *)xcalloc((size_t)NW, 8), *p0 = (double *)xcalloc((size_t)NP, 8);
+  oracle_get_fields(o, u0, v0, w0, p0);
+  /* recompute: U1 = BC(U0), the momentum right-hand sides and solutions, and
+   * the end-of-step fields (the objective's linearisation point) */
+  double *uin = (double *)xcalloc((size_t)ny * nz, 8);
+  for (long t = 0; t < (long)ny * nz; ++t) uin[t] = ramp * o->in.uin[t];
+  oracle_bc_cleanup(o, o->u, o->v, o->w, uin);
+  double *u1 = (double *)xcalloc((size_t)NU, 8), *v1 = (double *)xcalloc((size_t)NV, 8),
+         *w1 = (double *)xcalloc((size_t)NW, 8);
+  memcpy(u1, o->u, 8 * (size_t)NU); memcpy(v1, o->v, 8 * (size_t)NV); memcpy(w1, o->w, 8 * (size_t)NW);
+  const long nb[3] = {o->bu.N, o->bv.N, o->bw.N};
+  double *b[3], *x[3];
+  for (int f = 0; f < 3; ++f) { b[f] = (double *)xcalloc((size_t)nb[f], 8); x[f] = (double *)xcalloc((size_t)nb[f], 8); }
+  oracle_momentum_rhs(o, o->u, o->v, o->w, o->p, b[0], b[1], b[2]);
+  oracle_solve_stats ss;
+  int rc = 0;
+  for (int f = 0; f < 3; ++f) { oracle_solve(o, f, b[f], x[f], &ss); if (ss.status < 0) rc = -3; }
+  {
+    double *ut = (double *)xcalloc((size_t)NU, 8), *vt = (double *)xcalloc((size_t)NV, 8), *wt = (double *)xcalloc((size_t)NW, 8);
+    double *bp = (double *)xcalloc((size_t)NP, 8), *xp = (double *)xcalloc((size_t)NP, 8);
+    oracle_step_stats st;
+    oracle_tilde(o, x[0], x[1], x[2], ramp, ut, vt, wt);
+    oracle_pressure_rhs(o, ut, vt, wt, ramp, bp);
+    oracle_solve(o, 3, bp, xp, &ss);
+    oracle_projection(o, ut, vt, wt, xp, ramp, &st);
+    free(ut); free(vt); free(wt); free(bp); free(xp);
+  }
+  /* the objective's share of this step: weight * F_x at the end-of-step fields */
+  if (weight != 0.0) force_x_adjoint(o, weight, lu, lp, dnu);
+  /* BC cleanup after the projection */
+  bc_adjoint(o, lu, lv, lw, ramp, dg);
+  /* projection: q = q~ - (dt/rho) G phi, p += phi */
+  double *lq = (double *)xcalloc((size_t)o->nQ + 1, 8), *lphi = (double *)xcalloc((size_t)o->nP + 1, 8);
+  pack_q(o, lu, lv, lw, lq);
+  csr_apply_t(o->in.G_rowptr, o->in.G_col, o->in.G_val, o->nQ, lq, lphi);
+  double *rphi = (double *)xcalloc((size_t)NP, 8), *mu = (double *)xcalloc((size_t)NP, 8);
+  for (long c = 0; c < NP; ++c) {
+    const int id = o->in.id_p[c];
+    if (o->in.fluid_p[c] && id > 0) rphi[c] = lp[c] - factor * lphi[id];
+  }
+  /* pressure solve: mu = Ap^-T lambda_phi */
+  oracle_solve(ot, 3, rphi, mu, &ss);
+  if (ss.status < 0) rc = -3;
+  /* pressure right-hand side: b_p = -(rho/dt) (D q~ + ramp div_bc(g)) */
+  double *ldq = (double *)xcalloc((size_t)o->nP + 1, 8);
+  memset(lq, 0, sizeof(double) * ((size_t)o->nQ + 1));
+  for (long c = 0; c < NP; ++c) {
+    const int id = o->in.id_p[c];
+    if (!(o->in.fluid_p[c] && id > 0)) continue;
+    ldq[id] = -a * mu[c];
+    const int i = (int)(c % nx);
+    if (i == 0 && dg) {
+      const long jk = c / nx;
+      dg[jk] += a * ramp * mu[c] / (beta_p[c] * o->dx);
+    }
+  }
+  csr_apply_t(o->in.D_rowptr, o->in.D_col, o->in.D_val, o->nP, ldq, lq);
+  for (long f = 0; f < NU; ++f) { int id = o->in.id_qu[f]; if (id > 0) lu[f] += lq[id]; }
+  for (long f = 0; f < NV; ++f) { int id = o->in.id_qv[f]; if (id > 0) lv[f] += lq[o->nQu + id]; }
+  for (long f = 0; f < NW; ++f) { int id = o->in.id_qw[f]; if (id > 0) lw[f] += lq[o->nQu + o->nQv + id]; }
+  /* BC cleanup of u~ */
+  bc_adjoint(o, lu, lv, lw, ramp, dg);
+  /* scatter: the solve-box interior of u~ is x, the rest is U1 */
+  double *lx[3];
+  for (int f = 0; f < 3; ++f) lx[f] = (double *)xcalloc((size_t)nb[f], 8);
+  for (int k = 0; k < nz; ++k) for (int j = 0; j < ny; ++j) for (int i = 1; i < nx; ++i) {
+    const long f = U3(o, i, j, k);
+    lx[0][((long)k * ny + j) * (nx - 1) + (i - 1)] = lu[f]; lu[f] = 0.0;
+  }
+  for (int k = 0; k < nz; ++k) for (int j = 1; j < ny; ++j) for (int i = 0; i < nx; ++i) {
+    const long f = V3(o, i, j, k);
+    lx[1][((long)k * (ny - 1) + (j - 1)) * nx + i] = lv[f]; lv[f] = 0.0;
+  }
+  for (int k = 1; k < nz; ++k) for (int j = 0; j < ny; ++j) for (int i = 0; i < nx; ++i) {
+    const long f = W3(o, i, j, k);
+    lx[2][((long)(k - 1) * ny + j) * nx + i] = lw[f]; lw[f] = 0.0;
+  }
+  /* momentum solves: lambda_b = A^-T lambda_x; dnu from A(nu) and b(nu) */
+  double *lcu = (double *)xcalloc((size_t)NU, 8), *lcv = (double *)xcalloc((size_t)NV, 8),
+         *lcw = (double *)xcalloc((size_t)NW, 8);
+  double *lgu = (double *)xcalloc((size_t)NU, 8), *lgv = (double *)xcalloc((size_t)NV, 8),
+         *lgw = (double *)xcalloc((size_t)NW, 8);
+  for (int fld = 0; fld < 3; ++fld) {
+    double *lb = (double *)xcalloc((size_t)nb[fld], 8);
+    oracle_solve(ot, fld, lx[fld], lb, &ss);
+    if (ss.status < 0) rc = -3;
+    const int bx = fld == 0 ? nx - 1 : nx, by = fld == 1 ? ny - 1 : ny, bz = fld == 2 ? nz - 1 : nz;
+    for (int k = 0; k < bz; ++k)
+      for (int j = 0; j < by; ++j)
+        for (int i = 0; i < bx; ++i) {
+          const long r = ((long)k * by + j) * bx + i;
+          long f;
+          int id, act;
+          double sc, bc;
+          if (fld == 0) {
+            f = U3(o, i + 1, j, k); id = o->in.id_u[f]; act = o->in.active_u[f];
+            sc = id > 0 ? o->in.scale_u[id] : 0.0; bc = id > 0 ? o->in.rhs_u_bc[id] : 0.0;
+          } else if (fld == 1) {
+            f = V3(o, i, j + 1, k); id = o->in.id_v[f]; act = o->in.active_v[f];
+            sc = id > 0 ? o->in.scale_v[id] : 0.0; bc = id > 0 ? o->in.rhs_v_bc[id] : 0.0;
+          } else {
+            f = W3(o, i, j, k + 1); id = o->in.id_w[f]; act = o->in.active_w[f];
+            sc = id > 0 ? o->in.scale_w[id] : 0.0; bc = id > 0 ? o->in.rhs_w_bc[id] : 0.0;
+          }
+          if (!(id > 0 && act)) continue;
+          *dnu += lb[r] * (a * sc * x[fld][r] + sc * bc - b[fld][r]) / nu;
+          const double lt = sc * lb[r];
+          double *lf = fld == 0 ? lu : fld == 1 ? lv : lw;
+          double *lc = fld == 0 ? lcu : fld == 1 ? lcv : lcw;
+          double *lg = fld == 0 ? lgu : fld == 1 ? lgv : lgw;
+          lf[f] += a * lt;
+          lc[f] = -rho * lt;
+          lg[f] = -lt;
+        }
+    free(lb);
+  }
+  /* convection at U1 (the w rows use the active mask one plane below) */
+  for (int k = 1; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        if (!o->in.active_w[W3(o, i, j, k - 1)]) lcw[W3(o, i, j, k)] = 0.0;
+  for (long f = 0; f < NU; ++f) if (!o->in.active_u[f]) lcu[f] = 0.0;
+  for (long f = 0; f < NV; ++f) if (!o->in.active_v[f]) lcv[f] = 0.0;
+  conv_adjoint(o, u1, v1, w1, lcu, lcv, lcw, lu, lv, lw);
+  /* gradient of p^n on the q-faces */
+  memset(lq, 0, sizeof(double) * ((size_t)o->nQ + 1));
+  memset(lphi, 0, sizeof(double) * ((size_t)o->nP + 1));
+  pack_q(o, lgu, lgv, lgw, lq);
+  csr_apply_t(o->in.G_rowptr, o->in.G_col, o->in.G_val, o->nQ, lq, lphi);
+  for (long c = 0; c < NP; ++c) {
+    const int id = o->in.id_p[c];
+    if (o->in.fluid_p[c] && id > 0) lp[c] += lphi[id];
+  }
+  /* BC cleanup at the start of the step */
+  bc_adjoint(o, lu, lv, lw, ramp, dg);
+  oracle_set_fields(o, u0, v0, w0, p0);
+  free(u0); free(v0); free(w0); free(p0); free(uin); free(u1); free(v1); free(w1);
+  for (int f = 0; f < 3; ++f) { free(b[f]); free(x[f]); free(lx[f]); }
+  free(lq); free(lphi); free(rphi); free(mu); free(ldq);
+  free(lcu); free(lcv); free(lcw); free(lgu); free(lgv); free(lgw);
+  return rc;
+}

@@ -97,6 +97,21 @@ int oracle_mg_level_info(oracle *o, int l, int *dims /*3*/, int *cdir, int *nslo
 int oracle_mg_level_coef(oracle *o, int l, double *coef /* [n][27] */);
 void oracle_mg_vcycle(oracle *o, const double *b, double *x);
 
+/*
+ * Adjoint extension (the reference has none): reverse sweep of one step.
+ * o holds the step-start fields on entry and again on return (the step is
+ * recomputed from them); ot is an oracle on the transposed operators with the
+ * same parameters, used for the transposed solves; beta_p (cell open
+ * fractions) gives the inlet column's divergence lift, d(div_bc)/dg =
+ * -1/(beta dx). On entry (lu, lv, lw, lp) is the lambda of the end-of-step
+ * fields, to which weight * dF_x/d(end-of-step fields) is added (F_x the drag
+ * of oracle_forces); on return it is the lambda of the step-start fields.
+ * dg[ny*nz] (the inflow profile, u at the inlet = ramp g) and *dnu
+ * accumulate the parameter gradient. Returns 0, or -3 when a solve failed.
+ */
+int oracle_step_backward(oracle *o, oracle *ot, double ramp, const double *beta_p, double weight, double *lu,
+                         double *lv, double *lw, double *lp, double *dg, double *dnu);
+
 #ifdef __cplusplus
 }
 #endif

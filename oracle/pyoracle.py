@@ -86,6 +86,7 @@ def lib() -> C.CDLL:
         L.oracle_mg_level_info.argtypes = [vp, i, vp, C.POINTER(i), C.POINTER(i)]
         L.oracle_mg_level_coef.argtypes = [vp, i, vp]
         L.oracle_mg_vcycle.argtypes = [vp, vp, vp]
+        L.oracle_step_backward.argtypes = [vp, vp, d, vp, d, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -220,6 +221,90 @@ class Oracle:
         x = np.zeros_like(b)
         self.L.oracle_mg_vcycle(self.h, _p(b), _p(x))
         return x
+
+    def step_backward(self, ot: "Oracle", ramp: float, beta_p, weight: float, lam, dg) -> float:
+        """Reverse sweep of one step (oracle_step_backward): lam (u, v, w, p
+        lambdas) and dg are updated in place; returns the step's dJ/dnu."""
+        dnu = np.zeros(1)
+        beta = np.ascontiguousarray(beta_p, dtype=np.float64)
+        rc = self.L.oracle_step_backward(self.h, ot.h, C.c_double(ramp), _p(beta), C.c_double(weight),
+                                         *[_p(x) for x in lam], _p(dg), _p(dnu))
+        if rc != 0:
+            raise RuntimeError(f"oracle_step_backward failed ({rc})")
+        return float(dnu[0])
+
+
+def transpose7(vals, nb):
+    """Row-major 7-point operator [n][7] on a box nb = (nbx, nby, nbz) ->
+    its transpose in the same layout (slot order C,-x,+x,-y,+y,-z,+z)."""
+    nbx, nby, nbz = nb
+    A = np.asarray(vals, dtype=np.float64).reshape(nbz, nby, nbx, 7)
+    T = np.zeros_like(A)
+    T[..., 0] = A[..., 0]
+    T[:, :, 1:, 1] = A[:, :, :-1, 2]
+    T[:, :, :-1, 2] = A[:, :, 1:, 1]
+    T[:, 1:, :, 3] = A[:, :-1, :, 4]
+    T[:, :-1, :, 4] = A[:, 1:, :, 3]
+    T[1:, :, :, 5] = A[:-1, :, :, 6]
+    T[:-1, :, :, 6] = A[1:, :, :, 5]
+    return T.ravel()
+
+
+class TransposedCase:
+    """A case view whose four operators are transposed."""
+
+    def __init__(self, case):
+        self.base = case
+        self.params = case.params
+        nx, ny, nz = case.shape
+        boxes = {"Au_vals": (nx - 1, ny, nz), "Av_vals": (nx, ny - 1, nz), "Aw_vals": (nx, ny, nz - 1),
+                 "Ap_vals": (nx, ny, nz)}
+        self._t = {n: transpose7(case.array(n), b) for n, b in boxes.items()}
+
+    @property
+    def shape(self):
+        return self.base.shape
+
+    def array(self, name):
+        return self._t[name] if name in self._t else self.base.array(name)
+
+    def initial_fields(self):
+        return self.base.initial_fields()
+
+
+def drag_gradient(case, ramps, window, **oracle_kw):
+    """Objective J = mean over the steps in ``window`` (1-based step numbers)
+    of the end-of-step drag F_x, for len(ramps) steps from the case's initial
+    fields; returns (J, dJ/dg, dJ/dnu) by the oracle's reverse sweep (every
+    step-start state kept)."""
+    o = Oracle(case, **oracle_kw)
+    ot = Oracle(TransposedCase(case), **oracle_kw)
+    states, J = [], 0.0
+    w = 1.0 / len(window)
+    for n, ramp in enumerate(ramps, start=1):
+        states.append(o.fields())
+        o.step(ramp)
+        if n in window:
+            J += w * o.forces()[0]
+    lam = [np.zeros(s) for s in o.sizes()]
+    nx, ny, nz = case.shape
+    dg = np.zeros(ny * nz)
+    dnu = 0.0
+    beta = case.array("beta_p")
+    for n in range(len(ramps), 0, -1):
+        o.set_fields(*states[n - 1])
+        dnu += o.step_backward(ot, ramps[n - 1], beta, w if n in window else 0.0, lam, dg)
+    return J, dg, dnu, lam
+
+
+def drag_objective(case, ramps, window, **oracle_kw):
+    o = Oracle(case, **oracle_kw)
+    J = 0.0
+    for n, ramp in enumerate(ramps, start=1):
+        o.step(ramp)
+        if n in window:
+            J += o.forces()[0] / len(window)
+    return J
 
 
 class RefParams(C.Structure):

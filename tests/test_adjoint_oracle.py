@@ -1,0 +1,112 @@
+"""Adjoint extension on the CPU: the oracle's reverse sweep against central
+finite differences of the oracle's own forward steps, and the inflow
+parameterisation against the setup's arrays.
+
+Objective: mean end-of-step drag F_x over steps 2..4 of four steps (ramps
+0.5, 1, 1, 1) on a 48x16x16 channel; parameters: the inflow profile through
+8x8 Legendre coefficients (base parabolic profile plus a perturbation drawn
+as U(-0.05, 0.05) Um) and nu. Central differences with h = 1e-6; solves at a
+relative residual of 1e-13 so that the solver tolerance stays far below the
+difference quotient's own error.
+"""
+import importlib
+
+import numpy as np
+import pytest
+
+SHAPE = (48, 16, 16)
+ORACLE_KW = dict(vel_tol=1e-13, p_tol=1e-13, p_pc=1, mg_rap=0, mg_relax=2, mg_group_ratio=1.5)
+RAMPS = [0.5, 1.0, 1.0, 1.0]
+WINDOW = {2, 3, 4}
+
+
+@pytest.fixture(scope="module")
+def inflow():
+    return importlib.import_module("ibm-3d-fpc_gb300.inflow")
+
+
+def case_nu(ibm, nu):
+    return ibm.Case(ibm.channel_params(*SHAPE, Um=1.0, dt=2e-3, nu=nu))
+
+
+def test_inflow_case_reproduces_the_setup(ibm, inflow):
+    case = case_nu(ibm, 1e-3)
+    same = inflow.InflowCase(case, case.array("uin"))
+    for name in ("uin", "div_bc_unit", "rhs_u_bc", "Ap_vals"):
+        assert np.array_equal(same.array(name).view(np.uint8), case.array(name).view(np.uint8)), name
+    # the inlet weights are the derivative of the divergence lift
+    g = np.random.default_rng(1).standard_normal(case.shape[1] * case.shape[2])
+    lift = inflow.InflowCase(case, g).array("div_bc_unit")
+    nx, ny, nz = case.shape
+    idp = case.array("id_p").reshape(nz, ny, nx)[:, :, 0].ravel()
+    wts = inflow.inlet_weights(case)
+    m = wts != 0
+    assert np.allclose(lift[idp[m]], -g[m] * wts[m], rtol=1e-14, atol=0)
+
+
+def test_legendre_basis(ibm, inflow):
+    case = case_nu(ibm, 1e-3)
+    B = inflow.legendre_basis(case)
+    assert B.shape == (case.shape[1] * case.shape[2], 64)
+    assert np.allclose(B[:, 0], 1.0)
+    # L_1(yh) L_0(zh) is the y coordinate mapped to [-1, 1]
+    ny = case.shape[1]
+    yh = 2.0 * (np.arange(ny) + 0.5) / ny - 1.0
+    assert np.allclose(B[:ny, 1], yh)
+
+
+def test_oracle_adjoint_matches_finite_differences(ibm, pyoracle, inflow):
+    base = case_nu(ibm, 1e-3)
+    rng = np.random.default_rng(3)
+    c = rng.uniform(-0.05, 0.05, 64) * base.params.Um
+    g0 = inflow.inflow_from_coefficients(base, c)
+    J, dg, dnu, _ = pyoracle.drag_gradient(inflow.InflowCase(base, g0), RAMPS, WINDOW, **ORACLE_KW)
+    assert np.isfinite(J) and J != 0.0
+    B = inflow.legendre_basis(base)
+    dc = B.T @ dg
+    h = 1e-6
+    # a random direction in coefficient space
+    d = rng.standard_normal(64)
+    jp = pyoracle.drag_objective(inflow.InflowCase(base, g0 + B @ (h * d)), RAMPS, WINDOW, **ORACLE_KW)
+    jm = pyoracle.drag_objective(inflow.InflowCase(base, g0 - B @ (h * d)), RAMPS, WINDOW, **ORACLE_KW)
+    fd = (jp - jm) / (2 * h)
+    assert abs(dc @ d - fd) <= 1e-5 * abs(fd)
+    # the leading coefficient on its own
+    e = np.zeros(64)
+    e[0] = 1.0
+    jp = pyoracle.drag_objective(inflow.InflowCase(base, g0 + B @ (h * e)), RAMPS, WINDOW, **ORACLE_KW)
+    jm = pyoracle.drag_objective(inflow.InflowCase(base, g0 - B @ (h * e)), RAMPS, WINDOW, **ORACLE_KW)
+    fd = (jp - jm) / (2 * h)
+    assert abs(dc[0] - fd) <= 1e-5 * abs(fd)
+    # nu: the operators, row scales, inlet lift and wall shear all change
+    jp = pyoracle.drag_objective(inflow.InflowCase(case_nu(ibm, 1e-3 + h), g0), RAMPS, WINDOW, **ORACLE_KW)
+    jm = pyoracle.drag_objective(inflow.InflowCase(case_nu(ibm, 1e-3 - h), g0), RAMPS, WINDOW, **ORACLE_KW)
+    fd = (jp - jm) / (2 * h)
+    assert abs(dnu - fd) <= 1e-5 * abs(fd)
+
+
+def test_oracle_adjoint_is_the_transpose_of_the_step(ibm, pyoracle, inflow):
+    """<lambda_0, ds_0> = <lambda_1, ds_1> for the step's tangent, with the
+    tangent taken by central differences of one oracle step."""
+    case = case_nu(ibm, 1e-3)
+    o = pyoracle.Oracle(case, **ORACLE_KW)
+    ot = pyoracle.Oracle(pyoracle.TransposedCase(case), **ORACLE_KW)
+    o.step(1.0)
+    s0 = o.fields()
+    rng = np.random.default_rng(7)
+    lam1 = [rng.standard_normal(x.size) for x in s0]
+    lam = [x.copy() for x in lam1]
+    dg = np.zeros(case.shape[1] * case.shape[2])
+    o.step_backward(ot, 1.0, case.array("beta_p"), 0.0, lam, dg)
+    ds = [rng.standard_normal(x.size) * 1e-3 for x in s0]
+    h = 1e-4
+
+    def step_from(eps):
+        o.set_fields(*[x + eps * y for x, y in zip(s0, ds)])
+        o.step(1.0)
+        return o.fields()
+
+    sp, sm = step_from(h), step_from(-h)
+    lhs = sum(float(l @ d) for l, d in zip(lam, ds))
+    rhs = sum(float(l @ ((a - b) / (2 * h))) for l, a, b in zip(lam1, sp, sm))
+    assert abs(lhs - rhs) <= 1e-6 * abs(rhs)
