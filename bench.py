@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-pressure-only", action="store_true", help="skip the 512x96x96 pressure-solve measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the 256x48x48 adjoint-sensitivity measurement")
+    ap.add_argument("--adjoint-steps", type=int, default=200, help="steps of the adjoint workload (objective "
+                    "window: the second half)")
     ap.add_argument("--ensemble", type=int, default=32, help="instances of the batched ensemble")
     ap.add_argument("--mg-coarse-max", type=int, default=2560,
                     help="multigrid: largest level solved directly (dense inverse)")
@@ -292,6 +295,77 @@ def pressure_only_measure(ibm, args, local, plib, Prof, repeats=3):
                    "restart more often (each stops at a 1e-5 reduction) and leave a larger error in the "
                    "smoothest modes for the same residual; FP32 multigrid in FP64 FGMRES is the fast form here")
     return out
+
+
+def adjoint_measure(ibm, args, local):
+    """The adjoint-sensitivity workload: 256x48x48 channel (Um 0.45, nu 1e-3,
+    dt 1e-3, no ramp), FP64 graph-captured steps and FP64 transposed solves
+    at 1e-12; objective = mean drag over steps 100..200 of 200 from the
+    reference's initial state; parameters = 8x8 Legendre coefficients of the
+    inflow (drawn as U(-0.05, 0.05) Um, PCG64 seed 4) and nu; checkpoints
+    every 20 steps with recomputation. Gradient time against one forward
+    sweep; the gradient checked against central differences (h = 1e-6) along
+    a random coefficient direction and in nu."""
+    inflow = importlib.import_module("ibm-3d-fpc_gb300.inflow")
+    n = args.adjoint_steps
+    window = range(n // 2, n + 1)
+    ramps = [1.0] * n
+    shape = (256, 48, 48)
+
+    def case_nu(nu):
+        return ibm.Case(ibm.channel_params(*shape, Um=0.45, nu=nu, dt=1e-3))
+
+    prm = ibm.solver_params(vel_tol=1e-12, p_tol=1e-12, vel_maxit=500, p_maxit=500, p_pc=1, p_pc_rap_type=0,
+                            p_pc_relax_type=2, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_omega=1.0,
+                            mg_group_ratio=1.5, mg_coarse_max=args.mg_coarse_max, precision=0, use_graph=1,
+                            compute_forces=1)
+    base = case_nu(1e-3)
+    rng = np.random.default_rng(4)
+    g0 = inflow.inflow_from_coefficients(base, rng.uniform(-0.05, 0.05, 64) * base.params.Um)
+    B = inflow.legendre_basis(base)
+
+    def objective(case, g):
+        s = ibm.Solver(inflow.InflowCase(case, g), prm, device=local)
+        J = 0.0
+        for k in range(1, n + 1):
+            st = s.step(ramps[k - 1])
+            if k in window:
+                J += st.force[0] / len(window)
+        s.close()
+        return J
+
+    s = ibm.Solver(inflow.InflowCase(base, g0), prm, device=local)
+    s.adjoint_setup()
+    s.set_fields(*inflow.InflowCase(base, g0).initial_fields())
+    for _ in range(3):
+        s.step(1.0)  # graph capture and solver set-up outside the timings
+    s.set_fields(*inflow.InflowCase(base, g0).initial_fields())
+    t0 = time.perf_counter()
+    J_fwd = 0.0
+    for k in range(1, n + 1):
+        st = s.step(1.0)
+        if k in window:
+            J_fwd += st.force[0] / len(window)
+    t_fwd = time.perf_counter() - t0
+    s.set_fields(*inflow.InflowCase(base, g0).initial_fields())
+    t0 = time.perf_counter()
+    J, dg, dnu = s.drag_gradient(ramps, window, checkpoint_every=20)
+    t_grad = time.perf_counter() - t0
+    s.close()
+    dc = B.T @ dg
+    h = 1e-6
+    d = rng.standard_normal(64)
+    fd_dir = (objective(base, g0 + B @ (h * d)) - objective(base, g0 - B @ (h * d))) / (2 * h)
+    fd_nu = (objective(case_nu(1e-3 + h), g0) - objective(case_nu(1e-3 - h), g0)) / (2 * h)
+    return {"workload": f"adjoint sensitivity 256x48x48 channel, Um 0.45, nu 1e-3, dt 1e-3, {n} steps, objective "
+                        f"mean drag over steps {n // 2}..{n}, 64 Legendre inflow coefficients + nu, checkpoint every 20",
+            "J": J, "J_forward_only": J_fwd, "dJ_dnu": dnu, "dJ_dc_norm": float(np.linalg.norm(dc)),
+            "forward_s": t_fwd, "gradient_s": t_grad, "gradient_over_forward": t_grad / t_fwd,
+            "central_fd_all_params_s": 2 * 65 * t_fwd, "gradient_speedup_vs_fd": 2 * 65 * t_fwd / t_grad,
+            "fd_check": {"direction_rel_err": abs(dc @ d - fd_dir) / abs(fd_dir),
+                         "nu_rel_err": abs(dnu - fd_nu) / abs(fd_nu), "h": h},
+            "note": "host wall time (each step and solve waits for its results); FP64 steps and transposed solves "
+                    "at a 1e-12 relative residual"}
 
 
 def run_steps(solver, n):
@@ -609,6 +683,11 @@ def main():
             out["pressure_only"] = pressure_only_measure(ibm, args, local, plib, Prof)
         except Exception as e:  # the line must still print
             out["pressure_only"] = {"value": None, "error": str(e)}
+    if rank == 0 and not args.no_adjoint:
+        try:
+            out["adjoint"] = adjoint_measure(ibm, args, local)
+        except Exception as e:  # the line must still print
+            out["adjoint"] = {"value": None, "error": str(e)}
     if not args.no_ensemble:
         try:
             out["ensemble"] = ensemble_measure(ibm, args, ws, rank, local, steps=min(args.steps, 10), warmup=3)

@@ -257,6 +257,12 @@ class Solver:
         self._check(self._lib.ibm_adjoint_get(self._ctx, *[_ptr(x) for x in out]))
         return out[0], out[1], out[2], out[3], out[4], float(out[5][0])
 
+    def adjoint_solve_stats(self):
+        """Stats of the last reverse sweep's transposed solves (u, v, w, p)."""
+        out = (SolveStats * 4)()
+        self._check(self._lib.ibm_adjoint_solve_stats(self._ctx, out))
+        return list(out)
+
     def tape_depth(self) -> int:
         return self._check(self._lib.ibm_adjoint_tape_depth(self._ctx))
 

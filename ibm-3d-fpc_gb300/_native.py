@@ -157,6 +157,7 @@ def gpu() -> C.CDLL:
         lib.ibm_adjoint_set.argtypes = [vp, vp, vp, vp, vp]
         lib.ibm_adjoint_get.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         lib.ibm_adjoint_tape_depth.argtypes = [vp]
+        lib.ibm_adjoint_solve_stats.argtypes = [vp, P(SolveStats)]
         lib.ibm_checkpoint_save.argtypes = [vp, i]
         lib.ibm_checkpoint_load.argtypes = [vp, i]
         lib.ibm_checkpoint_clear.argtypes = [vp]

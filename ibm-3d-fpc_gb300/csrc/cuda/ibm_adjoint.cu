@@ -13,7 +13,10 @@
 
 namespace ibm {
 
-AdjState::~AdjState() = default;
+AdjState::~AdjState() {
+  if (gexec) cudaGraphExecDestroy(gexec);
+  if (hweight) cudaFreeHost(hweight);
+}
 
 namespace {
 
@@ -74,7 +77,8 @@ __global__ void k_zero_lists(double *u, const int *lu, int nu_, double *v, const
 
 // Reverse of the boundary planes of the BC cleanup (k_bc_planes): outlet copy
 // u[nx] = u[nx-1], inlet u[0] = ramp g, wall v and w set to zero.
-__global__ void k_bc_planes_t(double *lu, double *lv, double *lw, double *dg, double ramp, ADims d) {
+__global__ void k_bc_planes_t(double *lu, double *lv, double *lw, double *dg, const double *rampp, ADims d) {
+  const double ramp = *rampp;
   const long n = std::max((long)d.ny * d.nz, std::max((long)d.nx * d.nz, (long)d.nx * d.ny));
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     if (t < (long)d.ny * d.nz) {
@@ -100,7 +104,9 @@ __global__ void k_bc_planes_t(double *lu, double *lv, double *lw, double *dg, do
 // The x force of k_forces (staircase definition) is linear in p and u:
 // lambda += weight dF_x/d(p, u), acc += weight dF_x/dnu.
 __global__ void k_force_t(const uint8_t *fc, const double *u, double *lu, double *lp, double *acc, ADims d,
-                          double dx, double dy, double dz, double rho, double nu, double weight) {
+                          double dx, double dy, double dz, double rho, double nu, const double *weightp) {
+  const double weight = *weightp;
+  if (weight == 0.0) return;
   const long NP = (long)d.nx * d.ny * d.nz;
   auto fluid = [&](int i, int j, int k) { return (fc[d.P(i, j, k)] & kFluid) != 0; };
   auto solid = [&](int i, int j, int k) {
@@ -220,8 +226,10 @@ __global__ void k_div_t(ADims d, const uint8_t *fu, const uint8_t *fv, const uin
   }
 }
 
-// dg += coef mu / (beta dx) on the inlet column (cell (0, j, k) = t nx).
-__global__ void k_inlet_t(double *dg, const double *mu, const double *winl, double coef, int nx, int nyz) {
+// dg += coef ramp mu / (beta dx) on the inlet column (cell (0, j, k) = t nx).
+__global__ void k_inlet_t(double *dg, const double *mu, const double *winl, double coef, const double *ramp, int nx,
+                          int nyz) {
+  coef *= *ramp;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nyz; t += gridDim.x * blockDim.x)
     if (winl[t] != 0.0) dg[t] += coef * mu[(long)t * nx] * winl[t];
 }
@@ -424,6 +432,11 @@ __global__ void k_conv_t(ConvTArgs A) {
   }
 }
 
+__global__ void k_wscale(const double *x, const double *winv, double *y, long n, int divide) {
+  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x)
+    y[r] = divide ? x[r] / winv[r] : x[r] * winv[r];
+}
+
 // u at the inlet = g (the BC cleanup multiplies by the ramp); the inlet
 // column's divergence lift 0 - g / (beta dx), the operations of the setup.
 __global__ void k_set_inflow(const double *g, const double *bdx, double *uin, double *div_bc, int nx, int nyz) {
@@ -440,7 +453,7 @@ void launch_transpose7(cudaStream_t st, const double *planes, const Box &b, doub
   k_transpose7<<<adj_grid(b.n), kThreads, 0, st>>>(planes, b, rows);
 }
 
-void adj_bc(ibm_ctx *c, double *lu, double *lv, double *lw, double ramp) {
+void adj_bc(ibm_ctx *c, double *lu, double *lv, double *lw, const double *ramp) {
   const ADims d = adims(c);
   const long m = std::max((long)c->zl_u.n, std::max((long)c->zl_v.n, (long)c->zl_w.n));
   if (m > 0) {
@@ -453,14 +466,14 @@ void adj_bc(ibm_ctx *c, double *lu, double *lv, double *lw, double ramp) {
   k_bc_planes_t<<<adj_grid(n), kThreads, 0, c->st>>>(lu, lv, lw, c->adj->dg.p, ramp, d);
 }
 
-void adj_force(ibm_ctx *c, double weight) {
+void adj_force(ibm_ctx *c, const double *weight) {
   AdjState &a = *c->adj;
   LaunchScope ls(K_ADJOINT, c->st, 1.0 * c->g.NP + 24.0 * c->g.NU + 16.0 * c->g.NP);
   k_force_t<<<adj_grid(c->g.NP), kThreads, 0, c->st>>>(c->fc.p, c->u.p, a.lu.p, a.lp.p, a.acc.p, adims(c), c->g.dx,
                                                       c->g.dy, c->g.dz, c->g.rho, c->g.nu, weight);
 }
 
-void adj_projection(ibm_ctx *c) {
+void adj_projection(ibm_ctx *c, double *rphi) {
   AdjState &a = *c->adj;
   GradTArgs A;
   A.d = adims(c);
@@ -469,36 +482,35 @@ void adj_projection(ibm_ctx *c) {
   A.lu = a.lu.p; A.lv = a.lv.p; A.lw = a.lw.p;
   A.base = a.lp.p;
   A.coef = -(c->g.dt / c->g.rho);
-  A.out = a.rphi.p;
+  A.out = rphi;
   A.mode = 0;
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
   LaunchScope ls(K_ADJOINT, c->st, 25.0 * faces + 17.0 * c->g.NP);
   k_grad_t<<<adj_grid(c->g.NP), kThreads, 0, c->st>>>(A);
 }
 
-void adj_divergence(ibm_ctx *c, double ramp) {
+void adj_divergence(ibm_ctx *c, const double *mu, const double *ramp) {
   AdjState &a = *c->adj;
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
   const double rdt = c->g.rho / c->g.dt;
   {
     LaunchScope ls(K_ADJOINT, c->st, 17.0 * faces + 57.0 * c->g.NP);
     k_div_t<<<adj_grid(c->g.NU + c->g.NV + c->g.NW), kThreads, 0, c->st>>>(
-        adims(c), c->fu.p, c->fv.p, c->fw.p, c->fc.p, c->Dc.p, a.mu.p, -rdt, a.lu.p, a.lv.p, a.lw.p);
+        adims(c), c->fu.p, c->fv.p, c->fw.p, c->fc.p, c->Dc.p, mu, -rdt, a.lu.p, a.lv.p, a.lw.p);
   }
   const int nyz = c->g.ny * c->g.nz;
   LaunchScope ls(K_ADJOINT, c->st, 32.0 * nyz);
-  k_inlet_t<<<adj_grid(nyz), kThreads, 0, c->st>>>(a.dg.p, a.mu.p, a.winl.p, rdt * ramp, c->g.nx, nyz);
+  k_inlet_t<<<adj_grid(nyz), kThreads, 0, c->st>>>(a.dg.p, mu, a.winl.p, rdt, ramp, c->g.nx, nyz);
 }
 
-void adj_scatter(ibm_ctx *c) {
+void adj_scatter(ibm_ctx *c, double *const *lx) {
   AdjState &a = *c->adj;
   const long n = c->g.bu.n + c->g.bv.n + c->g.bw.n;
   LaunchScope ls(K_ADJOINT, c->st, 24.0 * n);
-  k_scatter_t<<<adj_grid(n), kThreads, 0, c->st>>>(adims(c), a.lu.p, a.lv.p, a.lw.p, a.lx[0].p, a.lx[1].p,
-                                                   a.lx[2].p);
+  k_scatter_t<<<adj_grid(n), kThreads, 0, c->st>>>(adims(c), a.lu.p, a.lv.p, a.lw.p, lx[0], lx[1], lx[2]);
 }
 
-void adj_momentum(ibm_ctx *c) {
+void adj_momentum(ibm_ctx *c, const double *const *lb) {
   AdjState &a = *c->adj;
   a.cu.zero(c->st); a.cv.zero(c->st); a.cw.zero(c->st);
   a.gu.zero(c->st); a.gv.zero(c->st); a.gw.zero(c->st);
@@ -507,7 +519,7 @@ void adj_momentum(ibm_ctx *c) {
   M.fu = c->fu.p; M.fv = c->fv.p; M.fw = c->fw.p;
   for (int f = 0; f < 3; ++f) {
     M.sc[f] = c->scale_box[f].p; M.bc[f] = c->bc_box[f].p; M.b[f] = c->bb[f].p; M.x[f] = c->xb[f].p;
-    M.lb[f] = a.lb[f].p;
+    M.lb[f] = lb[f];
   }
   M.nb[0] = c->g.bu.n; M.nb[1] = c->g.bv.n; M.nb[2] = c->g.bw.n;
   M.lu = a.lu.p; M.lv = a.lv.p; M.lw = a.lw.p;
@@ -545,6 +557,11 @@ void adj_gradient(ibm_ctx *c) {
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW);
   LaunchScope ls(K_ADJOINT, c->st, 25.0 * faces + 17.0 * c->g.NP);
   k_grad_t<<<adj_grid(c->g.NP), kThreads, 0, c->st>>>(A);
+}
+
+void adj_wscale(ibm_ctx *c, const double *x, double *y, bool divide) {
+  LaunchScope ls(K_ADJOINT, c->st, 24.0 * c->g.NP);
+  k_wscale<<<adj_grid(c->g.NP), kThreads, 0, c->st>>>(x, c->p_winv.p, y, c->g.NP, divide ? 1 : 0);
 }
 
 void adj_set_inflow(ibm_ctx *c, const double *g) {

@@ -1201,21 +1201,23 @@ void restore(ibm_ctx *c, const std::array<DBuf<double>, 4> &s) {
     IBM_CUDA_TRY(cudaMemcpyAsync(dst[q], s[q].p, sizeof(double) * s[q].n, cudaMemcpyDeviceToDevice, c->st));
 }
 
-// x = A^-T b on the transposed-operator context t (device vectors, zero
-// initial guess). The caller's stream must have produced b already.
-KResult transposed_solve(ibm_ctx *t, int field, const double *b, double *x) {
+// A^-T b on the transposed-operator context t, host-driven: the pressure
+// system alone or the three momentum systems batched in one solve, from
+// t->bb into t->xb (zero initial guesses). The caller's stream must have
+// produced b already. Returns the worst status; throws on a non-finite
+// solution.
+int transposed_solve(ibm_ctx *t, bool pressure) {
   Scope sc(t);
   ensure_solvers(t);
-  const long n = field_box(t, field).n;
-  IBM_CUDA_TRY(cudaMemcpyAsync(t->bb[field].p, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, t->st));
-  IBM_CUDA_TRY(cudaMemsetAsync(t->xb[field].p, 0, sizeof(double) * n, t->st));
+  const int f0 = pressure ? 3 : 0, nf = pressure ? 1 : 3;
+  for (int f = f0; f < f0 + nf; ++f)
+    IBM_CUDA_TRY(cudaMemsetAsync(t->xb[f].p, 0, sizeof(double) * field_box(t, f).n, t->st));
   KResult r[3];
-  if (field < 3) {
+  if (!pressure) {
     const double *bm[3] = {t->bb[0].p, t->bb[1].p, t->bb[2].p};
     double *xm[3] = {t->xb[0].p, t->xb[1].p, t->xb[2].p};
     Precond none;
-    t->kmom.solve(t->st, bm, xm, none, r, 1u << field, true);
-    r[0] = r[field];
+    t->kmom.solve(t->st, bm, xm, none, r, ~0u, true);
   } else {
     const double *bp[1] = {t->bb[3].p};
     double *xp[1] = {t->xb[3].p};
@@ -1225,10 +1227,190 @@ KResult transposed_solve(ibm_ctx *t, int field, const double *b, double *x) {
     t->kp.solve(t->st, bp, xp, mgp, r, ~0u, true);
   }
   t->graph_bound = false;
-  IBM_CUDA_TRY(cudaMemcpyAsync(x, t->xb[field].p, sizeof(double) * n, cudaMemcpyDeviceToDevice, t->st));
+  if (t->adj_owner) t->adj_owner->adj->graph_bound = false;
   IBM_CUDA_TRY(cudaStreamSynchronize(t->st));
   t->prof.drain();
-  return r[0];
+  int rc = IBM_OK;
+  for (int q = 0; q < nf; ++q) {
+    if (t->adj_owner) t->adj_owner->adj->last[f0 + q] = r[q];
+    if (r[q].nonfinite) throw Error(IBM_ERR_NONFINITE, "non-finite transposed solve");
+    rc = worst(rc, solve_status(r[q]));
+  }
+  return rc;
+}
+
+// The reverse sweep after the recomputed step, host-driven. The ramp is the
+// step's (c->dramp), the objective weight a.dweight.
+int reverse_host(ibm_ctx *c) {
+  ibm::AdjState &a = *c->adj;
+  ibm_ctx *t = a.t;
+  const double *ramp = c->dramp.p;
+  adj_force(c, a.dweight.p);
+  adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+  int rc = IBM_OK;
+  if (c->p_sym) {
+    // Ap^T mu = r  <=>  Ap (W mu) = W r, with the step's own pressure solver
+    adj_projection(c, a.mu.p);
+    adj_wscale(c, a.mu.p, c->bb[3].p, true);
+    IBM_CUDA_TRY(cudaMemsetAsync(c->xb[3].p, 0, sizeof(double) * c->g.NP, c->st));
+    const double *bp[1] = {c->bb[3].p};
+    double *xp[1] = {c->xb[3].p};
+    Precond mgp;
+    mgp.ctx = c;
+    mgp.apply = mg_apply_cb;
+    KResult r[1];
+    c->kp.solve(c->st, bp, xp, mgp, r, ~0u, true);
+    c->graph_bound = false;
+    a.last[3] = r[0];
+    if (r[0].nonfinite) throw Error(IBM_ERR_NONFINITE, "non-finite transposed solve");
+    rc = solve_status(r[0]);
+    adj_wscale(c, c->xb[3].p, a.mu.p, false);
+  } else {
+    adj_projection(c, t->bb[3].p);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    rc = transposed_solve(t, true);
+    IBM_CUDA_TRY(cudaMemcpyAsync(a.mu.p, t->xb[3].p, sizeof(double) * c->g.NP, cudaMemcpyDeviceToDevice, c->st));
+  }
+  adj_divergence(c, a.mu.p, ramp);
+  adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+  double *lx[3] = {t->bb[0].p, t->bb[1].p, t->bb[2].p};
+  adj_scatter(c, lx);
+  IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  rc = worst(rc, transposed_solve(t, false));
+  const double *lb[3] = {t->xb[0].p, t->xb[1].p, t->xb[2].p};
+  adj_momentum(c, lb);
+  adj_gradient(c);
+  adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+  IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  return rc;
+}
+
+// Binds the transposed context's Krylov systems to its bb / xb vectors for
+// the graph form (outside any capture).
+void bind_transposed(ibm_ctx *c) {
+  ibm::AdjState &a = *c->adj;
+  ibm_ctx *t = a.t;
+  Scope sc(t);
+  ensure_solvers(t);
+  const double *bm[3] = {t->bb[0].p, t->bb[1].p, t->bb[2].p};
+  double *xm[3] = {t->xb[0].p, t->xb[1].p, t->xb[2].p};
+  t->kmom.bind(t->st, bm, xm, ~0u, true);
+  const double *bp[1] = {t->bb[3].p};
+  double *xp[1] = {t->xb[3].p};
+  t->kp.bind(t->st, bp, xp, ~0u, true);
+  IBM_CUDA_TRY(cudaStreamSynchronize(t->st));
+  a.graph_bound = true;
+}
+
+// The reverse sweep captured as one graph on c->st: the adjoint kernels and
+// the graph forms of the transposed solves (restart and Arnoldi loops as
+// conditional nodes on the device). Inputs that change per call are read on
+// the device: the ramp (c->dramp, written by the recomputed step), the
+// weight (a.dweight, copied from pinned memory by the graph) and the
+// linearisation point (a.u1 / v1 / w1, copied in before the launch).
+void build_adjoint_graph(ibm_ctx *c) {
+  ibm::AdjState &a = *c->adj;
+  ibm_ctx *t = a.t;
+  if (a.gexec) cudaGraphExecDestroy(a.gexec);
+  a.gexec = nullptr;
+  a.graph_ready = false;
+  bind_transposed(c);
+  if (c->p_sym && !c->graph_bound) {
+    // the step's pressure solver, bound as the step graph binds it
+    const double *bp[1] = {c->bb[3].p};
+    double *xp[1] = {c->xb[3].p};
+    c->kp.bind(c->st, bp, xp, ~0u, c->prm.use_zero_initial_guess != 0);
+  }
+  cudaStream_t st = c->st;
+  Prof *saved_prof = current_prof();
+  long long *saved_counter = g_counter;
+  long long cap_count = 0;
+  current_prof() = nullptr;
+  g_counter = &cap_count;
+  cudaGraph_t graph = nullptr;
+  Krylov::GraphCounts gm, gp;
+  Precond none, mgp, mgc;
+  mgp.ctx = t;
+  mgp.apply = mg_apply_cb;
+  mgc.ctx = c;
+  mgc.apply = mg_apply_cb;
+  const double *ramp = c->dramp.p;
+  try {
+    IBM_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    IBM_CUDA_TRY(cudaMemcpyAsync(a.dweight.p, a.hweight, sizeof(double), cudaMemcpyHostToDevice, st));
+    IBM_CUDA_TRY(cudaMemsetAsync(t->dloops.p, 0, sizeof(unsigned long long) * 4, st));
+    launch_bc(c, a.u1.p, a.v1.p, a.w1.p);
+    adj_force(c, a.dweight.p);
+    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+    if (c->p_sym) {
+      adj_projection(c, a.mu.p);
+      adj_wscale(c, a.mu.p, c->bb[3].p, true);
+      IBM_CUDA_TRY(cudaMemsetAsync(c->xb[3].p, 0, sizeof(double) * c->g.NP, st));
+      gp = c->kp.enqueue_graph(st, c->cap, mgc, c->hflags_graph + 3, t->dloops.p + 2);
+      adj_wscale(c, c->xb[3].p, a.mu.p, false);
+    } else {
+      adj_projection(c, t->bb[3].p);
+      IBM_CUDA_TRY(cudaMemsetAsync(t->xb[3].p, 0, sizeof(double) * t->g.bp.n, st));
+      gp = t->kp.enqueue_graph(st, t->cap, mgp, t->hflags_graph + 3, t->dloops.p + 2);
+      IBM_CUDA_TRY(cudaMemcpyAsync(a.mu.p, t->xb[3].p, sizeof(double) * c->g.NP, cudaMemcpyDeviceToDevice, st));
+    }
+    adj_divergence(c, a.mu.p, ramp);
+    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+    double *lx[3] = {t->bb[0].p, t->bb[1].p, t->bb[2].p};
+    adj_scatter(c, lx);
+    for (int f = 0; f < 3; ++f)
+      IBM_CUDA_TRY(cudaMemsetAsync(t->xb[f].p, 0, sizeof(double) * field_box(t, f).n, st));
+    gm = t->kmom.enqueue_graph(st, t->cap, none, t->hflags_graph, t->dloops.p);
+    const double *lb[3] = {t->xb[0].p, t->xb[1].p, t->xb[2].p};
+    adj_momentum(c, lb);
+    adj_gradient(c);
+    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
+    IBM_CUDA_TRY(cudaMemcpyAsync(t->hloops, t->dloops.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, st));
+    IBM_CUDA_TRY(cudaStreamEndCapture(st, &graph));
+  } catch (...) {
+    cudaGraph_t junk = nullptr;
+    cudaStreamEndCapture(st, &junk);
+    if (junk) cudaGraphDestroy(junk);
+    current_prof() = saved_prof;
+    g_counter = saved_counter;
+    throw;
+  }
+  current_prof() = saved_prof;
+  g_counter = saved_counter;
+  const cudaError_t e = cudaGraphInstantiate(&a.gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  IBM_CUDA_TRY(e);
+  a.graph_fixed_launches = cap_count - gm.loop - gp.loop;
+  a.graph_body_launches[0] = gm.end_body;
+  a.graph_body_launches[1] = gm.arnoldi_body;
+  a.graph_body_launches[2] = gp.end_body;
+  a.graph_body_launches[3] = gp.arnoldi_body;
+  a.graph_ready = true;
+}
+
+// Launches the captured reverse sweep and reads the transposed solves' flags.
+int reverse_graph(ibm_ctx *c) {
+  ibm::AdjState &a = *c->adj;
+  ibm_ctx *t = a.t;
+  if (!a.graph_ready) build_adjoint_graph(c);
+  else if (!a.graph_bound) bind_transposed(c);
+  IBM_CUDA_TRY(cudaGraphLaunch(a.gexec, c->st));
+  IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+  IBM_CUDA_TRY(cudaGetLastError());
+  const unsigned long long *lp = t->hloops;
+  c->launches += a.graph_fixed_launches + (long long)lp[0] * a.graph_body_launches[0] +
+                 (long long)lp[1] * a.graph_body_launches[1] + (long long)lp[2] * a.graph_body_launches[2] +
+                 (long long)lp[3] * a.graph_body_launches[3];
+  int rc = IBM_OK;
+  for (int s = 0; s < 4; ++s) {
+    const KFlags &f = (s == 3 && c->p_sym) ? c->hflags_graph[3] : t->hflags_graph[s];
+    KResult r;
+    r.iters = f.iters; r.rel_res = f.rel; r.status = f.status; r.nonfinite = f.nonfinite;
+    a.last[s] = r;
+    if (r.nonfinite) throw Error(IBM_ERR_NONFINITE, "non-finite transposed solve");
+    rc = worst(rc, solve_status(r));
+  }
+  return rc;
 }
 
 void sync_transposed_params(ibm_ctx *c) {
@@ -1236,9 +1418,11 @@ void sync_transposed_params(ibm_ctx *c) {
   ibm_solver_params p = c->prm;
   p.use_graph = 0;
   p.compute_forces = 0;
+  if (c->p_sym) p.p_pc = 0;  // the pressure transpose is solved with the step's own solver
   if (memcmp(&p, &t->prm, sizeof(p)) != 0) {
     const int rc = ibm_set_solver_params(t, &p);
     if (rc < 0) throw Error(rc, "transposed context: " + t->err);
+    c->adj->graph_ready = false;
   }
 }
 
@@ -1250,9 +1434,13 @@ int ibm_adjoint_setup(ibm_ctx *c, const double *beta_p) {
     require_inputs(c);
     if (!c->adj) c->adj = new ibm::AdjState();
     ibm::AdjState &a = *c->adj;
+    if (a.gexec) cudaGraphExecDestroy(a.gexec);
+    a.gexec = nullptr;
+    a.graph_ready = false;
     if (a.t) { ibm_destroy(a.t); a.t = nullptr; }
     int rc = ibm_create(&c->grid, &a.t);
     if (rc < 0) throw Error(rc, "transposed context: " + g_create_error);
+    a.t->adj_owner = c;
     for (int f = 0; f < 4; ++f) {
       const Box &b = field_box(c, f);
       DBuf<double> rows;
@@ -1281,13 +1469,20 @@ int ibm_adjoint_setup(ibm_ctx *c, const double *beta_p) {
     a.cu.alloc(g.NU); a.cv.alloc(g.NV); a.cw.alloc(g.NW);
     a.gu.alloc(g.NU); a.gv.alloc(g.NV); a.gw.alloc(g.NW);
     a.u1.alloc(g.NU); a.v1.alloc(g.NV); a.w1.alloc(g.NW);
-    for (int f = 0; f < 3; ++f) { a.lx[f].alloc(field_box(c, f).n); a.lb[f].alloc(field_box(c, f).n); }
-    a.rphi.alloc(g.NP); a.mu.alloc(g.NP);
+    a.mu.alloc(g.NP);
     a.dg.alloc(nyz); a.acc.alloc(1);
+    a.dweight.alloc(1);
+    if (!a.hweight) IBM_CUDA_TRY(cudaMallocHost((void **)&a.hweight, sizeof(double)));
     a.lu.zero(c->st); a.lv.zero(c->st); a.lw.zero(c->st); a.lp.zero(c->st);
     a.dg.zero(c->st); a.acc.zero(c->st);
     a.tape.clear();
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    // solver set-up of both contexts now rather than in the first reverse step
+    ensure_solvers(c);
+    {
+      Scope sc(a.t);
+      ensure_solvers(a.t);
+    }
     return IBM_OK;
   });
 }
@@ -1334,31 +1529,16 @@ int ibm_step_backward(ibm_ctx *c, double ramp, double weight, ibm_step_stats *st
     IBM_CUDA_TRY(cudaMemcpyAsync(a.u1.p, s0[0].p, sizeof(double) * c->g.NU, cudaMemcpyDeviceToDevice, c->st));
     IBM_CUDA_TRY(cudaMemcpyAsync(a.v1.p, s0[1].p, sizeof(double) * c->g.NV, cudaMemcpyDeviceToDevice, c->st));
     IBM_CUDA_TRY(cudaMemcpyAsync(a.w1.p, s0[2].p, sizeof(double) * c->g.NW, cudaMemcpyDeviceToDevice, c->st));
-    launch_bc(c, a.u1.p, a.v1.p, a.w1.p);
-    // reverse sweep
-    if (weight != 0.0) adj_force(c, weight);
-    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
-    adj_projection(c);
-    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
-    KResult r = transposed_solve(a.t, 3, a.rphi.p, a.mu.p);
-    int worst_rc = solve_status(r);
-    if (r.nonfinite) throw Error(IBM_ERR_NONFINITE, "non-finite transposed pressure solve");
-    adj_divergence(c, ramp);
-    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
-    adj_scatter(c);
-    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
-    for (int f = 0; f < 3; ++f) {
-      r = transposed_solve(a.t, f, a.lx[f].p, a.lb[f].p);
-      worst_rc = worst(worst_rc, solve_status(r));
-      if (r.nonfinite) throw Error(IBM_ERR_NONFINITE, "non-finite transposed momentum solve");
-    }
-    adj_momentum(c);
-    adj_gradient(c);
-    adj_bc(c, a.lu.p, a.lv.p, a.lw.p, ramp);
-    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    *a.hweight = weight;
+    const int rr = c->prm.use_graph ? reverse_graph(c) : (
+        [&]() {
+          IBM_CUDA_TRY(cudaMemcpyAsync(a.dweight.p, a.hweight, sizeof(double), cudaMemcpyHostToDevice, c->st));
+          launch_bc(c, a.u1.p, a.v1.p, a.w1.p);
+          return reverse_host(c);
+        })();
     IBM_CUDA_TRY(cudaGetLastError());
     c->prof.drain();
-    return worst(rc, worst_rc);
+    return worst(rc, rr);
   });
 }
 
@@ -1395,6 +1575,15 @@ int ibm_adjoint_get(ibm_ctx *c, double *lu, double *lv, double *lw, double *lp, 
     for (int q = 0; q < 6; ++q)
       if (dst[q]) IBM_CUDA_TRY(cudaMemcpyAsync(dst[q], src[q]->p, sizeof(double) * src[q]->n, cudaMemcpyDefault, c->st));
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    return IBM_OK;
+  });
+}
+
+int ibm_adjoint_solve_stats(ibm_ctx *c, ibm_solve_stats *out) {
+  return guarded(c, [&]() {
+    if (!out) throw Error(IBM_ERR_ARG, "ibm_adjoint_solve_stats: null output");
+    ibm::AdjState &a = adj_of(c);
+    for (int q = 0; q < 4; ++q) fill_solve(out[q], a.last[q]);
     return IBM_OK;
   });
 }

@@ -91,4 +91,5 @@ struct ibm_ctx {
   long long graph_body_launches[4] = {0, 0, 0, 0};
   // Adjoint extension: transposed-operator context, lambdas, tape, checkpoints.
   ibm::AdjState *adj = nullptr;
+  ibm_ctx *adj_owner = nullptr;       // a transposed-operator context: the context it serves
 };

@@ -272,6 +272,8 @@ int ibm_adjoint_reset(ibm_ctx *ctx);
 int ibm_adjoint_set(ibm_ctx *ctx, const double *lu, const double *lv, const double *lw, const double *lp);
 /* Lambdas, dJ/dg[ny*nz] and dJ/dnu[1]; any pointer may be NULL. */
 int ibm_adjoint_get(ibm_ctx *ctx, double *lu, double *lv, double *lw, double *lp, double *dg, double *dnu);
+/* The transposed solves of the last reverse sweep: out[4] = u, v, w, p. */
+int ibm_adjoint_solve_stats(ibm_ctx *ctx, ibm_solve_stats *out);
 int ibm_adjoint_tape_depth(ibm_ctx *ctx);
 /* Checkpoints of the state fields in device memory, by slot number, for
  * checkpointing with recomputation across many steps. */

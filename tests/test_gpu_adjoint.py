@@ -37,13 +37,16 @@ def rel_err(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
-def test_backward_step_matches_oracle(ibm, pyoracle):
+@pytest.mark.parametrize("graph", [0, 1])
+def test_backward_step_matches_oracle(ibm, pyoracle, graph):
+    """One reverse step, host-driven or as the captured graph (transposed
+    solves with their loops on the device)."""
     case = case_nu(ibm)
     o = pyoracle.Oracle(case, **ORACLE_KW)
     ot = pyoracle.Oracle(pyoracle.TransposedCase(case), **ORACLE_KW)
     o.step(1.0)
     s0 = o.fields()
-    s = ibm.Solver(case, fp64_params(ibm))
+    s = ibm.Solver(case, fp64_params(ibm, use_graph=graph))
     s.adjoint_setup()
     s.set_fields(*s0)
     rng = np.random.default_rng(11)
@@ -68,6 +71,20 @@ def test_backward_step_matches_oracle(ibm, pyoracle):
     o.step(1.0)
     for x, y, name in zip(s.fields(), o.fields(), "uvwp"):
         assert rel_err(x, y) <= 1e-9, name
+    # a second reverse step reuses the captured graph with another weight
+    s.set_fields(*s0)
+    s.adjoint_reset()
+    s.step_forward(1.0)
+    s.adjoint_set(*lam1)
+    s.step_backward(1.0, weight=0.0)
+    lam = [x.copy() for x in lam1]
+    dg_o = np.zeros(SHAPE[1] * SHAPE[2])
+    o.set_fields(*s0)
+    o.step_backward(ot, 1.0, case.array("beta_p"), 0.0, lam, dg_o)
+    lu, lv, lw, lp, dg, _ = s.adjoint_get()
+    for x, y, name in zip((lu, lv, lw, lp), lam, "uvwp"):
+        assert rel_err(x, y) <= 1e-8, name
+    assert rel_err(dg, dg_o) <= 1e-8
 
 
 def test_set_inflow_is_the_setup(ibm, inflow):
