@@ -16,6 +16,17 @@
 
 namespace ibm {
 
+// One step on the tape: its start state and what the reverse sweep needs of
+// its forward computation (the momentum right-hand sides and solutions, the
+// end-of-step fields), so that the reverse step does not recompute it.
+struct TapeEntry {
+  std::array<DBuf<double>, 4> s0;         // u, v, w, p at the step start
+  std::array<DBuf<double>, 3> b, x;       // momentum right-hand sides and solutions (solve boxes)
+  std::array<DBuf<double>, 4> s1;         // u, v, w, p at the step end
+  double ramp = 0.0;
+  ibm_step_stats stats;
+};
+
 struct AdjState {
   ibm_ctx *t = nullptr;                   // context on the transposed operators
   DBuf<double> lu, lv, lw, lp;            // lambda of the current state (full MAC arrays, cells)
@@ -27,7 +38,8 @@ struct AdjState {
   DBuf<double> mu;                        // Ap^-T of the projection's lambda (cells)
   DBuf<double> dweight;                   // objective weight of the step being reversed (device copy)
   double *hweight = nullptr;              // pinned staging copy
-  std::vector<std::array<DBuf<double>, 4>> tape;    // step-start states pushed by ibm_step_forward
+  std::vector<TapeEntry> tape;            // steps pushed by ibm_step_forward
+  std::vector<TapeEntry> spare;           // popped entries kept for reuse (no allocation per step)
   std::map<int, std::array<DBuf<double>, 4>> ckpt;  // checkpoints (ibm_checkpoint_save)
   // The reverse sweep captured as one graph (forward steps in graph mode):
   // the transposed solves run their loops on the device.

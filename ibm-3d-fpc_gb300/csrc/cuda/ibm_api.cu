@@ -1195,6 +1195,12 @@ std::array<DBuf<double>, 4> snapshot(ibm_ctx *c) {
   return s;
 }
 
+// Device copy of n doubles into dst (allocated to n).
+void copy_into(ibm_ctx *c, DBuf<double> &dst, const double *src, long n) {
+  dst.alloc(n);
+  IBM_CUDA_TRY(cudaMemcpyAsync(dst.p, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->st));
+}
+
 void restore(ibm_ctx *c, const std::array<DBuf<double>, 4> &s) {
   double *dst[4] = {c->u.p, c->v.p, c->w.p, c->p.p};
   for (int q = 0; q < 4; ++q)
@@ -1315,12 +1321,6 @@ void build_adjoint_graph(ibm_ctx *c) {
   a.gexec = nullptr;
   a.graph_ready = false;
   bind_transposed(c);
-  if (c->p_sym && !c->graph_bound) {
-    // the step's pressure solver, bound as the step graph binds it
-    const double *bp[1] = {c->bb[3].p};
-    double *xp[1] = {c->xb[3].p};
-    c->kp.bind(c->st, bp, xp, ~0u, c->prm.use_zero_initial_guess != 0);
-  }
   cudaStream_t st = c->st;
   Prof *saved_prof = current_prof();
   long long *saved_counter = g_counter;
@@ -1392,6 +1392,17 @@ void build_adjoint_graph(ibm_ctx *c) {
 int reverse_graph(ibm_ctx *c) {
   ibm::AdjState &a = *c->adj;
   ibm_ctx *t = a.t;
+  if (c->p_sym && !c->graph_bound) {
+    // as the step graph binds them (a host-driven solve on this context unbinds)
+    const bool zg = c->prm.use_zero_initial_guess != 0;
+    const double *bm[3] = {c->bb[0].p, c->bb[1].p, c->bb[2].p};
+    double *xm[3] = {c->xb[0].p, c->xb[1].p, c->xb[2].p};
+    const double *bp[1] = {c->bb[3].p};
+    double *xp[1] = {c->xb[3].p};
+    c->kmom.bind(c->st, bm, xm, ~0u, zg);
+    c->kp.bind(c->st, bp, xp, ~0u, zg);
+    c->graph_bound = true;
+  }
   if (!a.graph_ready) build_adjoint_graph(c);
   else if (!a.graph_bound) bind_transposed(c);
   IBM_CUDA_TRY(cudaGraphLaunch(a.gexec, c->st));
@@ -1506,9 +1517,28 @@ int ibm_step_forward(ibm_ctx *c, double ramp, ibm_step_stats *stats) {
   return guarded(c, [&]() {
     ibm::AdjState &a = adj_of(c);
     require_inputs(c);
-    a.tape.push_back(snapshot(c));
+    ibm::TapeEntry e;
+    if (!a.spare.empty()) {
+      e = std::move(a.spare.back());
+      a.spare.pop_back();
+    }
+    double *f[4] = {c->u.p, c->v.p, c->w.p, c->p.p};
+    const long n[4] = {c->g.NU, c->g.NV, c->g.NW, c->g.NP};
+    for (int q = 0; q < 4; ++q) copy_into(c, e.s0[q], f[q], n[q]);
     step_launch(c, ramp);
-    return step_collect(c, ramp, stats);
+    const int rc = step_collect(c, ramp, &e.stats);
+    if (rc >= 0) {
+      for (int q = 0; q < 3; ++q) {
+        copy_into(c, e.b[q], c->bb[q].p, field_box(c, q).n);
+        copy_into(c, e.x[q], c->xb[q].p, field_box(c, q).n);
+      }
+      for (int q = 0; q < 4; ++q) copy_into(c, e.s1[q], f[q], n[q]);
+      e.ramp = ramp;
+      IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+      a.tape.push_back(std::move(e));
+    }
+    if (stats) *stats = e.stats;
+    return rc;
   });
 }
 
@@ -1516,19 +1546,23 @@ int ibm_step_backward(ibm_ctx *c, double ramp, double weight, ibm_step_stats *st
   return guarded(c, [&]() {
     ibm::AdjState &a = adj_of(c);
     if (a.tape.empty()) throw Error(IBM_ERR_STATE, "ibm_step_backward: no step on the tape (ibm_step_forward)");
+    if (ramp != a.tape.back().ramp) throw Error(IBM_ERR_ARG, "ibm_step_backward: ramp differs from the taped step's");
     sync_transposed_params(c);
-    std::array<DBuf<double>, 4> s0 = std::move(a.tape.back());
+    ibm::TapeEntry e = std::move(a.tape.back());
     a.tape.pop_back();
-    // recompute the step from its start state: the momentum right-hand sides
-    // and solutions stay in bb / xb, the end-of-step fields in u, v, w, p
-    restore(c, s0);
-    step_launch(c, ramp);
-    int rc = step_collect(c, ramp, stats);
-    if (rc < 0) return rc;
+    // the taped step's forward results: momentum right-hand sides and
+    // solutions into bb / xb, the end-of-step fields into u, v, w, p
+    for (int q = 0; q < 3; ++q) {
+      IBM_CUDA_TRY(cudaMemcpyAsync(c->bb[q].p, e.b[q].p, sizeof(double) * e.b[q].n, cudaMemcpyDeviceToDevice, c->st));
+      IBM_CUDA_TRY(cudaMemcpyAsync(c->xb[q].p, e.x[q].p, sizeof(double) * e.x[q].n, cudaMemcpyDeviceToDevice, c->st));
+    }
+    restore(c, e.s1);
+    *c->hramp = ramp;
+    IBM_CUDA_TRY(cudaMemcpyAsync(c->dramp.p, c->hramp, sizeof(double), cudaMemcpyHostToDevice, c->st));
     // post-BC start velocities: the convection's linearisation point
-    IBM_CUDA_TRY(cudaMemcpyAsync(a.u1.p, s0[0].p, sizeof(double) * c->g.NU, cudaMemcpyDeviceToDevice, c->st));
-    IBM_CUDA_TRY(cudaMemcpyAsync(a.v1.p, s0[1].p, sizeof(double) * c->g.NV, cudaMemcpyDeviceToDevice, c->st));
-    IBM_CUDA_TRY(cudaMemcpyAsync(a.w1.p, s0[2].p, sizeof(double) * c->g.NW, cudaMemcpyDeviceToDevice, c->st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(a.u1.p, e.s0[0].p, sizeof(double) * c->g.NU, cudaMemcpyDeviceToDevice, c->st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(a.v1.p, e.s0[1].p, sizeof(double) * c->g.NV, cudaMemcpyDeviceToDevice, c->st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(a.w1.p, e.s0[2].p, sizeof(double) * c->g.NW, cudaMemcpyDeviceToDevice, c->st));
     *a.hweight = weight;
     const int rr = c->prm.use_graph ? reverse_graph(c) : (
         [&]() {
@@ -1538,6 +1572,9 @@ int ibm_step_backward(ibm_ctx *c, double ramp, double weight, ibm_step_stats *st
         })();
     IBM_CUDA_TRY(cudaGetLastError());
     c->prof.drain();
+    if (stats) *stats = e.stats;
+    const int rc = e.stats.status;
+    a.spare.push_back(std::move(e));
     return worst(rc, rr);
   });
 }
@@ -1547,6 +1584,7 @@ int ibm_adjoint_reset(ibm_ctx *c) {
     ibm::AdjState &a = adj_of(c);
     a.lu.zero(c->st); a.lv.zero(c->st); a.lw.zero(c->st); a.lp.zero(c->st);
     a.dg.zero(c->st); a.acc.zero(c->st);
+    for (auto &e : a.tape) a.spare.push_back(std::move(e));
     a.tape.clear();
     IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
     return IBM_OK;

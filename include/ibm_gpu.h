@@ -258,13 +258,14 @@ int ibm_adjoint_setup(ibm_ctx *ctx, const double *beta_p);
  * the inlet column's divergence lift, computed as the setup computes them
  * (bitwise the setup's arrays when g is its uin). */
 int ibm_set_inflow(ibm_ctx *ctx, const double *g);
-/* ibm_step that first pushes the step-start fields onto the context's tape
- * (device memory, one state per step). */
+/* ibm_step that also pushes the step onto the context's tape (device
+ * memory): its start and end fields and its momentum right-hand sides and
+ * solutions, what the reverse step needs of the forward computation. */
 int ibm_step_forward(ibm_ctx *ctx, double ramp, ibm_step_stats *stats);
-/* Pops the last step-start state, recomputes that step from it (the context
- * then holds its end-of-step fields; stats are the recomputed step's), adds
- * weight * dF_x/d(end-of-step fields) to the lambdas, and runs the reverse
- * sweep. `ramp` must be the step's own. */
+/* Pops the last taped step (the context then holds its end-of-step fields;
+ * stats are the taped step's), adds weight * dF_x/d(end-of-step fields) to
+ * the lambdas, and runs the reverse sweep. `ramp` must be the taped step's
+ * own (IBM_ERR_ARG otherwise). */
 int ibm_step_backward(ibm_ctx *ctx, double ramp, double weight, ibm_step_stats *stats);
 /* Lambdas, dJ/dg and dJ/dnu to zero; tape emptied. */
 int ibm_adjoint_reset(ibm_ctx *ctx);
