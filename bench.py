@@ -67,6 +67,11 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 256x48x48 adjoint-sensitivity measurement")
     ap.add_argument("--adjoint-steps", type=int, default=200, help="steps of the adjoint workload (objective "
                     "window: the second half)")
+    ap.add_argument("--long-run", type=int, default=0,
+                    help="also step the mixed and FP64 forms side by side for this many steps (the 2000-step "
+                         "full-timestep configuration) and report the drag/lift series and the field error")
+    ap.add_argument("--long-run-tol", type=float, default=1e-8,
+                    help="relative residual tolerance of both forms' solves in the long run")
     ap.add_argument("--ensemble", type=int, default=32, help="instances of the batched ensemble")
     ap.add_argument("--mg-coarse-max", type=int, default=2560,
                     help="multigrid: largest level solved directly (dense inverse)")
@@ -366,6 +371,55 @@ def adjoint_measure(ibm, args, local):
                          "nu_rel_err": abs(dnu - fd_nu) / abs(fd_nu), "h": h},
             "note": "host wall time (each step and solve waits for its results); FP64 steps and transposed solves "
                     "at a 1e-12 relative residual"}
+
+
+def long_run_measure(ibm, args, local, nx, ny, nz):
+    """The full-timestep workload stepped n times in the mixed form and in
+    plain FP64 side by side (graph-captured both, from the same seeded
+    initial state, no ramp): drag and lift every 10 steps for both forms,
+    and every 100 steps the largest velocity difference relative to the
+    FP64 run's largest |u| (and the same for p)."""
+    n = args.long_run
+    case = ibm.Case(case_params(ibm, nx, ny, nz))
+    state = initial_state(case)
+    forms = []
+    for precision in (args.precision, 0):
+        prm = solver_params(ibm, precision, graph=1, coarse_max=args.mg_coarse_max)
+        prm.compute_forces = 1
+        prm.vel_tol = prm.p_tol = args.long_run_tol
+        s = ibm.Solver(case, prm, device=local)
+        s.set_fields(*state)
+        forms.append(s)
+    series, errors = [], []
+    worst = 0
+    t0 = time.perf_counter()
+    for k in range(1, n + 1):
+        st = [s.step(1.0) for s in forms]
+        worst = max(worst, st[0].status, st[1].status)
+        if k % 10 == 0:
+            series.append([k, st[0].force[0], st[0].force[1], st[1].force[0], st[1].force[1]])
+        if k % 100 == 0 or k == n:
+            fm, f64 = forms[0].fields(), forms[1].fields()
+            umax = max(float(np.abs(x).max()) for x in f64[:3])
+            vel = max(float(np.abs(a - b).max()) for a, b in zip(fm[:3], f64[:3])) / umax
+            pr = float(np.abs(fm[3] - f64[3]).max()) / max(float(np.abs(f64[3]).max()), 1e-300)
+            errors.append([k, vel, pr])
+    wall = time.perf_counter() - t0
+    for s in forms:
+        s.close()
+    D, U = 0.1, 1.0  # diameter; mean inflow over the square section (4/9 of the peak 2.25)
+    H = case.params.Ly
+    coef = 2.0 / (case.params.rho * U * U * D * H)
+    return {"workload": f"{n} steps of the full timestep {nx}x{ny}x{nz}, mixed (precision {args.precision}) and "
+                        f"plain FP64 side by side, graph-captured, no ramp, solves to {args.long_run_tol:g}",
+            "steps": n, "worst_status": int(worst), "wall_s": wall,
+            "velocity_rel_err_max": max(e[1] for e in errors), "velocity_rel_err_final": errors[-1][1],
+            "pressure_rel_err_final": errors[-1][2],
+            "errors_every_100": errors,
+            "force_coefficients": "c = 2 F / (rho U^2 D H), U = 1 (mean inflow), D = 0.1, H = Lz",
+            "cD_final": [series[-1][1] * coef, series[-1][3] * coef] if series else None,
+            "cL_final": [series[-1][2] * coef, series[-1][4] * coef] if series else None,
+            "drag_lift_every_10": series}
 
 
 def run_steps(solver, n):
@@ -683,6 +737,11 @@ def main():
             out["pressure_only"] = pressure_only_measure(ibm, args, local, plib, Prof)
         except Exception as e:  # the line must still print
             out["pressure_only"] = {"value": None, "error": str(e)}
+    if rank == 0 and args.long_run > 0:
+        try:
+            out["long_run"] = long_run_measure(ibm, args, local, nx, ny, nz)
+        except Exception as e:  # the line must still print
+            out["long_run"] = {"value": None, "error": str(e)}
     if rank == 0 and not args.no_adjoint:
         try:
             out["adjoint"] = adjoint_measure(ibm, args, local)
