@@ -110,3 +110,83 @@ def test_oracle_adjoint_is_the_transpose_of_the_step(ibm, pyoracle, inflow):
     lhs = sum(float(l @ d) for l, d in zip(lam, ds))
     rhs = sum(float(l @ ((a - b) / (2 * h))) for l, a, b in zip(lam1, sp, sm))
     assert abs(lhs - rhs) <= 1e-6 * abs(rhs)
+
+
+class _FakeSolver:
+    """Records the calls of Solver.drag_gradient (no GPU): each step adds
+    the ramp to a scalar state, the drag is the state itself."""
+
+    def __init__(self, ibm):
+        self.ibm = ibm
+        self.params = ibm._native.SolverParams()
+        self.state = 0.0
+        self.tape = []
+        self.ckpt = {}
+        self.calls = []
+
+    def set_params(self, p):
+        self.params = p
+
+    def adjoint_reset(self):
+        self.tape.clear()
+        self.calls.append("reset")
+
+    def checkpoint_clear(self):
+        self.ckpt.clear()
+
+    def checkpoint_save(self, slot):
+        self.ckpt[slot] = self.state
+
+    def checkpoint_load(self, slot):
+        self.state = self.ckpt[slot]
+
+    def _advance(self, ramp):
+        self.state += ramp
+        st = self.ibm.StepStats()
+        st.force[0] = self.state
+        return st
+
+    def step(self, ramp):
+        self.calls.append(("step", ramp))
+        return self._advance(ramp)
+
+    def step_forward(self, ramp):
+        self.calls.append(("fwd", ramp, self.state))
+        self.tape.append((self.state, ramp))
+        return self._advance(ramp)
+
+    def step_backward(self, ramp, weight):
+        start, r = self.tape.pop()
+        assert r == ramp
+        self.calls.append(("bwd", ramp, start, weight))
+        return self.ibm.StepStats()
+
+    def fields(self):
+        return (self.state,)
+
+    def set_fields(self, *f):
+        self.state = f[0]
+
+    def adjoint_get(self):
+        return None, None, None, None, "dg", "dnu"
+
+
+def test_drag_gradient_checkpoint_schedule(ibm):
+    """The reverse sweep replays each checkpoint segment and reverses its
+    steps in order, with the step's own ramp and weight 1/|window| inside
+    the objective window; the fields end at the forward sweep's end."""
+    fake = _FakeSolver(ibm)
+    ramps = [0.1 * k for k in range(1, 8)]
+    J, dg, dnu = ibm.Solver.drag_gradient(fake, ramps, window={5, 6, 7}, checkpoint_every=3)
+    states = np.cumsum(ramps)
+    assert J == pytest.approx(states[4:].mean())
+    assert fake.state == pytest.approx(states[-1])
+    bwd = [c for c in fake.calls if c[0] == "bwd"]
+    assert [b[1] for b in bwd] == ramps[::-1]
+    starts = np.concatenate([[0.0], states[:-1]])
+    assert [b[2] for b in bwd] == pytest.approx(list(starts[::-1]))
+    assert [b[3] for b in bwd] == pytest.approx([1 / 3] * 3 + [0.0] * 4)
+    # segments 7, 4-6, 1-3: each replayed from its checkpoint right before its reversal
+    order = [c[0] for c in fake.calls if c[0] in ("fwd", "bwd")]
+    assert order == ["fwd"] + ["bwd"] + ["fwd"] * 3 + ["bwd"] * 3 + ["fwd"] * 3 + ["bwd"] * 3
+    assert fake.params.compute_forces == 1
