@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--long-run-tol", type=float, default=1e-8,
                     help="relative residual tolerance of both forms' solves in the long run")
     ap.add_argument("--ensemble", type=int, default=32, help="instances of the batched ensemble")
+    ap.add_argument("--ensemble-autotune", action="store_true",
+                    help="also tune the ensemble's multigrid schedule by size class (autotune.py) and measure it")
     ap.add_argument("--mg-coarse-max", type=int, default=2560,
                     help="multigrid: largest level solved directly (dense inverse)")
     ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
@@ -239,10 +241,30 @@ def ensemble_measure(ibm, args, ws, rank, local, steps, warmup):
         for s in batch.solvers:
             s.step(1.0)
     t_seq = reduce_max_ms((time.perf_counter() - t0) * 1e3, ws, "cuda")
+    tuned = None
+    if args.ensemble_autotune:
+        at = importlib.import_module("ibm-3d-fpc_gb300.autotune")
+        t0 = time.perf_counter()
+        applied, report = at.tune_batch(batch.solvers, nbuckets=4)
+        tune_s = time.perf_counter() - t0
+        for _ in range(warmup):
+            batch.step(1.0)
+        if ws > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            worst = max(worst, max(st.status for st in batch.step(1.0)))
+        t_tuned = reduce_max_ms((time.perf_counter() - t0) * 1e3, ws, "cuda")
+        tuned = {"instance_steps_per_s": len(specs) * steps / (t_tuned / 1e3), "tune_s": tune_s,
+                 "classes": {k: {"representative": v["representative"], "instances": v["instances"],
+                                 "chosen": v["chosen"]} for k, v in report.items()},
+                 "note": "median instance of each of 4 log-spaced cell-count classes tuned over 5 multigrid "
+                         "schedules (3 timed steps each), the winner applied to its class"}
     cells = sum(nx * ny * nz for nx, ny, nz, *_ in specs)
     batch.close()
     n = len(specs)
-    return {"workload": f"{n} independent channels, seeded sizes {{96..256}}x{{16..48}}x{{16..48}} (multiples of 16), "
+    out_tuned = {"autotuned": tuned} if tuned else {}
+    return {**out_tuned, "workload": f"{n} independent channels, seeded sizes {{96..256}}x{{16..48}}x{{16..48}} (multiples of 16), "
                         "cylinder D U(0.06,0.14) at y U(0.15,0.26), Um U(0.2,2.25), dt 1e-3, same solver settings",
             "instances": n, "cells": cells, "steps": steps,
             "instance_steps_per_s": n * steps / (t_batch / 1e3),

@@ -69,3 +69,25 @@ def test_batch_reports_a_failing_instance(ibm):
         st = batch.solvers[i].step(1.0)
         assert st.status == ibm.IBM_OK
     batch.close()
+
+
+def test_autotuned_batch_converges_to_the_same_fields(ibm):
+    """The autotuner changes the multigrid schedule, not the tolerance: the
+    tuned instances step to the untuned fields within the solves' tolerance."""
+    import importlib
+    at = importlib.import_module("ibm-3d-fpc_gb300.autotune")
+    cases = instances(ibm)
+    prm = [params(ibm, 1) for _ in cases]
+    tuned = ibm.Batch(cases, prm)
+    plain = ibm.Batch(cases, prm)
+    applied, report = at.tune_batch(tuned.solvers, nbuckets=2, steps=2, warmup=1)
+    assert all(a is not None for a in applied)
+    assert any(r["trials"] for r in report.values())
+    for _ in range(3):
+        for st in tuned.step([1.0] * 3) + plain.step([1.0] * 3):
+            assert st.status == ibm.IBM_OK
+    for a, b in zip(tuned.solvers, plain.solvers):
+        for x, y, name in zip(a.fields(), b.fields(), "uvwp"):
+            assert np.abs(x - y).max() <= 1e-7 * max(np.abs(y).max(), 1e-30), name
+    tuned.close()
+    plain.close()
