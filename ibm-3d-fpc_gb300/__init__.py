@@ -326,6 +326,24 @@ class Solver:
         return out
 
 
+def write_vtk(path: str, case: Case, u, v, w, p) -> None:
+    """Fields in the reference's VTK format (ibm_write_vtk, include/ibm_host.h)."""
+    cp = case.params
+    arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (u, v, w, p)]
+    fluid = np.ascontiguousarray(case.array("fluid_p"), dtype=np.uint8)
+    rc = _native.host().ibm_write_vtk(path.encode(), *[_ptr(x) for x in arrs], _ptr(fluid), cp.nx, cp.ny, cp.nz,
+                                      cp.Lx, cp.Ly, cp.Lz)
+    if rc != 0:
+        raise IBMError(rc, f"ibm_write_vtk could not write {path}")
+
+
+def vtk_step_name(base: str, step: int) -> str:
+    """The reference's per-step VTK file name (stem + _%06d + extension)."""
+    buf = C.create_string_buffer(4096)
+    _native.host().ibm_vtk_step_name(base.encode(), step, buf, len(buf))
+    return buf.value.decode()
+
+
 def grid_desc(case: Case, device: int = 0) -> GridDesc:
     cp = case.params
     return GridDesc(cp.nx, cp.ny, cp.nz, cp.Lx, cp.Ly, cp.Lz, cp.rho, cp.nu, cp.dt, device)

@@ -102,6 +102,8 @@ def host() -> C.CDLL:
         lib.ibm_case_array.argtypes = [vp, C.c_char_p]
         lib.ibm_case_array.restype = vp
         lib.ibm_host_check_sum_order.argtypes = [C.c_int, C.c_uint]
+        lib.ibm_write_vtk.argtypes = [C.c_char_p] + [vp] * 5 + [C.c_int] * 3 + [C.c_double] * 3
+        lib.ibm_vtk_step_name.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_int]
         _host = lib
     return _host
 

@@ -26,6 +26,11 @@ struct Options {
   std::string checkpoint_prefix = "ibm_state";
   std::string restart;      // checkpoint file to resume from (its step + 1 is the first step run)
   std::string case_cache;   // case cache file (ibm_case_build_cached)
+  // VTK output with the reference's flags and file names (common.hpp:82-84,
+  // main.cu:370-378); off unless -write-vtk 1 is given: the reference's
+  // default writes an ASCII file every step, outside the hot path
+  int write_vtk = 0, vtk_every = 0;
+  std::string vtk_filename = "st3d_channel_cylinder_struct_mac_cuda.vtk";
 };
 
 bool arg(int &a, int argc, char **argv, const char *name) { return !std::strcmp(argv[a], name) && a + 1 < argc; }
@@ -65,9 +70,9 @@ void parse(int argc, char **argv, Options &o) {
     else if (arg(a, argc, argv, "-p-pc-maxit")) o.sp.p_pc_maxit = std::atoi(argv[++a]);
     else if (arg(a, argc, argv, "-p-pc-relax-type")) o.sp.p_pc_relax_type = std::atoi(argv[++a]);
     else if (arg(a, argc, argv, "-p-pc-rap-type")) o.sp.p_pc_rap_type = std::atoi(argv[++a]);
-    else if (arg(a, argc, argv, "-write-vtk")) ++a;  // file output is outside the hot path
-    else if (arg(a, argc, argv, "-vtk-every")) ++a;
-    else if (arg(a, argc, argv, "-vtk")) ++a;
+    else if (arg(a, argc, argv, "-write-vtk")) o.write_vtk = std::atoi(argv[++a]);
+    else if (arg(a, argc, argv, "-vtk-every")) o.vtk_every = std::atoi(argv[++a]);
+    else if (arg(a, argc, argv, "-vtk")) o.vtk_filename = argv[++a];
     // options of this implementation
     else if (arg(a, argc, argv, "-precision")) o.sp.precision = std::atoi(argv[++a]);
     else if (arg(a, argc, argv, "-use-graph")) o.sp.use_graph = std::atoi(argv[++a]);
@@ -204,6 +209,14 @@ int main(int argc, char **argv) {
         std::printf("  cD %.5f cL %.5f", st.force[0] * sc, st.force[1] * sc);
       }
       std::printf("\n");
+    }
+    if (o.write_vtk && (step == 1 || step == o.nsteps || step % std::max(1, o.vtk_every) == 0)) {
+      ibm_get_fields(ctx, u.data(), v.data(), w.data(), p.data());
+      char name[4096];
+      ibm_vtk_step_name(o.vtk_filename.c_str(), step, name, (int)sizeof(name));
+      if (ibm_write_vtk(name, u.data(), v.data(), w.data(), p.data(), arr<uint8_t>(cs, "fluid_p"), nx, ny, nz,
+                        o.cp.Lx, o.cp.Ly, o.cp.Lz) != 0)
+        std::fprintf(stderr, "step %d: could not write %s\n", step, name);
     }
     if (o.checkpoint_every > 0 && step % o.checkpoint_every == 0) {
       ibm_get_fields(ctx, u.data(), v.data(), w.data(), p.data());

@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <map>
@@ -723,6 +724,54 @@ int ibm_case_build_cached(const ibm_case_params *p, const char *path, ibm_case *
   if (b != 0) return b;
   ibm_case_save(*out, path);  // a cache that cannot be written is not an error
   return 0;
+}
+
+int ibm_write_vtk(const char *path, const double *u, const double *v, const double *w, const double *p,
+                  const uint8_t *fluid_p, int nx, int ny, int nz, double Lx, double Ly, double Lz) {
+  if (!path || !u || !v || !w || !p || !fluid_p || nx < 1 || ny < 1 || nz < 1) return -1;
+  std::FILE *f = std::fopen(path, "w");
+  if (!f) return -2;
+  const long sy = nx + 1, sz = (long)(nx + 1) * ny;              // u strides
+  const long vy = nx, vz = (long)nx * (ny + 1);                   // v strides
+  const long wz = (long)nx * ny;                                  // w plane
+  std::fprintf(f, "# vtk DataFile Version 3.0\n3D immersed cylinder MAC cell-centered\nASCII\n"
+                  "DATASET STRUCTURED_POINTS\nDIMENSIONS %d %d %d\nORIGIN 0 0 0\nSPACING %.16e %.16e %.16e\n"
+                  "CELL_DATA %d\n", nx + 1, ny + 1, nz + 1, Lx / nx, Ly / ny, Lz / nz, nx * ny * nz);
+  std::fprintf(f, "SCALARS ux double 1\nLOOKUP_TABLE default\n");
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const long a = k * sz + j * sy + i;
+        std::fprintf(f, "%.16e\n", 0.5 * (u[a] + u[a + 1]));
+      }
+  std::fprintf(f, "SCALARS uy double 1\nLOOKUP_TABLE default\n");
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        const long a = k * vz + j * vy + i;
+        std::fprintf(f, "%.16e\n", 0.5 * (v[a] + v[a + vy]));
+      }
+  std::fprintf(f, "SCALARS uz double 1\nLOOKUP_TABLE default\n");
+  for (long c = 0; c < (long)nx * ny * nz; ++c) std::fprintf(f, "%.16e\n", 0.5 * (w[c] + w[c + wz]));
+  std::fprintf(f, "SCALARS pressure double 1\nLOOKUP_TABLE default\n");
+  for (long c = 0; c < (long)nx * ny * nz; ++c) std::fprintf(f, "%.16e\n", p[c]);
+  std::fprintf(f, "SCALARS fluid_mask int 1\nLOOKUP_TABLE default\n");
+  for (long c = 0; c < (long)nx * ny * nz; ++c) std::fprintf(f, "%d\n", fluid_p[c] ? 1 : 0);
+  const int bad = std::ferror(f);
+  return (std::fclose(f) == 0 && !bad) ? 0 : -2;
+}
+
+int ibm_vtk_step_name(const char *base, int step, char *out, int len) {
+  if (!base || !out || len < 1) return -1;
+  const std::string b(base);
+  const size_t dot = b.find_last_of('.');
+  const std::string stem = dot == std::string::npos ? b : b.substr(0, dot);
+  const std::string ext = dot == std::string::npos ? std::string() : b.substr(dot);
+  char num[32];
+  std::snprintf(num, sizeof(num), "_%06d", step);
+  const std::string name = stem + num + ext;
+  std::snprintf(out, (size_t)len, "%s", name.c_str());
+  return (int)name.size();
 }
 
 int ibm_host_check_sum_order(int ntrials, unsigned seed) {

@@ -82,6 +82,18 @@ int ibm_case_load(const ibm_case_params *p, const char *path, ibm_case **out);
 int ibm_case_build_cached(const ibm_case_params *p, const char *path, ibm_case **out);
 
 /*
+ * Field output in the reference's VTK format (write_vtk_cellcentered,
+ * immersed_operators.hpp:1055-1076): legacy ASCII STRUCTURED_POINTS with
+ * cell data ux, uy, uz (face averages), pressure and fluid_mask, values as
+ * %.16e. Returns 0, -1 on bad arguments, -2 on I/O errors.
+ * ibm_vtk_step_name gives the reference's per-step name (base stem +
+ * "_%06d" + extension, solver_helpers.hpp:470-482) and returns its length.
+ */
+int ibm_write_vtk(const char *path, const double *u, const double *v, const double *w, const double *p,
+                  const uint8_t *fluid_p, int nx, int ny, int nz, double Lx, double Ly, double Lz);
+int ibm_vtk_step_name(const char *base, int step, char *out, int len);
+
+/*
  * Self-check of the hash-iteration-order model used to reproduce the
  * reference's summation order: inserts ntrials random key sets into the real
  * standard-library hash map this library was compiled with and compares the

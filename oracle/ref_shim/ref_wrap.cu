@@ -214,4 +214,21 @@ void ref_convection(double *cu, double *cv, double *cw, const double *u, const d
   std::memcpy(cu, CU.data(), NU * 8); std::memcpy(cv, CV.data(), NV * 8); std::memcpy(cw, CW.data(), NW * 8);
 }
 
+// The reference's VTK writer (immersed_operators.hpp:1055-1076) and its
+// per-step file name (solver_helpers.hpp:470-482).
+void ref_write_vtk(const char *path, const double *u, const double *v, const double *w, const double *p,
+                   const unsigned char *fluid, int nx, int ny, int nz, double Lx, double Ly, double Lz) {
+  size_t NU = (size_t)(nx + 1) * ny * nz, NV = (size_t)nx * (ny + 1) * nz, NW = (size_t)nx * ny * (nz + 1),
+         NP = (size_t)nx * ny * nz;
+  std::vector<double> U(u, u + NU), V(v, v + NV), W(w, w + NW), P(p, p + NP);
+  std::vector<char> F(fluid, fluid + NP);
+  write_vtk_cellcentered(path, U, V, W, P, F, nx, ny, nz, Lx, Ly, Lz);
+}
+
+int ref_vtk_step_name(const char *base, int step, char *out, int len) {
+  const std::string s = vtk_filename_with_step(base, step);
+  std::snprintf(out, (size_t)len, "%s", s.c_str());
+  return (int)s.size();
+}
+
 }  // extern "C"
