@@ -57,3 +57,21 @@ def test_restart_rejects_other_grid(tmp_path):
     args = [EXE, "-nx", "40", "-ny", "12", "-nz", "12", "-nsteps", "5", "-restart", str(tmp_path / "a_3.bin")]
     out = subprocess.run(args, cwd=tmp_path, capture_output=True, text=True, timeout=300)
     assert out.returncode != 0 and "not a checkpoint" in out.stderr
+
+
+def test_vtk_output_follows_the_reference_flags(tmp_path, ibm):
+    """-write-vtk 1 -vtk-every 4 over 6 steps writes steps 1, 4 and 6 (the
+    reference's rule: first, last and every N-th), named stem_%06d.vtk, and
+    the last file holds the last checkpoint's fields."""
+    if not os.path.exists(EXE):
+        pytest.skip("ibm_run not built")
+    _run(tmp_path, "-checkpoint", "c", "-write-vtk", "1", "-vtk-every", "4", "-vtk", "flow.vtk")
+    names = sorted(f for f in os.listdir(tmp_path) if f.endswith(".vtk"))
+    assert names == ["flow_000001.vtk", "flow_000004.vtk", "flow_000006.vtk"]
+    _, f6 = _fields(tmp_path / "c_6.bin")
+    nx, ny, nz = 32, 12, 12
+    nu_, nv_, nw_ = (nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1)
+    p = f6[nu_ + nv_ + nw_:]
+    lines = (tmp_path / "flow_000006.vtk").read_text().splitlines()
+    k = lines.index("SCALARS pressure double 1")
+    assert np.array_equal(np.array(lines[k + 2:k + 2 + nx * ny * nz], dtype=float), p)
