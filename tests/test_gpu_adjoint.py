@@ -171,3 +171,31 @@ def test_mixed_precision_graph_adjoint(ibm, inflow):
     assert abs(J1 - J0) <= 1e-8 * abs(J0)
     assert rel_err(dg1, dg0) <= 1e-6
     assert abs(dnu1 - dnu0) <= 1e-6 * abs(dnu0)
+
+
+@pytest.mark.parametrize("shape,graph", [((36, 10, 7), 0), ((20, 9, 11), 1)])
+def test_backward_step_odd_grids(ibm, pyoracle, shape, graph):
+    """Odd line and plane counts: the boundary planes, the convection's
+    fallbacks and the solve boxes' edges in the reverse kernels."""
+    case = ibm.Case(ibm.channel_params(*shape, Um=1.0, dt=2e-3))
+    o = pyoracle.Oracle(case, **ORACLE_KW)
+    ot = pyoracle.Oracle(pyoracle.TransposedCase(case), **ORACLE_KW)
+    o.step(1.0)
+    s0 = o.fields()
+    s = ibm.Solver(case, fp64_params(ibm, use_graph=graph))
+    s.adjoint_setup()
+    s.set_fields(*s0)
+    rng = np.random.default_rng(12)
+    lam1 = [rng.standard_normal(x.size) for x in s0]
+    s.step_forward(0.7)
+    s.adjoint_set(*lam1)
+    s.step_backward(0.7, weight=0.2)
+    lu, lv, lw, lp, dg, dnu = s.adjoint_get()
+    lam = [x.copy() for x in lam1]
+    dg_o = np.zeros(shape[1] * shape[2])
+    o.set_fields(*s0)
+    dnu_o = o.step_backward(ot, 0.7, case.array("beta_p"), 0.2, lam, dg_o)
+    for x, y, name in zip((lu, lv, lw, lp), lam, "uvwp"):
+        assert rel_err(x, y) <= 1e-8, name
+    assert rel_err(dg, dg_o) <= 1e-8
+    assert abs(dnu - dnu_o) <= 1e-8 * max(abs(dnu_o), 1e-30)
