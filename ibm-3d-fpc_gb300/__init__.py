@@ -221,6 +221,22 @@ class Solver:
         self._check(self._lib.ibm_profile_get(self._ctx, C.byref(p)))
         return p
 
+    def assemble_momentum(self):
+        """Assembles the three momentum operators on the GPU from the case's
+        masks and ids (ibm_assemble_momentum) and sets them on the context;
+        returns their row-major values and id-indexed row scales."""
+        nx, ny, nz = self.case.shape
+        cp = self.case.params
+        vals = [np.empty(7 * n) for n in ((nx - 1) * ny * nz, nx * (ny - 1) * nz, nx * ny * (nz - 1))]
+        act = [np.ascontiguousarray(self.case.array(f"active_{f}"), dtype=np.uint8) for f in "uvw"]
+        ids = [np.ascontiguousarray(self.case.array(f"id_{f}"), dtype=np.int32) for f in "uvw"]
+        scales = [np.empty(int(i.max()) + 1) for i in ids]
+        P = C.c_void_p * 3
+        self._check(self._lib.ibm_assemble_momentum(
+            self._ctx, cp.xcirc, cp.ycirc, cp.Rcirc, P(*[a.ctypes.data for a in act]),
+            P(*[a.ctypes.data for a in ids]), P(*[a.ctypes.data for a in vals]), P(*[a.ctypes.data for a in scales])))
+        return vals, scales
+
     # ---------------------------------------------------------- adjoint extension
     def adjoint_setup(self) -> None:
         """Transposed-operator context and inlet weights (ibm_adjoint_setup)."""

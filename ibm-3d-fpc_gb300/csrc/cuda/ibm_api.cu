@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "ibm_adjoint.cuh"
+#include "ibm_assembly.cuh"
 #include "ibm_ctx.cuh"
 #include "ibm_step.cuh"
 
@@ -564,6 +565,56 @@ int ibm_set_operator(ibm_ctx *c, int field, const double *vals7, int nbx, int nb
     o.set = true;
     c->solvers_ready = false;
     invalidate_graph(c);
+    return IBM_OK;
+  });
+}
+
+}  // extern "C"
+
+namespace ibm {
+void launch_assemble_momentum(cudaStream_t st, int f, long n, const asmb::Geo &g, const unsigned char *act,
+                              const int *id, double *rows, double *scale);
+}
+
+extern "C" {
+
+int ibm_assemble_momentum(ibm_ctx *c, double xcirc, double ycirc, double Rcirc, const uint8_t *const *active,
+                          const int32_t *const *id, double *const *vals_out, double *const *scale_out) {
+  return guarded(c, [&]() {
+    if (!active || !id) throw Error(IBM_ERR_ARG, "ibm_assemble_momentum: null masks or ids");
+    const Geometry &g = c->g;
+    asmb::Geo geo;
+    geo.nx = g.nx; geo.ny = g.ny; geo.nz = g.nz;
+    geo.Lx = c->grid.Lx; geo.Ly = c->grid.Ly; geo.Lz = c->grid.Lz;
+    geo.rho = c->grid.rho; geo.nu = c->grid.nu; geo.dt = c->grid.dt;
+    geo.xcirc = xcirc; geo.ycirc = ycirc; geo.Rcirc = Rcirc;
+    const long nf[3] = {g.NU, g.NV, g.NW};
+    for (int f = 0; f < 3; ++f) {
+      if (!active[f] || !id[f]) throw Error(IBM_ERR_ARG, "ibm_assemble_momentum: null mask or id array");
+      DBuf<uint8_t> dact;
+      DBuf<int32_t> did;
+      dact.alloc(nf[f]);
+      did.alloc(nf[f]);
+      IBM_CUDA_TRY(cudaMemcpyAsync(dact.p, active[f], nf[f], cudaMemcpyDefault, c->st));
+      IBM_CUDA_TRY(cudaMemcpyAsync(did.p, id[f], sizeof(int32_t) * nf[f], cudaMemcpyDefault, c->st));
+      const std::vector<int32_t> hid = to_host(id[f], (size_t)nf[f]);
+      const int nid = hid.empty() ? 0 : *std::max_element(hid.begin(), hid.end());
+      const Box &b = field_box(c, f);
+      DBuf<double> rows, sc;
+      rows.alloc((size_t)7 * b.n);
+      sc.alloc((size_t)nid + 1);
+      const std::vector<double> ones((size_t)nid + 1, 1.0);
+      IBM_CUDA_TRY(cudaMemcpyAsync(sc.p, ones.data(), sizeof(double) * ones.size(), cudaMemcpyHostToDevice, c->st));
+      launch_assemble_momentum(c->st, f, b.n, geo, dact.p, did.p, rows.p, sc.p);
+      IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+      IBM_CUDA_TRY(cudaGetLastError());
+      if (vals_out && vals_out[f])
+        IBM_CUDA_TRY(cudaMemcpy(vals_out[f], rows.p, sizeof(double) * 7 * b.n, cudaMemcpyDefault));
+      if (scale_out && scale_out[f])
+        IBM_CUDA_TRY(cudaMemcpy(scale_out[f], sc.p, sizeof(double) * ones.size(), cudaMemcpyDefault));
+      const int rc = ibm_set_operator(c, f, rows.p, b.nx, b.ny, b.nz);
+      if (rc < 0) throw Error(rc, c->err);
+    }
     return IBM_OK;
   });
 }

@@ -165,6 +165,18 @@ int ibm_set_projection_csr(ibm_ctx *ctx, const int32_t *D_rowptr, const int32_t 
                            int D_nrows, const int32_t *G_rowptr, const int32_t *G_col, const double *G_val,
                            int G_nrows);
 
+/* GPU assembly of the three momentum operators (immersed_operators.hpp:1-177,
+ * row-scaled as main.cu:98-100) from the active masks and 1-based ids of the
+ * u, v, w faces (full MAC layouts, as ibm_set_masks takes them; host or
+ * device pointers) and the cylinder (centre, radius), with the context's
+ * grid, rho, nu and dt. Every row and row scale is bitwise the CPU setup's.
+ * The operators are set on the context as ibm_set_operator sets them;
+ * vals_out[f] (the row-major [box rows][7] values) and scale_out[f] (the
+ * id-indexed row scales, max id + 1 values, index 0 = 1) are written when
+ * the arrays and their entries are not NULL (host or device pointers). */
+int ibm_assemble_momentum(ibm_ctx *ctx, double xcirc, double ycirc, double Rcirc, const uint8_t *const *active,
+                          const int32_t *const *id, double *const *vals_out, double *const *scale_out);
+
 /* Solver configuration (main.cu:173-221). */
 void ibm_solver_params_default(ibm_solver_params *p);
 int ibm_set_solver_params(ibm_ctx *ctx, const ibm_solver_params *p);
