@@ -237,6 +237,25 @@ class Solver:
             P(*[a.ctypes.data for a in ids]), P(*[a.ctypes.data for a in vals]), P(*[a.ctypes.data for a in scales])))
         return vals, scales
 
+    def assemble_pressure(self):
+        """Assembles the pressure operator on the GPU from the case's
+        fractions, masks and ids (ibm_assemble_pressure) and sets it on the
+        context; returns its row-major values."""
+        a = self.case.array
+        nx, ny, nz = self.case.shape
+        vals = np.empty(7 * nx * ny * nz)
+        fl = np.ascontiguousarray(a("fluid_p"), dtype=np.uint8)
+        idp = np.ascontiguousarray(a("id_p"), dtype=np.int32)
+        beta = np.ascontiguousarray(a("beta_p"), dtype=np.float64)
+        al = [np.ascontiguousarray(a(f"alpha_{f}"), dtype=np.float64) for f in "uvw"]
+        aq = [np.ascontiguousarray(a(f"active_q{f}"), dtype=np.uint8) for f in "uvw"]
+        iq = [np.ascontiguousarray(a(f"id_q{f}"), dtype=np.int32) for f in "uvw"]
+        P = C.c_void_p * 3
+        self._check(self._lib.ibm_assemble_pressure(
+            self._ctx, _ptr(fl), _ptr(idp), _ptr(beta), P(*[x.ctypes.data for x in al]),
+            P(*[x.ctypes.data for x in aq]), P(*[x.ctypes.data for x in iq]), _ptr(vals)))
+        return vals
+
     # ---------------------------------------------------------- adjoint extension
     def adjoint_setup(self) -> None:
         """Transposed-operator context and inlet weights (ibm_adjoint_setup)."""

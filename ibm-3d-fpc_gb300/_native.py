@@ -152,6 +152,7 @@ def gpu() -> C.CDLL:
         lib.ibm_kernel_launches.restype = C.c_longlong
         lib.ibm_device_query.argtypes = [i, C.c_char_p, i]
         lib.ibm_assemble_momentum.argtypes = [vp, d, d, d, vp * 3, vp * 3, vp * 3, vp * 3]
+        lib.ibm_assemble_pressure.argtypes = [vp, vp, vp, vp, vp * 3, vp * 3, vp * 3, vp]
         lib.ibm_adjoint_setup.argtypes = [vp, vp]
         lib.ibm_set_inflow.argtypes = [vp, vp]
         lib.ibm_step_forward.argtypes = [vp, d, P(StepStats)]

@@ -574,6 +574,7 @@ int ibm_set_operator(ibm_ctx *c, int field, const double *vals7, int nbx, int nb
 namespace ibm {
 void launch_assemble_momentum(cudaStream_t st, int f, long n, const asmb::Geo &g, const unsigned char *act,
                               const int *id, double *rows, double *scale);
+void launch_assemble_pressure(cudaStream_t st, long n, const asmb::Geo &g, const asmb::PInputs &in, double *rows);
 }
 
 extern "C" {
@@ -615,6 +616,52 @@ int ibm_assemble_momentum(ibm_ctx *c, double xcirc, double ycirc, double Rcirc, 
       const int rc = ibm_set_operator(c, f, rows.p, b.nx, b.ny, b.nz);
       if (rc < 0) throw Error(rc, c->err);
     }
+    return IBM_OK;
+  });
+}
+
+int ibm_assemble_pressure(ibm_ctx *c, const uint8_t *fluid_p, const int32_t *id_p, const double *beta_p,
+                          const double *const *alpha, const uint8_t *const *active_q, const int32_t *const *id_q,
+                          double *vals_out) {
+  return guarded(c, [&]() {
+    if (!fluid_p || !id_p || !beta_p || !alpha || !active_q || !id_q)
+      throw Error(IBM_ERR_ARG, "ibm_assemble_pressure: null input");
+    const Geometry &g = c->g;
+    asmb::Geo geo;
+    geo.nx = g.nx; geo.ny = g.ny; geo.nz = g.nz;
+    geo.Lx = c->grid.Lx; geo.Ly = c->grid.Ly; geo.Lz = c->grid.Lz;
+    geo.rho = c->grid.rho; geo.nu = c->grid.nu; geo.dt = c->grid.dt;
+    geo.xcirc = geo.ycirc = geo.Rcirc = 0.0;
+    const long nf[3] = {g.NU, g.NV, g.NW};
+    DBuf<uint8_t> dfl, dq[3];
+    DBuf<int32_t> dip, diq[3];
+    DBuf<double> dbeta, dal[3];
+    dfl.alloc(g.NP); dip.alloc(g.NP); dbeta.alloc(g.NP);
+    IBM_CUDA_TRY(cudaMemcpyAsync(dfl.p, fluid_p, g.NP, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(dip.p, id_p, sizeof(int32_t) * g.NP, cudaMemcpyDefault, c->st));
+    IBM_CUDA_TRY(cudaMemcpyAsync(dbeta.p, beta_p, sizeof(double) * g.NP, cudaMemcpyDefault, c->st));
+    asmb::PInputs in;
+    int nq[3];
+    for (int f = 0; f < 3; ++f) {
+      if (!alpha[f] || !active_q[f] || !id_q[f]) throw Error(IBM_ERR_ARG, "ibm_assemble_pressure: null face array");
+      dq[f].alloc(nf[f]); diq[f].alloc(nf[f]); dal[f].alloc(nf[f]);
+      IBM_CUDA_TRY(cudaMemcpyAsync(dq[f].p, active_q[f], nf[f], cudaMemcpyDefault, c->st));
+      IBM_CUDA_TRY(cudaMemcpyAsync(diq[f].p, id_q[f], sizeof(int32_t) * nf[f], cudaMemcpyDefault, c->st));
+      IBM_CUDA_TRY(cudaMemcpyAsync(dal[f].p, alpha[f], sizeof(double) * nf[f], cudaMemcpyDefault, c->st));
+      const std::vector<int32_t> h = to_host(id_q[f], (size_t)nf[f]);
+      nq[f] = h.empty() ? 0 : *std::max_element(h.begin(), h.end());
+      in.alpha[f] = dal[f].p; in.act_q[f] = dq[f].p; in.id_q[f] = diq[f].p;
+    }
+    in.fluid = dfl.p; in.id_p = dip.p; in.beta = dbeta.p;
+    in.nQu = nq[0]; in.nQv = nq[1];
+    DBuf<double> rows;
+    rows.alloc((size_t)7 * g.NP);
+    launch_assemble_pressure(c->st, g.NP, geo, in, rows.p);
+    IBM_CUDA_TRY(cudaStreamSynchronize(c->st));
+    IBM_CUDA_TRY(cudaGetLastError());
+    if (vals_out) IBM_CUDA_TRY(cudaMemcpy(vals_out, rows.p, sizeof(double) * 7 * g.NP, cudaMemcpyDefault));
+    const int rc = ibm_set_operator(c, 3, rows.p, g.nx, g.ny, g.nz);
+    if (rc < 0) throw Error(rc, c->err);
     return IBM_OK;
   });
 }

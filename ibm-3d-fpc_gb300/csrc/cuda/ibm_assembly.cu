@@ -1,5 +1,6 @@
-// GPU assembly of the momentum operators (ibm_assemble_momentum): one thread
-// per solve-box row, the row arithmetic of ibm_assembly.cuh.
+// GPU assembly of the momentum and pressure operators (ibm_assemble_momentum,
+// ibm_assemble_pressure): one thread per row, the row arithmetic of
+// ibm_assembly.cuh.
 #include <algorithm>
 
 #include "ibm_assembly.cuh"
@@ -21,7 +22,18 @@ __global__ void k_assemble_momentum(int f, long n, asmb::Geo g, const unsigned c
   }
 }
 
+__global__ void k_assemble_pressure(long n, asmb::Geo g, asmb::PInputs in, double *rows) {
+  for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x)
+    asmb::pressure_row(c, g, in, rows + 7 * c);
+}
+
 }  // namespace
+
+void launch_assemble_pressure(cudaStream_t st, long n, const asmb::Geo &g, const asmb::PInputs &in, double *rows) {
+  LaunchScope ls(K_SETUP, st, 120.0 * n);
+  const long b = std::max(1L, std::min((n + kThreads - 1) / kThreads, (long)sm_count() * 8));
+  k_assemble_pressure<<<(int)b, kThreads, 0, st>>>(n, g, in, rows);
+}
 
 void launch_assemble_momentum(cudaStream_t st, int f, long n, const asmb::Geo &g, const unsigned char *act,
                               const int *id, double *rows, double *scale) {

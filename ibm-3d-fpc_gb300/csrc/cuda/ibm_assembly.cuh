@@ -1,6 +1,6 @@
-// Assembly of the momentum operators' embedded 7-point rows on the GPU:
-// one thread per solve-box row computes the row the CPU setup computes
-// (immersed_operators.hpp:1-177 restated in csrc/host/ibm_setup.cpp), with
+// Assembly of the momentum and pressure operators' embedded 7-point rows on
+// the GPU. One thread per row computes the row that the CPU setup computes
+// (immersed_operators.hpp:1-250, restated in csrc/host/ibm_setup.cpp), with
 // the same operations in the same order, so the rows and row scales are
 // bitwise the setup's:
 //  - neighbours in the reference's insertion order (west, east, south,
@@ -218,6 +218,72 @@ IBM_HD double momentum_row(int f, long r, const Geo &g, const unsigned char *act
     else diag = add(diag, c.cz);
   }
   return row.finish(*P, diag, a);
+}
+
+// Inputs of the pressure rows: the cut-cell fractions and the q-face masks
+// and ids of the projection (immersed_operators.hpp:179-250).
+struct PInputs {
+  const unsigned char *fluid;
+  const int *id_p;
+  const double *beta;
+  const double *alpha[3];
+  const unsigned char *act_q[3];
+  const int *id_q[3];
+  int nQu, nQv;
+};
+
+// Row of cell c of the sign-flipped pressure operator -D G into a[7]: the
+// diagonal is sum over the cell's q-faces of D * G(self) in the iteration
+// order of the reference's row map, each neighbour -(D * G(neighbour)).
+IBM_HD void pressure_row(long cell, const Geo &g, const PInputs &in, double *a) {
+  for (int t = 0; t < 7; ++t) a[t] = 0.0;
+  if (!in.fluid[cell]) { a[C] = 1.0; return; }
+  const int nx = g.nx, ny = g.ny, nz = g.nz;
+  const int i = (int)(cell % nx), j = (int)((cell / nx) % ny), k = (int)(cell / ((long)nx * ny));
+  const double dx = dvd(g.Lx, (double)nx), dy = dvd(g.Ly, (double)ny), dz = dvd(g.Lz, (double)nz);
+  const double gx = dvd(1.0, dx), gy = dvd(1.0, dy), gz = dvd(1.0, dz), gout = dvd(2.0, dx);
+  const double beta = in.beta[cell];
+  auto P = [&](int ii, int jj, int kk) { return ((long)kk * ny + jj) * nx + ii; };
+  int keys[6], slot[6], n = 0;
+  double dv[6], gs[6], gn[6];
+  bool nb[6];
+  auto face = [&](int key, double d, int s, double gself, double gnb, bool has) {
+    keys[n] = key; dv[n] = d; slot[n] = s; gs[n] = gself; gn[n] = gnb; nb[n] = has; ++n;
+  };
+  {  // east x-face; the outlet face of the last column has G -2/dx on the cell alone
+    const long f = U(g, i + 1, j, k);
+    if (in.act_q[0][f]) {
+      if (i < nx - 1) face(in.id_q[0][f], dvd(in.alpha[0][f], mul(beta, dx)), XP, -gx, gx, in.id_p[P(i + 1, j, k)] != 0);
+      else face(in.id_q[0][f], dvd(in.alpha[0][f], mul(beta, dx)), XP, -gout, 0.0, false);
+    }
+  }
+  if (i > 0) {
+    const long f = U(g, i, j, k);
+    if (in.act_q[0][f]) face(in.id_q[0][f], dvd(-in.alpha[0][f], mul(beta, dx)), XM, gx, -gx, in.id_p[P(i - 1, j, k)] != 0);
+  }
+  if (j < ny - 1) {
+    const long f = V(g, i, j + 1, k);
+    if (in.act_q[1][f]) face(in.nQu + in.id_q[1][f], dvd(in.alpha[1][f], mul(beta, dy)), YP, -gy, gy, in.id_p[P(i, j + 1, k)] != 0);
+  }
+  if (j > 0) {
+    const long f = V(g, i, j, k);
+    if (in.act_q[1][f]) face(in.nQu + in.id_q[1][f], dvd(-in.alpha[1][f], mul(beta, dy)), YM, gy, -gy, in.id_p[P(i, j - 1, k)] != 0);
+  }
+  if (k < nz - 1) {
+    const long f = W(g, i, j, k + 1);
+    if (in.act_q[2][f]) face(in.nQu + in.nQv + in.id_q[2][f], dvd(in.alpha[2][f], mul(beta, dz)), ZP, -gz, gz, in.id_p[P(i, j, k + 1)] != 0);
+  }
+  if (k > 0) {
+    const long f = W(g, i, j, k);
+    if (in.act_q[2][f]) face(in.nQu + in.nQv + in.id_q[2][f], dvd(-in.alpha[2][f], mul(beta, dz)), ZM, gz, -gz, in.id_p[P(i, j, k - 1)] != 0);
+  }
+  int ord[7];
+  sum_order(keys, n, ord);
+  double diag = 0.0;
+  for (int t = 0; t < n; ++t) diag = add(diag, mul(dv[ord[t]], gs[ord[t]]));
+  a[C] = -diag;
+  for (int t = 0; t < n; ++t)
+    if (nb[t]) a[slot[t]] = -mul(dv[t], gn[t]);
 }
 
 }  // namespace asmb

@@ -177,6 +177,17 @@ int ibm_set_projection_csr(ibm_ctx *ctx, const int32_t *D_rowptr, const int32_t 
 int ibm_assemble_momentum(ibm_ctx *ctx, double xcirc, double ycirc, double Rcirc, const uint8_t *const *active,
                           const int32_t *const *id, double *const *vals_out, double *const *scale_out);
 
+/* GPU assembly of the sign-flipped pressure operator -D G
+ * (immersed_operators.hpp:179-250, main.cu:101-103) from the cells' fluid
+ * mask, ids and open fractions beta_p (nx*ny*nz) and the faces' open
+ * fractions alpha[3], q-face masks active_q[3] and q ids id_q[3] (full MAC
+ * layouts; host or device pointers), with the context's grid. Bitwise the
+ * CPU setup's rows; set on the context as ibm_set_operator sets them and
+ * written to vals_out (row-major [nx*ny*nz][7]) when it is not NULL. */
+int ibm_assemble_pressure(ibm_ctx *ctx, const uint8_t *fluid_p, const int32_t *id_p, const double *beta_p,
+                          const double *const *alpha, const uint8_t *const *active_q, const int32_t *const *id_q,
+                          double *vals_out);
+
 /* Solver configuration (main.cu:173-221). */
 void ibm_solver_params_default(ibm_solver_params *p);
 int ibm_set_solver_params(ibm_ctx *ctx, const ibm_solver_params *p);

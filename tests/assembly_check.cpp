@@ -1,7 +1,7 @@
 // Host check of the GPU assembly's row arithmetic (ibm_assembly.cuh, built
 // for the host with unfused IEEE operations) against the CPU setup
 // (libibmhost): every row value and row scale of the three momentum
-// operators, bit for bit. Usage: assembly_check nx ny nz [Um Rcirc ycirc nu dt]
+// operators and every row of the pressure operator, bit for bit. Usage: assembly_check nx ny nz [Um Rcirc ycirc nu dt]
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -43,6 +43,31 @@ int main(int argc, char **argv) {
       if (!ok && bad < 5) std::printf("field %d row %ld differs\n", f, r);
       bad += ok ? 0 : 1;
     }
+  }
+  // pressure rows
+  ibm::asmb::PInputs in;
+  in.fluid = (const unsigned char *)ibm_case_array(c, "fluid_p");
+  in.id_p = (const int *)ibm_case_array(c, "id_p");
+  in.beta = (const double *)ibm_case_array(c, "beta_p");
+  const char *al[3] = {"alpha_u", "alpha_v", "alpha_w"}, *aq[3] = {"active_qu", "active_qv", "active_qw"},
+             *iq[3] = {"id_qu", "id_qv", "id_qw"};
+  for (int f = 0; f < 3; ++f) {
+    in.alpha[f] = (const double *)ibm_case_array(c, al[f]);
+    in.act_q[f] = (const unsigned char *)ibm_case_array(c, aq[f]);
+    in.id_q[f] = (const int *)ibm_case_array(c, iq[f]);
+  }
+  ibm_case_counts cnt;
+  ibm_case_get_counts(c, &cnt);
+  in.nQu = cnt.nqu; in.nQv = cnt.nqv;
+  const double *ap = (const double *)ibm_case_array(c, "Ap_vals");
+  const long np = (long)p.nx * p.ny * p.nz;
+  for (long cell = 0; cell < np; ++cell) {
+    double row[7];
+    ibm::asmb::pressure_row(cell, g, in, row);
+    ++rows;
+    const bool ok = std::memcmp(row, ap + 7 * cell, sizeof(row)) == 0;
+    if (!ok && bad < 5) std::printf("pressure cell %ld differs\n", cell);
+    bad += ok ? 0 : 1;
   }
   std::printf("rows %ld mismatches %ld\n", rows, bad);
   ibm_case_free(c);

@@ -1,7 +1,7 @@
-"""GPU assembly of the momentum operators (ibm_assemble_momentum): the row
-arithmetic checked on the host against the CPU setup (the same source built
-for the host, unfused IEEE operations), and the device kernel against the
-setup's arrays, bit for bit."""
+"""GPU assembly of the momentum and pressure operators (ibm_assemble_momentum,
+ibm_assemble_pressure): the row arithmetic checked on the host against the
+CPU setup (the same source built for the host, unfused IEEE operations), and
+the device kernels against the setup's arrays, bit for bit."""
 import os
 import shutil
 import subprocess
@@ -38,6 +38,8 @@ def test_gpu_assembly_is_the_setup(ibm, shape):
     for f, v, sc in zip("uvw", vals, scales):
         assert np.array_equal(v.view(np.uint64), case.array(f"A{f}_vals").view(np.uint64)), f
         assert np.array_equal(sc.view(np.uint64), case.array(f"scale_{f}").view(np.uint64)), f
+    ap = s.assemble_pressure()
+    assert np.array_equal(ap.view(np.uint64), case.array("Ap_vals").view(np.uint64))
     # the assembled operators are the context's: a step equals one on the setup's operators
     ref = ibm.Solver(case, ibm.solver_params())
     a, b = s.step(1.0), ref.step(1.0)
