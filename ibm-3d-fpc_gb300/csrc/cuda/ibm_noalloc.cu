@@ -12,10 +12,12 @@
 // Its only scratch is the file-scope array below: per-tile partial sums of the
 // two norms and the counter that elects the block finishing the reduction.
 // The array lives in the library's module and is held on every device that
-// loads the library until the process exits. Its address on the current
-// device is obtained once per device with cudaGetSymbolAddress, on the first
-// call made with that device current; in host code the array's name is only
-// a stand-in for the symbol, never a device address.
+// loads the library until the process exits. Its address in the current
+// context is looked up with cudaGetSymbolAddress on every call made outside
+// stream capture, so a device reset or another context made current on the
+// device is followed; a call made while its stream is being captured reuses
+// the address found by the last uncaptured call on that device. In host code
+// the array's name is only a stand-in for the symbol, never a device address.
 #include <cmath>
 #include <mutex>
 
@@ -126,10 +128,14 @@ __global__ void __launch_bounds__(kThreads)
 std::mutex g_na_mutex;
 NoAllocScratch *g_na_ptr[kNaMaxDevices] = {};
 
-// The scratch address on the current device: looked up once per device.
-cudaError_t scratch_on_device(int dev, NoAllocScratch **out) {
+// The scratch address in the current context. Outside capture it is looked
+// up again (cheap, and correct after cudaDeviceReset or with a non-primary
+// context current); during capture the last address found on the device is
+// used, since the lookup itself may load the module and is not a stream
+// operation that capture records.
+cudaError_t scratch_on_device(int dev, bool capturing, NoAllocScratch **out) {
   std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_ptr[dev]) {
+  if (!capturing || !g_na_ptr[dev]) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
@@ -137,6 +143,12 @@ cudaError_t scratch_on_device(int dev, NoAllocScratch **out) {
   }
   *out = g_na_ptr[dev];
   return cudaSuccess;
+}
+
+// [a, a + na) and [b, b + nb) share a byte.
+bool overlaps(const void *a, size_t na, const void *b, size_t nb) {
+  const char *pa = (const char *)a, *pb = (const char *)b;
+  return pa < pb + nb && pb < pa + na;
 }
 
 bool on_device(const void *p, int dev) {
@@ -161,11 +173,20 @@ extern "C" int ibm_residual_noalloc(const double *vals, int nx, int ny, int nz, 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return IBM_ERR_CUDA;
   if (dev < 0 || dev >= kNaMaxDevices) return IBM_ERR_UNSUPPORTED;
-  NoAllocScratch *sc = nullptr;
-  if (scratch_on_device(dev, &sc) != cudaSuccess) return IBM_ERR_CUDA;
+  // r and norms are written while other blocks still read x and b (each row
+  // reads its six neighbours): an output sharing memory with an input races.
+  const size_t vb = (size_t)n * sizeof(double), nb = 2 * sizeof(double);
+  if (overlaps(r, vb, x, vb) || overlaps(r, vb, b, vb) || overlaps(r, vb, vals, 7 * vb) ||
+      overlaps(norms, nb, x, vb) || overlaps(norms, nb, b, vb) || overlaps(norms, nb, r, vb) ||
+      overlaps(norms, nb, vals, 7 * vb))
+    return IBM_ERR_ARG;
   for (const void *p : {(const void *)vals, (const void *)x, (const void *)b, (const void *)r, (const void *)norms})
     if (!on_device(p, dev)) return IBM_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return IBM_ERR_CUDA;
+  NoAllocScratch *sc = nullptr;
+  if (scratch_on_device(dev, cs != cudaStreamCaptureStatusNone, &sc) != cudaSuccess) return IBM_ERR_CUDA;
   if (cudaMemsetAsync(&sc->ticket, 0, sizeof(unsigned), st) != cudaSuccess) return IBM_ERR_CUDA;
   const int tiles = (int)((n + kTile - 1) / kTile);
   k_residual_noalloc<<<tiles, kThreads, 0, st>>>(vals, nx, ny, nz, n, x, b, r, norms, sc);
