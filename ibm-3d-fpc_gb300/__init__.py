@@ -221,15 +221,17 @@ class Solver:
         self._check(self._lib.ibm_profile_get(self._ctx, C.byref(p)))
         return p
 
-    def assemble_momentum(self):
-        """Assembles the three momentum operators on the GPU from the case's
-        masks and ids (ibm_assemble_momentum) and sets them on the context;
-        returns their row-major values and id-indexed row scales."""
-        nx, ny, nz = self.case.shape
-        cp = self.case.params
+    def assemble_momentum(self, case: Optional[Case] = None):
+        """Assembles the three momentum operators on the GPU from the masks,
+        ids and body of ``case`` (default: the solver's own case) with
+        ibm_assemble_momentum and sets them on the context; returns their
+        row-major values and id-indexed row scales."""
+        case = self.case if case is None else case
+        nx, ny, nz = case.shape
+        cp = case.params
         vals = [np.empty(7 * n) for n in ((nx - 1) * ny * nz, nx * (ny - 1) * nz, nx * ny * (nz - 1))]
-        act = [np.ascontiguousarray(self.case.array(f"active_{f}"), dtype=np.uint8) for f in "uvw"]
-        ids = [np.ascontiguousarray(self.case.array(f"id_{f}"), dtype=np.int32) for f in "uvw"]
+        act = [np.ascontiguousarray(case.array(f"active_{f}"), dtype=np.uint8) for f in "uvw"]
+        ids = [np.ascontiguousarray(case.array(f"id_{f}"), dtype=np.int32) for f in "uvw"]
         scales = [np.empty(int(i.max()) + 1) for i in ids]
         P = C.c_void_p * 3
         self._check(self._lib.ibm_assemble_momentum(
@@ -237,12 +239,14 @@ class Solver:
             P(*[a.ctypes.data for a in ids]), P(*[a.ctypes.data for a in vals]), P(*[a.ctypes.data for a in scales])))
         return vals, scales
 
-    def assemble_pressure(self):
-        """Assembles the pressure operator on the GPU from the case's
-        fractions, masks and ids (ibm_assemble_pressure) and sets it on the
-        context; returns its row-major values."""
-        a = self.case.array
-        nx, ny, nz = self.case.shape
+    def assemble_pressure(self, case: Optional[Case] = None):
+        """Assembles the pressure operator on the GPU from the fractions,
+        masks and ids of ``case`` (default: the solver's own case) with
+        ibm_assemble_pressure and sets it on the context; returns its
+        row-major values."""
+        case = self.case if case is None else case
+        a = case.array
+        nx, ny, nz = case.shape
         vals = np.empty(7 * nx * ny * nz)
         fl = np.ascontiguousarray(a("fluid_p"), dtype=np.uint8)
         idp = np.ascontiguousarray(a("id_p"), dtype=np.int32)

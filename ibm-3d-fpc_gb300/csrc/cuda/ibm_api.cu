@@ -615,6 +615,21 @@ int ibm_assemble_momentum(ibm_ctx *c, double xcirc, double ycirc, double Rcirc, 
         IBM_CUDA_TRY(cudaMemcpy(scale_out[f], sc.p, sizeof(double) * ones.size(), cudaMemcpyDefault));
       const int rc = ibm_set_operator(c, f, rows.p, b.nx, b.ny, b.nz);
       if (rc < 0) throw Error(rc, c->err);
+      // The right-hand side is scaled row by row with the same scales as the
+      // rows (gpu_dense_ops.hpp:16-18): the new scales replace the ones
+      // ibm_set_aux gave, so a moved body steps with consistent rows and
+      // right-hand sides.
+      if (c->aux_set && nid == c->n_id[f]) {
+        const std::vector<double> hs = to_host(sc.p, ones.size());
+        const std::vector<int32_t> *rmap[3] = {&c->h_id_u_rows, &c->h_id_v_rows, &c->h_id_w_rows};
+        std::vector<double> sbox(rmap[f]->size());
+        for (size_t r = 0; r < rmap[f]->size(); ++r) {
+          const int rid = (*rmap[f])[r];
+          sbox[r] = rid > 0 ? hs[(size_t)rid] : 0.0;
+        }
+        upload(c->scale_box[f], sbox, c->st);
+        invalidate_graph(c);
+      }
     }
     return IBM_OK;
   });
