@@ -173,7 +173,11 @@ int ibm_set_projection_csr(ibm_ctx *ctx, const int32_t *D_rowptr, const int32_t 
  * The operators are set on the context as ibm_set_operator sets them;
  * vals_out[f] (the row-major [box rows][7] values) and scale_out[f] (the
  * id-indexed row scales, max id + 1 values, index 0 = 1) are written when
- * the arrays and their entries are not NULL (host or device pointers). */
+ * the arrays and their entries are not NULL (host or device pointers).
+ * When ibm_set_aux has been called and the ids match the context's, the
+ * new row scales also replace the context's right-hand-side scales, so the
+ * next step scales its right-hand sides as the new rows are scaled; with
+ * other ids, call ibm_set_aux with scale_out before the next step. */
 int ibm_assemble_momentum(ibm_ctx *ctx, double xcirc, double ycirc, double Rcirc, const uint8_t *const *active,
                           const int32_t *const *id, double *const *vals_out, double *const *scale_out);
 
@@ -322,10 +326,18 @@ int ibm_device_query(int device, char *buf, int len);
  *    doubles) are caller-owned device (or managed) memory on the current
  *    device; host pointers are rejected with IBM_ERR_ARG.
  *  - nx*ny*nz above IBM_NOALLOC_MAX_ROWS returns IBM_ERR_TOO_LARGE.
+ *  - r and norms must not share memory with vals, x, b or each other
+ *    (IBM_ERR_ARG): r = x in place would race, since other rows still read
+ *    x while r is written.
  *  - scratch is one fixed array inside the library (512 KiB per device,
- *    held until the process exits). The first call on a device, made with
- *    that device current, looks up the array's address there
- *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *    held until the process exits). Each call made outside stream capture
+ *    looks up the array's address in the current context
+ *    (cudaGetSymbolAddress), so calls after cudaDeviceReset, or with another
+ *    context of the device made current, use the right address; a call
+ *    made during capture reuses the address the last uncaptured call on
+ *    that device found. Make the first call on a device before any stream
+ *    capture, and make one uncaptured call again after a device reset
+ *    before capturing.
  *  - work is queued on `stream` (a cudaStream_t; NULL = default stream) and
  *    the call returns without waiting: r and norms are valid once the stream
  *    has reached this point. Every call shares the array, which keeps the
