@@ -121,10 +121,15 @@ __device__ __forceinline__ double advect(double c, double dm, double dp, KnownDi
 __device__ __forceinline__ double avg4(double a, double b, double c, double d) {
   return quarter(__dadd_rn(__dadd_rn(__dadd_rn(a, b), c), d));
 }
-// ((rho/dt) u - rho conv - gp + bc) * scale, each operation rounded.
+// ((rho/dt) u - rho conv - gp + bc) * scale (gpu_dense_ops.hpp:16-18). The
+// reference leaves this expression to nvcc, which contracts its first
+// difference into one fused multiply-add, fma(rho/dt, u, -(rho conv)); the
+// rest is rounded operation by operation. Spelled out here so the result is
+// bitwise the reference kernel's (checked against the reference's own kernel
+// compiled from its sources).
 __device__ __forceinline__ double mom_rhs(double a, double rho, double uc, double conv, double gp, double bc,
                                           double sc) {
-  double t = __dsub_rn(__dmul_rn(a, uc), __dmul_rn(rho, conv));
+  double t = fma(a, uc, -__dmul_rn(rho, conv));
   t = __dsub_rn(t, gp);
   t = __dadd_rn(t, bc);
   return __dmul_rn(t, sc);

@@ -261,11 +261,13 @@ static void gradient_faces(const oracle *o, const double *p, double *gx, double 
 }
 
 /* rhs = ((rho/dt) u - rho conv - gp + rhs_bc[id]) scale[id] on active faces
- * (gpu_dense_ops.hpp:16-18), each operation rounded separately. */
+ * (gpu_dense_ops.hpp:16-18). The reference's kernel is compiled by nvcc with
+ * contraction on: its first difference becomes fma(rho/dt, u, -(rho conv))
+ * (found bit for bit against that kernel built from the reference's sources);
+ * the other operations are rounded one by one. */
 static double mom_rhs(double a, double rho, double uc, double conv, double gp, double bc, double sc) {
-  double t = a * uc;
   double t2 = rho * conv;
-  t = t - t2;
+  double t = fma(a, uc, -t2);
   t = t - gp;
   t = t + bc;
   return t * sc;

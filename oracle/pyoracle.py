@@ -15,13 +15,15 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libibmref.so")
-REFERENCE_DIR = "/root/reference"
+# The reference's source tree, where it is present (it is only needed to build
+# the reference checkers; IBM_REFERENCE_DIR overrides the default location).
+REFERENCE_DIR = os.environ.get("IBM_REFERENCE_DIR", "/root/reference")
 
 
 def build(with_reference: bool = True) -> None:
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     if with_reference and os.path.isdir(REFERENCE_DIR):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={REFERENCE_DIR}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "refcubin", f"REFERENCE={REFERENCE_DIR}"], check=True)
 
 
 class OracleParams(C.Structure):

@@ -11,7 +11,8 @@ Fixtures (all small, compressed):
                               and the run example of README_BUILD.txt (dt 2e-3)
   twins_channel_32x12x12.npz  seeded fields and the reference's CPU BC cleanup and
                               centred convection of them
-  oracle_channel_32x12x12.npz oracle state after 5 steps (ramp over 4 steps), tight tolerances
+  oracle_channel_32x12x12.npz oracle state after 5 steps (ramp over 4 steps), tight tolerances,
+                              PFMG's plain multigrid rules
 """
 import os
 import sys
@@ -64,7 +65,7 @@ def main():
     print("wrote twins")
 
     case = ibm.Case(chan)
-    orc = pyoracle.Oracle(case, vel_tol=1e-13, p_tol=1e-13)
+    orc = pyoracle.Oracle(case, vel_tol=1e-13, p_tol=1e-13, mg_options=0)  # PFMG's plain multigrid rules
     stats = []
     for step in range(1, 6):
         st = orc.step(min(1.0, step / 4.0))

@@ -10,6 +10,7 @@
   matrices.
 """
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -298,3 +299,34 @@ def test_forces_of_a_closed_body(case32, pyoracle):
     orc.set_fields(zu, zv, zw, 2.0 * p1 + p2)
     assert np.allclose(orc.forces(), 2.0 * f1 + f2, rtol=1e-12, atol=1e-14)
     assert np.abs(f1).max() > 0
+
+
+def test_oracle_dense_stages_match_reference_device_kernels_golden(pyoracle):
+    """The oracle's BC cleanup, convection, gradient and momentum
+    right-hand-side build, scatter, divergence and pressure right-hand side,
+    and projection, bit for bit against the reference's own device kernels
+    (gpu_dense_ops.hpp run on a GB300 by tests/golden/make_golden_device.py),
+    fed the same seeded state and seeded stand-ins for the solve outputs."""
+    path = os.path.join(GOLDEN, "refkernels_channel_32x12x12.npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated (tests/golden/make_golden_device.py needs a GPU)")
+    import importlib
+    sys.path.insert(0, GOLDEN)
+    mgd = importlib.import_module("make_golden_device")
+    g = np.load(path)
+    ibm = importlib.import_module("ibm-3d-fpc_gb300")
+    case = ibm.Case(ibm.channel_params(*mgd.SHAPE, Um=0.45, dt=1e-3))
+    (u, v, w, p), xs = mgd.state_and_solves(case)
+    ramp = float(g["ramp"])
+    orc = pyoracle.Oracle(case)
+    ub, vb, wb = orc.bc_cleanup(u, v, w, ramp)
+    got = dict(zip(("rhs_u", "rhs_v", "rhs_w"), orc.momentum_rhs(ub, vb, wb, p)))
+    orc.set_fields(ub, vb, wb, p)
+    ut, vt, wt = orc.tilde(*xs[:3], ramp)
+    got["rhs_p"] = orc.pressure_rhs(ut, vt, wt, ramp)
+    st = orc.projection(ut, vt, wt, xs[3], ramp)
+    got.update(zip("uvwp", orc.fields()))
+    for k, val in got.items():
+        assert np.array_equal(val.view(np.uint64), g[k].view(np.uint64)), k
+    assert st.umax == float(g["umax"]) and st.vmax == float(g["vmax"]) and st.wmax == float(g["wmax"])
+    assert abs(st.div_l2 - float(g["div_l2"])) <= 1e-12 * float(g["div_l2"])
