@@ -1,0 +1,149 @@
+"""CUDA path against the CPU oracle at the grid sizes the benchmark
+configurations name, through the C ABI.
+
+- Full timestep grid 640x128x128 (Um 2.25, dt 2e-4), pressure-solve grid
+  512x96x96 and adjoint grid 256x48x48 (Um 0.45, dt 1e-3): one step of the
+  benchmark's own solver configuration (FP32 Arnoldi cycles with FP64
+  restarts, FP32 multigrid, tolerance 1e-8, graph-captured) from the
+  benchmark's seeded initial state. Every dense stage of the device step
+  (BC + convection + gradient + momentum right-hand sides, scatter +
+  divergence + pressure right-hand side, projection, diagnostics) is
+  compared bit for bit with the oracle's stage applied to the device's own
+  solve outputs, which keeps the oracle's cost O(N). Every solve is checked
+  by its true residual b - A x, computed by the oracle's operator apply: it
+  must meet the 1e-8 tolerance the device reported meeting.
+- The 160x32x32 channel (Um 0.45, nu 1e-3, dt 1e-3) for its full 50 steps,
+  and the 256x48x48 channel for 3 steps, against the oracle's own steps at a
+  1e-13 tolerance on both sides: fields within 1e-10 relative.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-10
+SOLVE_TOL = 1e-8
+
+
+def bits_equal(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
+
+
+def rel_err(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
+
+
+def seeded_state(case, seed=2026):
+    """The benchmark's initial field: the parabolic inflow profile on every
+    active u face plus 1e-3 N(0,1) on active u, v, w faces (PCG64 seed)."""
+    nx, ny, nz = case.shape
+    rng = np.random.default_rng(seed)
+    au = case.array("active_u").reshape(nz, ny, nx + 1).astype(bool)
+    av = case.array("active_v").astype(bool)
+    aw = case.array("active_w").astype(bool)
+    prof = case.array("uin").reshape(nz, ny, 1)
+    u = np.where(au, prof, 0.0)
+    u[:, :, 0] = prof[:, :, 0]
+    u = u.ravel() + 1e-3 * rng.standard_normal(u.size) * au.ravel()
+    v = 1e-3 * rng.standard_normal(av.size) * av
+    w = 1e-3 * rng.standard_normal(aw.size) * aw
+    return u, v, w, np.zeros(nx * ny * nz)
+
+
+def benchmark_params(ibm):
+    """The benchmark's solver configuration (mixed form, graph-captured)."""
+    return ibm.solver_params(vel_tol=SOLVE_TOL, p_tol=SOLVE_TOL, vel_maxit=250, p_maxit=250, vel_kdim=50,
+                             p_kdim=50, p_pc=1, p_pc_rap_type=0, p_pc_relax_type=2, mg_nu1=3, mg_nu2=3,
+                             mg_nu_coarse=2, mg_omega=1.0, mg_group_ratio=1.5, mg_coarse_max=2560, mg_options=3,
+                             precision=2, vel_inner_sweeps=2, use_graph=1)
+
+
+SIZES = [((640, 128, 128), dict(Um=2.25, dt=2e-4)),
+         ((512, 96, 96), dict(Um=2.25, dt=2e-4)),
+         ((256, 48, 48), dict(Um=0.45, dt=1e-3))]
+
+
+@pytest.mark.parametrize("shape,kw", SIZES, ids=["640x128x128", "512x96x96", "256x48x48"])
+def test_step_stages_and_residuals_at_benchmark_size(ibm, pyoracle, shape, kw):
+    case = ibm.Case(ibm.channel_params(*shape, nu=1e-3, **kw))
+    s = ibm.Solver(case, benchmark_params(ibm))
+    try:
+        orc = pyoracle.Oracle(case, vel_tol=SOLVE_TOL, p_tol=SOLVE_TOL)
+        u, v, w, p = seeded_state(case)
+        # one step first, so the stages below start from a pressure that is
+        # not zero and a velocity that a step produced
+        s.set_fields(u, v, w, p)
+        assert s.step(1.0).status == ibm.IBM_OK
+        u, v, w, p = s.fields()
+        ramp = 1.0
+        st = s.step(ramp)
+        assert st.status == ibm.IBM_OK
+        ub, vb, wb = orc.bc_cleanup(u, v, w, ramp)
+        bu, bv, bw = orc.momentum_rhs(ub, vb, wb, p)
+        for f, ref in enumerate((bu, bv, bw)):
+            assert bits_equal(s.solver_vector(f, 0), ref), f"momentum rhs {'uvw'[f]}"
+        xu, xv, xw = (s.solver_vector(f, 1) for f in range(3))
+        orc.set_fields(ub, vb, wb, p)
+        ut, vt, wt = orc.tilde(xu, xv, xw, ramp)
+        assert bits_equal(s.solver_vector(3, 0), orc.pressure_rhs(ut, vt, wt, ramp)), "pressure rhs"
+        xp = s.solver_vector(3, 1)
+        ost = orc.projection(ut, vt, wt, xp, ramp)
+        for a, b, name in zip(s.fields(), orc.fields(), "uvwp"):
+            assert bits_equal(a, b), f"projected {name}"
+        assert st.umax == ost.umax and st.vmax == ost.vmax and st.wmax == ost.wmax
+        assert abs(st.div_l2 - ost.div_l2) <= 1e-12 * max(ost.div_l2, 1e-300) + 1e-300
+        # true residuals of the four device solves, by the oracle's operator
+        for f, name in enumerate("uvwp"):
+            b = s.solver_vector(f, 0)
+            x = s.solver_vector(f, 1)
+            rel = np.linalg.norm(b - orc.apply_operator(f, x)) / np.linalg.norm(b)
+            reported = getattr(st, name).rel_res
+            assert rel <= SOLVE_TOL * (1 + 1e-6), (name, rel)
+            # the device's restart residuals are double-float sums with a
+            # per-row error bound of 2^-41 (|b| + sum |c x|); near the
+            # tolerance the decision is taken again from an FP64 residual
+            assert abs(rel - reported) <= 2.0 ** -40, (name, rel, reported)
+    finally:
+        s.close()
+
+
+def tight(ibm):
+    return ibm.solver_params(vel_tol=1e-13, p_tol=1e-13, vel_maxit=500, p_maxit=500, mg_coarse_max=64)
+
+
+def test_channel_160x32x32_fifty_steps(ibm, pyoracle):
+    """The 160x32x32 configuration in full: 50 steps, inlet ramp over the
+    reference's default 200 steps (ramp = step / 200), both sides at 1e-13."""
+    case = ibm.Case(ibm.channel_params(160, 32, 32, Um=0.45, nu=1e-3, dt=1e-3))
+    s = ibm.Solver(case, tight(ibm))
+    try:
+        orc = pyoracle.Oracle(case, vel_tol=1e-13, p_tol=1e-13)
+        for step in range(1, 51):
+            ramp = min(1.0, step / 200.0)
+            st = s.step(ramp)
+            so = orc.step(ramp)
+            assert st.status == ibm.IBM_OK and so.status == 0, step
+        for a, b, name in zip(s.fields(), orc.fields(), "uvwp"):
+            assert rel_err(a, b) <= REL_TOL, name
+    finally:
+        s.close()
+
+
+def test_channel_256x48x48_steps(ibm, pyoracle):
+    """The adjoint configuration's grid, three full steps from the seeded
+    initial state, both sides at 1e-13."""
+    case = ibm.Case(ibm.channel_params(256, 48, 48, Um=0.45, nu=1e-3, dt=1e-3))
+    s = ibm.Solver(case, tight(ibm))
+    try:
+        orc = pyoracle.Oracle(case, vel_tol=1e-13, p_tol=1e-13)
+        state = seeded_state(case)
+        s.set_fields(*state)
+        orc.set_fields(*state)
+        for _ in range(3):
+            st = s.step(1.0)
+            so = orc.step(1.0)
+            assert st.status == ibm.IBM_OK and so.status == 0
+        for a, b, name in zip(s.fields(), orc.fields(), "uvwp"):
+            assert rel_err(a, b) <= REL_TOL, name
+    finally:
+        s.close()
