@@ -79,6 +79,17 @@ def parse():
                     help="multigrid: largest level solved directly (dense inverse)")
     ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
                     help="mixed form: 1 = FP32 preconditioners in FP64 GMRES, 2 = also FP32 Arnoldi cycles")
+    ap.add_argument("--profile-workload", choices=["pc", "step"], default=None,
+                    help="run a small fixed workload for a profiler capture instead of the benchmark: 'pc' applies "
+                         "the pressure preconditioner --repeat times, 'step' runs --repeat host-driven timesteps "
+                         "(every launch visible to a profiler); Krylov bases of 8 vectors keep the footprint at a "
+                         "few GB. No JSON line is printed")
+    ap.add_argument("--repeat", type=int, default=4, help="repetitions of --profile-workload")
+    ap.add_argument("--set", action="append", default=[],
+                    help="--profile-workload: override a solver parameter, name=value (e.g. mg_quads=0)")
+    ap.add_argument("--time-kernel", default=None,
+                    help="--profile-workload: time every launch of this kernel class with CUDA events after one "
+                         "untimed repetition and print its mean launch time and algorithmic bandwidth")
     return ap.parse_args()
 
 
@@ -625,10 +636,50 @@ def profile_pass(solver, plib, Prof, ibm):
     return dom, names[dom], pr, st, kernel_ms, kernel_gbs, n_classes + 2
 
 
+def profile_workload(args):
+    """The small fixed workloads the committed profiler summaries were
+    captured on (mixed precision, the benchmark's multigrid settings, Krylov
+    bases of 8 vectors, host-driven so every launch is visible)."""
+    ibm = importlib.import_module("ibm-3d-fpc_gb300")
+    case = ibm.Case(case_params(ibm, args.nx, args.ny, args.nz))
+    prm = ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, vel_kdim=8, p_kdim=8, p_pc_rap_type=0, p_pc_relax_type=2,
+                            mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_omega=1.0, mg_group_ratio=1.5, mg_options=3,
+                            precision=args.precision, use_graph=0)
+    for kv in args.set:
+        k, v = kv.split("=")
+        setattr(prm, k, type(getattr(prm, k))(float(v)) if "." in v else int(v))
+    s = ibm.Solver(case, prm)
+    timed = ibm.kernel_names().index(args.time_kernel) if args.time_kernel else None
+    r = np.random.default_rng(3).standard_normal(args.nx * args.ny * args.nz)
+    for rep in range(args.repeat):
+        if timed is not None and rep == 1:
+            s.profile_reset()
+            s._lib.ibm_profile_time_kernel(s._ctx, timed)
+        if args.profile_workload == "pc":
+            z = s.apply_preconditioner(ibm.FIELD_P, r)
+        else:
+            st = s.step(1.0)
+    if args.profile_workload == "pc":
+        print("pc ok", float(np.abs(z).max()))
+    else:
+        print("step ok", st.p.iters, st.div_l2)
+    if timed is not None:
+        pr = s.profile()
+        n = max(pr.timed_launches[timed], 1)
+        ms = pr.time_ms[timed] / n
+        gb = pr.bytes[timed] / max(pr.launches[timed], 1) / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+        print(f"{args.time_kernel}: {pr.timed_launches[timed]} launches, {ms * 1e3:.2f} us each, {gb:.0f} GB/s "
+              f"algorithmic")
+    s.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+        return
+    if args.profile_workload:
+        profile_workload(args)
         return
     ws, rank, local = dist()
     import torch
