@@ -18,14 +18,16 @@ e2e        : steps/s through the C ABI with host buffers: every step copies
 roofline   : the kernel class with the largest device time in the timed
              region, algorithmic bytes per launch over CUDA-event time.
 cpu_baseline: the CPU oracle (the reference's HYPRE path is not available
-             here) on all host cores, on a bounded sample.
+             here) with the reference's solver configuration, on all host
+             cores, timed on full 640x128x128 timesteps of the same workload.
 
 ensemble    : a batched ensemble of 32 seeded independent channels (96..256 x
              16..48 x 16..48) stepped together through ibm_batch_step, in
              instance-steps/s, beside the same contexts stepped one by one.
 
---impl reference times the CPU path alone (the oracle port, all cores) on
-bounded samples of the same workload and prints its own line.
+--impl reference times the CPU path alone (the oracle port with the
+reference's solver configuration, all cores), one full 640x128x128 timestep
+per step, and prints its own line with the same config.
 Multi-GPU: the single channel does not shard; N ranks run N replicas
 (weak scaling), timing is the max over ranks. The ensemble shards its
 instances over the ranks by cell count.
@@ -47,7 +49,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "steps/s @640x128x128: mixed vs FP64 plain (rel err ≤1e-6); solve HBM GB/s"
-CPU_SAMPLE_NZ = 8
 
 
 def parse():
@@ -290,15 +291,27 @@ def pressure_only_measure(ibm, args, local, plib, Prof, repeats=3):
     RHS ~ N(0,1) on fluid cells (numpy PCG64, seed 0; 0 elsewhere), its mean
     over the fluid cells removed, x0 = 0, tolerance 1e-10; FP64 (GMRES + FP64
     multigrid), FP32 multigrid inside FP64 FGMRES (precision 1) and FP32
-    Arnoldi cycles with FP64 restarts (precision 2). Error against an FP64
-    solve at 1e-13."""
+    Arnoldi cycles with FP64 restarts (precision 2). RHS and solution stay in
+    device memory (ibm_solve on device pointers); each solve is timed with
+    CUDA events on the solver's stream. The error of each solution is taken
+    against the CPU oracle's FP64 solve of the same system at 1e-13."""
     import torch
+    import ctypes as C
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
     case = ibm.Case(case_params(ibm, 512, 96, 96))
     fluid = case.array("fluid_p").astype(bool)
     rhs = np.random.default_rng(0).standard_normal(fluid.size) * fluid
     rhs[fluid] -= rhs[fluid].mean()
     out = {"workload": "pressure solve 512x96x96 channel, RHS N(0,1) on fluid cells (PCG64 seed 0), mean removed, "
                        "x0 = 0, tol 1e-10", "rows": int(fluid.size)}
+    t0 = time.perf_counter()
+    orc = pyoracle.Oracle(case, p_tol=1e-13, p_maxit=1000)
+    x_ref, ost = orc.solve(3, rhs)
+    out["truth"] = {"solver": "CPU oracle: FP64 GMRES(50) + FP64 semicoarsening multigrid at 1e-13 (an independent "
+                              "implementation; a direct factorisation is out of reach at 4.7M rows)",
+                    "iters": int(ost.iters), "rel_res": ost.rel_res, "cpu_s": time.perf_counter() - t0}
+    del orc
 
     def params(precision, tol):
         p = solver_params(ibm, precision, graph=0, coarse_max=args.mg_coarse_max)
@@ -306,32 +319,36 @@ def pressure_only_measure(ibm, args, local, plib, Prof, repeats=3):
         p.p_maxit = 500
         return p
 
-    tight = ibm.Solver(case, params(0, 1e-13), device=local)
-    x_ref, _ = tight.solve(ibm.FIELD_P, rhs)
-    tight.close()
+    dev = torch.device("cuda", local)
+    db = torch.from_numpy(rhs).to(dev)
     for name, precision in (("fp64", 0), ("fp32_multigrid", 1), ("fp32_cycles", 2)):
         s = ibm.Solver(case, params(precision, 1e-10), device=local)
         s.solve(ibm.FIELD_P, rhs)  # builds the hierarchy
+        xs = [torch.zeros(fluid.size, dtype=torch.float64, device=dev) for _ in range(repeats)]
         stream = device_timer(plib, s._ctx)
         plib.ibm_profile_reset(s._ctx)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st = ibm.SolveStats()
         e0.record(stream)
-        for _ in range(repeats):
-            x, st = s.solve(ibm.FIELD_P, rhs)
+        for x in xs:
+            s._check(s._lib.ibm_solve(s._ctx, ibm.FIELD_P, C.c_void_p(db.data_ptr()), C.c_void_p(x.data_ptr()),
+                                      C.byref(st)))
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / repeats
         pr = read_profile(plib, Prof, s._ctx)
         nbytes = sum(pr.bytes[k] for k in range(32)) / repeats
+        x = xs[-1].cpu().numpy()
         out[name] = {"ms": ms, "iters": int(st.iters), "rel_res": st.rel_res, "status": int(st.status),
                      "gbs": nbytes / (ms * 1e-3) / 1e9,
-                     "err_vs_tight": float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))}
+                     "err_vs_truth": float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))}
         s.close()
-    out["note"] = ("ms per solve with the RHS and solution copied in and out (host-driven, CUDA events); gbs = "
-                   "algorithmic bytes of every kernel of the solve / time. On this rough RHS the FP32 cycles "
-                   "restart more often (each stops at a 1e-5 reduction) and leave a larger error in the "
-                   "smoothest modes for the same residual; FP32 multigrid in FP64 FGMRES is the fast form here")
+    out["note"] = ("ms per solve with RHS and solution in device memory (ibm_solve on device pointers, host-driven "
+                   "Krylov loop, CUDA events); gbs = algorithmic bytes of every kernel of the solve / time. On this "
+                   "rough RHS the FP32 cycles restart more often (each stops at a 1e-5 reduction) and leave a larger "
+                   "error in the smoothest modes for the same residual; FP32 multigrid in FP64 FGMRES is the fast "
+                   "form here")
     return out
 
 
@@ -516,6 +533,30 @@ REFERENCE_ORACLE = dict(vel_tol=1e-8, p_tol=1e-8, mg_rap=1, mg_relax=1, mg_omega
                         mg_options=0)
 
 
+def cpu_info():
+    """Host cores this process may use and the CPU model (lscpu's model name)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not model:
+        import platform
+        model = platform.processor() or platform.machine()
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return cores, model
+
+
+def run_config(nx, ny, nz, ws):
+    """The workload both arms report (identical for the reference arm)."""
+    return {"workload": workload_name(nx, ny, nz), "grid": [nx, ny, nz], "parallelism": f"replicas x{ws}",
+            "l2": "inputs larger than L2 (fields and operators alone are ~3 GB)"}
+
+
 def workload_name(nx, ny, nz):
     return (f"full timestep {nx}x{ny}x{nz} channel (cylinder D=0.1 at (0.5,0.2)), Um=2.25, nu=1e-3, "
             f"dt=2e-4, seeded parabolic + 1e-3 N(0,1) initial field")
@@ -536,25 +577,36 @@ def replica_throughput(steps, ms_max, ws):
     return ws * steps / (ms_max / 1e3)
 
 
-def cpu_baseline(ibm, nx, ny, nz, steps=1):
-    """The CPU oracle on a z-slab of the workload (same x-y plane, nz = 8),
-    all host threads, scaled to the full grid by the cell count."""
+def oracle_steps(ibm, nx, ny, nz, warmup, steps):
+    """The CPU oracle with the reference's solver configuration on the full
+    workload: `warmup` untimed and `steps` timed timesteps from the seeded
+    initial state. Returns (seconds per timed step, iterations of the last)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build(with_reference=False)
-    nzs = min(CPU_SAMPLE_NZ, nz)
-    case = ibm.Case(case_params(ibm, nx, ny, nzs))
+    case = ibm.Case(case_params(ibm, nx, ny, nz))
     orc = pyoracle.Oracle(case, **REFERENCE_ORACLE)
     orc.set_fields(*initial_state(case))
-    orc.step(1.0)
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    for _ in range(warmup):
         orc.step(1.0)
-    dt = (time.perf_counter() - t0) / steps
-    scale = nz / float(nzs)
-    return {"value": 1.0 / (dt * scale), "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{steps} timestep(s) of a {nx}x{ny}x{nzs} z-slab of the same channel with the "
-                      f"reference's solver configuration, {dt:.2f} s each, scaled by the cell count ({scale:g}x)"}
+    t0 = time.perf_counter()
+    st = None
+    for _ in range(steps):
+        st = orc.step(1.0)
+    dt = (time.perf_counter() - t0) / max(1, steps)
+    its = {f: getattr(st, f).iters for f in "uvwp"} if st is not None else None
+    return dt, its
+
+
+def cpu_baseline(ibm, nx, ny, nz, warmup=1, steps=2):
+    """The CPU oracle (reference solver configuration, all host cores) on
+    full timesteps of the workload itself."""
+    cores, model = cpu_info()
+    dt, its = oracle_steps(ibm, nx, ny, nz, warmup, steps)
+    return {"value": 1.0 / dt, "unit": "steps/s", "cores": cores, "cpu_model": model, "kind": "port",
+            "sample": f"{steps} full timesteps of the {nx}x{ny}x{nz} workload after {warmup} untimed, {dt:.2f} s "
+                      f"each, on the CPU oracle with the reference's solver configuration (FP64 GMRES(50) + "
+                      f"Jacobi, GMRES(50) + PFMG-rule multigrid, tol 1e-8), iterations of the last step {its}"}
 
 
 def reference_arm(args):
@@ -562,32 +614,19 @@ def reference_arm(args):
     if rank != 0:
         return
     ibm = importlib.import_module("ibm-3d-fpc_gb300")
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle
-    pyoracle.build(with_reference=False)
-    nzs = min(CPU_SAMPLE_NZ, args.nz)
-    case = ibm.Case(case_params(ibm, args.nx, args.ny, nzs))
-    orc = pyoracle.Oracle(case, **REFERENCE_ORACLE)
-    orc.set_fields(*initial_state(case))
-    for _ in range(args.warmup):
-        orc.step(1.0)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        orc.step(1.0)
-    dt = (time.perf_counter() - t0) / max(1, args.steps)
-    scale = args.nz / float(nzs)
-    value = 1.0 / (dt * scale)
-    sample = (f"each step: one timestep of a {args.nx}x{args.ny}x{nzs} z-slab of the channel on the CPU "
-              f"oracle with the reference's solver configuration (FP64 GMRES + Jacobi, GMRES + PFMG-rule "
-              f"multigrid), scaled by the cell count ({scale:g}x)")
+    cores, model = cpu_info()
+    dt, its = oracle_steps(ibm, args.nx, args.ny, args.nz, args.warmup, args.steps)
+    value = 1.0 / dt
+    sample = (f"each step: one full {args.nx}x{args.ny}x{args.nz} timestep of the workload on the CPU oracle with "
+              f"the reference's solver configuration (FP64 GMRES(50) + Jacobi for u/v/w, GMRES(50) + PFMG-rule "
+              f"multigrid for p, tol 1e-8), {cores} threads; iterations of the last step {its}")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * scale * 1e3, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_name(args.nx, args.ny, args.nz),
-                       "grid": [args.nx, args.ny, args.nz], "parallelism": f"replicas x{ws} (rank 0 runs)",
-                       "solver": "CPU oracle, reference configuration: FP64 GMRES + Jacobi (momentum), "
-                                 "FP64 GMRES + PFMG-rule multigrid (pressure), tol 1e-8"},
-            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+            "config": run_config(args.nx, args.ny, args.nz, ws),
+            "solver": "CPU oracle, reference configuration: FP64 GMRES + Jacobi (momentum), FP64 GMRES + PFMG-rule "
+                      "multigrid (pressure), tol 1e-8; rank 0 runs, other ranks exit",
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "cpu_model": model, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -743,43 +782,49 @@ def main():
     out = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
-           "config": {"workload": workload_name(nx, ny, nz),
-                      "solver": ("FP32 Arnoldi cycles with FP64 restarts (FGMRES iterative refinement)"
-                                 if args.precision == 2 else "mixed FP32-preconditioned FP64 FGMRES")
-                                + ", true FP64 residual tol 1e-8, graph-captured step",
+           "config": run_config(nx, ny, nz, ws),
+           "solver": {"form": ("FP32 Arnoldi cycles with FP64 restarts (FGMRES iterative refinement)"
+                               if args.precision == 2 else "mixed FP32-preconditioned FP64 FGMRES")
+                              + ", true FP64 residual tol 1e-8, graph-captured step",
                       "precision": args.precision,
-                      "grid": [nx, ny, nz], "parallelism": f"replicas x{ws}",
-                      "l2": "inputs larger than L2 (operators + fields + Krylov bases, tens of GB resident)",
                       "pressure_pc": "semicoarsening MG (grouped, symmetrized, cut-cell-aware interpolation), "
                                      "Galerkin 27-point coarse levels, two-colour sweeps 3+3 (finest) / 2+2 (coarser), FP32",
-                      "momentum_pc": "2 FP32 Jacobi sweeps"},
+                      "momentum_pc": "2 FP32 Jacobi sweeps",
+                      "resident": "operators + fields + Krylov bases, tens of GB in HBM"},
            "phase_ms": phase_means(step_stats), "iterations_mean": iters_mean(step_stats),
            "solve_gbs": solve_gbs, "kernel_ms_per_step": kernel_ms, "kernel_gbs": kernel_gbs,
            "gpu_launches": int(launches),
            "setup_s": setup_s}
 
     if not args.no_fp64:
-        fp64 = ibm.Solver(case, solver_params(ibm, 0, graph=0), device=local)
-        fp64.set_fields(*state)
-        run_steps(fp64, steps_done - args.steps)
-        torch.cuda.synchronize()
-        s64 = device_timer(plib, fp64._ctx)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(s64)
-        st64 = [fp64.step(1.0) for _ in range(args.steps)]
-        e1.record(s64)
-        torch.cuda.synchronize()
-        ms64 = reduce_max_ms(e0.elapsed_time(e1), ws, "cuda")
-        f64 = fp64.fields()
-        vel_err = max(float(np.abs(a - b).max()) for a, b in zip(mixed_fields[:3], f64[:3])) / float(np.abs(f64[0]).max())
-        p_err = float(np.abs(mixed_fields[3] - f64[3]).max() / max(np.abs(f64[3]).max(), 1e-300))
-        out["fp64_plain"] = {"value": replica_throughput(args.steps, ms64, ws), "ms_per_step": ms64 / args.steps,
-                             "phase_ms": phase_means(st64), "iterations_mean": iters_mean(st64),
-                             "form": "FP64 throughout, host-driven step"}
+        # the plain FP64 form, graph-captured like the mixed form (like for
+        # like), and host-driven; both from the same state, same steps
+        for key, graph in (("fp64_plain", 1), ("fp64_plain_host_driven", 0)):
+            fp64 = ibm.Solver(case, solver_params(ibm, 0, graph=graph), device=local)
+            fp64.set_fields(*state)
+            run_steps(fp64, steps_done - args.steps)
+            torch.cuda.synchronize()
+            s64 = device_timer(plib, fp64._ctx)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s64)
+            st64 = [fp64.step(1.0) for _ in range(args.steps)]
+            e1.record(s64)
+            torch.cuda.synchronize()
+            ms64 = reduce_max_ms(e0.elapsed_time(e1), ws, "cuda")
+            f64 = fp64.fields()
+            fp64.close()
+            out[key] = {"value": replica_throughput(args.steps, ms64, ws), "ms_per_step": ms64 / args.steps,
+                        "phase_ms": phase_means(st64), "iterations_mean": iters_mean(st64),
+                        "form": "FP64 throughout (GMRES + Jacobi, GMRES + FP64 multigrid, same settings), "
+                                + ("graph-captured step" if graph else "host-driven step")}
+            if graph:
+                vel_err = (max(float(np.abs(a - b).max()) for a, b in zip(mixed_fields[:3], f64[:3]))
+                           / float(np.abs(f64[0]).max()))
+                p_err = float(np.abs(mixed_fields[3] - f64[3]).max() / max(np.abs(f64[3]).max(), 1e-300))
         out["speedup_vs_fp64"] = out["fp64_plain"]["ms_per_step"] / ms_per_step
+        out["speedup_vs_fp64_host_driven"] = out["fp64_plain_host_driven"]["ms_per_step"] / ms_per_step
         out["velocity_rel_err_vs_fp64"] = vel_err
         out["pressure_rel_err_vs_fp64"] = p_err
-        fp64.close()
 
     if not args.no_e2e:
         p = mixed.params

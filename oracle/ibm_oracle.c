@@ -31,6 +31,9 @@ typedef struct {
   double *pm, *pp;          /* interpolation weights at points odd along cdir */
   double *bv, *xv, *rv;     /* work vectors */
   double *dense_inv;        /* coarsest: explicit inverse [N][N] */
+  int ns;                   /* slots of A that are nonzero somewhere on the level */
+  int slot[27];             /* those slots, in increasing slot order */
+  double *Ac;               /* [N][ns]: A restricted to those slots */
 } mg_level;
 
 struct oracle {
@@ -77,6 +80,64 @@ static double dot(const double *a, const double *b, long n) {
   free(part);
   return s;
 }
+/* out[k] = dot(V + k N, w, N) for k < m, each summed exactly as dot() sums
+ * (per-chunk fused multiply-adds in index order, chunks in order), in one
+ * pass over w. */
+static void multi_dot(const double *V, long N, int m, const double *w, double *out) {
+  long nch = (N + CHUNK - 1) / CHUNK;
+  double *part = (double *)xcalloc((size_t)nch * (size_t)(m ? m : 1), sizeof(double));
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < nch; ++c) {
+    long lo = c * CHUNK, hi = lo + CHUNK < N ? lo + CHUNK : N;
+    for (int k = 0; k < m; ++k) {
+      const double *a = V + (size_t)k * N;
+      double s = 0.0;
+      for (long i = lo; i < hi; ++i) s = fma(a[i], w[i], s);
+      part[(size_t)k * nch + c] = s;
+    }
+  }
+  for (int k = 0; k < m; ++k) {
+    double s = 0.0;
+    for (long c = 0; c < nch; ++c) s += part[(size_t)k * nch + c];
+    out[k] = s;
+  }
+  free(part);
+}
+/* w[t] -= sum_k h[k] V_k[t] for t in each chunk (k ascending), then, in the
+ * same pass, the chunk's partial products V_k . w (part_dots[k nch + c]) or
+ * w . w (part_norm[c]) of the updated w, each summed as dot() sums a chunk. */
+static void orth_update(const double *V, long N, int m, const double *h, double *w, double *part_dots,
+                        double *part_norm) {
+  long nch = (N + CHUNK - 1) / CHUNK;
+#pragma omp parallel for schedule(static)
+  for (long c = 0; c < nch; ++c) {
+    long lo = c * CHUNK, hi = lo + CHUNK < N ? lo + CHUNK : N;
+    for (int k = 0; k < m; ++k) {
+      const double hk = -h[k];
+      const double *vk = V + (size_t)k * N;
+      for (long t = lo; t < hi; ++t) w[t] = fma(hk, vk[t], w[t]);
+    }
+    if (part_dots)
+      for (int k = 0; k < m; ++k) {
+        const double *vk = V + (size_t)k * N;
+        double s = 0.0;
+        for (long t = lo; t < hi; ++t) s = fma(vk[t], w[t], s);
+        part_dots[(size_t)k * nch + c] = s;
+      }
+    if (part_norm) {
+      double s = 0.0;
+      for (long t = lo; t < hi; ++t) s = fma(w[t], w[t], s);
+      part_norm[c] = s;
+    }
+  }
+}
+static void sum_parts(const double *part, long nch, int m, double *out) {
+  for (int k = 0; k < m; ++k) {
+    double s = 0.0;
+    for (long c = 0; c < nch; ++c) s += part[(size_t)k * nch + c];
+    out[k] = s;
+  }
+}
 static long U3(const oracle *o, int i, int j, int k) { return ((long)k * o->ny + j) * (o->nx + 1) + i; }
 static long V3(const oracle *o, int i, int j, int k) { return ((long)k * (o->ny + 1) + j) * o->nx + i; }
 static long W3(const oracle *o, int i, int j, int k) { return ((long)k * o->ny + j) * o->nx + i; }
@@ -106,27 +167,6 @@ static void spmv7(const box3 *b, const double *A, const double *x, double *y) {
         acc = fma(a[4], j < ny - 1 ? x[r + sy] : 0.0, acc);
         acc = fma(a[5], k > 0 ? x[r - sz] : 0.0, acc);
         acc = fma(a[6], k < nz - 1 ? x[r + sz] : 0.0, acc);
-        y[r] = acc;
-      }
-}
-
-/* y = A x for a 27-point operator stored [N][27]; accumulation in slot order */
-static void spmv27(const box3 *b, const double *A, const double *x, double *y) {
-  const int nx = b->n[0], ny = b->n[1], nz = b->n[2];
-#pragma omp parallel for schedule(static)
-  for (int k = 0; k < nz; ++k)
-    for (int j = 0; j < ny; ++j)
-      for (int i = 0; i < nx; ++i) {
-        long r = ((long)k * ny + j) * nx + i;
-        const double *a = A + 27 * r;
-        double acc = 0.0;
-        for (int s = 0; s < 27; ++s) {
-          int ox = s % 3 - 1, oy = (s / 3) % 3 - 1, oz = s / 9 - 1;
-          int ii = i + ox, jj = j + oy, kk = k + oz;
-          double xv = (ii >= 0 && ii < nx && jj >= 0 && jj < ny && kk >= 0 && kk < nz)
-                          ? x[((long)kk * ny + jj) * nx + ii] : 0.0;
-          acc = fma(a[s], xv, acc);
-        }
         y[r] = acc;
       }
 }
@@ -521,7 +561,51 @@ static void mg_collapse7(const oracle *o, mg_level *L) {
   free(coupled);
 }
 
+/* y = A x on a multigrid level, over the level's nonzero slots only, in slot
+ * order. Equal bit for bit to the product over all 27 slots for finite x: the sum starts at +0 and a fused multiply-add never turns it
+ * into -0, so adding an exact-zero product leaves it unchanged. */
+static void spmv_level(const mg_level *L, const double *x, double *y) {
+  const int nx = L->b.n[0], ny = L->b.n[1], nz = L->b.n[2], ns = L->ns;
+  long off[27];
+  int ox[27], oy[27], oz[27];
+  for (int q = 0; q < ns; ++q) {
+    const int s = L->slot[q];
+    ox[q] = s % 3 - 1; oy[q] = (s / 3) % 3 - 1; oz[q] = s / 9 - 1;
+    off[q] = ((long)oz[q] * ny + oy[q]) * nx + ox[q];
+  }
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j) {
+      const int inner = k > 0 && k < nz - 1 && j > 0 && j < ny - 1;
+      for (int i = 0; i < nx; ++i) {
+        const long r = ((long)k * ny + j) * nx + i;
+        const double *a = L->Ac + (long)ns * r;
+        double acc = 0.0;
+        if (inner && i > 0 && i < nx - 1) {
+          for (int q = 0; q < ns; ++q) acc = fma(a[q], x[r + off[q]], acc);
+        } else {
+          for (int q = 0; q < ns; ++q) {
+            const int ii = i + ox[q], jj = j + oy[q], kk = k + oz[q];
+            const int in = ii >= 0 && ii < nx && jj >= 0 && jj < ny && kk >= 0 && kk < nz;
+            acc = fma(a[q], in ? x[r + off[q]] : 0.0, acc);
+          }
+        }
+        y[r] = acc;
+      }
+    }
+}
+
 static void mg_finish_level(const oracle *o, mg_level *L) {
+  int used[27] = {0};
+  for (long r = 0; r < L->b.N; ++r)
+    for (int s = 0; s < 27; ++s)
+      if (L->A[27 * r + s] != 0.0) used[s] = 1;
+  L->ns = 0;
+  for (int s = 0; s < 27; ++s)
+    if (used[s]) L->slot[L->ns++] = s;
+  L->Ac = (double *)xcalloc((size_t)L->b.N * (size_t)(L->ns ? L->ns : 1), 8);
+  for (long r = 0; r < L->b.N; ++r)
+    for (int q = 0; q < L->ns; ++q) L->Ac[(long)L->ns * r + q] = L->A[27 * r + L->slot[q]];
   L->invd = (double *)xcalloc((size_t)L->b.N, 8);
   L->wd = (double *)xcalloc((size_t)L->b.N, 8);
   for (long r = 0; r < L->b.N; ++r) {
@@ -649,6 +733,7 @@ static void mg_relax(const oracle *o, const mg_level *L, const double *b, double
     double *snap = (double *)xcalloc((size_t)N, 8);
     for (int color = 0; color < 2; ++color) {
       memcpy(snap, x, sizeof(double) * (size_t)N);
+#pragma omp parallel for schedule(static)
       for (long r = 0; r < N; ++r) {
         int i = (int)(r % L->b.n[0]), j = (int)((r / L->b.n[0]) % L->b.n[1]), k = (int)(r / ((long)L->b.n[0] * L->b.n[1]));
         if (((i + j + k) & 1) != color) continue;
@@ -666,11 +751,13 @@ static void mg_relax(const oracle *o, const mg_level *L, const double *b, double
     return;
   }
   if (zero_guess) {
+#pragma omp parallel for schedule(static)
     for (long r = 0; r < N; ++r) x[r] = L->wd[r] * b[r];
     return;
   }
   double *ax = (double *)xcalloc((size_t)N, 8);
-  spmv27(&L->b, L->A, x, ax);
+  spmv_level(L, x, ax);
+#pragma omp parallel for schedule(static)
   for (long r = 0; r < N; ++r) x[r] = fma(L->wd[r], b[r] - ax[r], x[r]);
   free(ax);
 }
@@ -694,11 +781,13 @@ static void mg_cycle(oracle *o, int l, const double *b, double *x) {
   double *ax = L->rv;
   if (nu1 == 0) memcpy(ax, b, sizeof(double) * (size_t)N);
   else {
-    spmv27(&L->b, L->A, x, ax);
+    spmv_level(L, x, ax);
+#pragma omp parallel for schedule(static)
     for (long r = 0; r < N; ++r) ax[r] = b[r] - ax[r];
   }
   mg_level *C = &o->lev[l + 1];
   const int d = L->cdir;
+#pragma omp parallel for schedule(static)
   for (long I = 0; I < C->b.N; ++I) {
     int ci[3] = {(int)(I % C->b.n[0]), (int)((I / C->b.n[0]) % C->b.n[1]), (int)(I / ((long)C->b.n[0] * C->b.n[1]))};
     double acc = 0.0;
@@ -713,6 +802,7 @@ static void mg_cycle(oracle *o, int l, const double *b, double *x) {
     C->bv[I] = acc;
   }
   mg_cycle(o, l + 1, C->bv, C->xv);
+#pragma omp parallel for schedule(static)
   for (long r = 0; r < N; ++r) {
     int f[3] = {(int)(r % L->b.n[0]), (int)((r / L->b.n[0]) % L->b.n[1]), (int)(r / ((long)L->b.n[0] * L->b.n[1]))};
     double corr;
@@ -735,6 +825,7 @@ void oracle_mg_vcycle(oracle *o, const double *b, double *x) {
   if (!o->mg_sym) { mg_cycle(o, 0, b, x); return; }
   const long N = o->lev[0].b.N;
   double *bs = (double *)xcalloc((size_t)N, 8);
+#pragma omp parallel for schedule(static)
   for (long r = 0; r < N; ++r) bs[r] = b[r] * o->mg_winv[r];
   mg_cycle(o, 0, bs, x);
   free(bs);
@@ -766,11 +857,13 @@ static void precond(oracle *o, int field, const double *v, double *z) {
   if (field == 3 && o->prm.p_pc == 1) { oracle_mg_vcycle(o, v, z); return; }
   const int sweeps = field == 3 ? 1 : (o->prm.vel_jacobi_iters > 0 ? o->prm.vel_jacobi_iters : 1);
   const double *id = o->invd[field];
+#pragma omp parallel for schedule(static)
   for (long r = 0; r < N; ++r) z[r] = v[r] * id[r];
   if (sweeps > 1) {
     double *az = (double *)xcalloc((size_t)N, 8);
     for (int s = 1; s < sweeps; ++s) {
       spmv7(b, op_vals(o, field), z, az);
+#pragma omp parallel for schedule(static)
       for (long r = 0; r < N; ++r) z[r] = fma(id[r], v[r] - az[r], z[r]);
     }
     free(az);
@@ -790,9 +883,12 @@ int oracle_solve(oracle *o, int field, const double *b, double *x, oracle_solve_
   double *cs = (double *)xcalloc((size_t)kdim + 1, 8), *sn = (double *)xcalloc((size_t)kdim + 1, 8);
   double *g = (double *)xcalloc((size_t)kdim + 1, 8), *y = (double *)xcalloc((size_t)kdim + 1, 8);
   double *hc = (double *)xcalloc((size_t)kdim + 2, 8);
+  const long nch = (N + CHUNK - 1) / CHUNK;
+  double *part = (double *)xcalloc((size_t)nch * (size_t)(kdim + 1), 8);
 #define HH(i, j) H[(size_t)(i) * kdim + (j)]
   const double b_norm = sqrt(dot(b, b, N));
   spmv7(bx, A, x, r);
+#pragma omp parallel for schedule(static)
   for (long t = 0; t < N; ++t) r[t] = b[t] - r[t];
   double r_norm = sqrt(dot(r, r, N));
   int iters = 0, converged = 0;
@@ -803,25 +899,30 @@ int oracle_solve(oracle *o, int field, const double *b, double *x, oracle_solve_
   while (!converged) {
     if (r_norm <= eps) { converged = 1; break; }
     if (iters >= maxit) break;
+#pragma omp parallel for schedule(static)
     for (long t = 0; t < N; ++t) V[t] = r[t] / r_norm;
     g[0] = r_norm;
     int i = 0, claimed = 0;
     while (i < kdim && iters < maxit) {
       precond(o, field, V + (size_t)i * N, z);
       spmv7(bx, A, z, wv);
-      for (int pass = 0; pass < 2; ++pass) {
-        for (int k = 0; k <= i; ++k) hc[k] = dot(V + (size_t)k * N, wv, N);
-        for (long t = 0; t < N; ++t) {
-          double acc = wv[t];
-          for (int k = 0; k <= i; ++k) acc = fma(-hc[k], V[(size_t)k * N + t], acc);
-          wv[t] = acc;
-        }
-        for (int k = 0; k <= i; ++k) HH(k, i) = pass == 0 ? hc[k] : HH(k, i) + hc[k];
-      }
-      double hn = sqrt(dot(wv, wv, N));
+      /* classical Gram-Schmidt twice: hc = V^T w, w -= V hc, twice; then
+       * ||w||. Each update is fused with the products that follow it, chunk
+       * by chunk (the sums are those of dot(): per-chunk fused
+       * multiply-adds in index order, chunks added in order). */
+      multi_dot(V, N, i + 1, wv, hc);
+      for (int k = 0; k <= i; ++k) HH(k, i) = hc[k];
+      orth_update(V, N, i + 1, hc, wv, part, NULL);
+      sum_parts(part, nch, i + 1, hc);
+      for (int k = 0; k <= i; ++k) HH(k, i) = HH(k, i) + hc[k];
+      orth_update(V, N, i + 1, hc, wv, NULL, part);
+      sum_parts(part, nch, 1, hc);
+      double hn = sqrt(hc[0]);
       HH(i + 1, i) = hn;
-      if (hn != 0.0)
+      if (hn != 0.0) {
+#pragma omp parallel for schedule(static)
         for (long t = 0; t < N; ++t) V[(size_t)(i + 1) * N + t] = wv[t] / hn;
+      }
       for (int j = 0; j < i; ++j) {
         double t0 = HH(j, i);
         HH(j, i) = sn[j] * HH(j + 1, i) + cs[j] * t0;
@@ -843,14 +944,21 @@ int oracle_solve(oracle *o, int field, const double *b, double *x, oracle_solve_
       for (int j = k + 1; j < i; ++j) t0 -= HH(k, j) * y[j];
       y[k] = t0 / HH(k, k);
     }
-    for (long t = 0; t < N; ++t) {
-      double acc = 0.0;
-      for (int k = 0; k < i; ++k) acc = fma(y[k], V[(size_t)k * N + t], acc);
-      wv[t] = acc;
+#pragma omp parallel for schedule(static)
+    for (long c0 = 0; c0 < N; c0 += CHUNK) {
+      const long c1 = c0 + CHUNK < N ? c0 + CHUNK : N;
+      for (long t = c0; t < c1; ++t) wv[t] = 0.0;
+      for (int k = 0; k < i; ++k) {
+        const double yk = y[k];
+        const double *vk = V + (size_t)k * N;
+        for (long t = c0; t < c1; ++t) wv[t] = fma(yk, vk[t], wv[t]);
+      }
     }
     precond(o, field, wv, z);
+#pragma omp parallel for schedule(static)
     for (long t = 0; t < N; ++t) x[t] = x[t] + z[t];
     spmv7(bx, A, x, r);
+#pragma omp parallel for schedule(static)
     for (long t = 0; t < N; ++t) r[t] = b[t] - r[t];
     double rt = sqrt(dot(r, r, N));
     r_norm = rt;
@@ -863,7 +971,7 @@ int oracle_solve(oracle *o, int field, const double *b, double *x, oracle_solve_
   st->iters = iters;
   st->rel_res = b_norm > 0.0 ? r_norm / b_norm : r_norm;
   st->status = converged ? 0 : 1;
-  free(V); free(r); free(z); free(wv); free(H); free(cs); free(sn); free(g); free(y); free(hc);
+  free(V); free(r); free(z); free(wv); free(H); free(cs); free(sn); free(g); free(y); free(hc); free(part);
   return st->status;
 }
 
@@ -905,7 +1013,7 @@ void oracle_destroy(oracle *o) {
   for (int l = 0; l < o->nlev; ++l) {
     mg_level *L = &o->lev[l];
     free(L->A); free(L->wd); free(L->invd); free(L->pm); free(L->pp); free(L->bv); free(L->xv); free(L->rv);
-    free(L->dense_inv);
+    free(L->dense_inv); free(L->Ac);
   }
   free(o);
 }
