@@ -78,6 +78,9 @@ def parse():
                     help="also tune the ensemble's multigrid schedule by size class (autotune.py) and measure it")
     ap.add_argument("--mg-coarse-max", type=int, default=2560,
                     help="multigrid: largest level solved directly (dense inverse)")
+    ap.add_argument("--mg-fused-coarse", type=int, default=0,
+                    help="multigrid: fuse the levels from the first one with at most this many points into one "
+                         "persistent kernel per V-cycle (0: off, the library default; 1: 262144 points)")
     ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
                     help="mixed form: 1 = FP32 preconditioners in FP64 GMRES, 2 = also FP32 Arnoldi cycles")
     ap.add_argument("--profile-workload", choices=["pc", "step"], default=None,
@@ -122,11 +125,14 @@ def initial_state(case, seed=2026):
     return u, v, w, p
 
 
+FUSED_COARSE = [0]  # --mg-fused-coarse of this run
+
+
 def solver_params(ibm, precision, graph=0, coarse_max=2560):
     return ibm.solver_params(vel_tol=1e-8, p_tol=1e-8, vel_maxit=250, p_maxit=250, vel_kdim=50, p_kdim=50,
                              p_pc=1, p_pc_rap_type=0, p_pc_relax_type=2, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_omega=1.0,
                              mg_group_ratio=1.5, mg_coarse_max=coarse_max, mg_options=3, precision=precision,
-                             vel_inner_sweeps=2, use_graph=graph)
+                             vel_inner_sweeps=2, use_graph=graph, mg_fused_coarse=FUSED_COARSE[0])
 
 
 class ClockSampler:
@@ -714,6 +720,7 @@ def profile_workload(args):
 
 def main():
     args = parse()
+    FUSED_COARSE[0] = args.mg_fused_coarse
     if args.impl == "reference":
         reference_arm(args)
         return

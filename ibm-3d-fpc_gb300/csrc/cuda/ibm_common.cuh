@@ -301,6 +301,7 @@ enum KernelId {
   K_GM_INIT, K_GM_SPMV, K_GM_ORTH, K_GM_NEXT, K_GM_UPDATE, K_GM_RESID, K_GM_ADDZ, K_GM_JAC32,
   K_MG_LOAD, K_MG_RELAX, K_MG_RESID, K_MG_RESTRICT, K_MG_PROLONG, K_MG_DENSE, K_MG_STORE,
   K_MG_RELAX_FINE,  // in-place two-colour phases of 7-point levels (the finest)
+  K_MG_COARSE,      // all levels below the finest fused into one persistent kernel per V-cycle
   K_ADJOINT,        // reverse sweep of the adjoint step (dense transposes)
   K_SETUP, K_COUNT
 };

@@ -439,14 +439,15 @@ __global__ void k_split_colors27(const T *A, const T *invd, Box bx, T *R) {
   }
 }
 
+// Kernel bodies below take their first item and stride (t0, ts) so that the
+// stand-alone kernels and the fused coarse-level kernel (k_mg_tail) run the
+// same per-point arithmetic.
 template <class T>
-__global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(Recs<T, 28> R, const T *__restrict__ b,
-                                                         const T *__restrict__ x, T *__restrict__ t, Box bx,
-                                                         int color, int zero_x, const int *gate) {
-  if (gate_off(gate)) return;
+__device__ __forceinline__ void relax_rb27_body(const Recs<T, 28> &R, const T *b, const T *x, T *t, const Box &bx,
+                                                int color, int zero_x, long t0, long ts) {
   const long h = bx.n / 2;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
-  for (long m = (long)blockIdx.x * blockDim.x + threadIdx.x; m < h; m += (long)gridDim.x * blockDim.x) {
+  for (long m = t0; m < h; m += ts) {
     int i, j, k;
     const long r = rb_row(m, color, bx, i, j, k);
     const long idx = (long)color * h + m;
@@ -478,6 +479,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(Recs<T, 28> R, const
     t[r ^ 1] = x[r ^ 1];
   }
 }
+template <class T>
+__global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(Recs<T, 28> R, const T *__restrict__ b,
+                                                         const T *__restrict__ x, T *__restrict__ t, Box bx,
+                                                         int color, int zero_x, const int *gate) {
+  if (gate_off(gate)) return;
+  relax_rb27_body<T>(R, b, x, t, bx, color, zero_x, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                     (long)gridDim.x * blockDim.x);
+}
 
 // Quartet form of the FP32 27-point phase (nx a multiple of 4): a thread
 // takes four consecutive points of a line, loads the 9 x 6 window of x values
@@ -485,13 +494,12 @@ __global__ void __launch_bounds__(kThreads, 4) k_relax_rb27(Recs<T, 28> R, const
 // outside the box) and writes the pair's four outputs with one 16-byte store:
 // the phase colour's points relaxed, the others copied. Per point the
 // arithmetic is k_relax_rb27's, in the same slot order.
-__global__ void __launch_bounds__(kThreads) k_relax_rb27_quad(Recs<float, 28> R, const float *__restrict__ b,
-                                                              const float *__restrict__ x, float *__restrict__ t,
-                                                              Box bx, int color, int zero_x, const int *gate) {
-  if (gate_off(gate)) return;
+__device__ __forceinline__ void relax_rb27_quad_body(const Recs<float, 28> &R, const float *b, const float *x,
+                                                     float *t, const Box &bx, int color, int zero_x, long t0,
+                                                     long ts) {
   const long h = bx.n / 2, n4 = bx.n / 4;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
-  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+  for (long q = t0; q < n4; q += ts) {
     const long r0 = 4 * q;
     const unsigned line = fast_div((unsigned)r0, bx.dx);
     const int i0 = (int)((unsigned)r0 - line * (unsigned)nx);
@@ -541,17 +549,22 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb27_quad(Recs<float, 28> R,
     *reinterpret_cast<float4 *>(t + r0) = make_float4(o[0], o[1], o[2], o[3]);
   }
 }
+__global__ void __launch_bounds__(kThreads) k_relax_rb27_quad(Recs<float, 28> R, const float *__restrict__ b,
+                                                              const float *__restrict__ x, float *__restrict__ t,
+                                                              Box bx, int color, int zero_x, const int *gate) {
+  if (gate_off(gate)) return;
+  relax_rb27_quad_body(R, b, x, t, bx, color, zero_x, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                       (long)gridDim.x * blockDim.x);
+}
 
 // Quartet form of the FP32 27-point residual (nx a multiple of 4): the 9 x 6
 // window of x as in k_relax_rb27_quad, all four points b - A x in
 // k_residual_rb27's slot order, one 16-byte store.
-__global__ void __launch_bounds__(kThreads) k_residual_rb27_quad(Recs<float, 28> R, const float *__restrict__ b,
-                                                                 const float *__restrict__ x,
-                                                                 float *__restrict__ res, Box bx, const int *gate) {
-  if (gate_off(gate)) return;
+__device__ __forceinline__ void residual_rb27_quad_body(const Recs<float, 28> &R, const float *b, const float *x,
+                                                        float *res, const Box &bx, long t0, long ts) {
   const long h = bx.n / 2, n4 = bx.n / 4;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
-  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+  for (long q = t0; q < n4; q += ts) {
     const long r0 = 4 * q;
     const unsigned line = fast_div((unsigned)r0, bx.dx);
     const int i0 = (int)((unsigned)r0 - line * (unsigned)nx);
@@ -590,18 +603,23 @@ __global__ void __launch_bounds__(kThreads) k_residual_rb27_quad(Recs<float, 28>
     *reinterpret_cast<float4 *>(res + r0) = make_float4(o[0], o[1], o[2], o[3]);
   }
 }
+__global__ void __launch_bounds__(kThreads) k_residual_rb27_quad(Recs<float, 28> R, const float *__restrict__ b,
+                                                                 const float *__restrict__ x,
+                                                                 float *__restrict__ res, Box bx, const int *gate) {
+  if (gate_off(gate)) return;
+  residual_rb27_quad_body(R, b, x, res, bx, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                          (long)gridDim.x * blockDim.x);
+}
 
 // Residual of a 27-point level from its colour-split records: every point
 // (both colours; same-colour points are coupled), b - A x in apply_row's slot
 // order, so the result equals k_residual<T, 27> bit for bit.
 template <class T>
-__global__ void __launch_bounds__(kThreads, 4) k_residual_rb27(Recs<T, 28> R, const T *__restrict__ b,
-                                                            const T *__restrict__ x, T *__restrict__ res, Box bx,
-                                                            const int *gate) {
-  if (gate_off(gate)) return;
+__device__ __forceinline__ void residual_rb27_body(const Recs<T, 28> &R, const T *b, const T *x, T *res,
+                                                   const Box &bx, long t0, long ts) {
   const long h = bx.n / 2;
   const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < 2 * h; t += (long)gridDim.x * blockDim.x) {
+  for (long t = t0; t < 2 * h; t += ts) {
     const int color = t >= h;
     const long m = t - color * h;
     int i, j, k;
@@ -622,6 +640,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_residual_rb27(Recs<T, 28> R, co
     }
     res[r] = b[r] - acc;
   }
+}
+template <class T>
+__global__ void __launch_bounds__(kThreads, 4) k_residual_rb27(Recs<T, 28> R, const T *__restrict__ b,
+                                                            const T *__restrict__ x, T *__restrict__ res, Box bx,
+                                                            const int *gate) {
+  if (gate_off(gate)) return;
+  residual_rb27_body<T>(R, b, x, res, bx, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                        (long)gridDim.x * blockDim.x);
 }
 
 // Residual after a two-colour sweep that ended with colour 1: the colour-1
@@ -897,10 +923,10 @@ __global__ void k_residual(const T *A, const T *b, const T *x, T *res, Box bx, c
 }
 
 template <class T>
-__global__ void k_restrict(const T *res, const T *pm, const T *pp, Box fb, int d, T *bc, Box cb, const int *gate) {
-  if (gate_off(gate)) return;
+__device__ __forceinline__ void restrict_body(const T *res, const T *pm, const T *pp, const Box &fb, int d, T *bc,
+                                              const Box &cb, long t0, long ts) {
   const int fn[3] = {fb.nx, fb.ny, fb.nz};
-  for (long I = (long)blockIdx.x * blockDim.x + threadIdx.x; I < cb.n; I += (long)gridDim.x * blockDim.x) {
+  for (long I = t0; I < cb.n; I += ts) {
     int ci[3];
     box_ijk(I, cb, ci[0], ci[1], ci[2]);
     T acc = T(0);
@@ -915,19 +941,23 @@ __global__ void k_restrict(const T *res, const T *pm, const T *pp, Box fb, int d
     bc[I] = acc;
   }
 }
+template <class T>
+__global__ void k_restrict(const T *res, const T *pm, const T *pp, Box fb, int d, T *bc, Box cb, const int *gate) {
+  if (gate_off(gate)) return;
+  restrict_body<T>(res, pm, pp, fb, d, bc, cb, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                   (long)gridDim.x * blockDim.x);
+}
 
 // Restriction / interpolation along y or z on FP32 levels whose nx is a
 // multiple of 4: four consecutive x points share everything but their x, so a
 // thread moves them with 16-byte loads. Same operations as k_restrict /
 // k_prolong, lane by lane.
-__global__ void k_restrict_yz4(const float *__restrict__ res, const float *__restrict__ pm,
-                               const float *__restrict__ pp, Box fb, int d, float *__restrict__ bc, Box cb,
-                               const int *gate) {
-  if (gate_off(gate)) return;
+__device__ __forceinline__ void restrict_yz4_body(const float *res, const float *pm, const float *pp, const Box &fb,
+                                                  int d, float *bc, const Box &cb, long t0, long ts) {
   const long n4 = cb.n / 4;
   const long plane_f = (long)fb.nx * fb.ny;
   const int nfd = d == 1 ? fb.ny : fb.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n4; t += (long)gridDim.x * blockDim.x) {
+  for (long t = t0; t < n4; t += ts) {
     int i, J, k;
     box_ijk(4 * t, cb, i, J, k);
     const int cd = d == 1 ? J : k;
@@ -962,15 +992,20 @@ __global__ void k_restrict_yz4(const float *__restrict__ res, const float *__res
     *reinterpret_cast<float4 *>(bc + 4 * t) = o;
   }
 }
-
-__global__ void k_prolong_yz4(const float *__restrict__ xc, Box cb, const float *__restrict__ pm,
-                              const float *__restrict__ pp, Box fb, int d, float *x, int accumulate,
-                              const int *gate) {
+__global__ void k_restrict_yz4(const float *__restrict__ res, const float *__restrict__ pm,
+                               const float *__restrict__ pp, Box fb, int d, float *__restrict__ bc, Box cb,
+                               const int *gate) {
   if (gate_off(gate)) return;
+  restrict_yz4_body(res, pm, pp, fb, d, bc, cb, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                    (long)gridDim.x * blockDim.x);
+}
+
+__device__ __forceinline__ void prolong_yz4_body(const float *xc, const Box &cb, const float *pm, const float *pp,
+                                                 const Box &fb, int d, float *x, int accumulate, long t0, long ts) {
   const long n4 = fb.n / 4;
   const long plane_c = (long)cb.nx * cb.ny;
   const int ncd = d == 1 ? cb.ny : cb.nz;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n4; t += (long)gridDim.x * blockDim.x) {
+  for (long t = t0; t < n4; t += ts) {
     int i, y, k;
     box_ijk(4 * t, fb, i, y, k);
     const int fd = d == 1 ? y : k;
@@ -1000,17 +1035,23 @@ __global__ void k_prolong_yz4(const float *__restrict__ xc, Box cb, const float 
     *xo = corr;
   }
 }
+__global__ void k_prolong_yz4(const float *__restrict__ xc, Box cb, const float *__restrict__ pm,
+                              const float *__restrict__ pp, Box fb, int d, float *x, int accumulate,
+                              const int *gate) {
+  if (gate_off(gate)) return;
+  prolong_yz4_body(xc, cb, pm, pp, fb, d, x, accumulate, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                   (long)gridDim.x * blockDim.x);
+}
 
 // Restriction / interpolation along x on FP32 levels with fine nx = 2 coarse
 // nx and coarse nx a multiple of 4: a thread makes four coarse points from
 // fine points 2i0 - 1 .. 2i0 + 7 (restriction), or four fine points from
 // coarse points i0/2 .. i0/2 + 2 (interpolation), with 16-byte loads. Same
 // operations as k_restrict / k_prolong, point by point.
-__global__ void k_restrict_x4(const float *__restrict__ res, const float *__restrict__ pm,
-                              const float *__restrict__ pp, Box fb, float *__restrict__ bc, Box cb, const int *gate) {
-  if (gate_off(gate)) return;
+__device__ __forceinline__ void restrict_x4_body(const float *res, const float *pm, const float *pp, const Box &fb,
+                                                 float *bc, const Box &cb, long t0, long ts) {
   const long n4 = cb.n / 4;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n4; t += (long)gridDim.x * blockDim.x) {
+  for (long t = t0; t < n4; t += ts) {
     const long c0 = 4 * t;
     const unsigned cline = fast_div((unsigned)c0, cb.dx);
     const int ci0 = (int)((unsigned)c0 - cline * (unsigned)cb.nx);
@@ -1041,12 +1082,17 @@ __global__ void k_restrict_x4(const float *__restrict__ res, const float *__rest
     *reinterpret_cast<float4 *>(bc + c0) = make_float4(o[0], o[1], o[2], o[3]);
   }
 }
-
-__global__ void k_prolong_x4(const float *__restrict__ xc, Box cb, const float *__restrict__ pm,
-                             const float *__restrict__ pp, Box fb, float *x, int accumulate, const int *gate) {
+__global__ void k_restrict_x4(const float *__restrict__ res, const float *__restrict__ pm,
+                              const float *__restrict__ pp, Box fb, float *__restrict__ bc, Box cb, const int *gate) {
   if (gate_off(gate)) return;
+  restrict_x4_body(res, pm, pp, fb, bc, cb, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                   (long)gridDim.x * blockDim.x);
+}
+
+__device__ __forceinline__ void prolong_x4_body(const float *xc, const Box &cb, const float *pm, const float *pp,
+                                                const Box &fb, float *x, int accumulate, long t0, long ts) {
   const long n4 = fb.n / 4;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n4; t += (long)gridDim.x * blockDim.x) {
+  for (long t = t0; t < n4; t += ts) {
     const long r0 = 4 * t;
     const unsigned line = fast_div((unsigned)r0, fb.dx);
     const int i0 = (int)((unsigned)r0 - line * (unsigned)fb.nx);
@@ -1068,13 +1114,18 @@ __global__ void k_prolong_x4(const float *__restrict__ xc, Box cb, const float *
     *xo = corr;
   }
 }
+__global__ void k_prolong_x4(const float *__restrict__ xc, Box cb, const float *__restrict__ pm,
+                             const float *__restrict__ pp, Box fb, float *x, int accumulate, const int *gate) {
+  if (gate_off(gate)) return;
+  prolong_x4_body(xc, cb, pm, pp, fb, x, accumulate, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                  (long)gridDim.x * blockDim.x);
+}
 
 template <class T>
-__global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb, int d, T *x, int accumulate,
-                          const int *gate) {
-  if (gate_off(gate)) return;
+__device__ __forceinline__ void prolong_body(const T *xc, const Box &cb, const T *pm, const T *pp, const Box &fb,
+                                             int d, T *x, int accumulate, long t0, long ts) {
   const int cn[3] = {cb.nx, cb.ny, cb.nz};
-  for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < fb.n; r += (long)gridDim.x * blockDim.x) {
+  for (long r = t0; r < fb.n; r += ts) {
     int f[3];
     box_ijk(r, fb, f[0], f[1], f[2]);
     T corr;
@@ -1097,6 +1148,13 @@ __global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb,
     x[r] = accumulate ? x[r] + corr : corr;
   }
 }
+template <class T>
+__global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb, int d, T *x, int accumulate,
+                          const int *gate) {
+  if (gate_off(gate)) return;
+  prolong_body<T>(xc, cb, pm, pp, fb, d, x, accumulate, (long)blockIdx.x * blockDim.x + threadIdx.x,
+                  (long)gridDim.x * blockDim.x);
+}
 
 // Coarsest level: x = Ainv b (one warp per row).
 // Coarsest level: x = A^-1 b, one warp per row. FP64 hierarchies accumulate
@@ -1104,10 +1162,9 @@ __global__ void k_prolong(const T *xc, Box cb, const T *pm, const T *pp, Box fb,
 // the warp, so a dense level of a few thousand points does not wait on the
 // FP64 pipe.
 template <class T>
-__global__ void k_dense(const T *Ainv, const T *b, T *x, int n, const int *gate) {
-  if (gate_off(gate)) return;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+__device__ __forceinline__ void dense_body(const T *Ainv, const T *b, T *x, int n, long t0, long ts) {
+  const int warp = (int)(t0 >> 5), lane = threadIdx.x & 31;
+  const int nw = (int)(ts >> 5);
   for (int r = warp; r < n; r += nw) {
     double acc;
     if constexpr (sizeof(T) == 4) {
@@ -1133,6 +1190,113 @@ __global__ void k_dense(const T *Ainv, const T *b, T *x, int n, const int *gate)
     }
     acc = warp_sum(acc);
     if (lane == 0) x[r] = (T)acc;
+  }
+}
+template <class T>
+__global__ void k_dense(const T *Ainv, const T *b, T *x, int n, const int *gate) {
+  if (gate_off(gate)) return;
+  dense_body<T>(Ainv, b, x, n, (long)blockIdx.x * blockDim.x + threadIdx.x, (long)gridDim.x * blockDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// Fused coarse levels. Below the finest level every phase of the V-cycle
+// (restrictions, two-colour 27-point sweeps, residuals, the dense coarsest
+// solve, interpolations) runs in one persistent cooperative kernel: its blocks
+// run the phases of a precomputed list in order, each over all its points
+// (the same per-point arithmetic as the stand-alone kernels, through the
+// shared bodies above), with a grid-wide barrier between phases. On the
+// 640x128x128 channel that replaces about 50 launches per V-cycle whose work
+// is a few microseconds each. Data written by one phase is read by the next
+// with ordinary (coherent) loads: the phase list is the only read-only input.
+// ---------------------------------------------------------------------------
+enum TailKind : int {
+  TK_RELAX27Q = 0, TK_RELAX27, TK_RESID27Q, TK_RESID27, TK_RESTRICT, TK_RESTRICT_YZ4, TK_RESTRICT_X4, TK_PROLONG,
+  TK_PROLONG_YZ4, TK_PROLONG_X4, TK_DENSE
+};
+
+struct TailOp {
+  int kind = 0, color = 0, zero = 0, d = 0, accumulate = 0, n = 0;
+  Box fb, cb;               // the level (fine box) and, for transfers, the coarse box
+  Recs<float, 28> R;        // colour-split records of a relaxed level
+  const float *a = nullptr;   // right-hand side (sweeps, residuals) or the dense inverse
+  const float *src = nullptr; // x read (sweeps, residuals), residual (restriction), coarse x (interpolation)
+  const float *pm = nullptr, *pp = nullptr;  // interpolation weights
+  float *dst = nullptr;
+};
+
+// Barrier state, cleared before every launch: blocks arrived at the current
+// barrier, the barrier's generation, and an error flag set when a block gave
+// up waiting.
+struct TailBar {
+  unsigned arrived, gen, err, pad;
+};
+
+// A cooperative launch keeps every block resident, so each barrier completes
+// once all blocks reach it; the bound only keeps a fault elsewhere from
+// turning into an endless wait (about a second of polling).
+constexpr unsigned kTailSpin = 1u << 21;
+
+// Grid-wide barrier; returns true when the error flag is set (a block timed
+// out), after which the blocks stop.
+__device__ __forceinline__ bool tail_sync(TailBar *tb, unsigned &gen) {
+  __shared__ int s_err;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned g = gen;
+    __threadfence();  // this block's writes before the arrival
+    if (atomicAdd(&tb->arrived, 1u) == gridDim.x - 1) {
+      atomicExch(&tb->arrived, 0u);
+      __threadfence();
+      atomicExch(&tb->gen, g + 1);
+    } else {
+      unsigned it = 0;
+      while (*reinterpret_cast<volatile unsigned *>(&tb->gen) == g) {
+        if (++it > kTailSpin) {
+          atomicExch(&tb->err, 1u);
+          break;
+        }
+        __nanosleep(40);
+      }
+    }
+    gen = g + 1;
+    __threadfence();  // the other blocks' writes after the barrier
+    s_err = *reinterpret_cast<volatile unsigned *>(&tb->err) != 0u;
+  }
+  __syncthreads();
+  return s_err != 0;
+}
+
+__global__ void __launch_bounds__(kThreads) k_mg_tail(const TailOp *__restrict__ ops, int nops, TailBar *tb,
+                                                      float *out, const int *gate) {
+  if (gate_off(gate)) return;
+  const long t0 = (long)blockIdx.x * blockDim.x + threadIdx.x, ts = (long)gridDim.x * blockDim.x;
+  unsigned gen = 0;
+  for (int o = 0; o < nops; ++o) {
+    const TailOp op = ops[o];
+    switch (op.kind) {
+      case TK_RELAX27Q: relax_rb27_quad_body(op.R, op.a, op.src, op.dst, op.fb, op.color, op.zero, t0, ts); break;
+      case TK_RELAX27: relax_rb27_body<float>(op.R, op.a, op.src, op.dst, op.fb, op.color, op.zero, t0, ts); break;
+      case TK_RESID27Q: residual_rb27_quad_body(op.R, op.a, op.src, op.dst, op.fb, t0, ts); break;
+      case TK_RESID27: residual_rb27_body<float>(op.R, op.a, op.src, op.dst, op.fb, t0, ts); break;
+      case TK_RESTRICT: restrict_body<float>(op.src, op.pm, op.pp, op.fb, op.d, op.dst, op.cb, t0, ts); break;
+      case TK_RESTRICT_YZ4: restrict_yz4_body(op.src, op.pm, op.pp, op.fb, op.d, op.dst, op.cb, t0, ts); break;
+      case TK_RESTRICT_X4: restrict_x4_body(op.src, op.pm, op.pp, op.fb, op.dst, op.cb, t0, ts); break;
+      case TK_PROLONG:
+        prolong_body<float>(op.src, op.cb, op.pm, op.pp, op.fb, op.d, op.dst, op.accumulate, t0, ts);
+        break;
+      case TK_PROLONG_YZ4:
+        prolong_yz4_body(op.src, op.cb, op.pm, op.pp, op.fb, op.d, op.dst, op.accumulate, t0, ts);
+        break;
+      case TK_PROLONG_X4: prolong_x4_body(op.src, op.cb, op.pm, op.pp, op.fb, op.dst, op.accumulate, t0, ts); break;
+      case TK_DENSE: dense_body<float>(op.a, op.src, op.dst, op.n, t0, ts); break;
+      default: break;
+    }
+    if (o + 1 < nops && tail_sync(tb, gen)) {
+      // a block timed out: stop, and make the result non-finite so the
+      // solver reports it (IBM_ERR_NONFINITE) instead of using it
+      if (blockIdx.x == 0 && threadIdx.x == 0) out[0] = __int_as_float(0x7fc00000);
+      return;
+    }
   }
 }
 
@@ -1361,6 +1525,9 @@ void Multigrid::build<double>(cudaStream_t st, std::vector<MgLevelT<double>> &L,
   IBM_CUDA_TRY(cudaGetLastError());
 }
 
+static float *record_tail(std::vector<MgLevelT<float>> &L, int l, const MgParams &p, std::vector<TailOp> &ops,
+                          double &bytes);
+
 void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const float *A7f, const double h[3],
                       const MgParams &p, bool fp64, bool fp32, const double *winv) {
   prm = p;
@@ -1405,15 +1572,147 @@ void Multigrid::setup(cudaStream_t st, const Box &b, const double *A7, const flo
     }
     IBM_CUDA_TRY(cudaStreamSynchronize(st));
   }
+  build_tail(st);
+}
+
+void Multigrid::build_tail(cudaStream_t st) {
+  tail_nops_ = 0;
+  tail_ops_.release();
+  tail_bar_.release();
+  if (prm.fused_coarse <= 0 || prm.relax != 2 || L32.size() < 2 || L32[0].cdir < 0) return;
+  // the first level below the finest that is small enough: its phases (and
+  // the coarser ones') are bound by launch latency, not by their work
+  int lt = 1;
+  while (lt < (int)L32.size() && L32[lt].b.n > prm.fused_coarse) ++lt;
+  if (lt >= (int)L32.size()) return;
+  std::vector<TailOp> ops;
+  double bytes = 0.0;
+  float *out = record_tail(L32, lt, prm, ops, bytes);
+  if (!out || ops.empty()) return;
+  int per_sm = 0;
+  IBM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mg_tail, kThreads, 0));
+  if (per_sm < 1) return;
+  tail_blocks_ = std::min(per_sm, 2) * sm_count();
+  tail_ops_.alloc(sizeof(TailOp) * ops.size());
+  IBM_CUDA_TRY(cudaMemcpyAsync(tail_ops_.p, ops.data(), sizeof(TailOp) * ops.size(), cudaMemcpyHostToDevice, st));
+  tail_bar_.alloc(sizeof(TailBar) / sizeof(unsigned));
+  IBM_CUDA_TRY(cudaStreamSynchronize(st));
+  tail_nops_ = (int)ops.size();
+  tail_level_ = lt;
+  tail_out_ = out;
+  tail_bytes_ = bytes;
 }
 
 // Runs the V-cycle from level l with zero initial guess; returns (through the
 // level's x buffer pointer swap-free scheme) the buffer holding the result.
+// The fused coarse levels of an FP32 hierarchy, ready to launch.
+struct TailLaunch {
+  const TailOp *ops = nullptr;
+  int nops = 0, blocks = 0, level = 1;  // the first fused level
+  TailBar *bar = nullptr;
+  float *out = nullptr;
+  double bytes = 0.0;
+};
+
+// Records the V-cycle from level l (>= 1) of an FP32 hierarchy as phases of
+// k_mg_tail, in the order and with the buffers vcycle() below would launch
+// them, adding each phase's algorithmic bytes (vcycle's accounting) to
+// `bytes`. Returns the buffer that holds level l's result, or nullptr when a
+// level needs a phase the fused kernel does not have (7-point or Jacobi
+// relaxation): the hierarchy then keeps one launch per phase.
+static float *record_tail(std::vector<MgLevelT<float>> &L, int l, const MgParams &p, std::vector<TailOp> &ops,
+                          double &bytes) {
+  MgLevelT<float> &F = L[l];
+  const long n = F.b.n;
+  const double T_ = 4.0;
+  if (F.cdir < 0) {
+    TailOp op;
+    op.kind = TK_DENSE;
+    op.a = F.dense.p; op.src = F.bv.p; op.dst = F.x.p; op.n = (int)n; op.fb = F.b;
+    ops.push_back(op);
+    bytes += T_ * ((double)n * n + 2.0 * n);
+    return F.x.p;
+  }
+  const int c1 = (l > 0 && p.nu_coarse > 0) ? p.nu_coarse : p.nu1, c2 = (l > 0 && p.nu_coarse > 0) ? p.nu_coarse : p.nu2;
+  const int nu1 = F.relax ? c1 : 0, nu2 = F.relax ? c2 : 0;
+  const Recs<float, 28> R27 = recs_of<float, 28>(F.rb27, F.rbc);
+  const bool rb27 = R27.R || R27.code;
+  if ((nu1 > 0 || nu2 > 0) && !(p.relax == 2 && rb27 && F.ns == 27)) return nullptr;
+  const double rec27 = R27.code ? 2.0 : 28.0 * T_;
+  const bool quad = p.quads && F.b.nx % 4 == 0;
+  float *cur = F.x.p, *oth = F.t.p;
+  auto relax = [&](bool zero) {
+    for (int color = 0; color < 2; ++color) {
+      const bool z = zero && color == 0;
+      TailOp op;
+      op.kind = quad ? TK_RELAX27Q : TK_RELAX27;
+      op.R = R27; op.a = F.bv.p; op.src = cur; op.dst = oth; op.fb = F.b; op.color = color; op.zero = z;
+      ops.push_back(op);
+      bytes += z ? 0.5 * n * (R27.code ? 2.0 : T_) + 1.5 * T_ * n : 0.5 * n * rec27 + 2.5 * T_ * n;
+      std::swap(cur, oth);
+    }
+  };
+  for (int s = 0; s < nu1; ++s) relax(s == 0);
+  const float *res = F.bv.p;
+  if (nu1 > 0) {
+    TailOp op;
+    op.kind = quad ? TK_RESID27Q : TK_RESID27;
+    op.R = R27; op.a = F.bv.p; op.src = cur; op.dst = F.r.p; op.fb = F.b;
+    ops.push_back(op);
+    bytes += n * rec27 + 3.0 * T_ * n;
+    res = F.r.p;
+  }
+  MgLevelT<float> &C = L[l + 1];
+  const bool yz4 = F.cdir != 0 && F.b.nx % 4 == 0;
+  const bool x4 = !yz4 && p.quads && F.cdir == 0 && F.b.nx == 2 * C.b.nx && C.b.nx % 4 == 0;
+  {
+    TailOp op;
+    op.kind = yz4 ? TK_RESTRICT_YZ4 : x4 ? TK_RESTRICT_X4 : TK_RESTRICT;
+    op.src = res; op.pm = F.pm.p; op.pp = F.pp.p; op.fb = F.b; op.d = F.cdir; op.dst = C.bv.p; op.cb = C.b;
+    ops.push_back(op);
+    bytes += T_ * (3.0 * n + C.b.n);
+  }
+  float *xc = record_tail(L, l + 1, p, ops, bytes);
+  if (!xc) return nullptr;
+  {
+    TailOp op;
+    op.kind = yz4 ? TK_PROLONG_YZ4 : x4 ? TK_PROLONG_X4 : TK_PROLONG;
+    op.src = xc; op.cb = C.b; op.pm = F.pm.p; op.pp = F.pp.p; op.fb = F.b; op.d = F.cdir; op.dst = cur;
+    op.accumulate = nu1 > 0;
+    ops.push_back(op);
+    bytes += T_ * ((nu1 > 0 ? 4.0 : 3.0) * n + C.b.n);
+  }
+  for (int s = 0; s < nu2; ++s) relax(false);
+  return cur;
+}
+
+// One cooperative launch of the fused coarse levels (a memset clears the
+// barrier state first); returns the buffer holding the first fused level's
+// correction.
+static float *launch_tail(cudaStream_t st, const TailLaunch &t, const int *gate) {
+  IBM_CUDA_TRY(cudaMemsetAsync(t.bar, 0, sizeof(TailBar), st));
+  LaunchScope ls(K_MG_COARSE, st, t.bytes);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)t.blocks);
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  IBM_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_mg_tail, t.ops, t.nops, t.bar, t.out, gate));
+  return t.out;
+}
+
 template <class T>
 // fin / fout (finest level only, may be null): the V-cycle's input load and
 // output store, fused into the first and the last relaxation phases.
+// tail (FP32 hierarchies, may be null): the levels from tail->level on run as
+// the fused coarse kernel instead of one launch per phase.
 static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgParams &p, const int *gate,
-                 const VecRef *fin = nullptr, const OutRef *fout = nullptr, const float *winvf = nullptr) {
+                 const VecRef *fin = nullptr, const OutRef *fout = nullptr, const float *winvf = nullptr,
+                 const TailLaunch *tail = nullptr) {
   MgLevelT<T> &F = L[l];
   const long n = F.b.n;
   const double T_ = sizeof(T);
@@ -1547,7 +1846,11 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
       k_restrict<T><<<grid_all(C.b.n), kThreads, 0, st>>>(res, F.pm.p, F.pp.p, F.b, F.cdir, C.bv.p, C.b, gate);
     }
   }
-  T *xc = vcycle<T>(st, L, l + 1, p, gate);
+  T *xc = nullptr;
+  if constexpr (sizeof(T) == 4) {
+    if (tail && l + 1 == tail->level) xc = launch_tail(st, *tail, gate);
+  }
+  if (!xc) xc = vcycle<T>(st, L, l + 1, p, gate, nullptr, nullptr, nullptr, tail);
   {
     LaunchScope ls(K_MG_PROLONG, st, T_ * ((nu1 > 0 ? 4.0 : 3.0) * n + C.b.n));
     if constexpr (sizeof(T) == 4) {
@@ -1576,8 +1879,16 @@ void Multigrid::apply(cudaStream_t st, const VecRef &in, const OutRef &out, cons
     const bool fuse = in.basef && out.f && !out.d && F.b.n % 4 == 0 && (in.ld % 4) == 0 && prm.quads &&
                       prm.relax == 2 && F.relax && F.cdir >= 0 && F.ns == 7 && (F.rb.p || F.rbc.ok()) &&
                       F.b.nx % 4 == 0 && prm.nu1 > 0 && prm.nu2 > 0;
+    TailLaunch tl;
+    if (tail_nops_ > 0) {
+      tl.ops = reinterpret_cast<const TailOp *>(tail_ops_.p);
+      tl.nops = tail_nops_; tl.blocks = tail_blocks_; tl.level = tail_level_;
+      tl.bar = reinterpret_cast<TailBar *>(tail_bar_.p);
+      tl.out = tail_out_; tl.bytes = tail_bytes_;
+    }
+    const TailLaunch *tp = tail_nops_ > 0 ? &tl : nullptr;
     if (fuse) {
-      vcycle<float>(st, L32, 0, prm, gate, &in, &out, winvf_.p);
+      vcycle<float>(st, L32, 0, prm, gate, &in, &out, winvf_.p, tp);
       return;
     }
     {
@@ -1589,7 +1900,7 @@ void Multigrid::apply(cudaStream_t st, const VecRef &in, const OutRef &out, cons
         k_load_input<float><<<grid_for(F.b.n), kThreads, 0, st>>>(F.bv.p, F.b.n, in, winv_, gate);
       }
     }
-    float *x = vcycle<float>(st, L32, 0, prm, gate);
+    float *x = vcycle<float>(st, L32, 0, prm, gate, nullptr, nullptr, nullptr, tp);
     LaunchScope ls(K_MG_STORE, st, (4.0 + ob) * F.b.n);
     k_store_output<float><<<grid_for(F.b.n), kThreads, 0, st>>>(x, F.b.n, out, gate);
   } else {

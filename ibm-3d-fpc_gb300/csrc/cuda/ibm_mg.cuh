@@ -18,6 +18,8 @@ struct MgParams {
   int options = 3;      // see ibm_solver_params.mg_options
   int classes = 1;      // colour-split records as record classes where they repeat (ibm_classes.cu)
   int quads = 1;        // FP32 7-point phases and residual four points per thread (nx % 4 == 0)
+  long fused_coarse = 0;  // FP32: levels from the first one below the finest with at most this many
+                          // points run as one persistent cooperative kernel (ibm_mg.cu); 0: off
 };
 
 template <class T>
@@ -55,8 +57,17 @@ class Multigrid {
   void build(cudaStream_t st, std::vector<MgLevelT<T>> &L, const Box &b, const T *A7, const double h[3]);
   template <class T>
   void cycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const int *gate);
+  void build_tail(cudaStream_t st);
   std::vector<MgLevelT<double>> L64;
   std::vector<MgLevelT<float>> L32;
+  // The fused coarse levels of the FP32 hierarchy: the phase list (device
+  // copy of the kernel's descriptors), its barrier state, the buffer the
+  // phases leave level 1's correction in, their algorithmic bytes, blocks.
+  DBuf<unsigned char> tail_ops_;
+  DBuf<unsigned> tail_bar_;
+  int tail_nops_ = 0, tail_blocks_ = 0, tail_level_ = 0;
+  float *tail_out_ = nullptr;
+  double tail_bytes_ = 0.0;
   const double *winv_ = nullptr;
   DBuf<float> winvf_;   // FP32 copy of winv_ for the FP32 hierarchy
 };

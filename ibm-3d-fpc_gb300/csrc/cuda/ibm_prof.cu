@@ -9,7 +9,7 @@ static const char *kNames[K_COUNT] = {
     "gmres_init", "gmres_spmv_dots", "gmres_orth", "gmres_next", "gmres_update", "gmres_residual", "gmres_add",
     "gmres_fp32_jacobi",
     "mg_load", "mg_relax", "mg_residual", "mg_restrict", "mg_prolong", "mg_dense", "mg_store",
-    "mg_relax_fine", "adjoint", "setup"};
+    "mg_relax_fine", "mg_coarse", "adjoint", "setup"};
 
 const char *kernel_name(int k) { return (k >= 0 && k < K_COUNT) ? kNames[k] : "?"; }
 

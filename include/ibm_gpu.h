@@ -106,6 +106,14 @@ typedef struct ibm_solver_params {
   int df_residual;       /* precision 2 with row classes, 1 (default): the true residual at each restart
                             is computed in double-float on the FP32 pipe (about 48 significant bits;
                             GB300's FP64 rate makes the FP64 stencil the bound there). 0: FP64 */
+  int mg_fused_coarse;   /* FP32 multigrid with two-colour relaxation on 27-point coarse levels: the
+                            coarse end of the V-cycle, from the first level below the finest with at
+                            most this many points, runs as one persistent cooperative kernel per
+                            V-cycle (one phase per former launch, grid-wide barriers between them;
+                            bitwise the same results). 0 (default): one launch per phase; 1: from
+                            the first level of at most 262144 points. Measured on the 640x128x128
+                            channel: no faster (each fused phase stays bound by the latency of its
+                            dependent loads plus the grid barrier, about 5 us) */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {
