@@ -83,6 +83,9 @@ def parse():
                          "persistent kernel per V-cycle (0: off, the library default; 1: 262144 points)")
     ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
                     help="mixed form: 1 = FP32 preconditioners in FP64 GMRES, 2 = also FP32 Arnoldi cycles")
+    ap.add_argument("--drag-validation", type=int, default=0, metavar="NX",
+                    help="run the Schaefer-Turek 3D-1Z case (Re 20, steady) on an NX x NX/5 x NX/5 grid until the "
+                         "drag settles and print c_D, c_L of the cut-surface and staircase forces (no bench line)")
     ap.add_argument("--profile-workload", choices=["pc", "step"], default=None,
                     help="run a small fixed workload for a profiler capture instead of the benchmark: 'pc' applies "
                          "the pressure preconditioner --repeat times, 'step' runs --repeat host-driven timesteps "
@@ -733,9 +736,53 @@ def profile_workload(args):
     s.close()
 
 
+def drag_validation(args):
+    """Schaefer-Turek 3D-1Z: the channel with Um 0.45 (mean inflow U = 4 Um / 9
+    = 0.2), nu 1e-3, cylinder D 0.1: Re = U D / nu = 20, steady. Steps (dt
+    2e-3, mixed form, graph-captured) until c_D changes by less than 1e-6
+    relative over 200 steps; c = 2 F / (rho U^2 D H) with H = 0.41. The
+    benchmark values are c_D 6.185, c_L 0.009."""
+    ibm = importlib.import_module("ibm-3d-fpc_gb300")
+    nx = args.drag_validation
+    case = ibm.Case(ibm.channel_params(nx, nx // 5, nx // 5, Um=0.45, nu=1e-3, dt=2e-3))
+    out = {"case": f"Schaefer-Turek 3D-1Z, {nx}x{nx // 5}x{nx // 5}, dt 2e-3", "reference_cD": 6.185,
+           "reference_cL": 0.009}
+    U, D, H = 4.0 * 0.45 / 9.0, 0.1, case.params.Lz
+    coef = 2.0 / (case.params.rho * U * U * D * H)
+    prm = solver_params(ibm, 2, graph=1)
+    prm.compute_forces = 2
+    s = ibm.Solver(case, prm)
+    t0 = time.perf_counter()
+    prev, k, hist = None, 0, []
+    while k < 20000:
+        for _ in range(200):
+            st = s.step(1.0)
+            k += 1
+        cd = st.force[0] * coef
+        hist.append([k, cd, st.force[1] * coef])
+        if prev is not None and abs(cd - prev) <= 1e-6 * abs(cd):
+            break
+        prev = cd
+    out["cut_surface"] = {"cD": hist[-1][1], "cL": hist[-1][2], "steps": k}
+    # the staircase force of the same settled flow (one more step)
+    p = s.params
+    p.compute_forces = 1
+    s.set_params(p)
+    st = s.step(1.0)
+    out["staircase"] = {"cD": st.force[0] * coef, "cL": st.force[1] * coef}
+    out["cD_rel_err_cut"] = abs(out["cut_surface"]["cD"] - 6.185) / 6.185
+    out["wall_s"] = time.perf_counter() - t0
+    out["history_every_200"] = hist
+    s.close()
+    print(json.dumps({"drag_validation": out}), flush=True)
+
+
 def main():
     args = parse()
     FUSED_COARSE[0] = args.mg_fused_coarse
+    if args.drag_validation:
+        drag_validation(args)
+        return
     if args.impl == "reference":
         reference_arm(args)
         return

@@ -144,6 +144,11 @@ class Solver:
         self._check(self._lib.ibm_set_projection_csr(
             self._ctx, _ptr(a("D_rowptr")), _ptr(a("D_col")), _ptr(a("D_val")), cnt["np"],
             _ptr(a("G_rowptr")), _ptr(a("G_col")), _ptr(a("G_val")), nq))
+        # the body, for the cut-surface force (compute_forces = 2)
+        cp = case.params
+        self._check(self._lib.ibm_set_body(self._ctx, cp.xcirc, cp.ycirc, cp.Rcirc,
+                                           _ptr(np.ascontiguousarray(a("alpha_u"), dtype=np.float64)),
+                                           _ptr(np.ascontiguousarray(a("alpha_v"), dtype=np.float64))))
         self.set_params(params if params is not None else solver_params())
         self.set_fields(*case.initial_fields())
 

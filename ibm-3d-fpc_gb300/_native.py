@@ -124,6 +124,7 @@ def gpu() -> C.CDLL:
         lib.ibm_set_masks.argtypes = [vp] + [vp] * 7 + [vp] * 7
         lib.ibm_set_aux.argtypes = [vp] + [vp] * 7 + [vp]
         lib.ibm_set_projection_csr.argtypes = [vp, vp, vp, vp, i, vp, vp, vp, i]
+        lib.ibm_set_body.argtypes = [vp, d, d, d, vp, vp]
         lib.ibm_set_solver_params.argtypes = [vp, P(SolverParams)]
         lib.ibm_get_solver_params.argtypes = [vp, P(SolverParams)]
         lib.ibm_solver_params_default.argtypes = [P(SolverParams)]

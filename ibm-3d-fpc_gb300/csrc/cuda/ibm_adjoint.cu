@@ -468,6 +468,10 @@ void adj_bc(ibm_ctx *c, double *lu, double *lv, double *lw, const double *ramp) 
 
 void adj_force(ibm_ctx *c, const double *weight) {
   AdjState &a = *c->adj;
+  if (c->prm.compute_forces == 2) {
+    adj_force_cut(c, weight, a.lu.p, a.lp.p, a.acc.p);
+    return;
+  }
   LaunchScope ls(K_ADJOINT, c->st, 1.0 * c->g.NP + 24.0 * c->g.NU + 16.0 * c->g.NP);
   k_force_t<<<adj_grid(c->g.NP), kThreads, 0, c->st>>>(c->fc.p, c->u.p, a.lu.p, a.lp.p, a.acc.p, adims(c), c->g.dx,
                                                       c->g.dy, c->g.dz, c->g.rho, c->g.nu, weight);

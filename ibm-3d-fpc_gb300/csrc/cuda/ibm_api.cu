@@ -754,6 +754,8 @@ int ibm_set_masks(ibm_ctx *c, const uint8_t *active_u, const uint8_t *active_v, 
     for (int f : zw) fw[f] |= kBcSet;
     upload(c->fu, fu, c->st); upload(c->fv, fv, c->st); upload(c->fw, fw, c->st); upload(c->fc, fc, c->st);
     upload(c->zl_u, zu, c->st); upload(c->zl_v, zv, c->st); upload(c->zl_w, zw, c->st);
+    c->h_act_u = au; c->h_act_v = av; c->h_act_w = aw; c->h_fluid = fp;
+    c->body_set = false;
     c->masks_set = true;
     c->aux_set = false;
     c->csr_set = false;
@@ -818,6 +820,17 @@ int ibm_set_aux(ibm_ctx *c, const double *scale_u, const double *scale_v, const 
     upload(c->div_bc_cell, dcell, c->st);
     upload(c->uin, to_host(uin, (size_t)c->g.ny * c->g.nz), c->st);
     c->aux_set = true;
+    invalidate_graph(c);
+    return IBM_OK;
+  });
+}
+
+int ibm_set_body(ibm_ctx *c, double xcirc, double ycirc, double Rcirc, const double *alpha_u,
+                 const double *alpha_v) {
+  return guarded(c, [&]() {
+    if (!c->masks_set) throw Error(IBM_ERR_STATE, "ibm_set_body: call ibm_set_masks first");
+    if (!alpha_u || !alpha_v || !(Rcirc > 0.0)) throw Error(IBM_ERR_ARG, "ibm_set_body: bad arguments");
+    build_cut_force(c, xcirc, ycirc, Rcirc, to_host(alpha_u, c->g.NU), to_host(alpha_v, c->g.NV));
     invalidate_graph(c);
     return IBM_OK;
   });

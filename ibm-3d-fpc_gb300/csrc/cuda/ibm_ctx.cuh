@@ -35,6 +35,15 @@ struct AdjState;  // adjoint extension (ibm_adjoint.cuh)
 
 }  // namespace ibm
 
+struct ibm_ctx;
+namespace ibm {
+// cut-surface force (ibm_force.cu)
+void launch_forces_cut(ibm_ctx *c);
+void adj_force_cut(ibm_ctx *c, const double *weight, double *lu, double *lp, double *acc);
+void build_cut_force(ibm_ctx *c, double xcirc, double ycirc, double Rcirc, const std::vector<double> &alpha_u,
+                     const std::vector<double> &alpha_v);
+}  // namespace ibm
+
 struct ibm_ctx {
   ibm_grid_desc grid;
   ibm::Geometry g;
@@ -59,6 +68,13 @@ struct ibm_ctx {
   std::vector<int32_t> h_id_p, h_id_qu, h_id_qv, h_id_qw;
   std::vector<int32_t> h_id_u_rows, h_id_v_rows, h_id_w_rows;  // id of each solve-box row (0: identity row)
   int n_id[3] = {0, 0, 0};       // largest momentum ids
+  std::vector<uint8_t> h_act_u, h_act_v, h_act_w, h_fluid;  // masks (for ibm_set_body)
+  // cut-surface force (ibm_set_body; ibm_force.cu): entry codes, indices, weights
+  bool body_set = false;
+  long cf_n = 0;
+  ibm::DBuf<uint8_t> cf_code;
+  ibm::DBuf<int> cf_idx;
+  ibm::DBuf<double> cf_w;
 
   ibm::DBuf<double> u, v, w, p, ut, vt, wt;
   ibm::DBuf<double> xb[4], bb[4];

@@ -780,6 +780,10 @@ __global__ void __launch_bounds__(kThreads) k_forces(ForceArgs A) {
 }
 
 void launch_forces(ibm_ctx *c) {
+  if (c->prm.compute_forces == 2) {
+    launch_forces_cut(c);
+    return;
+  }
   ForceArgs A;
   A.d = dims_of(c);
   A.u = c->u.p; A.v = c->v.p; A.w = c->w.p; A.p = c->p.p;

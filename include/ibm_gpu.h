@@ -95,7 +95,8 @@ typedef struct ibm_solver_params {
   double cycle_rtol32;   /* precision 2: an FP32 Arnoldi cycle stops once its residual estimate fell by
                             this factor (default 1e-5, about what an FP32 basis resolves); the FP64
                             restart then measures the true residual */
-  int compute_forces;    /* 1: fill ibm_step_stats.force each step (one extra kernel); default 0 */
+  int compute_forces;    /* fill ibm_step_stats.force each step (one extra kernel): 1 staircase force,
+                            2 cut-surface force (needs ibm_set_body); default 0 */
   int row_classes;       /* 1 (default): where an operator repeats few distinct rows (every fluid cell
                             away from walls and bodies has the same ones), kernels read a 2-byte class
                             per row and the row from a table of the distinct rows; results are bitwise
@@ -199,6 +200,20 @@ int ibm_assemble_momentum(ibm_ctx *ctx, double xcirc, double ycirc, double Rcirc
 int ibm_assemble_pressure(ibm_ctx *ctx, const uint8_t *fluid_p, const int32_t *id_p, const double *beta_p,
                           const double *const *alpha, const uint8_t *const *active_q, const int32_t *const *id_q,
                           double *vals_out);
+
+/* The body for the cut-surface force (compute_forces = 2); the reference
+ * computes no force. Cylinder centre and radius as the geometry code takes
+ * them (common.hpp:64-66) and the open fractions of the u and v faces
+ * (alpha_u, alpha_v: full MAC layouts, host or device pointers; the
+ * fractions immersed_geometry.hpp:29-73 computes, extruded in z). The shear
+ * is the wall flux the momentum operators apply where a row meets the body
+ * (rho nu u_P / d_P over the control-volume face, d_P from
+ * segmentCircleDistance, immersed_operators.hpp:1-177); the pressure acts
+ * on each fluid cell's cut surface, -sum_f alpha_f A_f n_f, with faces
+ * towards non-fluid cells closed. Requires ibm_set_masks; a later
+ * ibm_set_masks drops the body. */
+int ibm_set_body(ibm_ctx *ctx, double xcirc, double ycirc, double Rcirc, const double *alpha_u,
+                 const double *alpha_v);
 
 /* Solver configuration (main.cu:173-221). */
 void ibm_solver_params_default(ibm_solver_params *p);

@@ -50,6 +50,10 @@ struct oracle {
   double *mg_winv;          /* 1 / W (ones when not symmetrized) */
   int nlev;
   mg_level lev[40];
+  /* the body, for the cut-surface force (oracle_set_body) */
+  int body_set;
+  double xcirc, ycirc, Rcirc;
+  double *alpha_u, *alpha_v;
 };
 
 /* ------------------------------------------------------------------------ */
@@ -1010,6 +1014,7 @@ void oracle_destroy(oracle *o) {
   free(o->u); free(o->v); free(o->w); free(o->p);
   for (int f = 0; f < 4; ++f) free(o->invd[f]);
   free(o->mg_winv);
+  free(o->alpha_u); free(o->alpha_v);
   for (int l = 0; l < o->nlev; ++l) {
     mg_level *L = &o->lev[l];
     free(L->A); free(L->wd); free(L->invd); free(L->pm); free(L->pp); free(L->bv); free(L->xv); free(L->rv);
@@ -1109,7 +1114,132 @@ static int o_fluid(const oracle *o, int i, int j, int k) {
 static int o_solid(const oracle *o, int i, int j, int k) {
   return i >= 0 && i < o->nx && j >= 0 && j < o->ny && k >= 0 && k < o->nz && !o_fluid(o, i, j, k);
 }
+/* Distance from P along the segment P->S to the cylinder surface, +inf when
+ * the segment does not reach it: the reference's segmentCircleDistance
+ * (common.hpp:262-280), the root t in [0, 1] of |P + t (S - P) - C| = R
+ * nearest P, times |S - P|. */
+static double seg_circle(const oracle *o, double xP, double yP, double xS, double yS) {
+  const double ddx = xS - xP, ddy = yS - yP;
+  const double a = ddx * ddx + ddy * ddy;
+  if (a <= 0.0) return INFINITY;
+  const double ox = xP - o->xcirc, oy = yP - o->ycirc;
+  const double b = 2.0 * (ddx * ox + ddy * oy);
+  const double c = ox * ox + oy * oy - o->Rcirc * o->Rcirc;
+  const double disc = b * b - 4.0 * a * c;
+  if (disc < 0.0) return INFINITY;
+  const double sd = sqrt(disc > 0.0 ? disc : 0.0);
+  const double t1 = (-b - sd) / (2.0 * a), t2 = (-b + sd) / (2.0 * a);
+  double t = INFINITY;
+  if (t1 >= 0.0 && t1 <= 1.0) t = t1;
+  else if (t2 >= 0.0 && t2 <= 1.0) t = t2;
+  if (!isfinite(t)) return INFINITY;
+  return sqrt(a) * t;
+}
+static double inv_seg(const oracle *o, double xP, double yP, double xS, double yS) {
+  const double d = seg_circle(o, xP, yP, xS, yS);
+  return isfinite(d) ? 1.0 / d : 0.0;
+}
+
+/* The cut-surface shear weight of one velocity row: sum over the directions
+ * where the row meets the body (an inactive neighbour that is not a domain
+ * boundary, as the momentum operators decide it, immersed_operators.hpp:1-177)
+ * of the control-volume face area over the distance to the cylinder, times
+ * rho. field 0, 1, 2 = u, v, w; (i, j, k) the face. */
+static double cut_shear_weight(const oracle *o, int field, int i, int j, int k) {
+  const int nx = o->nx, ny = o->ny;
+  const double dx = o->dx, dy = o->dy, dz = o->dz, ax = dy * dz, ay = dx * dz;
+  double s = 0.0;
+  if (field == 0) {
+    const double xP = i * dx, yP = (j + 0.5) * dy;
+#define AU(ii, jj) (o->in.active_u[U3(o, ii, jj, k)] != 0)
+    if (!(i > 1 && AU(i - 1, j)) && i != 1) s += ax * inv_seg(o, xP, yP, xP - dx, yP);
+    if (!(i < nx - 1 && AU(i + 1, j)) && i != nx - 1) s += ax * inv_seg(o, xP, yP, xP + dx, yP);
+    if (!(j > 0 && AU(i, j - 1)) && j != 0) s += ay * inv_seg(o, xP, yP, xP, yP - dy);
+    if (!(j < ny - 1 && AU(i, j + 1)) && j != ny - 1) s += ay * inv_seg(o, xP, yP, xP, yP + dy);
+#undef AU
+  } else if (field == 1) {
+    const double xP = (i + 0.5) * dx, yP = j * dy;
+#define AV(ii, jj) (o->in.active_v[V3(o, ii, jj, k)] != 0)
+    if (!(i > 0 && AV(i - 1, j)) && i != 0) s += ax * inv_seg(o, xP, yP, xP - dx, yP);
+    if (!(i < nx - 1 && AV(i + 1, j)) && i != nx - 1) s += ax * inv_seg(o, xP, yP, xP + dx, yP);
+    if (!(j > 1 && AV(i, j - 1)) && j != 1) s += ay * inv_seg(o, xP, yP, xP, yP - dy);
+    if (!(j < ny - 1 && AV(i, j + 1)) && j != ny - 1) s += ay * inv_seg(o, xP, yP, xP, yP + dy);
+#undef AV
+  } else {
+    const double xP = (i + 0.5) * dx, yP = (j + 0.5) * dy;
+#define AW(ii, jj) (o->in.active_w[W3(o, ii, jj, k)] != 0)
+    if (!(i > 0 && AW(i - 1, j)) && i != 0) s += ax * inv_seg(o, xP, yP, xP - dx, yP);
+    if (!(i < nx - 1 && AW(i + 1, j)) && i != nx - 1) s += ax * inv_seg(o, xP, yP, xP + dx, yP);
+    if (!(j > 0 && AW(i, j - 1)) && j != 0) s += ay * inv_seg(o, xP, yP, xP, yP - dy);
+    if (!(j < ny - 1 && AW(i, j + 1)) && j != ny - 1) s += ay * inv_seg(o, xP, yP, xP, yP + dy);
+#undef AW
+  }
+  return o->prm.rho * s;
+}
+
+/* Pressure weights of a fluid cell for the x and y force: the cell's part of
+ * the body surface, -sum over its faces of alpha_f A_f n_f. A face to a
+ * non-fluid cell is closed (the body's surface), a domain-boundary face open;
+ * so the faces of the fluid cells close around the body and a uniform
+ * pressure gives no force. */
+static void cut_pressure_weight(const oracle *o, int i, int j, int k, double *wx, double *wy) {
+  const int nx = o->nx, ny = o->ny;
+  const double ax = o->dy * o->dz, ay = o->dx * o->dz;
+  const double aw = i > 0 ? (o_fluid(o, i - 1, j, k) ? o->alpha_u[U3(o, i, j, k)] : 0.0) : 1.0;
+  const double ae = i < nx - 1 ? (o_fluid(o, i + 1, j, k) ? o->alpha_u[U3(o, i + 1, j, k)] : 0.0) : 1.0;
+  const double as = j > 0 ? (o_fluid(o, i, j - 1, k) ? o->alpha_v[V3(o, i, j, k)] : 0.0) : 1.0;
+  const double an = j < ny - 1 ? (o_fluid(o, i, j + 1, k) ? o->alpha_v[V3(o, i, j + 1, k)] : 0.0) : 1.0;
+  *wx = (aw - ae) * ax;
+  *wy = (as - an) * ay;
+}
+
+void oracle_set_body(oracle *o, double xcirc, double ycirc, double Rcirc, const double *alpha_u,
+                     const double *alpha_v) {
+  const long NU = (long)(o->nx + 1) * o->ny * o->nz, NV = (long)o->nx * (o->ny + 1) * o->nz;
+  free(o->alpha_u); free(o->alpha_v);
+  o->alpha_u = (double *)xcalloc((size_t)NU, 8);
+  o->alpha_v = (double *)xcalloc((size_t)NV, 8);
+  memcpy(o->alpha_u, alpha_u, sizeof(double) * (size_t)NU);
+  memcpy(o->alpha_v, alpha_v, sizeof(double) * (size_t)NV);
+  o->xcirc = xcirc; o->ycirc = ycirc; o->Rcirc = Rcirc;
+  o->body_set = 1;
+}
+
+/* Cut-surface force: shear nu w u over the u, v, w rows, then pressure over
+ * the fluid cells. */
+static void forces_cut(const oracle *o, double f[3]) {
+  const int nx = o->nx, ny = o->ny, nz = o->nz;
+  const double nu = o->prm.nu;
+  f[0] = f[1] = f[2] = 0.0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 1; i < nx; ++i)
+        if (o->in.active_u[U3(o, i, j, k)]) f[0] += nu * cut_shear_weight(o, 0, i, j, k) * o->u[U3(o, i, j, k)];
+  for (int k = 0; k < nz; ++k)
+    for (int j = 1; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        if (o->in.active_v[V3(o, i, j, k)]) f[1] += nu * cut_shear_weight(o, 1, i, j, k) * o->v[V3(o, i, j, k)];
+  for (int k = 1; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+        if (o->in.active_w[W3(o, i, j, k)]) f[2] += nu * cut_shear_weight(o, 2, i, j, k) * o->w[W3(o, i, j, k)];
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        if (!o_fluid(o, i, j, k)) continue;
+        double wx, wy;
+        cut_pressure_weight(o, i, j, k, &wx, &wy);
+        const double pc = o->p[((long)k * ny + j) * nx + i];
+        f[0] += wx * pc;
+        f[1] += wy * pc;
+      }
+}
+
 void oracle_forces(const oracle *o, double f[3]) {
+  if (o->body_set) {
+    forces_cut(o, f);
+    return;
+  }
   const int nx = o->nx, ny = o->ny, nz = o->nz;
   const double dx = o->dx, dy = o->dy, dz = o->dz, t2 = 2.0 * o->prm.rho * o->prm.nu;
   const double ax = dy * dz, ay = dx * dz, az = dx * dy;
@@ -1342,6 +1472,26 @@ static void conv_adjoint(const oracle *o, const double *u, const double *v, cons
  * proportional to nu). */
 static void force_x_adjoint(const oracle *o, double weight, double *lu, double *lp, double *dnu) {
   const int nx = o->nx, ny = o->ny, nz = o->nz;
+  if (o->body_set) {  /* cut-surface force: linear in u and p */
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 1; i < nx; ++i) {
+          const long f = U3(o, i, j, k);
+          if (!o->in.active_u[f]) continue;
+          const double s = cut_shear_weight(o, 0, i, j, k);
+          lu[f] += weight * o->prm.nu * s;
+          *dnu += weight * s * o->u[f];
+        }
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nx; ++i) {
+          if (!o_fluid(o, i, j, k)) continue;
+          double wx, wy;
+          cut_pressure_weight(o, i, j, k, &wx, &wy);
+          lp[((long)k * ny + j) * nx + i] += weight * wx;
+        }
+    return;
+  }
   const double dx = o->dx, dy = o->dy, dz = o->dz, t2 = 2.0 * o->prm.rho * o->prm.nu;
   const double ax = dy * dz;
   for (int k = 0; k < nz; ++k)

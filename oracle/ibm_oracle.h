@@ -75,6 +75,11 @@ void oracle_get_fields(const oracle *o, double *u, double *v, double *w, double 
 int oracle_step(oracle *o, double ramp, oracle_step_stats *st);
 /* Force of the fluid on the body from the current fields (the step fills st->force). */
 void oracle_forces(const oracle *o, double f[3]);
+/* Switch oracle_forces (and the adjoint's drag seed) to the cut-surface
+ * force of the cylinder (xcirc, ycirc, Rcirc) with the u and v faces' open
+ * fractions (full MAC layouts; copied). */
+void oracle_set_body(oracle *o, double xcirc, double ycirc, double Rcirc, const double *alpha_u,
+                     const double *alpha_v);
 
 /* Pieces of the step, for kernel-level checks. */
 void oracle_bc_cleanup(const oracle *o, double *u, double *v, double *w, const double *uin_step);

@@ -89,6 +89,7 @@ def lib() -> C.CDLL:
         L.oracle_mg_level_coef.argtypes = [vp, i, vp]
         L.oracle_mg_vcycle.argtypes = [vp, vp, vp]
         L.oracle_step_backward.argtypes = [vp, vp, d, vp, d, vp, vp, vp, vp, vp, vp]
+        L.oracle_set_body.argtypes = [vp, d, d, d, vp, vp]
         _lib = L
     return _lib
 
@@ -104,7 +105,7 @@ class Oracle:
     def __init__(self, case, *, vel_tol=1e-13, vel_maxit=500, vel_kdim=50, vel_jacobi_iters=1, p_tol=1e-13,
                  p_maxit=500, p_kdim=50, p_pc=1, mg_rap=1, mg_relax=1, mg_nu1=1, mg_nu2=1, mg_omega=2.0 / 3.0,
                  mg_coarse_max=64, mg_max_levels=40, mg_group_ratio=0.0, mg_options=3, mg_nu_coarse=0,
-                 use_zero_initial_guess=1):
+                 use_zero_initial_guess=1, cut_force=False):
         self.L = lib()
         cp = case.params
         self.shape = (cp.nx, cp.ny, cp.nz)
@@ -116,6 +117,9 @@ class Oracle:
         self._keep = {n: np.ascontiguousarray(case.array(names.get(n, n))) for n in _IN_FIELDS}
         self.inp = OracleInputs(*[_p(self._keep[n]) for n in _IN_FIELDS])
         self.h = self.L.oracle_create(C.byref(self.prm), C.byref(self.inp))
+        if cut_force:  # forces (and the adjoint's drag seed) on the cut surface of the cylinder
+            self._alpha = [np.ascontiguousarray(case.array(n), dtype=np.float64) for n in ("alpha_u", "alpha_v")]
+            self.L.oracle_set_body(self.h, cp.xcirc, cp.ycirc, cp.Rcirc, _p(self._alpha[0]), _p(self._alpha[1]))
         u, v, w, p = case.initial_fields()
         self.set_fields(u, v, w, p)
 

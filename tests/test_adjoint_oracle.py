@@ -55,32 +55,34 @@ def test_legendre_basis(ibm, inflow):
     assert np.allclose(B[:ny, 1], yh)
 
 
-def test_oracle_adjoint_matches_finite_differences(ibm, pyoracle, inflow):
+@pytest.mark.parametrize("cut_force", [False, True], ids=["staircase", "cut-surface"])
+def test_oracle_adjoint_matches_finite_differences(ibm, pyoracle, inflow, cut_force):
     base = case_nu(ibm, 1e-3)
     rng = np.random.default_rng(3)
     c = rng.uniform(-0.05, 0.05, 64) * base.params.Um
     g0 = inflow.inflow_from_coefficients(base, c)
-    J, dg, dnu, _ = pyoracle.drag_gradient(inflow.InflowCase(base, g0), RAMPS, WINDOW, **ORACLE_KW)
+    kw = dict(ORACLE_KW, cut_force=cut_force)
+    J, dg, dnu, _ = pyoracle.drag_gradient(inflow.InflowCase(base, g0), RAMPS, WINDOW, **kw)
     assert np.isfinite(J) and J != 0.0
     B = inflow.legendre_basis(base)
     dc = B.T @ dg
     h = 1e-6
     # a random direction in coefficient space
     d = rng.standard_normal(64)
-    jp = pyoracle.drag_objective(inflow.InflowCase(base, g0 + B @ (h * d)), RAMPS, WINDOW, **ORACLE_KW)
-    jm = pyoracle.drag_objective(inflow.InflowCase(base, g0 - B @ (h * d)), RAMPS, WINDOW, **ORACLE_KW)
+    jp = pyoracle.drag_objective(inflow.InflowCase(base, g0 + B @ (h * d)), RAMPS, WINDOW, **kw)
+    jm = pyoracle.drag_objective(inflow.InflowCase(base, g0 - B @ (h * d)), RAMPS, WINDOW, **kw)
     fd = (jp - jm) / (2 * h)
     assert abs(dc @ d - fd) <= 1e-5 * abs(fd)
     # the leading coefficient on its own
     e = np.zeros(64)
     e[0] = 1.0
-    jp = pyoracle.drag_objective(inflow.InflowCase(base, g0 + B @ (h * e)), RAMPS, WINDOW, **ORACLE_KW)
-    jm = pyoracle.drag_objective(inflow.InflowCase(base, g0 - B @ (h * e)), RAMPS, WINDOW, **ORACLE_KW)
+    jp = pyoracle.drag_objective(inflow.InflowCase(base, g0 + B @ (h * e)), RAMPS, WINDOW, **kw)
+    jm = pyoracle.drag_objective(inflow.InflowCase(base, g0 - B @ (h * e)), RAMPS, WINDOW, **kw)
     fd = (jp - jm) / (2 * h)
     assert abs(dc[0] - fd) <= 1e-5 * abs(fd)
     # nu: the operators, row scales, inlet lift and wall shear all change
-    jp = pyoracle.drag_objective(inflow.InflowCase(case_nu(ibm, 1e-3 + h), g0), RAMPS, WINDOW, **ORACLE_KW)
-    jm = pyoracle.drag_objective(inflow.InflowCase(case_nu(ibm, 1e-3 - h), g0), RAMPS, WINDOW, **ORACLE_KW)
+    jp = pyoracle.drag_objective(inflow.InflowCase(case_nu(ibm, 1e-3 + h), g0), RAMPS, WINDOW, **kw)
+    jm = pyoracle.drag_objective(inflow.InflowCase(case_nu(ibm, 1e-3 - h), g0), RAMPS, WINDOW, **kw)
     fd = (jp - jm) / (2 * h)
     assert abs(dnu - fd) <= 1e-5 * abs(fd)
 
@@ -227,3 +229,20 @@ def test_oracle_adjoint_transpose_odd_grids(ibm, pyoracle, shape):
     lhs = sum(float(l @ d) for l, d in zip(lam, ds)) + float(dg @ dgdir)
     rhs = sum(float(l @ ((a - b) / (2 * h))) for l, a, b in zip(lam1, sp, sm))
     assert abs(lhs - rhs) <= 1e-9 * abs(rhs)
+
+
+def test_cut_surface_force_of_a_closed_body(ibm, pyoracle):
+    """A uniform pressure on the fluid cells and no flow give no cut-surface
+    force: the fluid cells' faces (partly open where the cylinder cuts them,
+    closed towards non-fluid cells) close around the body."""
+    case = case_nu(ibm, 1e-3)
+    o = pyoracle.Oracle(case, cut_force=True)
+    u, v, w, p = o.fields()
+    o.set_fields(np.zeros_like(u), np.zeros_like(v), np.zeros_like(w), 3.0 * case.array("fluid_p"))
+    f = o.forces()
+    assert np.abs(f).max() <= 1e-15
+    # a pressure rising along x pushes the body against it: F_x < 0
+    nx, ny, nz = case.shape
+    ramp = np.broadcast_to(np.arange(nx, dtype=float), (nz, ny, nx)).ravel() * case.array("fluid_p")
+    o.set_fields(np.zeros_like(u), np.zeros_like(v), np.zeros_like(w), ramp)
+    assert o.forces()[0] < 0

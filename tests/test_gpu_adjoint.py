@@ -37,16 +37,18 @@ def rel_err(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
-@pytest.mark.parametrize("graph", [0, 1])
-def test_backward_step_matches_oracle(ibm, pyoracle, graph):
+@pytest.mark.parametrize("graph,model", [(0, 1), (1, 1), (0, 2), (1, 2)],
+                         ids=["host-staircase", "graph-staircase", "host-cut", "graph-cut"])
+def test_backward_step_matches_oracle(ibm, pyoracle, graph, model):
     """One reverse step, host-driven or as the captured graph (transposed
-    solves with their loops on the device)."""
+    solves with their loops on the device), with the staircase (1) or the
+    cut-surface (2) drag as the objective's force."""
     case = case_nu(ibm)
-    o = pyoracle.Oracle(case, **ORACLE_KW)
+    o = pyoracle.Oracle(case, cut_force=model == 2, **ORACLE_KW)
     ot = pyoracle.Oracle(pyoracle.TransposedCase(case), **ORACLE_KW)
     o.step(1.0)
     s0 = o.fields()
-    s = ibm.Solver(case, fp64_params(ibm, use_graph=graph))
+    s = ibm.Solver(case, fp64_params(ibm, use_graph=graph, compute_forces=model))
     s.adjoint_setup()
     s.set_fields(*s0)
     rng = np.random.default_rng(11)
@@ -129,13 +131,14 @@ def gpu_objective(ibm, case, g, ramps, window, params):
     return J
 
 
-def test_gpu_gradient_matches_finite_differences(ibm, inflow):
+@pytest.mark.parametrize("model", [1, 2], ids=["staircase", "cut-surface"])
+def test_gpu_gradient_matches_finite_differences(ibm, inflow, model):
     base = case_nu(ibm)
     rng = np.random.default_rng(5)
     g0 = inflow.inflow_from_coefficients(base, rng.uniform(-0.05, 0.05, 64))
     ramps = [0.5, 1.0, 1.0, 1.0]
     window = {2, 3, 4}
-    prm = fp64_params(ibm)
+    prm = fp64_params(ibm, compute_forces=model)
     s = ibm.Solver(base, prm)
     s.adjoint_setup()
     s.set_inflow(g0)

@@ -215,11 +215,14 @@ def test_fp32_cycles_reach_tight_tolerance(ibm, pyoracle, case48):
         assert rel_err(a, b) <= 1e-9, name
 
 
-def test_forces_match_oracle(ibm, pyoracle, case48):
-    """Body force (staircase pressure + wall shear) of the device step equals
-    the oracle's on the same fields; off by default."""
-    s = ibm.Solver(case48, tight(ibm, compute_forces=1))
-    orc = pyoracle.Oracle(case48, vel_tol=1e-13, p_tol=1e-13)
+@pytest.mark.parametrize("model", [1, 2], ids=["staircase", "cut-surface"])
+def test_forces_match_oracle(ibm, pyoracle, case48, model):
+    """Body force of the device step equals the oracle's on the same fields
+    (1: staircase pressure and wall shear; 2: cut-surface force from the
+    operators' wall distances and the faces' open fractions); off by
+    default."""
+    s = ibm.Solver(case48, tight(ibm, compute_forces=model))
+    orc = pyoracle.Oracle(case48, vel_tol=1e-13, p_tol=1e-13, cut_force=model == 2)
     for step in range(1, 5):
         st = s.step(min(1.0, step / 2.0))
         so = orc.step(min(1.0, step / 2.0))
