@@ -45,6 +45,11 @@ import time
 
 import numpy as np
 
+# 32 hardware work queues for the ensemble's 32 streams (the library's own
+# default; set here too because torch may create the CUDA context before the
+# library is imported)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -73,6 +78,8 @@ def parse():
                          "full-timestep configuration) and report the drag/lift series and the field error")
     ap.add_argument("--long-run-tol", type=float, default=1e-8,
                     help="relative residual tolerance of both forms' solves in the long run")
+    ap.add_argument("--long-run-mixed-p-tol", type=float, default=0.0,
+                    help="pressure tolerance of the mixed form in the long run (0: --long-run-tol)")
     ap.add_argument("--ensemble", type=int, default=32, help="instances of the batched ensemble")
     ap.add_argument("--ensemble-autotune", action="store_true",
                     help="also tune the ensemble's multigrid schedule by size class (autotune.py) and measure it")
@@ -449,6 +456,8 @@ def long_run_measure(ibm, args, local, nx, ny, nz):
         prm = solver_params(ibm, precision, graph=1, coarse_max=args.mg_coarse_max)
         prm.compute_forces = 1
         prm.vel_tol = prm.p_tol = args.long_run_tol
+        if precision != 0 and args.long_run_mixed_p_tol > 0:
+            prm.p_tol = args.long_run_mixed_p_tol
         prm.mg_nu1 = prm.mg_nu2 = nu
         s = ibm.Solver(case, prm, device=local)
         s.set_fields(*state)
@@ -479,9 +488,10 @@ def long_run_measure(ibm, args, local, nx, ny, nz):
     D, U = 0.1, 1.0  # diameter; mean inflow over the square section (4/9 of the peak 2.25)
     H = case.params.Ly
     coef = 2.0 / (case.params.rho * U * U * D * H)
+    mixed_p = args.long_run_mixed_p_tol if args.long_run_mixed_p_tol > 0 else args.long_run_tol
     return {"workload": f"{n} steps of the full timestep {nx}x{ny}x{nz}, mixed (precision {args.precision}), "
                         f"plain FP64 and an FP64 control side by side, graph-captured, no ramp, solves to "
-                        f"{args.long_run_tol:g}",
+                        f"{args.long_run_tol:g} (mixed pressure solve to {mixed_p:g})",
             "steps": n, "worst_status": int(worst), "wall_s": wall,
             "velocity_rel_err_max": max(e[1] for e in errors), "velocity_rel_err_final": errors[-1][1],
             "pressure_rel_err_final": errors[-1][2],

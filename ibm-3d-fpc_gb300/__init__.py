@@ -14,7 +14,16 @@ from __future__ import annotations
 
 import ctypes as C
 import dataclasses
+import os
 from typing import Optional
+
+# A batch steps every instance on its own stream. CUDA maps streams onto
+# CUDA_DEVICE_MAX_CONNECTIONS hardware work queues (8 unless set), and streams
+# that share a queue serialise; 32 queues let the 32-channel ensemble run
+# concurrently (1513 -> 2531 instance-steps/s on a GB300). It takes effect
+# only if set before the process creates its CUDA context, and a value the
+# caller set is kept.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np
 
