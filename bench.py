@@ -81,6 +81,9 @@ def parse():
     ap.add_argument("--long-run-mixed-p-tol", type=float, default=0.0,
                     help="pressure tolerance of the mixed form in the long run (0: --long-run-tol)")
     ap.add_argument("--ensemble", type=int, default=32, help="instances of the batched ensemble")
+    ap.add_argument("--ensemble-steps", type=int, default=500,
+                    help="steps of the ensemble's accuracy run: the mixed batch and an FP64 batch from the same "
+                         "initial states, each instance's velocity difference reported (0: skip)")
     ap.add_argument("--ensemble-autotune", action="store_true",
                     help="also tune the ensemble's multigrid schedule by size class (autotune.py) and measure it")
     ap.add_argument("--mg-coarse-max", type=int, default=2560,
@@ -289,10 +292,44 @@ def ensemble_measure(ibm, args, ws, rank, local, steps, warmup):
                  "note": "median instance of each of 4 log-spaced cell-count classes tuned over 5 multigrid "
                          "schedules (3 timed steps each), the winner applied to its class"}
     cells = sum(nx * ny * nz for nx, ny, nz, *_ in specs)
-    batch.close()
+    accuracy = None
+    if args.ensemble_steps > 0:
+        # the configuration's full run: every instance args.ensemble_steps
+        # steps in the mixed form and, from the same initial states, in FP64
+        # (graph-captured both); the mixed batch's run is timed too
+        nst = args.ensemble_steps
+        for s, c in zip(batch.solvers, cases):
+            s.set_fields(*initial_state(c))
+        if ws > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(nst):
+            worst = max(worst, max(st.status for st in batch.step(1.0)))
+        t_long = reduce_max_ms((time.perf_counter() - t0) * 1e3, ws, "cuda")
+        mixed_fields = [s.fields() for s in batch.solvers]
+        batch.close()
+        b64 = ibm.Batch(cases, solver_params(ibm, 0, graph=1, coarse_max=args.mg_coarse_max), device=local)
+        for s, c in zip(b64.solvers, cases):
+            s.set_fields(*initial_state(c))
+        for _ in range(nst):
+            worst = max(worst, max(st.status for st in b64.step(1.0)))
+        errs = []
+        for fm, s in zip(mixed_fields, b64.solvers):
+            f64 = s.fields()
+            umax = max(float(np.abs(x).max()) for x in f64[:3])
+            errs.append(max(float(np.abs(a - b).max()) for a, b in zip(fm[:3], f64[:3])) / umax)
+        b64.close()
+        accuracy = {"steps": nst, "instance_steps_per_s": len(specs) * nst / (t_long / 1e3),
+                    "velocity_rel_err_vs_fp64": errs, "velocity_rel_err_max": max(errs),
+                    "note": "each instance's largest velocity difference from an FP64 batch of the same instance "
+                            "after the same steps, relative to the FP64 run's largest |u|; instance order as "
+                            "'instances' of this rank"}
+    else:
+        batch.close()
     n = len(specs)
     out_tuned = {"autotuned": tuned} if tuned else {}
-    return {**out_tuned, "workload": f"{n} independent channels, seeded sizes {{96..256}}x{{16..48}}x{{16..48}} (multiples of 16), "
+    out_acc = {"accuracy_run": accuracy} if accuracy else {}
+    return {**out_tuned, **out_acc, "workload": f"{n} independent channels, seeded sizes {{96..256}}x{{16..48}}x{{16..48}} (multiples of 16), "
                         "cylinder D U(0.06,0.14) at y U(0.15,0.26), Um U(0.2,2.25), dt 1e-3, same solver settings",
             "instances": n, "cells": cells, "steps": steps,
             "instance_steps_per_s": n * steps / (t_batch / 1e3),
@@ -371,7 +408,7 @@ def pressure_only_measure(ibm, args, local, plib, Prof, repeats=3):
 def adjoint_measure(ibm, args, local):
     """The adjoint-sensitivity workload: 256x48x48 channel (Um 0.45, nu 1e-3,
     dt 1e-3, no ramp), FP64 graph-captured steps and FP64 transposed solves
-    at 1e-12; objective = mean drag over steps 100..200 of 200 from the
+    at 1e-12; objective = mean cut-surface drag over steps 100..200 of 200 from the
     reference's initial state; parameters = 8x8 Legendre coefficients of the
     inflow (drawn as U(-0.05, 0.05) Um, PCG64 seed 4) and nu; checkpoints
     every 20 steps with recomputation. Gradient time against one forward
@@ -389,7 +426,7 @@ def adjoint_measure(ibm, args, local):
     prm = ibm.solver_params(vel_tol=1e-12, p_tol=1e-12, vel_maxit=500, p_maxit=500, p_pc=1, p_pc_rap_type=0,
                             p_pc_relax_type=2, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_omega=1.0,
                             mg_group_ratio=1.5, mg_coarse_max=args.mg_coarse_max, precision=0, use_graph=1,
-                            compute_forces=1)
+                            compute_forces=2)
     base = case_nu(1e-3)
     rng = np.random.default_rng(4)
     g0 = inflow.inflow_from_coefficients(base, rng.uniform(-0.05, 0.05, 64) * base.params.Um)
@@ -454,7 +491,7 @@ def long_run_measure(ibm, args, local, nx, ny, nz):
     # the same tolerance along other iterates
     for precision, nu in ((args.precision, 3), (0, 3), (0, 2)):
         prm = solver_params(ibm, precision, graph=1, coarse_max=args.mg_coarse_max)
-        prm.compute_forces = 1
+        prm.compute_forces = 2
         prm.vel_tol = prm.p_tol = args.long_run_tol
         if precision != 0 and args.long_run_mixed_p_tol > 0:
             prm.p_tol = args.long_run_mixed_p_tol
@@ -500,7 +537,7 @@ def long_run_measure(ibm, args, local, nx, ny, nz):
             "errors_columns": "step, mixed vs FP64 velocity, mixed vs FP64 pressure, control (FP64 with 2+2 "
                               "finest-level sweeps) vs FP64 velocity; velocity differences relative to the FP64 "
                               "run's largest |u|",
-            "force_coefficients": "c = 2 F / (rho U^2 D H), U = 1 (mean inflow), D = 0.1, H = Lz",
+            "force_coefficients": "cut-surface force, c = 2 F / (rho U^2 D H), U = 1 (mean inflow), D = 0.1, H = Lz",
             "cD_final": [series[-1][1] * coef, series[-1][3] * coef] if series else None,
             "cL_final": [series[-1][2] * coef, series[-1][4] * coef] if series else None,
             "drag_lift_every_10": series}
