@@ -54,7 +54,8 @@ class SolverParams(C.Structure):
                 ("vel_inner_sweeps", C.c_int), ("mg_group_ratio", C.c_double), ("mg_options", C.c_int),
                 ("mg_nu_coarse", C.c_int), ("cycle_rtol32", C.c_double), ("compute_forces", C.c_int),
                 ("row_classes", C.c_int), ("mg_quads", C.c_int),
-                ("df_residual", C.c_int), ("mg_fused_coarse", C.c_int)]
+                ("df_residual", C.c_int), ("mg_fused_coarse", C.c_int),
+                ("mg_fused_sweep", C.c_int)]
 
 
 class Profile(C.Structure):

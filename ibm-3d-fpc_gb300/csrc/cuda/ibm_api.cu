@@ -313,6 +313,7 @@ void ensure_solvers(ibm_ctx *c) {
     mp.classes = p.row_classes ? 1 : 0;
     mp.quads = p.mg_quads ? 1 : 0;
     mp.fused_coarse = p.mg_fused_coarse == 1 ? 262144 : std::max(0, p.mg_fused_coarse);
+    mp.fused_sweep = p.mg_fused_sweep ? 1 : 0;
     const double h[3] = {c->g.dx, c->g.dy, c->g.dz};
     const double *winv = ((p.mg_options & 2) && c->p_sym) ? c->p_winv.p : nullptr;
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
@@ -439,6 +440,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->mg_quads = 1;
   p->df_residual = 1;
   p->mg_fused_coarse = 0;
+  p->mg_fused_sweep = 0;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }

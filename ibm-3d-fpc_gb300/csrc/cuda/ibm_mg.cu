@@ -841,6 +841,136 @@ __global__ void __launch_bounds__(kThreads) k_relax_rb_quad(Recs<float, 8> R, co
   }
 }
 
+// One whole two-colour sweep of a 7-point FP32 level (colour 0, then colour
+// 1) in one kernel, out of place: x_new = sweep(x_old). A block takes a tile
+// of kSwJ x kSwK lines and kSwX points of each, loads x_old over the tile
+// and a two-line (two-point) halo into shared memory, relaxes the colour-0
+// points of the tile and of a one-line halo ring there, then the colour-1
+// points of the tile from those, and writes the tile's points of both
+// colours to x_new. The halo ring's colour-0 values are computed again by
+// every tile that needs them, from the same old values, so every point gets
+// exactly the value of the two in-place phases (k_relax_rb_quad with colour
+// 0, then 1): same records, same operations, same order. Reading x_old and
+// writing x_new keeps one tile's writes out of another tile's halo. With
+// zero_x the sweep starts from x = 0 (the V-cycle's first sweep): x_old is
+// not read. Each x value moves from L2 once per sweep instead of about five
+// times per phase.
+constexpr int kSwX = 64, kSwJ = 8, kSwK = 8;
+constexpr int kSwXS = kSwX + 8;  // shared row: points i0 - 4 .. i0 + kSwX + 3 (16-byte loads)
+
+// One colour phase of k_relax_rb_sweep on the shared tile: LINES lines of
+// PER_LINE points of the colour, the lines starting FIRST lines into the
+// tile's shared rows in j and k (1: the halo ring included; 2: the tile);
+// colour 0 takes the records [0, h), colour 1 [h, 2h) (rec_base). A thread
+// takes its points kSwChunk at a time: first the class codes and
+// right-hand sides of the chunk (independent loads in flight together),
+// then the relaxations from shared memory.
+constexpr int kSwChunk = 4;
+template <int LINES, int PER_LINE, int FIRST>
+__device__ __forceinline__ void sweep_phase(const Recs<float, 8> &R, const float *__restrict__ b,
+                                            float (*sx)[kSwJ + 4][kSwXS], const Box &bx, int i0, int j0, int k0,
+                                            long rec_base) {
+  constexpr int NI = (LINES * PER_LINE + kThreads - 1) / kThreads;
+  constexpr int LW = kSwJ + 4 - 2 * FIRST;  // lines of the phase in j: kSwJ + 2 with the ring, kSwJ without
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const int colour = FIRST == 1 ? 0 : 1;
+  const int istart = FIRST == 1 ? i0 - 1 : i0;
+#pragma unroll 1
+  for (int t0 = 0; t0 < NI; t0 += kSwChunk) {
+    int rr[kSwChunk], li[kSwChunk], lj[kSwChunk], lk[kSwChunk];
+    float bv[kSwChunk];
+    unsigned short code[kSwChunk];
+#pragma unroll
+    for (int u = 0; u < kSwChunk; ++u) {
+      const int e = threadIdx.x + (t0 + u) * kThreads;
+      rr[u] = -1;
+      if (t0 + u >= NI || e >= LINES * PER_LINE) continue;
+      const int sidx = e % PER_LINE, line = e / PER_LINE;
+      lj[u] = line % LW + FIRST;
+      lk[u] = line / LW + FIRST;
+      const int j = j0 - 2 + lj[u], k = k0 - 2 + lk[u];
+      const int i = istart + ((istart + j + k + colour) & 1) + 2 * sidx;
+      if (j < 0 || j >= ny || k < 0 || k >= nz || i < 0 || i >= nx || i > i0 + kSwX) continue;
+      const int r = (k * ny + j) * nx + i;
+      rr[u] = r;
+      li[u] = i - i0 + 4;
+      bv[u] = b[r];
+      code[u] = R.code ? __ldcs(R.code + rec_base + (r >> 1)) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < kSwChunk; ++u) {
+      if (rr[u] < 0) continue;
+      float c[8];
+      if (R.code) {
+        const float4 *qq = reinterpret_cast<const float4 *>(R.tab + 8 * (long)code[u]);
+        const float4 p0 = __ldg(qq), p1 = __ldg(qq + 1);
+        c[0] = p0.x; c[1] = p0.y; c[2] = p0.z; c[3] = p0.w; c[4] = p1.x; c[5] = p1.y; c[6] = p1.z; c[7] = p1.w;
+      } else {
+        load_rec<float, 8>(R.R + (rec_base + (rr[u] >> 1)) * 8, c);
+      }
+      const int a = lk[u], bj = lj[u], ci = li[u];
+      float acc = 0.0f;
+      acc = fmaf(c[1], sx[a][bj][ci - 1], acc);
+      acc = fmaf(c[2], sx[a][bj][ci + 1], acc);
+      acc = fmaf(c[3], sx[a][bj - 1][ci], acc);
+      acc = fmaf(c[4], sx[a][bj + 1][ci], acc);
+      acc = fmaf(c[5], sx[a - 1][bj][ci], acc);
+      acc = fmaf(c[6], sx[a + 1][bj][ci], acc);
+      sx[a][bj][ci] = c[0] * (bv[u] - acc);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 3) k_relax_rb_sweep(Recs<float, 8> R, const float *__restrict__ b,
+                                                             const float *__restrict__ xo, float *__restrict__ xn,
+                                                             Box bx, int zero_x, const int *gate) {
+  if (gate_off(gate)) return;
+  __shared__ __align__(16) float sx[kSwK + 4][kSwJ + 4][kSwXS];
+  const int nx = bx.nx, ny = bx.ny, nz = bx.nz;
+  const long h = bx.n / 2;
+  const int tx = (nx + kSwX - 1) / kSwX, tyj = (ny + kSwJ - 1) / kSwJ, tzk = (nz + kSwK - 1) / kSwK;
+  const long ntiles = (long)tx * tyj * tzk;
+  for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int ti = (int)(tile % tx), tj = (int)((tile / tx) % tyj), tk = (int)(tile / ((long)tx * tyj));
+    const int i0 = ti * kSwX, j0 = tj * kSwJ, k0 = tk * kSwK;
+    // x_old over the tile and its halo; 0 outside the box (the stencil's zero)
+    constexpr int nq = kSwXS / 4, nlines = (kSwK + 4) * (kSwJ + 4);
+#pragma unroll 4
+    for (int e = threadIdx.x; e < nlines * nq; e += blockDim.x) {
+      const int q = e % nq, line = e / nq;
+      const int lj = line % (kSwJ + 4), lk = line / (kSwJ + 4);
+      const int j = j0 - 2 + lj, k = k0 - 2 + lk, gi = i0 - 4 + 4 * q;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (!zero_x && j >= 0 && j < ny && k >= 0 && k < nz && gi >= 0 && gi < nx)
+        v = *reinterpret_cast<const float4 *>(xo + ((long)k * ny + j) * nx + gi);
+      *reinterpret_cast<float4 *>(&sx[lk][lj][4 * q]) = v;
+    }
+    __syncthreads();
+    // colour 0 over the tile and the one-line ring: lines j0-1 .. j0+kSwJ,
+    // k0-1 .. k0+kSwK, points i0-1 .. i0+kSwX (kSwX/2 + 1 of each colour a
+    // line); then colour 1 over the tile. Each thread first issues the class
+    // codes and right-hand sides of all its points (independent loads in
+    // flight together), then relaxes them from shared memory.
+    sweep_phase<(kSwK + 2) * (kSwJ + 2), kSwX / 2 + 1, 1>(R, b, sx, bx, i0, j0, k0, 0L);
+    __syncthreads();
+    sweep_phase<kSwK * kSwJ, kSwX / 2, 2>(R, b, sx, bx, i0, j0, k0, h);
+    __syncthreads();
+    // the tile's points of both colours to x_new
+    {
+      constexpr int nq4 = kSwX / 4, lines = kSwK * kSwJ;
+      for (int e = threadIdx.x; e < lines * nq4; e += blockDim.x) {
+        const int q = e % nq4, line = e / nq4;
+        const int lj = line % kSwJ + 2, lk = line / kSwJ + 2;
+        const int j = j0 - 2 + lj, k = k0 - 2 + lk, gi = i0 + 4 * q;
+        if (j >= ny || k >= nz || gi >= nx) continue;
+        *reinterpret_cast<float4 *>(xn + ((long)k * ny + j) * nx + gi) =
+            *reinterpret_cast<const float4 *>(&sx[lk][lj][4 + 4 * q]);
+      }
+    }
+    __syncthreads();  // the shared tile is reused by the next tile
+  }
+}
+
 // Residual after a sweep that ended with colour 1 (k_residual_rb), quartet
 // form: colour-0 points b - A x in k_residual_rb's order, colour-1 points 0.
 template <int P>
@@ -1336,6 +1466,17 @@ int resident_grid(K kernel, long n) {
   return (int)std::min<long>(grid_all(n), (long)per_sm * sm_count());
 }
 
+// Blocks of k_relax_rb_sweep: one tile each, at most as many as stay resident.
+int sweep_grid(const Box &b) {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    IBM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_relax_rb_sweep, kThreads, 0));
+    per_sm = std::max(1, per_sm);
+  }
+  const long tiles = (long)((b.nx + kSwX - 1) / kSwX) * ((b.ny + kSwJ - 1) / kSwJ) * ((b.nz + kSwK - 1) / kSwK);
+  return (int)std::max(1L, std::min(tiles, (long)per_sm * sm_count()));
+}
+
 // Gauss-Jordan inverse with partial pivoting of the assembled coarsest operator.
 void dense_inverse(const std::vector<double> &A, int ns, const Box &b, std::vector<double> &inv) {
   const long n = b.n;
@@ -1736,6 +1877,15 @@ static T *vcycle(cudaStream_t st, std::vector<MgLevelT<T>> &L, int l, const MgPa
   const double rec7 = R7.code ? 2.0 : 8.0 * T_, rec27 = R27.code ? 2.0 : 28.0 * T_;
   auto relax = [&](bool zero, bool last) {
     if constexpr (sizeof(T) == 4) {
+      if (p.relax == 2 && rb7 && quad && p.fused_sweep && !(zero && fin) && !(last && fout)) {
+        // both colour phases in one kernel, out of place
+        LaunchScope ls(K_MG_RELAX_FINE, st, (zero ? 0.5 * n * (R7.code ? 2.0 : T_) + 1.5 * T_ * n
+                                                  : 0.5 * n * rec7 + 1.5 * T_ * n) +
+                                                0.5 * n * rec7 + 1.5 * T_ * n);
+        k_relax_rb_sweep<<<sweep_grid(F.b), kThreads, 0, st>>>(R7, F.bv.p, cur, oth, F.b, zero ? 1 : 0, gate);
+        std::swap(cur, oth);
+        return;
+      }
       if (p.relax == 2 && rb7 && quad) {
         for (int color = 0; color < 2; ++color) {
           const bool z = zero && color == 0;

@@ -18,6 +18,7 @@ struct MgParams {
   int options = 3;      // see ibm_solver_params.mg_options
   int classes = 1;      // colour-split records as record classes where they repeat (ibm_classes.cu)
   int quads = 1;        // FP32 7-point phases and residual four points per thread (nx % 4 == 0)
+  int fused_sweep = 0;    // FP32 7-point levels: one kernel per two-colour sweep (k_relax_rb_sweep)
   long fused_coarse = 0;  // FP32: levels from the first one below the finest with at most this many
                           // points run as one persistent cooperative kernel (ibm_mg.cu); 0: off
 };

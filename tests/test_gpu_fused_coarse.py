@@ -1,8 +1,12 @@
-"""The fused coarse levels of the FP32 multigrid (mg_fused_coarse: every phase
-below the finest level in one persistent cooperative kernel with grid-wide
-barriers) against one launch per phase: the same per-point arithmetic, so
-V-cycles and whole steps must agree bit for bit, repeatedly (a missed
-barrier or a stale read would show as a difference)."""
+"""Fused multigrid kernels against one launch per phase: the same per-point
+arithmetic, so V-cycles and whole steps must agree bit for bit, repeatedly
+(a missed barrier, a stale read or a halo mistake would show as a
+difference).
+
+- mg_fused_coarse: every phase below a level in one persistent cooperative
+  kernel with grid-wide barriers;
+- mg_fused_sweep: both colour phases of a 7-point level's sweep in one
+  kernel on shared-memory tiles with a halo, out of place."""
 import numpy as np
 import pytest
 
@@ -57,6 +61,44 @@ def test_fused_graph_steps_bitwise(ibm, shape, steps):
     case = ibm.Case(ibm.channel_params(*shape, Um=2.25, dt=2e-4))
     a = ibm.Solver(case, bench_like(ibm, precision=2, use_graph=1, vel_inner_sweeps=2, mg_fused_coarse=1 << 30))
     b = ibm.Solver(case, bench_like(ibm, precision=2, use_graph=1, vel_inner_sweeps=2, mg_fused_coarse=0))
+    try:
+        for _ in range(steps):
+            sa, sb = a.step(1.0), b.step(1.0)
+            assert sa.status == sb.status == ibm.IBM_OK
+            assert sa.p.iters == sb.p.iters
+        for x, y, name in zip(a.fields(), b.fields(), "uvwp"):
+            assert bits_equal(x, y), name
+    finally:
+        a.close()
+        b.close()
+
+
+@pytest.mark.parametrize("shape", [(48, 16, 16), (96, 32, 16), (200, 40, 24), (640, 128, 128)])
+def test_fused_sweep_vcycle_bitwise(ibm, shape):
+    """48 and 200 points a line leave a partial tile in x, 40 and 24 lines
+    partial tiles in y and z."""
+    case = ibm.Case(ibm.channel_params(*shape, Um=2.25, dt=2e-4))
+    fused = ibm.Solver(case, bench_like(ibm, precision=1, mg_fused_sweep=1))
+    plain = ibm.Solver(case, bench_like(ibm, precision=1, mg_fused_sweep=0))
+    try:
+        rng = np.random.default_rng(8)
+        n = shape[0] * shape[1] * shape[2]
+        for _ in range(3):
+            r = rng.standard_normal(n)
+            za = fused.apply_preconditioner(ibm.FIELD_P, r)
+            zb = plain.apply_preconditioner(ibm.FIELD_P, r)
+            assert np.all(np.isfinite(za))
+            assert bits_equal(za, zb)
+    finally:
+        fused.close()
+        plain.close()
+
+
+@pytest.mark.parametrize("shape,steps", [((160, 32, 32), 4), ((640, 128, 128), 2)])
+def test_fused_sweep_graph_steps_bitwise(ibm, shape, steps):
+    case = ibm.Case(ibm.channel_params(*shape, Um=2.25, dt=2e-4))
+    a = ibm.Solver(case, bench_like(ibm, precision=2, use_graph=1, vel_inner_sweeps=2, mg_fused_sweep=1))
+    b = ibm.Solver(case, bench_like(ibm, precision=2, use_graph=1, vel_inner_sweeps=2, mg_fused_sweep=0))
     try:
         for _ in range(steps):
             sa, sb = a.step(1.0), b.step(1.0)
