@@ -268,12 +268,22 @@ void use_classes(const Op7 &o, KSysHost &h) {
   if (o.clsj.ok()) { h.clsj = o.clsj.code.p; h.tabj = o.clsj.tab.p; }
 }
 
+// Precision key of the configured solvers: the pressure's and the momentum's.
+int precision_key(const ibm_solver_params &p) {
+  const int vp = p.vel_precision >= 0 ? p.vel_precision : p.precision;
+  return 4 * p.precision + vp;
+}
+
 void ensure_solvers(ibm_ctx *c) {
-  if (c->solvers_ready && c->solvers_precision == c->prm.precision) return;
+  if (c->solvers_ready && c->solvers_precision == precision_key(c->prm)) return;
   const ibm_solver_params &p = c->prm;
   const bool mixed = p.precision >= 1;
   const int a32 = p.precision == 2;
-  if (!mixed && p.vel_jacobi_iters != 1)
+  // the momentum solves may take another precision than the pressure solve
+  const int vprec = p.vel_precision >= 0 ? p.vel_precision : p.precision;
+  const bool vmixed = vprec >= 1;
+  const int va32 = vprec == 2;
+  if (!vmixed && p.vel_jacobi_iters != 1)
     throw Error(IBM_ERR_UNSUPPORTED, "FP64 momentum solves support one Jacobi sweep per application");
   KSysHost hs[3];
   for (int f = 0; f < 3; ++f) {
@@ -284,9 +294,9 @@ void ensure_solvers(ibm_ctx *c) {
     h.invd = o.invd.p;
     h.Af = o.cf.p; h.invdf = o.invdf.p; h.Ajf = o.cjf.p;
     h.kdim = p.vel_kdim; h.maxit = p.vel_maxit; h.tol = p.vel_tol;
-    if (mixed) {
+    if (vmixed) {
       h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps);
-      h.a32 = a32; h.cycle_rtol = p.cycle_rtol32; h.df_residual = p.df_residual;
+      h.a32 = va32; h.cycle_rtol = p.cycle_rtol32; h.df_residual = p.df_residual;
     }
     else { h.pc = 0; h.A = o.cj.p; }
     if (p.row_classes) {
@@ -335,7 +345,7 @@ void ensure_solvers(ibm_ctx *c) {
   }
   c->kp.configure(1, &hp);
   c->solvers_ready = true;
-  c->solvers_precision = p.precision;
+  c->solvers_precision = precision_key(p);
   c->graph_ready = false;
   c->graph_bound = false;
 }
@@ -441,6 +451,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->df_residual = 1;
   p->mg_fused_coarse = 0;
   p->mg_fused_sweep = 0;
+  p->vel_precision = -1;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -937,6 +948,7 @@ int ibm_set_solver_params(ibm_ctx *c, const ibm_solver_params *p) {
     if (p->vel_maxit < 0 || p->p_maxit < 0 || !(p->vel_tol >= 0) || !(p->p_tol >= 0))
       throw Error(IBM_ERR_ARG, "bad tolerance or iteration limit");
     if (p->precision < 0 || p->precision > 2) throw Error(IBM_ERR_ARG, "precision must be 0, 1 or 2");
+    if (p->vel_precision < -1 || p->vel_precision > 2) throw Error(IBM_ERR_ARG, "vel_precision must be -1, 0, 1 or 2");
     if (!(p->cycle_rtol32 > 0.0 && p->cycle_rtol32 < 1.0)) throw Error(IBM_ERR_ARG, "cycle_rtol32 must be in (0, 1)");
     if (p->p_pc != 0 && p->p_pc != 1) throw Error(IBM_ERR_ARG, "p_pc must be 0 or 1");
     if (p->mg_nu1 < 0 || p->mg_nu2 < 0 || p->mg_nu_coarse < 0 || p->mg_coarse_max < 1 || p->mg_max_levels < 1)

@@ -119,6 +119,8 @@ typedef struct ibm_solver_params {
                             on shared-memory tiles with a halo, out of place (bitwise the two in-place
                             phases); 0 (default): one launch per phase. Measured on the 640x128x128
                             channel: about 96 us a sweep against 62 us for the two phases */
+  int vel_precision;     /* precision of the three momentum solves (0, 1, 2 as `precision`); -1
+                            (default): `precision` */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {
