@@ -1,11 +1,18 @@
 """Autotuner of the solver schedule for a channel or a batched ensemble.
 
-The knobs are the multigrid V-cycle's depth and work and the relaxation
-kernels' shape:
+The knobs are the multigrid V-cycle's depth and work and the shape of its
+kernels:
 - mg_coarse_max: the largest level solved directly;
 - mg_nu1 / mg_nu2 / mg_nu_coarse: the sweeps on the finest and the coarser
   levels;
-- mg_quads: four points of a line per thread, or one.
+- mg_quads: four points of a line per thread, or one;
+- mg_fused_sweep: a 7-point level's two colour phases as one kernel over
+  64 x 8 x 8 shared-memory tiles with a halo, or one grid-stride launch per
+  phase;
+- mg_fused_coarse: the coarse end of the V-cycle as one persistent
+  cooperative kernel (from the first level of at most that many points), or
+  one launch per phase. On small grids, whose phases are bound by launch
+  latency, the fused forms can win; on the 640x128x128 channel they do not.
 Every candidate solves to the same tolerances, so the choice changes the time
 per step and nothing else. It is measured on the GPU: host wall time of
 graph-captured steps, each waiting for its results, from the context's own
@@ -32,6 +39,10 @@ CANDIDATES = (
     dict(mg_coarse_max=2560, mg_nu1=2, mg_nu2=2, mg_nu_coarse=2, mg_quads=1),
     dict(mg_coarse_max=2560, mg_nu1=2, mg_nu2=2, mg_nu_coarse=1, mg_quads=1),
     dict(mg_coarse_max=2560, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_quads=0),
+    dict(mg_coarse_max=2560, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_quads=1, mg_fused_sweep=1),
+    dict(mg_coarse_max=2560, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_quads=1, mg_fused_coarse=1 << 30),
+    dict(mg_coarse_max=2560, mg_nu1=3, mg_nu2=3, mg_nu_coarse=2, mg_quads=1, mg_fused_sweep=1,
+         mg_fused_coarse=1 << 30),
 )
 
 
