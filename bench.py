@@ -100,6 +100,8 @@ def parse():
                     help="mixed form: 1 = FP32 preconditioners in FP64 GMRES, 2 = also FP32 Arnoldi cycles")
     ap.add_argument("--vel-precision", type=int, default=-1, choices=[-1, 0, 1, 2],
                     help="mixed form: precision of the momentum solves (-1: as --precision)")
+    ap.add_argument("--mixed-set", action="append", default=[],
+                    help="mixed form: override a solver parameter, name=value (e.g. cycle_rtol32=1e-6)")
     ap.add_argument("--drag-validation", type=int, default=0, metavar="NX",
                     help="run the Schaefer-Turek 3D-1Z case (Re 20, steady) on an NX x NX/5 x NX/5 grid until the "
                          "drag settles and print c_D, c_L of the cut-surface and staircase forces (no bench line)")
@@ -148,6 +150,7 @@ def initial_state(case, seed=2026):
 FUSED_COARSE = [0]  # --mg-fused-coarse of this run
 FUSED_SWEEP = [-1]  # --mg-fused-sweep of this run
 VEL_PRECISION = [-1]  # --vel-precision of this run (the mixed form's momentum solves)
+MIXED_SET = []  # --mixed-set overrides of this run (the mixed form)
 
 
 def solver_params(ibm, precision, graph=0, coarse_max=2560):
@@ -159,6 +162,10 @@ def solver_params(ibm, precision, graph=0, coarse_max=2560):
         p.mg_fused_sweep = FUSED_SWEEP[0]
     if precision != 0 and VEL_PRECISION[0] >= 0:
         p.vel_precision = VEL_PRECISION[0]
+    if precision != 0:
+        for kv in MIXED_SET:
+            k, v = kv.split("=")
+            setattr(p, k, type(getattr(p, k))(float(v)))
     return p
 
 
@@ -846,6 +853,7 @@ def main():
     FUSED_COARSE[0] = args.mg_fused_coarse
     FUSED_SWEEP[0] = args.mg_fused_sweep
     VEL_PRECISION[0] = args.vel_precision
+    MIXED_SET[:] = args.mixed_set
     if args.drag_validation:
         drag_validation(args)
         return
