@@ -8,11 +8,18 @@ disabled, initial field = the parabolic inflow profile on every active u
 face plus 1e-3 N(0,1) seeded perturbations on active u, v, w faces.
 Synthetic data (no dataset exists for this path).
 
-value      : steps/s of the mixed-precision form (FP32 multigrid / Jacobi
-             preconditioners inside FP64 flexible GMRES, tolerance 1e-8),
-             fields and operators resident in HBM (~25 GB, far above L2).
-fp64_plain : the same steps in FP64 throughout; the velocity error of the
-             mixed form against it is reported (must be <= 1e-6).
+value      : steps/s of the mixed-precision form, graph-captured: the
+             pressure solve in FP32 Arnoldi cycles with FP64 restarts and an
+             FP32 multigrid preconditioner, the momentum solves in FP64
+             flexible GMRES with FP32 Jacobi sweeps, every solve to a true
+             FP64 relative residual of 1e-8; fields and operators resident
+             in HBM (~25 GB, far above L2). This form stays within 1e-6 of
+             FP64 over the 2000-step run.
+fp64_plain : the same steps in FP64 throughout, graph-captured (and a
+             host-driven copy); the velocity error of the mixed form
+             against it is reported (must be <= 1e-6).
+fastest_form: FP32 Arnoldi cycles for every solve, the same steps: faster,
+             but past 1e-6 of FP64 after about 1300 steps of the long run.
 e2e        : steps/s through the C ABI with host buffers: every step copies
              the state in from pinned host memory, steps, and reads it back.
 roofline   : the kernel class with the largest device time in the timed
@@ -98,8 +105,12 @@ def parse():
                          "persistent kernel per V-cycle (0: off, the library default; 1: 262144 points)")
     ap.add_argument("--precision", type=int, default=2, choices=[1, 2],
                     help="mixed form: 1 = FP32 preconditioners in FP64 GMRES, 2 = also FP32 Arnoldi cycles")
-    ap.add_argument("--vel-precision", type=int, default=-1, choices=[-1, 0, 1, 2],
-                    help="mixed form: precision of the momentum solves (-1: as --precision)")
+    ap.add_argument("--vel-precision", type=int, default=1, choices=[-1, 0, 1, 2],
+                    help="mixed form: precision of the momentum solves (-1: as --precision). Default 1: FP64 "
+                         "Krylov with FP32 Jacobi; with FP32 Arnoldi cycles (2) the momentum solves' errors, "
+                         "amplified by the wake, take the velocity past 1e-6 of FP64 after about 1300 steps")
+    ap.add_argument("--no-fastest", action="store_true",
+                    help="skip the fastest form (FP32 Arnoldi cycles for every solve) reported beside the value")
     ap.add_argument("--mixed-set", action="append", default=[],
                     help="mixed form: override a solver parameter, name=value (e.g. cycle_rtol32=1e-6)")
     ap.add_argument("--drag-validation", type=int, default=0, metavar="NX",
@@ -149,7 +160,7 @@ def initial_state(case, seed=2026):
 
 FUSED_COARSE = [0]  # --mg-fused-coarse of this run
 FUSED_SWEEP = [-1]  # --mg-fused-sweep of this run
-VEL_PRECISION = [-1]  # --vel-precision of this run (the mixed form's momentum solves)
+VEL_PRECISION = [1]  # --vel-precision of this run (the mixed form's momentum solves)
 MIXED_SET = []  # --mixed-set overrides of this run (the mixed form)
 
 
@@ -926,10 +937,13 @@ def main():
            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
            "config": run_config(nx, ny, nz, ws),
-           "solver": {"form": ("FP32 Arnoldi cycles with FP64 restarts (FGMRES iterative refinement)"
-                               if args.precision == 2 else "mixed FP32-preconditioned FP64 FGMRES")
-                              + ", true FP64 residual tol 1e-8, graph-captured step",
-                      "precision": args.precision,
+           "solver": {"form": ("pressure: FP32 Arnoldi cycles with FP64 restarts (FGMRES iterative refinement)"
+                               if args.precision == 2 else "pressure: FP32 multigrid inside FP64 FGMRES")
+                              + "; momentum: " + {0: "FP64 GMRES + Jacobi", 1: "FP64 FGMRES + FP32 Jacobi",
+                                                  2: "FP32 Arnoldi cycles with FP64 restarts",
+                                                  -1: "as the pressure"}[args.vel_precision]
+                              + "; true FP64 residual tol 1e-8 on every solve, graph-captured step",
+                      "precision": args.precision, "vel_precision": args.vel_precision,
                       "pressure_pc": "semicoarsening MG (grouped, symmetrized, cut-cell-aware interpolation), "
                                      "Galerkin 27-point coarse levels, two-colour sweeps 3+3 (finest) / 2+2 (coarser), FP32",
                       "momentum_pc": "2 FP32 Jacobi sweeps",
@@ -961,6 +975,7 @@ def main():
                         "form": "FP64 throughout (GMRES + Jacobi, GMRES + FP64 multigrid, same settings), "
                                 + ("graph-captured step" if graph else "host-driven step")}
             if graph:
+                f64_graph = f64
                 vel_err = (max(float(np.abs(a - b).max()) for a, b in zip(mixed_fields[:3], f64[:3]))
                            / float(np.abs(f64[0]).max()))
                 p_err = float(np.abs(mixed_fields[3] - f64[3]).max() / max(np.abs(f64[3]).max(), 1e-300))
@@ -968,6 +983,35 @@ def main():
         out["speedup_vs_fp64_host_driven"] = out["fp64_plain_host_driven"]["ms_per_step"] / ms_per_step
         out["velocity_rel_err_vs_fp64"] = vel_err
         out["pressure_rel_err_vs_fp64"] = p_err
+
+    if not args.no_fastest:
+        # FP32 Arnoldi cycles for every solve (the momentum solves too): the
+        # same steps from the same state, graph-captured
+        pf = solver_params(ibm, args.precision, graph=1, coarse_max=args.mg_coarse_max)
+        pf.vel_precision = -1
+        fast = ibm.Solver(case, pf, device=local)
+        fast.set_fields(*state)
+        run_steps(fast, steps_done - args.steps)
+        torch.cuda.synchronize()
+        sfs = device_timer(plib, fast._ctx)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(sfs)
+        stf = [fast.step(1.0) for _ in range(args.steps)]
+        e1.record(sfs)
+        torch.cuda.synchronize()
+        msf = reduce_max_ms(e0.elapsed_time(e1), ws, "cuda")
+        ff = fast.fields()
+        fast.close()
+        out["fastest_form"] = {
+            "value": replica_throughput(args.steps, msf, ws), "ms_per_step": msf / args.steps,
+            "phase_ms": phase_means(stf), "form": "FP32 Arnoldi cycles with FP64 restarts for every solve, "
+                                                  "graph-captured", "worst_status": int(max(x.status for x in stf)),
+            "note": "over the 2000-step full-timestep run its velocity difference from FP64 passes 1e-6 after about "
+                    "1300 steps (1.41e-6 at step 2000; the value's form stays at 4.5e-7), so it is not the value"}
+        if not args.no_fp64:
+            out["fastest_form"]["speedup_vs_fp64"] = out["fp64_plain"]["ms_per_step"] / (msf / args.steps)
+            out["fastest_form"]["velocity_rel_err_vs_fp64"] = (
+                max(float(np.abs(a - b).max()) for a, b in zip(ff[:3], f64_graph[:3])) / float(np.abs(f64_graph[0]).max()))
 
     if not args.no_e2e:
         p = mixed.params
