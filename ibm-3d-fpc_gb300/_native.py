@@ -55,7 +55,8 @@ class SolverParams(C.Structure):
                 ("mg_nu_coarse", C.c_int), ("cycle_rtol32", C.c_double), ("compute_forces", C.c_int),
                 ("row_classes", C.c_int), ("mg_quads", C.c_int),
                 ("df_residual", C.c_int), ("mg_fused_coarse", C.c_int),
-                ("mg_fused_sweep", C.c_int), ("vel_precision", C.c_int)]
+                ("mg_fused_sweep", C.c_int), ("vel_precision", C.c_int),
+                ("df_spmv", C.c_int), ("df_rhs", C.c_int)]
 
 
 class Profile(C.Structure):

@@ -297,6 +297,7 @@ void ensure_solvers(ibm_ctx *c) {
     if (vmixed) {
       h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps);
       h.a32 = va32; h.cycle_rtol = p.cycle_rtol32; h.df_residual = p.df_residual;
+      h.df_spmv = p.df_spmv;
     }
     else { h.pc = 0; h.A = o.cj.p; }
     if (p.row_classes) {
@@ -329,13 +330,14 @@ void ensure_solvers(ibm_ctx *c) {
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
     if (mixed) {
       hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32;
-      hp.df_residual = p.df_residual;
+      hp.df_residual = p.df_residual; hp.df_spmv = p.df_spmv;
     }
     else { hp.pc = 1; hp.A = op.c.p; }
   } else {
     if (mixed) {
       hp.pc = 2; hp.pc_cb = 0; hp.A = op.c.p; hp.inner_sweeps = 1;
       hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32; hp.df_residual = p.df_residual;
+      hp.df_spmv = p.df_spmv;
     }
     else { hp.pc = 0; hp.A = op.cj.p; }
   }
@@ -452,6 +454,8 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->mg_fused_coarse = 0;
   p->mg_fused_sweep = 0;
   p->vel_precision = -1;
+  p->df_spmv = 1;
+  p->df_rhs = 1;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }

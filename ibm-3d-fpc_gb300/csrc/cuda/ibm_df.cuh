@@ -38,6 +38,17 @@ __device__ __forceinline__ void df_fma(float &hi, float &lo, float ch, float cl,
   df_fast_two_sum(s, e, hi, lo);
 }
 
+// (hi, lo) += (ch + cl) * x for a float x: ch * x exactly (fma residual),
+// cl * x rounded in FP32 (2^-48 of the product); then a double-float addition.
+__device__ __forceinline__ void df_fma1(float &hi, float &lo, float ch, float cl, float x) {
+  const float p = __fmul_rn(ch, x);
+  const float pe = __fmaf_rn(cl, x, __fmaf_rn(ch, x, -p));
+  float s, e;
+  df_two_sum(hi, p, s, e);
+  e = __fadd_rn(e, __fadd_rn(lo, pe));
+  df_fast_two_sum(s, e, hi, lo);
+}
+
 // (rh, rl) = (ah, al) - (bh, bl).
 __device__ __forceinline__ void df_sub(float ah, float al, float bh, float bl, float &rh, float &rl) {
   float s, e;
@@ -72,5 +83,62 @@ __device__ __forceinline__ void df_split(double v, float &hi, float &lo) {
   const float l = __fmul_rn(__uint2float_rn(L), __uint_as_float((unsigned)le << 23));
   lo = sgn ? -l : l;
 }
+
+// v == hi + lo to within 2^-46 |v| from the bits of v, on the integer and
+// FP32 pipes without an int-to-float conversion: hi holds the leading 24
+// significand bits (truncated), lo the next 23 (truncated), built as
+// (2^23 + L) - 2^23 from an exponent-forced float and scaled by a power of
+// two. |v| below 2^-126 gives a signed zero, lo is dropped below 2^-81;
+// |v| at or above 2^128, infinities and NaN take df_split.
+__device__ __forceinline__ void df_split_fast(double v, float &hi, float &lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+  const unsigned uh = (unsigned)(u >> 32), ul = (unsigned)u;
+  const unsigned sgn = uh & 0x80000000u;
+  const int e = (int)((uh >> 20) & 0x7ff);
+  const int fe = e - 896;  // float biased exponent of the leading bit
+  if (fe <= 0) { hi = __uint_as_float(sgn); lo = 0.0f; return; }
+  if (fe >= 255) { df_split(v, hi, lo); return; }
+  hi = __uint_as_float(sgn | ((unsigned)fe << 23) | ((uh & 0xFFFFFu) << 3) | (ul >> 29));
+  // significand bits 28..6 (L, weight 2^(e - 1069)): float exponent e - 942
+  const unsigned L = (ul & 0x1FFFFFFFu) >> 6;
+  const int se = e - 942;
+  const float lf = __fsub_rn(__uint_as_float(0x4B000000u | L), 8388608.0f);
+  const float lm = se > 0 ? __fmul_rn(lf, __uint_as_float((unsigned)se << 23)) : 0.0f;
+  lo = __uint_as_float(__float_as_uint(lm) | sgn);
+}
+
+// A double-float value and the operations the dense kernels need. Sums and
+// products carry about 2^-47 of their operands' size.
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF df_of(double v) {
+  DF r;
+  df_split_fast(v, r.h, r.l);
+  return r;
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s, e;
+  df_two_sum(a.h, b.h, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  DF r;
+  df_fast_two_sum(s, e, r.h, r.l);
+  return r;
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+__device__ __forceinline__ DF df_sub(DF a, DF b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, e));
+  DF r;
+  df_fast_two_sum(p, e, r.h, r.l);
+  return r;
+}
+// times an exact power of two (no rounding unless the result leaves the
+// normal range)
+__device__ __forceinline__ DF df_scale(DF a, float p2) { return DF{__fmul_rn(a.h, p2), __fmul_rn(a.l, p2)}; }
+// widened to FP64: two exact conversions and one rounding add
+__device__ __forceinline__ double df_to_double(DF a) { return __dadd_rn((double)a.h, (double)a.l); }
 
 }  // namespace ibm

@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(kThreads) k_init(KSys *sys, int nsys) {
           }
           if (S.a32) S.Vf[r] = (float)rv;
           else S.V[r] = rv;
+          if (S.vcur) S.vcur[r] = (float)rv;
           pb = fma(bv, bv, pb);
         }
       }
@@ -230,6 +231,21 @@ __device__ void arnoldi_finalize(KScal *sc, int j, double hn) {
   }
 }
 
+// FP64 Arnoldi kernels with a short basis (at most kDots64 vectors) keep each
+// dot product as a per-thread sum over all the thread's rows and reduce it
+// across the warp once per kernel; a reduction per tile of rows cost about as
+// much FP64 issue as the products themselves.
+constexpr int kDots64 = 8;
+__device__ __forceinline__ void flush_dots64(const double (&pd)[kDots64], int nd, double *sacc, int warp,
+                                             int lane) {
+#pragma unroll
+  for (int kk = 0; kk < kDots64; ++kk) {
+    if (kk >= nd) break;
+    const double p = warp_sum(pd[kk]);
+    if (lane == 0) sacc[kk * kWarps + warp] += p;
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
   KSys &S = sys[blockIdx.y];
   KScal *sc = S.s;
@@ -242,6 +258,9 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double *vj = S.V + (long)j * S.ldv;
+  double pd[kDots64];
+#pragma unroll
+  for (int kk = 0; kk < kDots64; ++kk) pd[kk] = 0.0;
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
     double wv[kRowsPerThread];
 #pragma unroll
@@ -254,12 +273,40 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
         double w;
         long cs;
         const double *c0 = a_row(S, r, cs);
-        if (S.pc == 0) w = stencil7_at(c0, cs, vj, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
+        if (S.df_spmv) {
+          // A z_j with z_j exact in FP32: the seven products and their sum in
+          // double-float, widened once (two conversions and one FP64 add)
+          const float *c = S.tabdf + 16 * (long)S.cls[r];
+          const float *zj = S.Z + (long)j * S.ldv;
+          const long sy = S.nx, sz = (long)S.nx * S.ny;
+          float ah = 0.0f, al = 0.0f;
+          df_fma1(ah, al, c[0], c[8], zj[r]);
+          if (i > 0) df_fma1(ah, al, c[1], c[9], zj[r - 1]);
+          if (i < S.nx - 1) df_fma1(ah, al, c[2], c[10], zj[r + 1]);
+          if (jj > 0) df_fma1(ah, al, c[3], c[11], zj[r - sy]);
+          if (jj < S.ny - 1) df_fma1(ah, al, c[4], c[12], zj[r + sy]);
+          if (k > 0) df_fma1(ah, al, c[5], c[13], zj[r - sz]);
+          if (k < S.nz - 1) df_fma1(ah, al, c[6], c[14], zj[r + sz]);
+          w = (double)ah + (double)al;
+        } else if (S.pc == 0) w = stencil7_at(c0, cs, vj, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
         else if (S.pc == 1) w = stencil7_at(c0, cs, S.z, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
         else w = stencil7_at(c0, cs, S.Z + (long)j * S.ldv, (int)r, i, jj, k, S.nx, S.ny, S.nz);
         S.w[r] = w;
         wv[t] = w;
       }
+    }
+    if (nd <= kDots64) {  // per-thread sums over all the thread's rows (reduced once below)
+#pragma unroll
+      for (int kk = 0; kk < kDots64; ++kk) {
+        if (kk >= nd) break;
+        const double *vk = S.V + (long)kk * S.ldv;
+#pragma unroll
+        for (int t = 0; t < kRowsPerThread; ++t) {
+          const long r = t0 + t * kThreads + threadIdx.x;
+          if (r < S.n) pd[kk] = fma(vk[r], wv[t], pd[kk]);
+        }
+      }
+      continue;
     }
     for (int kk = 0; kk < nd; ++kk) {
       const double *vk = S.V + (long)kk * S.ldv;
@@ -273,6 +320,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
       if (lane == 0) sacc[kk * kWarps + warp] += p;
     }
   }
+  if (nd <= kDots64) flush_dots64(pd, nd, sacc, warp, lane);
   if (!block_partials_and_last(sacc, nd, S.part, &sc->ticket)) return;
   __shared__ double tot[kMaxKdim + 1];
   reduce_partials(S.part, gridDim.x, nd, tot);
@@ -298,6 +346,9 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
   for (int t = threadIdx.x; t < nd; t += blockDim.x) cf[t] = sc->coef[t];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double pd[kDots64];
+#pragma unroll
+  for (int kk = 0; kk < kDots64; ++kk) pd[kk] = 0.0;
   for (long t0 = (long)blockIdx.x * kTile; t0 < S.n; t0 += (long)gridDim.x * kTile) {
     double wv[kRowsPerThread];
 #pragma unroll
@@ -311,6 +362,18 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
         wv[t] = w;
       }
     }
+    if (nd <= kDots64) {
+#pragma unroll
+      for (int kk = 0; kk < kDots64; ++kk) {
+        if (kk >= nd) break;
+#pragma unroll
+        for (int t = 0; t < kRowsPerThread; ++t) {
+          const long r = t0 + t * kThreads + threadIdx.x;
+          if (r < S.n) pd[kk] = fma(S.V[(long)kk * S.ldv + r], wv[t], pd[kk]);
+        }
+      }
+      continue;
+    }
     for (int kk = 0; kk < nd; ++kk) {
       double p = 0.0;
 #pragma unroll
@@ -322,6 +385,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
       if (lane == 0) sacc[kk * kWarps + warp] += p;
     }
   }
+  if (nd <= kDots64) flush_dots64(pd, nd, sacc, warp, lane);
   if (!block_partials_and_last(sacc, nd, S.part, &sc->ticket)) return;
   __shared__ double tot[kMaxKdim + 1];
   reduce_partials(S.part, gridDim.x, nd, tot);
@@ -358,7 +422,10 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_next(KSys *sys) {
       if (r < S.n) {
         double w = S.w[r];
         for (int kk = 0; kk < nd; ++kk) w = fma(-cf[kk], S.V[(long)kk * S.ldv + r], w);
-        if (store) vn[r] = w;
+        if (store) {
+          vn[r] = w;
+          if (S.vcur) S.vcur[r] = (float)w;
+        }
         p = fma(w, w, p);
       }
     }
@@ -531,6 +598,7 @@ __global__ void __launch_bounds__(kThreads) k_cycle_residual(KSys *sys) {
         const double rv = S.b[r] - stencil7_at(c0, cs, S.x, (int)r, i, j, k, S.nx, S.ny, S.nz);
         if (S.a32) S.Vf[r] = (float)rv;
         else S.V[r] = rv;
+        if (S.vcur) S.vcur[r] = (float)rv;
         pr = fma(rv, rv, pr);
       }
     }
@@ -977,8 +1045,12 @@ __global__ void __launch_bounds__(kThreads) k_jacobi32_two(KSys *sys) {
   const int j = sc->i;
   const float inv_nu = (float)(1.0 / sc->nu[j]);
   float *out = S.Z + (long)j * S.ldv;
-  if (S.a32 && S.vec4) jacobi_two_rows4(S, S.Vf + (long)j * S.ldv, inv_nu, out);
-  else if (S.a32) jacobi_two_rows<float>(S, S.Vf + (long)j * S.ldv, inv_nu, out);
+  // an FP64 basis is read through its FP32 copy when there is one: the same
+  // values ((float) V_j), one conversion per row where the vector is formed
+  // instead of one per row and neighbour here
+  const float *vf = S.a32 ? S.Vf + (long)j * S.ldv : S.vcur;
+  if (vf && S.vec4) jacobi_two_rows4(S, vf, inv_nu, out);
+  else if (vf) jacobi_two_rows<float>(S, vf, inv_nu, out);
   else jacobi_two_rows<double>(S, S.V + (long)j * S.ldv, inv_nu, out);
 }
 
@@ -1093,6 +1165,8 @@ void Krylov::configure(int nsys_, const KSysHost *hs) {
       sl.Z.alloc((size_t)h.kdim * h.n);
       if (!h.pc_cb) { sl.zf.alloc(h.n); sl.zf2.alloc(h.n); }
     }
+    if (h.pc == 2 && !h.pc_cb && !h.a32) sl.vcur.alloc(h.n);
+    else sl.vcur.release();
     sl.part.alloc(need_part);
   }
   scal.alloc(nsys);
@@ -1106,7 +1180,8 @@ size_t Krylov::bytes() const {
   for (int s = 0; s < nsys; ++s) {
     const Slot &sl = slot[s];
     b += sl.V.bytes() + sl.w.bytes() + sl.z.bytes() + sl.z2.bytes() + sl.part.bytes() +
-         sl.Z.bytes() + sl.zf.bytes() + sl.zf2.bytes() + sl.Vf.bytes() + sl.wf.bytes() + sl.xs.bytes();
+         sl.Z.bytes() + sl.zf.bytes() + sl.zf2.bytes() + sl.Vf.bytes() + sl.wf.bytes() + sl.xs.bytes() +
+         sl.vcur.bytes();
   }
   return b;
 }
@@ -1129,12 +1204,14 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     k.cls = h.cls; k.tab = h.tab; k.tabf = h.tabf; k.clsj = h.clsj; k.tabj = h.tabj;
     k.tabdf = h.tabdf;
     k.df_resid = (h.a32 && h.cls && h.tabdf && h.df_residual) ? 1 : 0;
+    k.df_spmv = (h.pc == 2 && !h.a32 && h.cls && h.tabdf && h.A == h.Ar && h.df_spmv) ? 1 : 0;
     k.xs = slot[s].xs.p;
     k.V = slot[s].V.p; k.ldv = h.n;
     k.Z = slot[s].Z.p;
     k.w = slot[s].w.p; k.z = slot[s].z.p; k.z2 = slot[s].z2.p;
     k.zf = slot[s].zf.p; k.zf2 = slot[s].zf2.p;
     k.Vf = slot[s].Vf.p; k.wf = slot[s].wf.p; k.a32 = h.a32;
+    k.vcur = slot[s].vcur.p;
     k.x_zero = x_zero ? 1 : 0;
     k.vec4 = (h.n % 4 == 0) ? 1 : 0;
     k.x = x[s]; k.b = b[s];
@@ -1181,7 +1258,7 @@ void Krylov::launch_cycle_end(cudaStream_t st, const Precond &pc, const KFlags *
       const int m = fl[s].i, pcm = slot[s].host.pc;
       bu += rows(s) * (pcm == 2 ? 4.0 * m + 16.0 : pcm == 1 ? 8.0 * m + 8.0 : 8.0 * m + 24.0);
       // a classed row is its 2-byte class instead of 7 FP64 coefficients
-      br += (slot[s].host.cls ? 34.0 : 88.0) * rows(s);
+      br += ((slot[s].host.cls ? 34.0 : 88.0) + (slot[s].vcur.p ? 4.0 : 0.0)) * rows(s);
       if (pcm == 1) ba += 24.0 * rows(s);
     }
   }
@@ -1232,7 +1309,7 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
   }
   int inner_sweeps = 0;
   bool any64 = false, any32 = false;
-  double r32 = 0.0, j32two = 0.0, bsp = 0.0, bor = 0.0, bsp32 = 0.0, bor32 = 0.0;
+  double r32 = 0.0, j32two = 0.0, bsp = 0.0, bor = 0.0, bnx = 0.0, bsp32 = 0.0, bor32 = 0.0;
   for (int s = 0; s < nsys; ++s) {
     if (!((mask >> s) & 1u)) continue;
     const bool a32 = slot[s].host.a32 != 0;
@@ -1247,7 +1324,8 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
     if (h.pc == 2 && !h.pc_cb) {
       r32 += rows(s) * (a32 ? 0.75 : 1.0);
       // two sweeps in one pass: v, z and a 2-byte class instead of 7 FP32 values
-      j32two += rows(s) * (h.clsj ? (a32 ? 10.0 : 14.0) : (a32 ? 27.0 : 36.0));
+      j32two += rows(s) * (h.clsj ? 10.0 : 27.0);  // v read as FP32 (basis or copy)
+      if (!a32) bnx += 4.0 * rows(s);                // the copy, written by k_arnoldi_next
     }
     if (a32) {
       bsp32 += rows(s) * (c32 + 8.0 + 4.0 * j1);
@@ -1286,7 +1364,7 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
       LaunchScope ls(K_GM_ORTH, st, bor);
       k_arnoldi_orth<<<wave(k_arnoldi_orth), kThreads, 0, st>>>(dev);
     }
-    LaunchScope ls(K_GM_NEXT, st, bor);
+    LaunchScope ls(K_GM_NEXT, st, bor + bnx);
     k_arnoldi_next<<<wave(k_arnoldi_next), kThreads, 0, st>>>(dev);
   }
   if (any32) {
@@ -1319,7 +1397,8 @@ void Krylov::solve(cudaStream_t st, const double *const *b, double *const *x, co
   const dim3 grid(nblk, nsys);
   double init_bytes = 0.0;
   for (int s = 0; s < nsys; ++s)
-    if ((mask >> s) & 1u) init_bytes += (x_zero ? 16.0 : slot[s].host.cls ? 26.0 : 80.0) * slot[s].host.n;
+    if ((mask >> s) & 1u)
+      init_bytes += ((x_zero ? 16.0 : slot[s].host.cls ? 26.0 : 80.0) + (slot[s].vcur.p ? 4.0 : 0.0)) * slot[s].host.n;
   {
     LaunchScope ls(K_GM_INIT, st, init_bytes);
     k_init<<<wave(k_init), kThreads, 0, st>>>(dsys.p, nsys);

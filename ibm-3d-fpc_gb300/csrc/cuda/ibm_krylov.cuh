@@ -51,6 +51,7 @@ struct KSysHost {
   const float *tabj = nullptr;
   const float *tabdf = nullptr;  // with a32: true residuals in double-float
   int df_residual = 1;           // use them when a32 and tabdf are set
+  int df_spmv = 1;               // pc 2 without a32: A z_j in double-float from tabdf
 };
 
 struct KResult {
@@ -87,6 +88,7 @@ class Krylov {
     KSysHost host;
     DBuf<double> V, w, z, z2, part;
     DBuf<float> Z, zf, zf2, Vf, wf;
+    DBuf<float> vcur;  // FP64 basis with FP32 Jacobi: FP32 copy of the current basis vector
     DBuf<float2> xs;  // double-float copy of x for the double-float residual
   };
   void read_flags(cudaStream_t st);

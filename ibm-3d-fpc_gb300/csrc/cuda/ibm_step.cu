@@ -12,6 +12,7 @@
 #include <cmath>
 
 #include "ibm_ctx.cuh"
+#include "ibm_df.cuh"
 #include "ibm_step.cuh"
 
 namespace ibm {
@@ -181,11 +182,53 @@ struct RhsArgs {
   long nb[3];
   double a, rho;
   KnownDiv tdx, tdy, tdz;  // 2 dx, 2 dy, 2 dz
+  DF da, drho, drx, dry, drz;  // double-float a, rho, 1 / (2 dx), 1 / (2 dy), 1 / (2 dz)
   int zero_guess;
 };
 
+// Arithmetic of the right-hand side. RhsF64: the reference's operations,
+// each rounded in FP64 as above (bitwise the reference kernel). RhsDF: the
+// same expressions in double-float on the FP32 and integer pipes (every
+// input split from its FP64 bits, divisions by 2h as products with the
+// double-float reciprocal), widened to FP64 once per row; about 2^-44 of
+// the row's largest term, for the mixed-precision forms, where GB300's FP64
+// rate bounds the FP64 kernel.
+struct RhsF64 {
+  using T = double;
+  __device__ static T in(double x) { return x; }
+  __device__ static T zero() { return 0.0; }
+  __device__ static T avg(T a, T b, T c, T d) { return avg4(a, b, c, d); }
+  __device__ static T adv(const RhsArgs &A, T c, T dm, T dp, T a2, T em, T ep, T a3, T fm, T fp) {
+    return advect(c, dm, dp, A.tdx, a2, em, ep, A.tdy, a3, fm, fp, A.tdz);
+  }
+  __device__ static T grad(T gl, T pl, T gr, T pr) { return grad_face(gl, pl, gr, pr); }
+  __device__ static double rhs(const RhsArgs &A, T uc, T conv, T gp, double bc, double sc) {
+    return mom_rhs(A.a, A.rho, uc, conv, gp, bc, sc);
+  }
+};
+struct RhsDF {
+  using T = DF;
+  __device__ static T in(double x) { return df_of(x); }
+  __device__ static T zero() { return DF{0.0f, 0.0f}; }
+  __device__ static T avg(T a, T b, T c, T d) { return df_scale(df_add(df_add(df_add(a, b), c), d), 0.25f); }
+  __device__ static T adv(const RhsArgs &A, T c, T dm, T dp, T a2, T em, T ep, T a3, T fm, T fp) {
+    const T t1 = df_mul(df_mul(c, df_sub(dp, dm)), A.drx);
+    const T t2 = df_mul(df_mul(a2, df_sub(ep, em)), A.dry);
+    const T t3 = df_mul(df_mul(a3, df_sub(fp, fm)), A.drz);
+    return df_add(df_add(t1, t2), t3);
+  }
+  __device__ static T grad(T gl, T pl, T gr, T pr) { return df_add(df_mul(gl, pl), df_mul(gr, pr)); }
+  __device__ static double rhs(const RhsArgs &A, T uc, T conv, T gp, double bc, double sc) {
+    T t = df_sub(df_mul(A.da, uc), df_mul(A.drho, conv));
+    t = df_add(df_sub(t, gp), df_of(bc));
+    return df_to_double(df_mul(t, df_of(sc)));
+  }
+};
+
 // One thread per solve-box row of u, v and w (flat index over the three boxes).
+template <class M>
 __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
+  using T = typename M::T;
   const Dims &d = A.d;
   const long total = A.nb[0] + A.nb[1] + A.nb[2];
   const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
@@ -200,29 +243,30 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
       const int j = udivmod(q, d.dny, kq), k = (int)kq;
       const long f = U3(d, i, j, k);
       const uint8_t fl = A.fu[f];
-      const double uc = A.u[f];
+      const double ucd = A.u[f];
       double rhs = 0.0;
       if (fl & kRhsRow) {
-        double conv = 0.0;
+        const T uc = M::in(ucd);
+        T conv = M::zero();
         if (fl & kActive) {
-          const double va = avg4(ld_v(A.v, d, i - 1, j, k, 0.0), ld_v(A.v, d, i - 1, j + 1, k, 0.0),
-                                 ld_v(A.v, d, i, j, k, 0.0), ld_v(A.v, d, i, j + 1, k, 0.0));
-          const double wa = avg4(ld_w(A.w, d, i - 1, j, k, 0.0), ld_w(A.w, d, i - 1, j, k + 1, 0.0),
-                                 ld_w(A.w, d, i, j, k, 0.0), ld_w(A.w, d, i, j, k + 1, 0.0));
-          conv = advect(uc, ld_u(A.u, d, i - 1, j, k, uc), ld_u(A.u, d, i + 1, j, k, uc), A.tdx, va,
-                        ld_u(A.u, d, i, j - 1, k, uc), ld_u(A.u, d, i, j + 1, k, uc), A.tdy, wa,
-                        ld_u(A.u, d, i, j, k - 1, uc), ld_u(A.u, d, i, j, k + 1, uc), A.tdz);
+          const T va = M::avg(M::in(ld_v(A.v, d, i - 1, j, k, 0.0)), M::in(ld_v(A.v, d, i - 1, j + 1, k, 0.0)),
+                              M::in(ld_v(A.v, d, i, j, k, 0.0)), M::in(ld_v(A.v, d, i, j + 1, k, 0.0)));
+          const T wa = M::avg(M::in(ld_w(A.w, d, i - 1, j, k, 0.0)), M::in(ld_w(A.w, d, i - 1, j, k + 1, 0.0)),
+                              M::in(ld_w(A.w, d, i, j, k, 0.0)), M::in(ld_w(A.w, d, i, j, k + 1, 0.0)));
+          conv = M::adv(A, uc, M::in(ld_u(A.u, d, i - 1, j, k, ucd)), M::in(ld_u(A.u, d, i + 1, j, k, ucd)), va,
+                        M::in(ld_u(A.u, d, i, j - 1, k, ucd)), M::in(ld_u(A.u, d, i, j + 1, k, ucd)), wa,
+                        M::in(ld_u(A.u, d, i, j, k - 1, ucd)), M::in(ld_u(A.u, d, i, j, k + 1, ucd)));
         }
-        double gp = 0.0;
+        T gp = M::zero();
         if (fl & kQFace) {
           const double pl = (A.fc[P3(d, i - 1, j, k)] & kFluid) ? A.p[P3(d, i - 1, j, k)] : 0.0;
           const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
-          gp = grad_face(A.Gu[f], pl, A.Gu[NU + f], pr);
+          gp = M::grad(M::in(A.Gu[f]), M::in(pl), M::in(A.Gu[NU + f]), M::in(pr));
         }
-        rhs = mom_rhs(A.a, A.rho, uc, conv, gp, A.bc[0][r], A.sc[0][r]);
+        rhs = M::rhs(A, uc, conv, gp, A.bc[0][r], A.sc[0][r]);
       }
       A.b[0][r] = rhs;
-      A.x0[0][r] = A.zero_guess ? 0.0 : uc;
+      A.x0[0][r] = A.zero_guess ? 0.0 : ucd;
     } else if (t < A.nb[0] + A.nb[1]) {  // v row: face (i, j+1, k)
       const long r = t - A.nb[0];
       long q;
@@ -231,29 +275,30 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
       const int j = udivmod(q, d.dnym, kq) + 1, k = (int)kq;
       const long f = V3(d, i, j, k);
       const uint8_t fl = A.fv[f];
-      const double vc = A.v[f];
+      const double vcd = A.v[f];
       double rhs = 0.0;
       if (fl & kRhsRow) {
-        double conv = 0.0;
+        const T vc = M::in(vcd);
+        T conv = M::zero();
         if (fl & kActive) {
-          const double ua = avg4(ld_u(A.u, d, i, j - 1, k, 0.0), ld_u(A.u, d, i + 1, j - 1, k, 0.0),
-                                 ld_u(A.u, d, i, j, k, 0.0), ld_u(A.u, d, i + 1, j, k, 0.0));
-          const double wa = avg4(ld_w(A.w, d, i, j - 1, k, 0.0), ld_w(A.w, d, i, j, k, 0.0),
-                                 ld_w(A.w, d, i, j - 1, k + 1, 0.0), ld_w(A.w, d, i, j, k + 1, 0.0));
-          conv = advect(ua, ld_v(A.v, d, i - 1, j, k, vc), ld_v(A.v, d, i + 1, j, k, vc), A.tdx, vc,
-                        ld_v(A.v, d, i, j - 1, k, vc), ld_v(A.v, d, i, j + 1, k, vc), A.tdy, wa,
-                        ld_v(A.v, d, i, j, k - 1, vc), ld_v(A.v, d, i, j, k + 1, vc), A.tdz);
+          const T ua = M::avg(M::in(ld_u(A.u, d, i, j - 1, k, 0.0)), M::in(ld_u(A.u, d, i + 1, j - 1, k, 0.0)),
+                              M::in(ld_u(A.u, d, i, j, k, 0.0)), M::in(ld_u(A.u, d, i + 1, j, k, 0.0)));
+          const T wa = M::avg(M::in(ld_w(A.w, d, i, j - 1, k, 0.0)), M::in(ld_w(A.w, d, i, j, k, 0.0)),
+                              M::in(ld_w(A.w, d, i, j - 1, k + 1, 0.0)), M::in(ld_w(A.w, d, i, j, k + 1, 0.0)));
+          conv = M::adv(A, ua, M::in(ld_v(A.v, d, i - 1, j, k, vcd)), M::in(ld_v(A.v, d, i + 1, j, k, vcd)), vc,
+                        M::in(ld_v(A.v, d, i, j - 1, k, vcd)), M::in(ld_v(A.v, d, i, j + 1, k, vcd)), wa,
+                        M::in(ld_v(A.v, d, i, j, k - 1, vcd)), M::in(ld_v(A.v, d, i, j, k + 1, vcd)));
         }
-        double gp = 0.0;
+        T gp = M::zero();
         if (fl & kQFace) {
           const double pl = (A.fc[P3(d, i, j - 1, k)] & kFluid) ? A.p[P3(d, i, j - 1, k)] : 0.0;
           const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
-          gp = grad_face(A.Gv[f], pl, A.Gv[NV + f], pr);
+          gp = M::grad(M::in(A.Gv[f]), M::in(pl), M::in(A.Gv[NV + f]), M::in(pr));
         }
-        rhs = mom_rhs(A.a, A.rho, vc, conv, gp, A.bc[1][r], A.sc[1][r]);
+        rhs = M::rhs(A, vc, conv, gp, A.bc[1][r], A.sc[1][r]);
       }
       A.b[1][r] = rhs;
-      A.x0[1][r] = A.zero_guess ? 0.0 : vc;
+      A.x0[1][r] = A.zero_guess ? 0.0 : vcd;
     } else {  // w row: face (i, j, k+1)
       const long r = t - A.nb[0] - A.nb[1];
       long q;
@@ -262,30 +307,31 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
       const int j = udivmod(q, d.dny, kq), k = (int)kq + 1;
       const long f = W3(d, i, j, k);
       const uint8_t fl = A.fw[f];
-      const double wc = A.w[f];
+      const double wcd = A.w[f];
       double rhs = 0.0;
       if (fl & kRhsRow) {
-        double conv = 0.0;
+        const T wc = M::in(wcd);
+        T conv = M::zero();
         // the convection of w uses the mask one plane below (gpu_dense_ops.hpp:14)
         if (A.fw[f - plane_w] & kActive) {
-          const double ua = avg4(ld_u(A.u, d, i, j, k - 1, 0.0), ld_u(A.u, d, i + 1, j, k - 1, 0.0),
-                                 ld_u(A.u, d, i, j, k, 0.0), ld_u(A.u, d, i + 1, j, k, 0.0));
-          const double va = avg4(ld_v(A.v, d, i, j, k - 1, 0.0), ld_v(A.v, d, i, j + 1, k - 1, 0.0),
-                                 ld_v(A.v, d, i, j, k, 0.0), ld_v(A.v, d, i, j + 1, k, 0.0));
-          conv = advect(ua, ld_w(A.w, d, i - 1, j, k, wc), ld_w(A.w, d, i + 1, j, k, wc), A.tdx, va,
-                        ld_w(A.w, d, i, j - 1, k, wc), ld_w(A.w, d, i, j + 1, k, wc), A.tdy, wc,
-                        ld_w(A.w, d, i, j, k - 1, wc), ld_w(A.w, d, i, j, k + 1, wc), A.tdz);
+          const T ua = M::avg(M::in(ld_u(A.u, d, i, j, k - 1, 0.0)), M::in(ld_u(A.u, d, i + 1, j, k - 1, 0.0)),
+                              M::in(ld_u(A.u, d, i, j, k, 0.0)), M::in(ld_u(A.u, d, i + 1, j, k, 0.0)));
+          const T va = M::avg(M::in(ld_v(A.v, d, i, j, k - 1, 0.0)), M::in(ld_v(A.v, d, i, j + 1, k - 1, 0.0)),
+                              M::in(ld_v(A.v, d, i, j, k, 0.0)), M::in(ld_v(A.v, d, i, j + 1, k, 0.0)));
+          conv = M::adv(A, ua, M::in(ld_w(A.w, d, i - 1, j, k, wcd)), M::in(ld_w(A.w, d, i + 1, j, k, wcd)), va,
+                        M::in(ld_w(A.w, d, i, j - 1, k, wcd)), M::in(ld_w(A.w, d, i, j + 1, k, wcd)), wc,
+                        M::in(ld_w(A.w, d, i, j, k - 1, wcd)), M::in(ld_w(A.w, d, i, j, k + 1, wcd)));
         }
-        double gp = 0.0;
+        T gp = M::zero();
         if (fl & kQFace) {
           const double pl = (A.fc[P3(d, i, j, k - 1)] & kFluid) ? A.p[P3(d, i, j, k - 1)] : 0.0;
           const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
-          gp = grad_face(A.Gw[f], pl, A.Gw[NW + f], pr);
+          gp = M::grad(M::in(A.Gw[f]), M::in(pl), M::in(A.Gw[NW + f]), M::in(pr));
         }
-        rhs = mom_rhs(A.a, A.rho, wc, conv, gp, A.bc[2][r], A.sc[2][r]);
+        rhs = M::rhs(A, wc, conv, gp, A.bc[2][r], A.sc[2][r]);
       }
       A.b[2][r] = rhs;
-      A.x0[2][r] = A.zero_guess ? 0.0 : wc;
+      A.x0[2][r] = A.zero_guess ? 0.0 : wcd;
     }
   }
 }
@@ -629,6 +675,11 @@ void launch_bc(ibm_ctx *c, double *u, double *v, double *w) {
   }
 }
 
+bool momentum_rhs_df(const ibm_solver_params &p) {
+  const int vp = p.vel_precision >= 0 ? p.vel_precision : p.precision;
+  return p.df_rhs != 0 && vp >= 1;
+}
+
 void launch_momentum_rhs(ibm_ctx *c) {
   RhsArgs A;
   A.d = dims_of(c);
@@ -646,9 +697,20 @@ void launch_momentum_rhs(ibm_ctx *c) {
   A.tdy = make_known_div(2 * c->g.dy);
   A.tdz = make_known_div(2 * c->g.dz);
   A.zero_guess = c->prm.use_zero_initial_guess != 0;
+  // host split of a constant: RN to FP32 and the rounded remainder (2^-48)
+  auto split = [](double x) {
+    const float h = (float)x;
+    return DF{h, (float)(x - (double)h)};
+  };
+  A.da = split(A.a); A.drho = split(A.rho);
+  A.drx = split(1.0 / (2 * c->g.dx)); A.dry = split(1.0 / (2 * c->g.dy)); A.drz = split(1.0 / (2 * c->g.dz));
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW), nbox = (double)(A.nb[0] + A.nb[1] + A.nb[2]);
   LaunchScope ls(K_RHS, c->st, 8.0 * faces + 9.0 * c->g.NP + nbox * (1 + 16 + 32));
-  k_momentum_rhs<<<wave_blocks(k_momentum_rhs, A.nb[0] + A.nb[1] + A.nb[2]), kThreads, 0, c->st>>>(A);
+  const long rows = A.nb[0] + A.nb[1] + A.nb[2];
+  if (momentum_rhs_df(c->prm))
+    k_momentum_rhs<RhsDF><<<wave_blocks(k_momentum_rhs<RhsDF>, rows), kThreads, 0, c->st>>>(A);
+  else
+    k_momentum_rhs<RhsF64><<<wave_blocks(k_momentum_rhs<RhsF64>, rows), kThreads, 0, c->st>>>(A);
 }
 
 void launch_tilde(ibm_ctx *c) {

@@ -121,6 +121,15 @@ typedef struct ibm_solver_params {
                             channel: about 96 us a sweep against 62 us for the two phases */
   int vel_precision;     /* precision of the three momentum solves (0, 1, 2 as `precision`); -1
                             (default): `precision` */
+  int df_spmv;           /* precision 1 with row classes, 1 (default): the Arnoldi product A z_j of the
+                            FP32 flexible basis is formed in double-float on the FP32 pipe (about 46
+                            significant bits of the row's magnitude) and widened to FP64 once per row;
+                            the Arnoldi dot products and everything after them stay FP64. 0: FP64 */
+  int df_rhs;            /* momentum solves in precision 1 or 2, 1 (default): the convection / momentum
+                            right-hand side (ibm_step, ibm_assemble_momentum) is evaluated in
+                            double-float on the FP32 and integer pipes, inputs split from their FP64
+                            bits, and widened to FP64 once per row (about 2^-44 of the row's largest
+                            term). 0, or FP64 momentum solves: the FP64 kernel, bitwise the reference's */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {

@@ -199,6 +199,32 @@ def test_mixed_precision_error(ibm, pyoracle, case48, precision):
     assert vel_err <= 1e-6
 
 
+@pytest.mark.parametrize("vel_precision", [1, 2])
+def test_double_float_momentum_rhs(ibm, pyoracle, case48, vel_precision):
+    """With mixed-precision momentum solves the momentum right-hand side is
+    evaluated in double-float (df_rhs 1, the default): against the oracle's
+    FP64 right-hand side from the same seeded random state it is within
+    2^-40 of the largest entry and not bitwise equal (the double-float kernel
+    ran); df_rhs 0 keeps the FP64 kernel, bitwise the oracle's."""
+    orc = pyoracle.Oracle(case48, vel_tol=1e-13, p_tol=1e-13)
+    u, v, w, p = random_state(case48, 77)
+    ramp = 0.6
+    ub, vb, wb = orc.bc_cleanup(u, v, w, ramp)
+    ref = orc.momentum_rhs(ub, vb, wb, p)
+    for df in (1, 0):
+        s = ibm.Solver(case48, ibm.solver_params(precision=1, vel_precision=vel_precision, df_rhs=df))
+        s.set_fields(u, v, w, p)
+        s.step(ramp)
+        for f in range(3):
+            got = s.solver_vector(f, 0)
+            if df:
+                assert np.abs(got - ref[f]).max() <= 2.0 ** -40 * np.abs(ref[f]).max(), f
+                assert not bits_equal(got, ref[f]), f
+            else:
+                assert bits_equal(got, ref[f]), f
+        s.close()
+
+
 def test_fp32_cycles_reach_tight_tolerance(ibm, pyoracle, case48):
     """precision 2 restarts its FP32 cycles from FP64 true residuals, so it
     reaches tolerances far below FP32 resolution: 1e-12 on every solve."""
