@@ -56,7 +56,7 @@ class SolverParams(C.Structure):
                 ("row_classes", C.c_int), ("mg_quads", C.c_int),
                 ("df_residual", C.c_int), ("mg_fused_coarse", C.c_int),
                 ("mg_fused_sweep", C.c_int), ("vel_precision", C.c_int),
-                ("df_spmv", C.c_int), ("df_rhs", C.c_int)]
+                ("df_spmv", C.c_int), ("df_rhs", C.c_int), ("arnoldi_passes", C.c_int)]
 
 
 class Profile(C.Structure):

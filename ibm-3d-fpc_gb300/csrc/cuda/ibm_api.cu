@@ -297,7 +297,7 @@ void ensure_solvers(ibm_ctx *c) {
     if (vmixed) {
       h.pc = 2; h.pc_cb = 0; h.A = o.c.p; h.inner_sweeps = std::max(1, p.vel_inner_sweeps);
       h.a32 = va32; h.cycle_rtol = p.cycle_rtol32; h.df_residual = p.df_residual;
-      h.df_spmv = p.df_spmv;
+      h.df_spmv = p.df_spmv; h.arnoldi_passes = p.arnoldi_passes;
     }
     else { h.pc = 0; h.A = o.cj.p; }
     if (p.row_classes) {
@@ -330,14 +330,14 @@ void ensure_solvers(ibm_ctx *c) {
     c->mg.setup(c->st, op.b, op.c.p, op.cf.p, h, mp, true, mixed, winv);
     if (mixed) {
       hp.pc = 2; hp.pc_cb = 1; hp.A = op.c.p; hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32;
-      hp.df_residual = p.df_residual; hp.df_spmv = p.df_spmv;
+      hp.df_residual = p.df_residual; hp.df_spmv = p.df_spmv; hp.arnoldi_passes = p.arnoldi_passes;
     }
     else { hp.pc = 1; hp.A = op.c.p; }
   } else {
     if (mixed) {
       hp.pc = 2; hp.pc_cb = 0; hp.A = op.c.p; hp.inner_sweeps = 1;
       hp.a32 = a32; hp.cycle_rtol = p.cycle_rtol32; hp.df_residual = p.df_residual;
-      hp.df_spmv = p.df_spmv;
+      hp.df_spmv = p.df_spmv; hp.arnoldi_passes = p.arnoldi_passes;
     }
     else { hp.pc = 0; hp.A = op.cj.p; }
   }
@@ -456,6 +456,7 @@ void ibm_solver_params_default(ibm_solver_params *p) {
   p->vel_precision = -1;
   p->df_spmv = 1;
   p->df_rhs = 1;
+  p->arnoldi_passes = 2;
 }
 
 const char *ibm_last_error(ibm_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
@@ -953,6 +954,7 @@ int ibm_set_solver_params(ibm_ctx *c, const ibm_solver_params *p) {
       throw Error(IBM_ERR_ARG, "bad tolerance or iteration limit");
     if (p->precision < 0 || p->precision > 2) throw Error(IBM_ERR_ARG, "precision must be 0, 1 or 2");
     if (p->vel_precision < -1 || p->vel_precision > 2) throw Error(IBM_ERR_ARG, "vel_precision must be -1, 0, 1 or 2");
+    if (p->arnoldi_passes != 1 && p->arnoldi_passes != 2) throw Error(IBM_ERR_ARG, "arnoldi_passes must be 1 or 2");
     if (!(p->cycle_rtol32 > 0.0 && p->cycle_rtol32 < 1.0)) throw Error(IBM_ERR_ARG, "cycle_rtol32 must be in (0, 1)");
     if (p->p_pc != 0 && p->p_pc != 1) throw Error(IBM_ERR_ARG, "p_pc must be 0 or 1");
     if (p->mg_nu1 < 0 || p->mg_nu2 < 0 || p->mg_nu_coarse < 0 || p->mg_coarse_max < 1 || p->mg_max_levels < 1)

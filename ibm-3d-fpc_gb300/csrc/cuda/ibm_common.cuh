@@ -203,6 +203,7 @@ struct KSys {
   int df_resid;         // FP32 cycles with classes: true residuals in double-float (FP32 pipe)
   float2 *xs;           // df_resid: x as double-float pairs, written with every update of x
   int df_spmv;          // pc 2, FP64 cycles, classes: A z_j in double-float (tabdf) on the FP32 pipe
+  int cgs1;             // pc 2, FP64 cycles: one classical Gram-Schmidt pass (no k_arnoldi_orth)
   float *vcur;          // pc 2 with FP32 Jacobi and an FP64 basis: (float) V_j of the current j, written
                         // by the kernel that forms V_j, read by the Jacobi sweeps (null: read V_j)
 };

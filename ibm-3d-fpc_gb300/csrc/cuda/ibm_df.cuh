@@ -85,26 +85,27 @@ __device__ __forceinline__ void df_split(double v, float &hi, float &lo) {
 }
 
 // v == hi + lo to within 2^-46 |v| from the bits of v, on the integer and
-// FP32 pipes without an int-to-float conversion: hi holds the leading 24
-// significand bits (truncated), lo the next 23 (truncated), built as
-// (2^23 + L) - 2^23 from an exponent-forced float and scaled by a power of
-// two. |v| below 2^-126 gives a signed zero, lo is dropped below 2^-81;
-// |v| at or above 2^128, infinities and NaN take df_split.
+// FP32 pipes without a conversion instruction: hi holds the leading 24
+// significand bits (truncated), lo the next 23 (truncated). For a biased
+// exponent e in (896, 1151) one funnel shift brings the low 8 exponent bits
+// and 23 fraction bits into place and flipping bit 30 rebiases the exponent
+// (e - 896 == (e mod 256) xor 128 there); lo is (2^23 + L) 2^-46 - 2^-23,
+// exact in one FMA, times hi's signed power of two. |v| below 2^-126 gives
+// a signed zero, lo underflows gradually below 2^-81 (an absolute error under
+// 2^-104); |v| at or above 2^128, infinities and NaN take df_split.
 __device__ __forceinline__ void df_split_fast(double v, float &hi, float &lo) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(v);
   const unsigned uh = (unsigned)(u >> 32), ul = (unsigned)u;
+  const unsigned e = (uh >> 20) & 0x7FFu;
+  if (e >= 1151u) { df_split(v, hi, lo); return; }
   const unsigned sgn = uh & 0x80000000u;
-  const int e = (int)((uh >> 20) & 0x7ff);
-  const int fe = e - 896;  // float biased exponent of the leading bit
-  if (fe <= 0) { hi = __uint_as_float(sgn); lo = 0.0f; return; }
-  if (fe >= 255) { df_split(v, hi, lo); return; }
-  hi = __uint_as_float(sgn | ((unsigned)fe << 23) | ((uh & 0xFFFFFu) << 3) | (ul >> 29));
-  // significand bits 28..6 (L, weight 2^(e - 1069)): float exponent e - 942
-  const unsigned L = (ul & 0x1FFFFFFFu) >> 6;
-  const int se = e - 942;
-  const float lf = __fsub_rn(__uint_as_float(0x4B000000u | L), 8388608.0f);
-  const float lm = se > 0 ? __fmul_rn(lf, __uint_as_float((unsigned)se << 23)) : 0.0f;
-  lo = __uint_as_float(__float_as_uint(lm) | sgn);
+  const unsigned hb = ((__funnelshift_l(ul, uh, 3) ^ 0x40000000u) & 0x7FFFFFFFu) | sgn;
+  const float raw = __uint_as_float(0x4B000000u | ((ul >> 6) & 0x7FFFFFu));
+  const float lf = __fmaf_rn(raw, 1.4210854715202004e-14f, -1.1920928955078125e-07f);  // L 2^-46
+  const float lm = __fmul_rn(lf, __uint_as_float(hb & 0xFF800000u));
+  const bool tiny = e <= 896u;
+  hi = __uint_as_float(tiny ? sgn : hb);
+  lo = tiny ? 0.0f : lm;
 }
 
 // A double-float value and the operations the dense kernels need. Sums and

@@ -276,17 +276,23 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
         if (S.df_spmv) {
           // A z_j with z_j exact in FP32: the seven products and their sum in
           // double-float, widened once (two conversions and one FP64 add)
-          const float *c = S.tabdf + 16 * (long)S.cls[r];
+          // (a neighbour outside the box reads as 0: its product and sum are
+          // exact no-ops, so all seven loads issue together)
+          const float4 *c4 = reinterpret_cast<const float4 *>(S.tabdf + 16 * (long)S.cls[r]);
           const float *zj = S.Z + (long)j * S.ldv;
           const long sy = S.nx, sz = (long)S.nx * S.ny;
+          const float z0 = zj[r], zxm = i > 0 ? zj[r - 1] : 0.0f, zxp = i < S.nx - 1 ? zj[r + 1] : 0.0f,
+                      zym = jj > 0 ? zj[r - sy] : 0.0f, zyp = jj < S.ny - 1 ? zj[r + sy] : 0.0f,
+                      zzm = k > 0 ? zj[r - sz] : 0.0f, zzp = k < S.nz - 1 ? zj[r + sz] : 0.0f;
+          const float4 h0 = __ldg(c4), h1 = __ldg(c4 + 1), l0 = __ldg(c4 + 2), l1 = __ldg(c4 + 3);
           float ah = 0.0f, al = 0.0f;
-          df_fma1(ah, al, c[0], c[8], zj[r]);
-          if (i > 0) df_fma1(ah, al, c[1], c[9], zj[r - 1]);
-          if (i < S.nx - 1) df_fma1(ah, al, c[2], c[10], zj[r + 1]);
-          if (jj > 0) df_fma1(ah, al, c[3], c[11], zj[r - sy]);
-          if (jj < S.ny - 1) df_fma1(ah, al, c[4], c[12], zj[r + sy]);
-          if (k > 0) df_fma1(ah, al, c[5], c[13], zj[r - sz]);
-          if (k < S.nz - 1) df_fma1(ah, al, c[6], c[14], zj[r + sz]);
+          df_fma1(ah, al, h0.x, l0.x, z0);
+          df_fma1(ah, al, h0.y, l0.y, zxm);
+          df_fma1(ah, al, h0.z, l0.z, zxp);
+          df_fma1(ah, al, h0.w, l0.w, zym);
+          df_fma1(ah, al, h1.x, l1.x, zyp);
+          df_fma1(ah, al, h1.y, l1.y, zzm);
+          df_fma1(ah, al, h1.z, l1.z, zzp);
           w = (double)ah + (double)al;
         } else if (S.pc == 0) w = stencil7_at(c0, cs, vj, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
         else if (S.pc == 1) w = stencil7_at(c0, cs, S.z, (int)r, i, jj, k, S.nx, S.ny, S.nz) * inv_nu;
@@ -329,6 +335,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
     const double h = tot[kk] / sc->nu[kk];
     sc->h1[kk] = h;
     sc->coef[kk] = h / sc->nu[kk];
+    if (S.cgs1) sc->H[kk * kMaxKdim + j] = h;  // one pass: the column is the first projection
   }
   if (threadIdx.x == 0) sc->ticket = 0;
 }
@@ -338,7 +345,7 @@ __global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(KSys *sys) {
 __global__ void __launch_bounds__(kThreads) k_arnoldi_orth(KSys *sys) {
   KSys &S = sys[blockIdx.y];
   KScal *sc = S.s;
-  if (!sc->active || S.a32) return;
+  if (!sc->active || S.a32 || S.cgs1) return;
   const int j = sc->i, nd = j + 1;
   __shared__ double sacc[(kMaxKdim + 1) * kWarps];
   __shared__ double cf[kMaxKdim + 1];
@@ -1065,6 +1072,12 @@ __global__ void __launch_bounds__(kThreads) k_jacobi32_first(KSys *sys, int to_z
   const double *vj = S.V + (long)j * S.ldv;
   const float *vjf = S.Vf + (long)j * S.ldv;
   float *out = to_z ? S.Z + (long)j * S.ldv : S.zf;
+  if (S.vcur) {  // FP64 basis through its FP32 copy: no FP64 instruction
+    const float inv_nuf = (float)inv_nu;
+    for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x)
+      out[r] = (S.vcur[r] * inv_nuf) * S.invdf[r];
+    return;
+  }
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x)
     out[r] = (float)((S.a32 ? (double)vjf[r] : vj[r]) * inv_nu) * S.invdf[r];
 }
@@ -1079,13 +1092,14 @@ __global__ void __launch_bounds__(kThreads) k_jacobi32_sweep(KSys *sys, int src_
   const float *vjf = S.Vf + (long)j * S.ldv;
   const float *src = src_is_zf ? S.zf : S.zf2;
   float *dst = to_z ? S.Z + (long)j * S.ldv : (src_is_zf ? S.zf2 : S.zf);
+  const float inv_nuf = (float)inv_nu;
   for (long r = (long)blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += (long)gridDim.x * blockDim.x) {
     int i, jj, k;
     sys_ijk(r, S, i, jj, k);
     long cs;
     const float *c0 = af_row(S, r, cs);
     const float az = stencil7_at_f(c0, cs, src, (int)r, i, jj, k, S.nx, S.ny, S.nz);
-    const float v = (float)((S.a32 ? (double)vjf[r] : vj[r]) * inv_nu);
+    const float v = S.vcur ? S.vcur[r] * inv_nuf : (float)((S.a32 ? (double)vjf[r] : vj[r]) * inv_nu);
     dst[r] = fmaf(S.invdf[r], v - az, src[r]);
   }
 }
@@ -1212,6 +1226,7 @@ void Krylov::bind(cudaStream_t st, const double *const *b, double *const *x, uns
     k.zf = slot[s].zf.p; k.zf2 = slot[s].zf2.p;
     k.Vf = slot[s].Vf.p; k.wf = slot[s].wf.p; k.a32 = h.a32;
     k.vcur = slot[s].vcur.p;
+    k.cgs1 = cgs1(h) ? 1 : 0;
     k.x_zero = x_zero ? 1 : 0;
     k.vec4 = (h.n % 4 == 0) ? 1 : 0;
     k.x = x[s]; k.b = b[s];
@@ -1308,12 +1323,13 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
     }
   }
   int inner_sweeps = 0;
-  bool any64 = false, any32 = false;
-  double r32 = 0.0, j32two = 0.0, bsp = 0.0, bor = 0.0, bnx = 0.0, bsp32 = 0.0, bor32 = 0.0;
+  bool any64 = false, any32 = false, any_orth = false;
+  double r32 = 0.0, j32two = 0.0, bsp = 0.0, bor = 0.0, bor_orth = 0.0, bnx = 0.0, bsp32 = 0.0, bor32 = 0.0;
   for (int s = 0; s < nsys; ++s) {
     if (!((mask >> s) & 1u)) continue;
     const bool a32 = slot[s].host.a32 != 0;
     (a32 ? any32 : any64) = true;
+    if (!a32 && !cgs1(slot[s].host)) any_orth = true;
     if (slot[s].host.pc == 2 && !slot[s].host.pc_cb && (!fl || fl[s].active))
       inner_sweeps = std::max(inner_sweeps, std::max(1, slot[s].host.inner_sweeps));
     if (!fl || !fl[s].active) continue;
@@ -1322,7 +1338,7 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
     // coefficient bytes of a row: 7 values, or a 2-byte class
     const double c64 = (h.cls && h.A == h.Ar) ? 2.0 : 56.0, c32 = h.cls ? 2.0 : 28.0;
     if (h.pc == 2 && !h.pc_cb) {
-      r32 += rows(s) * (a32 ? 0.75 : 1.0);
+      r32 += rows(s) * ((a32 || slot[s].vcur.p) ? 0.75 : 1.0);  // v read as FP32 or FP64
       // two sweeps in one pass: v, z and a 2-byte class instead of 7 FP32 values
       j32two += rows(s) * (h.clsj ? 10.0 : 27.0);  // v read as FP32 (basis or copy)
       if (!a32) bnx += 4.0 * rows(s);                // the copy, written by k_arnoldi_next
@@ -1333,6 +1349,7 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
     } else {
       bsp += rows(s) * ((h.pc == 2 ? 12.0 : 16.0) + c64 + 8.0 * j1);
       bor += rows(s) * (16.0 + 8.0 * j1);
+      if (!cgs1(h)) bor_orth += rows(s) * (16.0 + 8.0 * j1);
     }
   }
   if (inner_sweeps > 0) {
@@ -1360,8 +1377,8 @@ void Krylov::launch_arnoldi(cudaStream_t st, const Precond &pc, const KFlags *fl
       LaunchScope ls(K_GM_SPMV, st, bsp);
       k_arnoldi_spmv<<<wave(k_arnoldi_spmv), kThreads, 0, st>>>(dev);
     }
-    {
-      LaunchScope ls(K_GM_ORTH, st, bor);
+    if (any_orth) {
+      LaunchScope ls(K_GM_ORTH, st, bor_orth);
       k_arnoldi_orth<<<wave(k_arnoldi_orth), kThreads, 0, st>>>(dev);
     }
     LaunchScope ls(K_GM_NEXT, st, bor + bnx);

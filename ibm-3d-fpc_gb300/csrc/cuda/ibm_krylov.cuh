@@ -52,7 +52,13 @@ struct KSysHost {
   const float *tabdf = nullptr;  // with a32: true residuals in double-float
   int df_residual = 1;           // use them when a32 and tabdf are set
   int df_spmv = 1;               // pc 2 without a32: A z_j in double-float from tabdf
+  int arnoldi_passes = 2;        // pc 2 without a32: Gram-Schmidt passes per Arnoldi step (1 or 2)
 };
+
+// One classical Gram-Schmidt pass per Arnoldi step (no re-orthogonalisation):
+// FP64 cycles of the flexible form when configured. The FP64 true residual
+// at each cycle end still decides convergence.
+inline bool cgs1(const KSysHost &h) { return h.pc == 2 && !h.a32 && h.arnoldi_passes == 1; }
 
 struct KResult {
   int iters = 0;

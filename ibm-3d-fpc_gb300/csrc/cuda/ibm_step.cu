@@ -44,17 +44,6 @@ __device__ __forceinline__ long V3(const Dims &d, int i, int j, int k) { return 
 __device__ __forceinline__ long W3(const Dims &d, int i, int j, int k) { return ((long)k * d.ny + j) * d.nx + i; }
 __device__ __forceinline__ long P3(const Dims &d, int i, int j, int k) { return ((long)k * d.ny + j) * d.nx + i; }
 
-// Bounds-guarded loads with a fallback outside the arrays (gpu_dense_ops.hpp:1-3).
-__device__ __forceinline__ double ld_u(const double *u, const Dims &d, int i, int j, int k, double fb) {
-  return (i < 0 || i > d.nx || j < 0 || j >= d.ny || k < 0 || k >= d.nz) ? fb : u[U3(d, i, j, k)];
-}
-__device__ __forceinline__ double ld_v(const double *v, const Dims &d, int i, int j, int k, double fb) {
-  return (i < 0 || i >= d.nx || j < 0 || j > d.ny || k < 0 || k >= d.nz) ? fb : v[V3(d, i, j, k)];
-}
-__device__ __forceinline__ double ld_w(const double *w, const Dims &d, int i, int j, int k, double fb) {
-  return (i < 0 || i >= d.nx || j < 0 || j >= d.ny || k < 0 || k > d.nz) ? fb : w[W3(d, i, j, k)];
-}
-
 // x / b correctly rounded for a divisor known in advance, without a division:
 // rb = RN(1/b) is computed once on the host, q0 = RN(x rb) is within an ulp of
 // x / b, and one correction with the exact remainder r = x - b q0 (a single
@@ -226,6 +215,12 @@ struct RhsDF {
 };
 
 // One thread per solve-box row of u, v and w (flat index over the three boxes).
+// The loads are those of the reference's bounds-guarded loads
+// (gpu_dense_ops.hpp:1-3) with the guards that a solve-box row can never fail
+// dropped: on a u row (1 <= i <= nx-1) the x neighbours of u and the four v
+// and w points of the averages always lie inside their arrays, only the y
+// and z neighbours of u can fall back to the centre value; likewise for v
+// (x and z neighbours guarded) and w (x and y neighbours guarded).
 template <class M>
 __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
   using T = typename M::T;
@@ -233,7 +228,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
   const long total = A.nb[0] + A.nb[1] + A.nb[2];
   const long NU = (long)(d.nx + 1) * d.ny * d.nz, NV = (long)d.nx * (d.ny + 1) * d.nz,
              NW = (long)d.nx * d.ny * (d.nz + 1);
-  const long plane_w = (long)d.nx * d.ny;
+  const long su = d.nx + 1, pu = (long)(d.nx + 1) * d.ny;  // u strides along y and z
+  const long sv = d.nx, pv = (long)d.nx * (d.ny + 1);     // v
+  const long sw = d.nx, pw = (long)d.nx * d.ny;           // w and cells
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
     if (t < A.nb[0]) {  // u row: face (i+1, j, k) with i in [0, nx-2]
       const long r = t;
@@ -249,18 +246,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
         const T uc = M::in(ucd);
         T conv = M::zero();
         if (fl & kActive) {
-          const T va = M::avg(M::in(ld_v(A.v, d, i - 1, j, k, 0.0)), M::in(ld_v(A.v, d, i - 1, j + 1, k, 0.0)),
-                              M::in(ld_v(A.v, d, i, j, k, 0.0)), M::in(ld_v(A.v, d, i, j + 1, k, 0.0)));
-          const T wa = M::avg(M::in(ld_w(A.w, d, i - 1, j, k, 0.0)), M::in(ld_w(A.w, d, i - 1, j, k + 1, 0.0)),
-                              M::in(ld_w(A.w, d, i, j, k, 0.0)), M::in(ld_w(A.w, d, i, j, k + 1, 0.0)));
-          conv = M::adv(A, uc, M::in(ld_u(A.u, d, i - 1, j, k, ucd)), M::in(ld_u(A.u, d, i + 1, j, k, ucd)), va,
-                        M::in(ld_u(A.u, d, i, j - 1, k, ucd)), M::in(ld_u(A.u, d, i, j + 1, k, ucd)), wa,
-                        M::in(ld_u(A.u, d, i, j, k - 1, ucd)), M::in(ld_u(A.u, d, i, j, k + 1, ucd)));
+          const long vb = V3(d, i - 1, j, k), wb = W3(d, i - 1, j, k);
+          const T va = M::avg(M::in(A.v[vb]), M::in(A.v[vb + sv]), M::in(A.v[vb + 1]), M::in(A.v[vb + 1 + sv]));
+          const T wa = M::avg(M::in(A.w[wb]), M::in(A.w[wb + pw]), M::in(A.w[wb + 1]), M::in(A.w[wb + 1 + pw]));
+          conv = M::adv(A, uc, M::in(A.u[f - 1]), M::in(A.u[f + 1]), va,
+                        M::in(j > 0 ? A.u[f - su] : ucd), M::in(j < d.ny - 1 ? A.u[f + su] : ucd), wa,
+                        M::in(k > 0 ? A.u[f - pu] : ucd), M::in(k < d.nz - 1 ? A.u[f + pu] : ucd));
         }
         T gp = M::zero();
         if (fl & kQFace) {
-          const double pl = (A.fc[P3(d, i - 1, j, k)] & kFluid) ? A.p[P3(d, i - 1, j, k)] : 0.0;
-          const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
+          const long c = P3(d, i - 1, j, k);
+          const double pl = (A.fc[c] & kFluid) ? A.p[c] : 0.0;
+          const double pr = (A.fc[c + 1] & kFluid) ? A.p[c + 1] : 0.0;
           gp = M::grad(M::in(A.Gu[f]), M::in(pl), M::in(A.Gu[NU + f]), M::in(pr));
         }
         rhs = M::rhs(A, uc, conv, gp, A.bc[0][r], A.sc[0][r]);
@@ -281,18 +278,18 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
         const T vc = M::in(vcd);
         T conv = M::zero();
         if (fl & kActive) {
-          const T ua = M::avg(M::in(ld_u(A.u, d, i, j - 1, k, 0.0)), M::in(ld_u(A.u, d, i + 1, j - 1, k, 0.0)),
-                              M::in(ld_u(A.u, d, i, j, k, 0.0)), M::in(ld_u(A.u, d, i + 1, j, k, 0.0)));
-          const T wa = M::avg(M::in(ld_w(A.w, d, i, j - 1, k, 0.0)), M::in(ld_w(A.w, d, i, j, k, 0.0)),
-                              M::in(ld_w(A.w, d, i, j - 1, k + 1, 0.0)), M::in(ld_w(A.w, d, i, j, k + 1, 0.0)));
-          conv = M::adv(A, ua, M::in(ld_v(A.v, d, i - 1, j, k, vcd)), M::in(ld_v(A.v, d, i + 1, j, k, vcd)), vc,
-                        M::in(ld_v(A.v, d, i, j - 1, k, vcd)), M::in(ld_v(A.v, d, i, j + 1, k, vcd)), wa,
-                        M::in(ld_v(A.v, d, i, j, k - 1, vcd)), M::in(ld_v(A.v, d, i, j, k + 1, vcd)));
+          const long ub = U3(d, i, j - 1, k), wb = W3(d, i, j - 1, k);
+          const T ua = M::avg(M::in(A.u[ub]), M::in(A.u[ub + 1]), M::in(A.u[ub + su]), M::in(A.u[ub + su + 1]));
+          const T wa = M::avg(M::in(A.w[wb]), M::in(A.w[wb + sw]), M::in(A.w[wb + pw]), M::in(A.w[wb + pw + sw]));
+          conv = M::adv(A, ua, M::in(i > 0 ? A.v[f - 1] : vcd), M::in(i < d.nx - 1 ? A.v[f + 1] : vcd), vc,
+                        M::in(A.v[f - sv]), M::in(A.v[f + sv]), wa,
+                        M::in(k > 0 ? A.v[f - pv] : vcd), M::in(k < d.nz - 1 ? A.v[f + pv] : vcd));
         }
         T gp = M::zero();
         if (fl & kQFace) {
-          const double pl = (A.fc[P3(d, i, j - 1, k)] & kFluid) ? A.p[P3(d, i, j - 1, k)] : 0.0;
-          const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
+          const long c = P3(d, i, j - 1, k);
+          const double pl = (A.fc[c] & kFluid) ? A.p[c] : 0.0;
+          const double pr = (A.fc[c + sw] & kFluid) ? A.p[c + sw] : 0.0;
           gp = M::grad(M::in(A.Gv[f]), M::in(pl), M::in(A.Gv[NV + f]), M::in(pr));
         }
         rhs = M::rhs(A, vc, conv, gp, A.bc[1][r], A.sc[1][r]);
@@ -313,19 +310,19 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
         const T wc = M::in(wcd);
         T conv = M::zero();
         // the convection of w uses the mask one plane below (gpu_dense_ops.hpp:14)
-        if (A.fw[f - plane_w] & kActive) {
-          const T ua = M::avg(M::in(ld_u(A.u, d, i, j, k - 1, 0.0)), M::in(ld_u(A.u, d, i + 1, j, k - 1, 0.0)),
-                              M::in(ld_u(A.u, d, i, j, k, 0.0)), M::in(ld_u(A.u, d, i + 1, j, k, 0.0)));
-          const T va = M::avg(M::in(ld_v(A.v, d, i, j, k - 1, 0.0)), M::in(ld_v(A.v, d, i, j + 1, k - 1, 0.0)),
-                              M::in(ld_v(A.v, d, i, j, k, 0.0)), M::in(ld_v(A.v, d, i, j + 1, k, 0.0)));
-          conv = M::adv(A, ua, M::in(ld_w(A.w, d, i - 1, j, k, wcd)), M::in(ld_w(A.w, d, i + 1, j, k, wcd)), va,
-                        M::in(ld_w(A.w, d, i, j - 1, k, wcd)), M::in(ld_w(A.w, d, i, j + 1, k, wcd)), wc,
-                        M::in(ld_w(A.w, d, i, j, k - 1, wcd)), M::in(ld_w(A.w, d, i, j, k + 1, wcd)));
+        if (A.fw[f - pw] & kActive) {
+          const long ub = U3(d, i, j, k - 1), vb = V3(d, i, j, k - 1);
+          const T ua = M::avg(M::in(A.u[ub]), M::in(A.u[ub + 1]), M::in(A.u[ub + pu]), M::in(A.u[ub + pu + 1]));
+          const T va = M::avg(M::in(A.v[vb]), M::in(A.v[vb + sv]), M::in(A.v[vb + pv]), M::in(A.v[vb + pv + sv]));
+          conv = M::adv(A, ua, M::in(i > 0 ? A.w[f - 1] : wcd), M::in(i < d.nx - 1 ? A.w[f + 1] : wcd), va,
+                        M::in(j > 0 ? A.w[f - sw] : wcd), M::in(j < d.ny - 1 ? A.w[f + sw] : wcd), wc,
+                        M::in(A.w[f - pw]), M::in(A.w[f + pw]));
         }
         T gp = M::zero();
         if (fl & kQFace) {
-          const double pl = (A.fc[P3(d, i, j, k - 1)] & kFluid) ? A.p[P3(d, i, j, k - 1)] : 0.0;
-          const double pr = (A.fc[P3(d, i, j, k)] & kFluid) ? A.p[P3(d, i, j, k)] : 0.0;
+          const long c = P3(d, i, j, k - 1);
+          const double pl = (A.fc[c] & kFluid) ? A.p[c] : 0.0;
+          const double pr = (A.fc[c + pw] & kFluid) ? A.p[c + pw] : 0.0;
           gp = M::grad(M::in(A.Gw[f]), M::in(pl), M::in(A.Gw[NW + f]), M::in(pr));
         }
         rhs = M::rhs(A, wc, conv, gp, A.bc[2][r], A.sc[2][r]);

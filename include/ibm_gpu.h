@@ -130,6 +130,10 @@ typedef struct ibm_solver_params {
                             double-float on the FP32 and integer pipes, inputs split from their FP64
                             bits, and widened to FP64 once per row (about 2^-44 of the row's largest
                             term). 0, or FP64 momentum solves: the FP64 kernel, bitwise the reference's */
+  int arnoldi_passes;    /* precision 1 (FP64 flexible GMRES): classical Gram-Schmidt passes per Arnoldi
+                            step, 2 (default: one re-orthogonalisation, as the FP64 form) or 1 (one
+                            pass and one fewer sweep over the basis; the FP64 true residual at each
+                            restart still decides convergence) */
 } ibm_solver_params;
 
 typedef struct ibm_solve_stats {

@@ -225,6 +225,37 @@ def test_double_float_momentum_rhs(ibm, pyoracle, case48, vel_precision):
         s.close()
 
 
+@pytest.mark.parametrize("graph", [0, 1])
+def test_single_pass_gram_schmidt(ibm, pyoracle, case48, graph):
+    """FP64 flexible GMRES with one classical Gram-Schmidt pass per Arnoldi
+    step (arnoldi_passes 1) against two passes: iteration counts within one
+    and fields within 1e-7 over five steps; at 1e-12 every solve still
+    converges (true FP64 residuals) and the fields agree with the FP64
+    oracle to 1e-9."""
+    kw = dict(vel_tol=1e-8, p_tol=1e-8, precision=1, use_graph=graph)
+    a = ibm.Solver(case48, ibm.solver_params(arnoldi_passes=2, **kw))
+    b = ibm.Solver(case48, ibm.solver_params(arnoldi_passes=1, **kw))
+    for step in range(1, 6):
+        ramp = min(1.0, step / 3.0)
+        sa, sb = a.step(ramp), b.step(ramp)
+        assert sa.status == sb.status == ibm.IBM_OK
+        for f in "uvwp":
+            assert abs(getattr(sa, f).iters - getattr(sb, f).iters) <= 1, f
+    for x, y, name in zip(a.fields(), b.fields(), "uvwp"):
+        assert rel_err(y, x) <= 1e-7, name
+    s = ibm.Solver(case48, ibm.solver_params(vel_tol=1e-12, p_tol=1e-12, precision=1, arnoldi_passes=1,
+                                             vel_maxit=500, p_maxit=500, use_graph=graph))
+    orc = pyoracle.Oracle(case48, vel_tol=1e-13, p_tol=1e-13)
+    for step in range(1, 4):
+        st = s.step(min(1.0, step / 2.0))
+        orc.step(min(1.0, step / 2.0))
+        assert st.status == ibm.IBM_OK
+        for f in "uvwp":
+            assert getattr(st, f).rel_res <= 1e-12, f
+    for x, y, name in zip(s.fields(), orc.fields(), "uvwp"):
+        assert rel_err(x, y) <= 1e-9, name
+
+
 def test_fp32_cycles_reach_tight_tolerance(ibm, pyoracle, case48):
     """precision 2 restarts its FP32 cycles from FP64 true residuals, so it
     reaches tolerances far below FP32 resolution: 1e-12 on every solve."""
