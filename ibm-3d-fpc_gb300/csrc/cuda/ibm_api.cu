@@ -1024,7 +1024,7 @@ void step_launch(ibm_ctx *c, double ramp) {
     if (!c->graph_ready || !c->graph_bound) {
       const bool zg = c->prm.use_zero_initial_guess != 0;
       c->kmom.bind(st, bm, xm, ~0u, zg);
-      c->kp.bind(st, bp, xp, ~0u, zg);
+      c->kp.bind(st, bp, xp, ~0u, true);  // k_pressure_rhs zeroes the pressure's x0 every step
       c->graph_bound = true;
     }
     if (!c->graph_ready) build_step_graph(c, none, mgp);
@@ -1053,7 +1053,7 @@ void step_launch(ibm_ctx *c, double ramp) {
   IBM_CUDA_TRY(cudaEventRecord(c->ev[5], st));
   {
     PhaseScope ph(PH_P);
-    c->kp.solve(st, bp, xp, mgp, rp, ~0u, c->prm.use_zero_initial_guess != 0);
+    c->kp.solve(st, bp, xp, mgp, rp, ~0u, true);  // x0 = 0 (k_pressure_rhs), as the reference
   }
   IBM_CUDA_TRY(cudaEventRecord(c->ev[3], st));
   {
@@ -1548,7 +1548,7 @@ int reverse_graph(ibm_ctx *c) {
     const double *bp[1] = {c->bb[3].p};
     double *xp[1] = {c->xb[3].p};
     c->kmom.bind(c->st, bm, xm, ~0u, zg);
-    c->kp.bind(c->st, bp, xp, ~0u, zg);
+    c->kp.bind(c->st, bp, xp, ~0u, true);
     c->graph_bound = true;
   }
   if (!a.graph_ready) build_adjoint_graph(c);

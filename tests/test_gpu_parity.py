@@ -181,6 +181,22 @@ def test_benchmark_channel_160x32x32(ibm, pyoracle):
         assert rel_err(a, b) <= REL_TOL, name
 
 
+@pytest.mark.parametrize("graph", [0, 1])
+def test_nonzero_initial_guess_matches_oracle(ibm, pyoracle, case48, graph):
+    """use_zero_initial_guess 0: the momentum solves start from the current
+    velocities (main.cu's x0, immersed_operators.hpp:500-530), the pressure
+    solve still from zero as the reference's pressure right-hand side kernel
+    sets it; fields match the oracle to the hot path's 1e-10."""
+    s = ibm.Solver(case48, tight(ibm, use_zero_initial_guess=0, use_graph=graph))
+    orc = pyoracle.Oracle(case48, vel_tol=1e-13, p_tol=1e-13, use_zero_initial_guess=0)
+    for step in range(1, 4):
+        st = s.step(min(1.0, step / 2.0))
+        orc.step(min(1.0, step / 2.0))
+        assert st.status == ibm.IBM_OK
+    for a, b, name in zip(s.fields(), orc.fields(), "uvwp"):
+        assert rel_err(a, b) <= REL_TOL, name
+
+
 @pytest.mark.parametrize("precision", [1, 2])
 def test_mixed_precision_error(ibm, pyoracle, case48, precision):
     """FP32 preconditioners inside FP64 flexible GMRES (precision 1), and FP32

@@ -3,13 +3,16 @@ configurations name, through the C ABI.
 
 - Full timestep grid 640x128x128 (Um 2.25, dt 2e-4), pressure-solve grid
   512x96x96 and adjoint grid 256x48x48 (Um 0.45, dt 1e-3): one step of the
-  benchmark's own solver configuration (FP32 Arnoldi cycles with FP64
-  restarts, FP32 multigrid, tolerance 1e-8, graph-captured) from the
+  benchmark's own solver configuration (pressure: FP32 Arnoldi cycles with
+  FP64 restarts and FP32 multigrid; momentum: FP64 flexible GMRES with FP32
+  Jacobi, one Gram-Schmidt pass; tolerance 1e-8, graph-captured) from the
   benchmark's seeded initial state. Every dense stage of the device step
   (BC + convection + gradient + momentum right-hand sides, scatter +
   divergence + pressure right-hand side, projection, diagnostics) is
   compared bit for bit with the oracle's stage applied to the device's own
-  solve outputs, which keeps the oracle's cost O(N). Every solve is checked
+  solve outputs, which keeps the oracle's cost O(N); with the double-float
+  momentum right-hand side (df_rhs 1, the benchmark's form) that stage is
+  held to 2^-40 of the oracle's largest entry instead. Every solve is checked
   by its true residual b - A x, computed by the oracle's operator apply: it
   must meet the 1e-8 tolerance the device reported meeting.
 - The 160x32x32 channel (Um 0.45, nu 1e-3, dt 1e-3) for its full 50 steps,
@@ -50,12 +53,13 @@ def seeded_state(case, seed=2026):
     return u, v, w, np.zeros(nx * ny * nz)
 
 
-def benchmark_params(ibm):
+def benchmark_params(ibm, df_rhs):
     """The benchmark's solver configuration (mixed form, graph-captured)."""
     return ibm.solver_params(vel_tol=SOLVE_TOL, p_tol=SOLVE_TOL, vel_maxit=250, p_maxit=250, vel_kdim=50,
                              p_kdim=50, p_pc=1, p_pc_rap_type=0, p_pc_relax_type=2, mg_nu1=3, mg_nu2=3,
                              mg_nu_coarse=2, mg_omega=1.0, mg_group_ratio=1.5, mg_coarse_max=2560, mg_options=3,
-                             precision=2, vel_inner_sweeps=2, use_graph=1)
+                             precision=2, vel_precision=1, arnoldi_passes=1, vel_inner_sweeps=2, use_graph=1,
+                             df_rhs=df_rhs)
 
 
 SIZES = [((640, 128, 128), dict(Um=2.25, dt=2e-4)),
@@ -63,10 +67,11 @@ SIZES = [((640, 128, 128), dict(Um=2.25, dt=2e-4)),
          ((256, 48, 48), dict(Um=0.45, dt=1e-3))]
 
 
+@pytest.mark.parametrize("df_rhs", [0, 1], ids=["fp64-rhs", "df-rhs"])
 @pytest.mark.parametrize("shape,kw", SIZES, ids=["640x128x128", "512x96x96", "256x48x48"])
-def test_step_stages_and_residuals_at_benchmark_size(ibm, pyoracle, shape, kw):
+def test_step_stages_and_residuals_at_benchmark_size(ibm, pyoracle, shape, kw, df_rhs):
     case = ibm.Case(ibm.channel_params(*shape, nu=1e-3, **kw))
-    s = ibm.Solver(case, benchmark_params(ibm))
+    s = ibm.Solver(case, benchmark_params(ibm, df_rhs))
     try:
         orc = pyoracle.Oracle(case, vel_tol=SOLVE_TOL, p_tol=SOLVE_TOL)
         u, v, w, p = seeded_state(case)
@@ -81,7 +86,11 @@ def test_step_stages_and_residuals_at_benchmark_size(ibm, pyoracle, shape, kw):
         ub, vb, wb = orc.bc_cleanup(u, v, w, ramp)
         bu, bv, bw = orc.momentum_rhs(ub, vb, wb, p)
         for f, ref in enumerate((bu, bv, bw)):
-            assert bits_equal(s.solver_vector(f, 0), ref), f"momentum rhs {'uvw'[f]}"
+            got = s.solver_vector(f, 0)
+            if df_rhs:
+                assert np.abs(got - ref).max() <= 2.0 ** -40 * np.abs(ref).max(), f"momentum rhs {'uvw'[f]}"
+            else:
+                assert bits_equal(got, ref), f"momentum rhs {'uvw'[f]}"
         xu, xv, xw = (s.solver_vector(f, 1) for f in range(3))
         orc.set_fields(ub, vb, wb, p)
         ut, vt, wt = orc.tilde(xu, xv, xw, ramp)
