@@ -1008,6 +1008,7 @@ namespace {
 void step_launch(ibm_ctx *c, double ramp) {
   require_inputs(c);
   ensure_solvers(c);
+  ensure_rhs_df(c);
   cudaStream_t st = c->st;
   *c->hramp = ramp;
   KResult *rm = c->last_rm, *rp = c->last_rp;

@@ -77,6 +77,7 @@ struct ibm_ctx {
   ibm::DBuf<double> cf_w;
 
   ibm::DBuf<double> u, v, w, p, ut, vt, wt;
+  ibm::DBuf<float2> df_u, df_v, df_w, df_p;  // double-float copies of u, v, w, p (df_rhs)
   ibm::DBuf<double> xb[4], bb[4];
   ibm::DBuf<double> part;        // diagnostics block partials
   ibm::DBuf<ibm::StepDiag> diag;

@@ -172,6 +172,7 @@ struct RhsArgs {
   double a, rho;
   KnownDiv tdx, tdy, tdz;  // 2 dx, 2 dy, 2 dz
   DF da, drho, drx, dry, drz;  // double-float a, rho, 1 / (2 dx), 1 / (2 dy), 1 / (2 dz)
+  const float2 *u2, *v2, *w2, *p2;  // double-float copies of u, v, w, p (RhsDF; k_split_fields)
   int zero_guess;
 };
 
@@ -185,6 +186,7 @@ struct RhsArgs {
 struct RhsF64 {
   using T = double;
   __device__ static T in(double x) { return x; }
+  __device__ static T fld(const double *a, const float2 *, long i) { return a[i]; }
   __device__ static T zero() { return 0.0; }
   __device__ static T avg(T a, T b, T c, T d) { return avg4(a, b, c, d); }
   __device__ static T adv(const RhsArgs &A, T c, T dm, T dp, T a2, T em, T ep, T a3, T fm, T fp) {
@@ -198,6 +200,11 @@ struct RhsF64 {
 struct RhsDF {
   using T = DF;
   __device__ static T in(double x) { return df_of(x); }
+  // a field value from the field's double-float copy (split once per step)
+  __device__ static T fld(const double *, const float2 *a2, long i) {
+    const float2 v = a2[i];
+    return DF{v.x, v.y};
+  }
   __device__ static T zero() { return DF{0.0f, 0.0f}; }
   __device__ static T avg(T a, T b, T c, T d) { return df_scale(df_add(df_add(df_add(a, b), c), d), 0.25f); }
   __device__ static T adv(const RhsArgs &A, T c, T dm, T dp, T a2, T em, T ep, T a3, T fm, T fp) {
@@ -240,30 +247,31 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
       const int j = udivmod(q, d.dny, kq), k = (int)kq;
       const long f = U3(d, i, j, k);
       const uint8_t fl = A.fu[f];
-      const double ucd = A.u[f];
       double rhs = 0.0;
       if (fl & kRhsRow) {
-        const T uc = M::in(ucd);
+        const T uc = M::fld(A.u, A.u2, f);
         T conv = M::zero();
         if (fl & kActive) {
           const long vb = V3(d, i - 1, j, k), wb = W3(d, i - 1, j, k);
-          const T va = M::avg(M::in(A.v[vb]), M::in(A.v[vb + sv]), M::in(A.v[vb + 1]), M::in(A.v[vb + 1 + sv]));
-          const T wa = M::avg(M::in(A.w[wb]), M::in(A.w[wb + pw]), M::in(A.w[wb + 1]), M::in(A.w[wb + 1 + pw]));
-          conv = M::adv(A, uc, M::in(A.u[f - 1]), M::in(A.u[f + 1]), va,
-                        M::in(j > 0 ? A.u[f - su] : ucd), M::in(j < d.ny - 1 ? A.u[f + su] : ucd), wa,
-                        M::in(k > 0 ? A.u[f - pu] : ucd), M::in(k < d.nz - 1 ? A.u[f + pu] : ucd));
+          const T va = M::avg(M::fld(A.v, A.v2, vb), M::fld(A.v, A.v2, vb + sv),
+                              M::fld(A.v, A.v2, vb + 1), M::fld(A.v, A.v2, vb + 1 + sv));
+          const T wa = M::avg(M::fld(A.w, A.w2, wb), M::fld(A.w, A.w2, wb + pw),
+                              M::fld(A.w, A.w2, wb + 1), M::fld(A.w, A.w2, wb + 1 + pw));
+          conv = M::adv(A, uc, M::fld(A.u, A.u2, f - 1), M::fld(A.u, A.u2, f + 1), va,
+                        (j > 0 ? M::fld(A.u, A.u2, f - su) : uc), (j < d.ny - 1 ? M::fld(A.u, A.u2, f + su) : uc), wa,
+                        (k > 0 ? M::fld(A.u, A.u2, f - pu) : uc), (k < d.nz - 1 ? M::fld(A.u, A.u2, f + pu) : uc));
         }
         T gp = M::zero();
         if (fl & kQFace) {
           const long c = P3(d, i - 1, j, k);
-          const double pl = (A.fc[c] & kFluid) ? A.p[c] : 0.0;
-          const double pr = (A.fc[c + 1] & kFluid) ? A.p[c + 1] : 0.0;
-          gp = M::grad(M::in(A.Gu[f]), M::in(pl), M::in(A.Gu[NU + f]), M::in(pr));
+          const T pl = (A.fc[c] & kFluid) ? M::fld(A.p, A.p2, c) : M::zero();
+          const T pr = (A.fc[c + 1] & kFluid) ? M::fld(A.p, A.p2, c + 1) : M::zero();
+          gp = M::grad(M::in(A.Gu[f]), pl, M::in(A.Gu[NU + f]), pr);
         }
         rhs = M::rhs(A, uc, conv, gp, A.bc[0][r], A.sc[0][r]);
       }
       A.b[0][r] = rhs;
-      A.x0[0][r] = A.zero_guess ? 0.0 : ucd;
+      A.x0[0][r] = A.zero_guess ? 0.0 : A.u[f];
     } else if (t < A.nb[0] + A.nb[1]) {  // v row: face (i, j+1, k)
       const long r = t - A.nb[0];
       long q;
@@ -272,30 +280,32 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
       const int j = udivmod(q, d.dnym, kq) + 1, k = (int)kq;
       const long f = V3(d, i, j, k);
       const uint8_t fl = A.fv[f];
-      const double vcd = A.v[f];
       double rhs = 0.0;
       if (fl & kRhsRow) {
-        const T vc = M::in(vcd);
+        const T vc = M::fld(A.v, A.v2, f);
         T conv = M::zero();
         if (fl & kActive) {
           const long ub = U3(d, i, j - 1, k), wb = W3(d, i, j - 1, k);
-          const T ua = M::avg(M::in(A.u[ub]), M::in(A.u[ub + 1]), M::in(A.u[ub + su]), M::in(A.u[ub + su + 1]));
-          const T wa = M::avg(M::in(A.w[wb]), M::in(A.w[wb + sw]), M::in(A.w[wb + pw]), M::in(A.w[wb + pw + sw]));
-          conv = M::adv(A, ua, M::in(i > 0 ? A.v[f - 1] : vcd), M::in(i < d.nx - 1 ? A.v[f + 1] : vcd), vc,
-                        M::in(A.v[f - sv]), M::in(A.v[f + sv]), wa,
-                        M::in(k > 0 ? A.v[f - pv] : vcd), M::in(k < d.nz - 1 ? A.v[f + pv] : vcd));
+          const T ua = M::avg(M::fld(A.u, A.u2, ub), M::fld(A.u, A.u2, ub + 1),
+                              M::fld(A.u, A.u2, ub + su), M::fld(A.u, A.u2, ub + su + 1));
+          const T wa = M::avg(M::fld(A.w, A.w2, wb), M::fld(A.w, A.w2, wb + sw),
+                              M::fld(A.w, A.w2, wb + pw), M::fld(A.w, A.w2, wb + pw + sw));
+          conv = M::adv(A, ua, (i > 0 ? M::fld(A.v, A.v2, f - 1) : vc),
+                        (i < d.nx - 1 ? M::fld(A.v, A.v2, f + 1) : vc), vc,
+                        M::fld(A.v, A.v2, f - sv), M::fld(A.v, A.v2, f + sv), wa,
+                        (k > 0 ? M::fld(A.v, A.v2, f - pv) : vc), (k < d.nz - 1 ? M::fld(A.v, A.v2, f + pv) : vc));
         }
         T gp = M::zero();
         if (fl & kQFace) {
           const long c = P3(d, i, j - 1, k);
-          const double pl = (A.fc[c] & kFluid) ? A.p[c] : 0.0;
-          const double pr = (A.fc[c + sw] & kFluid) ? A.p[c + sw] : 0.0;
-          gp = M::grad(M::in(A.Gv[f]), M::in(pl), M::in(A.Gv[NV + f]), M::in(pr));
+          const T pl = (A.fc[c] & kFluid) ? M::fld(A.p, A.p2, c) : M::zero();
+          const T pr = (A.fc[c + sw] & kFluid) ? M::fld(A.p, A.p2, c + sw) : M::zero();
+          gp = M::grad(M::in(A.Gv[f]), pl, M::in(A.Gv[NV + f]), pr);
         }
         rhs = M::rhs(A, vc, conv, gp, A.bc[1][r], A.sc[1][r]);
       }
       A.b[1][r] = rhs;
-      A.x0[1][r] = A.zero_guess ? 0.0 : vcd;
+      A.x0[1][r] = A.zero_guess ? 0.0 : A.v[f];
     } else {  // w row: face (i, j, k+1)
       const long r = t - A.nb[0] - A.nb[1];
       long q;
@@ -304,32 +314,54 @@ __global__ void __launch_bounds__(kThreads, 4) k_momentum_rhs(RhsArgs A) {
       const int j = udivmod(q, d.dny, kq), k = (int)kq + 1;
       const long f = W3(d, i, j, k);
       const uint8_t fl = A.fw[f];
-      const double wcd = A.w[f];
       double rhs = 0.0;
       if (fl & kRhsRow) {
-        const T wc = M::in(wcd);
+        const T wc = M::fld(A.w, A.w2, f);
         T conv = M::zero();
         // the convection of w uses the mask one plane below (gpu_dense_ops.hpp:14)
         if (A.fw[f - pw] & kActive) {
           const long ub = U3(d, i, j, k - 1), vb = V3(d, i, j, k - 1);
-          const T ua = M::avg(M::in(A.u[ub]), M::in(A.u[ub + 1]), M::in(A.u[ub + pu]), M::in(A.u[ub + pu + 1]));
-          const T va = M::avg(M::in(A.v[vb]), M::in(A.v[vb + sv]), M::in(A.v[vb + pv]), M::in(A.v[vb + pv + sv]));
-          conv = M::adv(A, ua, M::in(i > 0 ? A.w[f - 1] : wcd), M::in(i < d.nx - 1 ? A.w[f + 1] : wcd), va,
-                        M::in(j > 0 ? A.w[f - sw] : wcd), M::in(j < d.ny - 1 ? A.w[f + sw] : wcd), wc,
-                        M::in(A.w[f - pw]), M::in(A.w[f + pw]));
+          const T ua = M::avg(M::fld(A.u, A.u2, ub), M::fld(A.u, A.u2, ub + 1),
+                              M::fld(A.u, A.u2, ub + pu), M::fld(A.u, A.u2, ub + pu + 1));
+          const T va = M::avg(M::fld(A.v, A.v2, vb), M::fld(A.v, A.v2, vb + sv),
+                              M::fld(A.v, A.v2, vb + pv), M::fld(A.v, A.v2, vb + pv + sv));
+          conv = M::adv(A, ua, (i > 0 ? M::fld(A.w, A.w2, f - 1) : wc),
+                        (i < d.nx - 1 ? M::fld(A.w, A.w2, f + 1) : wc), va,
+                        (j > 0 ? M::fld(A.w, A.w2, f - sw) : wc), (j < d.ny - 1 ? M::fld(A.w, A.w2, f + sw) : wc), wc,
+                        M::fld(A.w, A.w2, f - pw), M::fld(A.w, A.w2, f + pw));
         }
         T gp = M::zero();
         if (fl & kQFace) {
           const long c = P3(d, i, j, k - 1);
-          const double pl = (A.fc[c] & kFluid) ? A.p[c] : 0.0;
-          const double pr = (A.fc[c + pw] & kFluid) ? A.p[c + pw] : 0.0;
-          gp = M::grad(M::in(A.Gw[f]), M::in(pl), M::in(A.Gw[NW + f]), M::in(pr));
+          const T pl = (A.fc[c] & kFluid) ? M::fld(A.p, A.p2, c) : M::zero();
+          const T pr = (A.fc[c + pw] & kFluid) ? M::fld(A.p, A.p2, c + pw) : M::zero();
+          gp = M::grad(M::in(A.Gw[f]), pl, M::in(A.Gw[NW + f]), pr);
         }
         rhs = M::rhs(A, wc, conv, gp, A.bc[2][r], A.sc[2][r]);
       }
       A.b[2][r] = rhs;
-      A.x0[2][r] = A.zero_guess ? 0.0 : wcd;
+      A.x0[2][r] = A.zero_guess ? 0.0 : A.w[f];
     }
+  }
+}
+
+// Double-float copies of u, v, w and p for RhsDF: each value is split once
+// per step instead of at each of its (about seven) uses by the right-hand
+// side. Block row y takes field y.
+struct SplitArgs {
+  const double *src[4];
+  float2 *dst[4];
+  long n[4];
+};
+__global__ void __launch_bounds__(kThreads) k_split_fields(SplitArgs A) {
+  const int a = blockIdx.y;
+  const double *src = a == 0 ? A.src[0] : a == 1 ? A.src[1] : a == 2 ? A.src[2] : A.src[3];
+  float2 *dst = a == 0 ? A.dst[0] : a == 1 ? A.dst[1] : a == 2 ? A.dst[2] : A.dst[3];
+  const long n = a == 0 ? A.n[0] : a == 1 ? A.n[1] : a == 2 ? A.n[2] : A.n[3];
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    float h, l;
+    df_split_fast(src[i], h, l);
+    dst[i] = make_float2(h, l);
   }
 }
 
@@ -677,6 +709,11 @@ bool momentum_rhs_df(const ibm_solver_params &p) {
   return p.df_rhs != 0 && vp >= 1;
 }
 
+void ensure_rhs_df(ibm_ctx *c) {
+  if (!momentum_rhs_df(c->prm) || c->df_u.p) return;
+  c->df_u.alloc(c->g.NU); c->df_v.alloc(c->g.NV); c->df_w.alloc(c->g.NW); c->df_p.alloc(c->g.NP);
+}
+
 void launch_momentum_rhs(ibm_ctx *c) {
   RhsArgs A;
   A.d = dims_of(c);
@@ -702,12 +739,28 @@ void launch_momentum_rhs(ibm_ctx *c) {
   A.da = split(A.a); A.drho = split(A.rho);
   A.drx = split(1.0 / (2 * c->g.dx)); A.dry = split(1.0 / (2 * c->g.dy)); A.drz = split(1.0 / (2 * c->g.dz));
   const double faces = (double)(c->g.NU + c->g.NV + c->g.NW), nbox = (double)(A.nb[0] + A.nb[1] + A.nb[2]);
-  LaunchScope ls(K_RHS, c->st, 8.0 * faces + 9.0 * c->g.NP + nbox * (1 + 16 + 32));
   const long rows = A.nb[0] + A.nb[1] + A.nb[2];
-  if (momentum_rhs_df(c->prm))
+  if (momentum_rhs_df(c->prm)) {
+    if (!c->df_u.p || !c->df_v.p || !c->df_w.p || !c->df_p.p)
+      throw Error(IBM_ERR_STATE, "double-float field copies not allocated");
+    SplitArgs S;
+    S.src[0] = c->u.p; S.src[1] = c->v.p; S.src[2] = c->w.p; S.src[3] = c->p.p;
+    S.dst[0] = c->df_u.p; S.dst[1] = c->df_v.p; S.dst[2] = c->df_w.p; S.dst[3] = c->df_p.p;
+    S.n[0] = c->g.NU; S.n[1] = c->g.NV; S.n[2] = c->g.NW; S.n[3] = c->g.NP;
+    {
+      LaunchScope ls(K_RHS, c->st, 16.0 * (faces + c->g.NP));
+      const long nmax = std::max(std::max(S.n[0], S.n[1]), std::max(S.n[2], S.n[3]));
+      const dim3 grid(std::max(1, wave_blocks(k_split_fields, nmax) / 4), 4);
+      k_split_fields<<<grid, kThreads, 0, c->st>>>(S);
+    }
+    A.u2 = c->df_u.p; A.v2 = c->df_v.p; A.w2 = c->df_w.p; A.p2 = c->df_p.p;
+    LaunchScope ls(K_RHS, c->st, 8.0 * faces + 9.0 * c->g.NP + nbox * (1 + 16 + 32));
     k_momentum_rhs<RhsDF><<<wave_blocks(k_momentum_rhs<RhsDF>, rows), kThreads, 0, c->st>>>(A);
-  else
+  } else {
+    A.u2 = A.v2 = A.w2 = A.p2 = nullptr;
+    LaunchScope ls(K_RHS, c->st, 8.0 * faces + 9.0 * c->g.NP + nbox * (1 + 16 + 32));
     k_momentum_rhs<RhsF64><<<wave_blocks(k_momentum_rhs<RhsF64>, rows), kThreads, 0, c->st>>>(A);
+  }
 }
 
 void launch_tilde(ibm_ctx *c) {
