@@ -342,15 +342,16 @@ def ensemble_measure(ibm, args, ws, rank, local, steps, warmup):
         t_long = reduce_max_ms((time.perf_counter() - t0) * 1e3, ws, "cuda")
         mixed_fields = [s.fields() for s in batch.solvers]
         batch.close()
-        # FP64, and the control: FP64 again along other iterates to the same
-        # tolerances (GMRES(2) momentum solves, 2+2 finest-level sweeps), as
-        # the long run's
+        # FP64 at the mixed form's tolerances, and FP64 at 1e-10 as the
+        # truth both are measured against: in the fast channels the wake
+        # amplifies tolerance-level differences, so the mixed form's error is
+        # read beside the FP64 form's own error at the same tolerances
         runs = []
-        for nu in (3, 2):
+        for tol in (None, 1e-10):
             p64 = solver_params(ibm, 0, graph=1, coarse_max=args.mg_coarse_max)
-            p64.mg_nu1 = p64.mg_nu2 = nu
-            if nu == 2:
-                p64.vel_kdim = 2
+            if tol is not None:
+                p64.vel_tol = p64.p_tol = tol
+                p64.vel_maxit = p64.p_maxit = 500
             b64 = ibm.Batch(cases, p64, device=local)
             for s, c in zip(b64.solvers, cases):
                 s.set_fields(*initial_state(c))
@@ -364,16 +365,17 @@ def ensemble_measure(ibm, args, ws, rank, local, steps, warmup):
             return max(float(np.abs(a - b).max()) for a, b in zip(fa[:3], fb[:3])) / umax
 
         errs = [rel_vel(fm, f64) for fm, f64 in zip(mixed_fields, runs[0])]
-        ctrl = [rel_vel(fc, f64) for fc, f64 in zip(runs[1], runs[0])]
+        e_mixed = [rel_vel(fm, ft) for fm, ft in zip(mixed_fields, runs[1])]
+        e_fp64 = [rel_vel(f64, ft) for f64, ft in zip(runs[0], runs[1])]
         accuracy = {"steps": nst, "instance_steps_per_s": len(specs) * nst / (t_long / 1e3),
                     "velocity_rel_err_vs_fp64": errs, "velocity_rel_err_max": max(errs),
-                    "control_fp64_vs_fp64": ctrl, "control_max": max(ctrl),
+                    "mixed_vs_fp64_tight": e_mixed, "mixed_vs_fp64_tight_max": max(e_mixed),
+                    "fp64_vs_fp64_tight": e_fp64, "fp64_vs_fp64_tight_max": max(e_fp64),
                     "instances_within_1e-6": int(sum(e <= 1e-6 for e in errs)),
-                    "instances_within_control": int(sum(e <= max(c, 1e-6) for e, c in zip(errs, ctrl))),
-                    "note": "each instance's largest velocity difference from an FP64 batch of the same instance "
-                            "after the same steps, relative to the FP64 run's largest |u|; the control is a second "
-                            "FP64 batch with GMRES(2) momentum solves and 2+2 finest-level multigrid sweeps (same "
-                            "tolerances, other iterates) against the first; instance order as 'instances' of this "
+                    "instances_mixed_within_fp64_error": int(sum(m <= max(f, 1e-6) for m, f in zip(e_mixed, e_fp64))),
+                    "note": "velocity differences after the same steps from the same initial states, relative to "
+                            "the reference run's largest |u|: mixed against FP64 at the same tolerances, and both "
+                            "against an FP64 batch at 1e-10 (the truth); instance order as 'instances' of this "
                             "rank"}
     else:
         batch.close()
