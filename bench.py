@@ -274,6 +274,29 @@ def shard_by_cells(specs, ws, rank):
     return sorted(mine)
 
 
+def rel_velocity_diff(fa, fb):
+    """Largest velocity difference of two (u, v, w, p) field sets, relative to
+    the second set's largest |u|, |v|, |w|."""
+    umax = max(float(np.abs(x).max()) for x in fb[:3])
+    return max(float(np.abs(a - b).max()) for a, b in zip(fa[:3], fb[:3])) / max(umax, 1e-300)
+
+
+def ensemble_accuracy(mixed, fp64, truth):
+    """Per-instance accuracy of the ensemble's mixed form: against FP64 at
+    the same tolerances, and both forms against a tighter FP64 truth."""
+    errs = [rel_velocity_diff(m, f) for m, f in zip(mixed, fp64)]
+    e_mixed = [rel_velocity_diff(m, t) for m, t in zip(mixed, truth)]
+    e_fp64 = [rel_velocity_diff(f, t) for f, t in zip(fp64, truth)]
+    return {"velocity_rel_err_vs_fp64": errs, "velocity_rel_err_max": max(errs),
+            "mixed_vs_fp64_tight": e_mixed, "mixed_vs_fp64_tight_max": max(e_mixed),
+            "fp64_vs_fp64_tight": e_fp64, "fp64_vs_fp64_tight_max": max(e_fp64),
+            "instances_within_1e-6": int(sum(e <= 1e-6 for e in errs)),
+            "instances_mixed_within_fp64_error": int(sum(m <= max(f, 1e-6) for m, f in zip(e_mixed, e_fp64))),
+            "note": "velocity differences after the same steps from the same initial states, relative to the "
+                    "reference run's largest |u|: mixed against FP64 at the same tolerances, and both against an "
+                    "FP64 batch at 1e-10 (the truth); instance order as 'instances' of this rank"}
+
+
 def ensemble_measure(ibm, args, ws, rank, local, steps, warmup):
     """Instance-steps/s of the batched ensemble (ibm_batch_step: every
     instance's graph-captured step queued before any is waited for) and of
@@ -360,23 +383,8 @@ def ensemble_measure(ibm, args, ws, rank, local, steps, warmup):
             runs.append([s.fields() for s in b64.solvers])
             b64.close()
 
-        def rel_vel(fa, fb):
-            umax = max(float(np.abs(x).max()) for x in fb[:3])
-            return max(float(np.abs(a - b).max()) for a, b in zip(fa[:3], fb[:3])) / umax
-
-        errs = [rel_vel(fm, f64) for fm, f64 in zip(mixed_fields, runs[0])]
-        e_mixed = [rel_vel(fm, ft) for fm, ft in zip(mixed_fields, runs[1])]
-        e_fp64 = [rel_vel(f64, ft) for f64, ft in zip(runs[0], runs[1])]
         accuracy = {"steps": nst, "instance_steps_per_s": len(specs) * nst / (t_long / 1e3),
-                    "velocity_rel_err_vs_fp64": errs, "velocity_rel_err_max": max(errs),
-                    "mixed_vs_fp64_tight": e_mixed, "mixed_vs_fp64_tight_max": max(e_mixed),
-                    "fp64_vs_fp64_tight": e_fp64, "fp64_vs_fp64_tight_max": max(e_fp64),
-                    "instances_within_1e-6": int(sum(e <= 1e-6 for e in errs)),
-                    "instances_mixed_within_fp64_error": int(sum(m <= max(f, 1e-6) for m, f in zip(e_mixed, e_fp64))),
-                    "note": "velocity differences after the same steps from the same initial states, relative to "
-                            "the reference run's largest |u|: mixed against FP64 at the same tolerances, and both "
-                            "against an FP64 batch at 1e-10 (the truth); instance order as 'instances' of this "
-                            "rank"}
+                    **ensemble_accuracy(mixed_fields, runs[0], runs[1])}
     else:
         batch.close()
     n = len(specs)

@@ -82,3 +82,26 @@ def test_ensemble_shards_cover_every_instance_once(ws):
         assert 96 <= nx <= 256 and 16 <= ny <= 48 and 16 <= nz <= 48
         assert nx % 16 == ny % 16 == nz % 16 == 0
         assert 0.06 <= d <= 0.14 and 0.15 <= yc <= 0.26 and 0.2 <= um <= 2.25
+
+
+def test_ensemble_accuracy_summary():
+    """The ensemble's accuracy record: per-instance velocity differences
+    relative to the reference set's largest velocity, against FP64 at the
+    same tolerances and both forms against the tighter truth."""
+    import numpy as np
+    b = _bench()
+    rng = np.random.default_rng(3)
+    truth = [[rng.standard_normal(50) for _ in range(4)] for _ in range(3)]
+    fp64 = [[x + d for x in t] for t, d in zip(truth, (1e-7, 5e-6, 2e-7))]
+    mixed = [[x + d for x in t] for t, d in zip(truth, (3e-7, 2e-6, 4e-6))]
+    acc = b.ensemble_accuracy(mixed, fp64, truth)
+    scale = [max(float(np.abs(x).max()) for x in t[:3]) for t in truth]
+    assert np.allclose(acc["mixed_vs_fp64_tight"], [3e-7 / scale[0], 2e-6 / scale[1], 4e-6 / scale[2]])
+    assert np.allclose(acc["fp64_vs_fp64_tight"], [1e-7 / scale[0], 5e-6 / scale[1], 2e-7 / scale[2]])
+    assert acc["mixed_vs_fp64_tight_max"] == max(acc["mixed_vs_fp64_tight"])
+    assert len(acc["velocity_rel_err_vs_fp64"]) == 3
+    # instance 0: within 1e-6; 1: within FP64's own error; 2: neither
+    assert acc["instances_mixed_within_fp64_error"] == 2
+    # the pressure (index 3) does not enter the velocity differences
+    mixed[0][3] = mixed[0][3] + 1.0
+    assert b.ensemble_accuracy(mixed, fp64, truth)["mixed_vs_fp64_tight"][0] == acc["mixed_vs_fp64_tight"][0]
